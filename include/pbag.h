@@ -1,0 +1,238 @@
+/*
+ * pbag.h - C ABI of the GB300 comoving-radiation step for PyBlastAfterglowMag.
+ *
+ * One "blastwave" is one (layer, shock) pair: one ElectronAndRadiation object
+ * in the reference (src/microphysics/microphysics.h:60). One "step" of a
+ * blastwave is the pair of calls the reference's blastwave driver makes at one
+ * burster-frame time index (src/blastwave/blastwave_radiation.h:1109-1182):
+ *   initializeElectronDistribution      (microphysics.h:347)   on the first valid step, or
+ *   evaluateElectronDistributionNumericMixed (microphysics.h:359) on later ones,
+ * followed by
+ *   computeRadiationNumericMixed(it)     (microphysics.h:492).
+ *
+ * A caller records one pbag_step_rec per (blastwave, time index) - the scalar
+ * arguments of those calls plus the members that computeEleSpectrumLimits()
+ * (microphysics_base.h:642) set just before them - and hands the whole history
+ * of a batch of blastwaves to pbag_run_batch(), which evolves all of them on
+ * one GPU and fills the same time-major "*_all" arrays the reference fills
+ * (base_state.h:200-211, 288-296).
+ *
+ * All functions return PBAG_OK (0) or a negative pbag_status code; they never
+ * throw and never exit the process. Pointers are plain host or device pointers
+ * as each function documents; sizes are element counts.
+ */
+#ifndef PBAG_H
+#define PBAG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBAG_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum pbag_status_code {
+  PBAG_OK = 0,
+  PBAG_ERR_ARG = -1,        /* bad argument (null pointer, size out of range) */
+  PBAG_ERR_CUDA = -2,       /* a CUDA runtime call failed                      */
+  PBAG_ERR_NONFINITE = -3,  /* NaN / negative value where the reference exits  */
+  PBAG_ERR_NELE = -4,       /* total electron number <= 0 (microphysics.h:560) */
+  PBAG_ERR_PARAM = -5,      /* B<=0, gamma_min<1, ... (microphysics.h:372)     */
+  PBAG_ERR_DLNVDT = -6,     /* dlnV/dt negative or not finite (microphysics.h:406) */
+  PBAG_ERR_UNSUPPORTED = -7,/* option the GPU path does not implement          */
+  PBAG_ERR_TIMEOUT = -8,    /* a bounded device-side wait ran out              */
+  PBAG_ERR_NOMEM = -9       /* device allocation failed                        */
+};
+
+/* ---- options (same meaning as the reference's parfile options) ----------- */
+enum pbag_mode {            /* what the blastwave driver does at this step      */
+  PBAG_SKIP = 0,            /* blastwave not valid at this step: no call        */
+  PBAG_INIT = 1,            /* valid step; the driver's first valid step calls   */
+  PBAG_EVOLVE = 2           /* initializeElectronDistribution, later ones call    */
+                            /* evaluateElectronDistributionNumericMixed; both are */
+                            /* followed by computeRadiationNumericMixed. INIT and */
+                            /* EVOLVE are equivalent: like the driver, the step   */
+                            /* initialises iff no earlier step of this blastwave  */
+                            /* was valid (blastwave_radiation.h:1160-1175).       */
+};
+enum pbag_syn_method {      /* method_synchrotron_{fs,rs} (microphysics_base.h:304-349) */
+  PBAG_SYN_CSYN = 0,        /* "CSYN": SynKernel::cycSynch (kernels.h:414), the default */
+  PBAG_SYN_DER09 = 1,       /* "Dermer09": SynKernel::synchDermer (kernels.h:451)      */
+  PBAG_SYN_GSL = 2,         /* "GSL": SynKernel::synchGSL (kernels.h:211)              */
+  PBAG_SYN_BESSEL = 3       /* "Bessel": SynKernel::synchBessel (kernels.h:396)        */
+};
+enum pbag_ele_method {      /* method_ele_{fs,rs} (microphysics_base.h:254-276) */
+  PBAG_ELE_NUMERIC = 1,     /* "numeric": Chang-Cooper evolution                */
+  PBAG_ELE_MIX = 2          /* "mix": analytic N(gamma), numeric radiation      */
+};
+
+/* Grid description: the electron grid is rebuilt as e[i] = step^i with
+ * step = exp(ln(gam2)/ngam) (base_state.h:217-253); the photon grid is
+ * logspace(log10 freq1, log10 freq2, nfreq) built by repeated multiplication
+ * (utils.h MakeLogspaceVec), shared by synchrotron, SSC and total spectra. */
+typedef struct pbag_grid_desc {
+  int32_t ngam;             /* G, 8..1024                                       */
+  int32_t nfreq;            /* F, 8..1024                                       */
+  double gam1, gam2;        /* gam1_{fs,rs}, gam2_{fs,rs}                       */
+  double freq1, freq2;      /* freq1_{fs,rs}, freq2_{fs,rs} [Hz]                */
+} pbag_grid_desc;
+
+/* Per-blastwave options and parameters read by the numeric step. */
+typedef struct pbag_shock_params {
+  double p;                 /* p_{fs,rs}: injection index                       */
+  double eps_e;             /* eps_e_{fs,rs} (diagnostics only)                 */
+  int32_t max_substeps;     /* max_substeps_{fs,rs} (default 1000)              */
+  int32_t ele_method;       /* pbag_ele_method                                  */
+  int32_t syn_method;       /* pbag_syn_method                                  */
+  int32_t ssa_on;           /* use_ssa_{fs,rs}                                  */
+  int32_t ssc_on;           /* method_ssc_{fs,rs} == "numeric"                  */
+  int32_t adi_on;           /* num_ele_use_adi_loss_{fs,rs} (default yes)       */
+  int32_t pp_on;            /* method_pp_{fs,rs}: must be 0 (not implemented)   */
+  int32_t reserved;
+} pbag_shock_params;
+
+/* One step record: the arguments of the reference's per-step calls plus the
+ * members computeEleSpectrumLimits() set before them.
+ *  EVOLVE: evaluateElectronDistributionNumericMixed(tc, tc_p1, m, m_p1, rho, rho_p1,
+ *          r, rp1, dr, dr_p1, u_p, u_p_p1)   (r, rp1 are unused by the reference)
+ *  INIT:   initializeElectronDistribution(tc_p1, m_p1, rho_p1, u_p_p1, dr)        */
+typedef struct pbag_step_rec {
+  int32_t mode;             /* pbag_mode                                        */
+  int32_t reserved;
+  double tc, tc_p1;         /* comoving time at it-1, it [s]                    */
+  double m, m_p1;           /* swept-up mass at it-1, it [g]                    */
+  double rho, rho_p1;       /* comoving density at it-1, it [g/cm^3]            */
+  double dr, dr_p1;         /* comoving shock thickness at it-1, it [cm]        */
+  double u_p, u_p_p1;       /* comoving energy density at it-1, it [erg/cm^3]   */
+  double B;                 /* comoving magnetic field [G]                      */
+  double gamma_min, gamma_max, gamma_c, accel_frac, n_prime;
+} pbag_step_rec;
+
+/* Output histories. Row r of every array belongs to record r (rows of one
+ * blastwave are consecutive, in step order); F = nfreq, G = ngam doubles per
+ * row. Any pointer may be NULL: that history is not produced. Skipped steps
+ * produce zero rows, as the reference's zero-initialised vectors do. */
+typedef struct pbag_outputs {
+  double* j_all;            /* total_rad.j_all  [nrec x F] emissivity per electron */
+  double* a_all;            /* total_rad.a_all  [nrec x F] absorption             */
+  double* f_all;            /* total_rad.f_all  [nrec x F] photon density         */
+  double* i_all;            /* total_rad.i_all  [nrec x F] intensity              */
+  double* ele_f_all;        /* ele.f_all        [nrec x G]  (save_spec)           */
+  double* gdot_syn_all;     /* ele.gam_dot_syn_all [nrec x G]                     */
+  double* gdot_adi_all;     /* ele.gam_dot_adi_all [nrec x G]                     */
+  double* gdot_ssc_all;     /* ele.gam_dot_ssc_all [nrec x G]                     */
+  double* syn_j_all;        /* syn.j_all        [nrec x F]                        */
+  double* syn_a_all;        /* syn.a_all        [nrec x F]                        */
+  double* syn_i_all;        /* syn.i_all        [nrec x F]                        */
+  double* ssc_j_all;        /* ssc.j_all        [nrec x F]                        */
+  double* ssc_i_all;        /* ssc.i_all        [nrec x F]                        */
+} pbag_outputs;
+
+/* First failure, in the reference's order of checks. */
+typedef struct pbag_status {
+  int32_t code;             /* pbag_status_code                                 */
+  int32_t bw;               /* blastwave index of the first failure, or -1      */
+  int32_t step;             /* step index within that blastwave, or -1          */
+  int32_t reserved;
+} pbag_status;
+
+/* ---- per-step shock scalars (host) --------------------------------------
+ * Options of ElectronAndRadiaionBase::computeEleSpectrumLimits
+ * (microphysics_base.h:642-966); the enum values follow the parfile strings. */
+typedef struct pbag_limits_opts {
+  double p, eps_e, eps_b, eps_t;     /* p_, eps_e_, eps_b_, eps_t_{fs,rs}          */
+  double beta_min;                   /* beta_min_{fs,rs} (default 1e-5)            */
+  double mu, mu_e;                   /* 0.62, 1.18 (microphysics_base.h:103-104)   */
+  int32_t method_B;                  /* 0 "useU_b", 1 "useMAG21", 2 "useGammaSh"    */
+  int32_t method_gamma_min;          /* 0 "useU_e", 1 "useNumeric", 2 "useBeta",   */
+                                     /* 3 "useGamma", 4 "useTheta"                  */
+  int32_t method_gamma_c;            /* 0 "useTe", 1 "useTcomov", 2 "useConst"      */
+  int32_t method_gamma_max;          /* 0 "useB", 1 "useConst"                      */
+  int32_t method_nonrel;             /* 0 "none", 1 "use_gamma_min", 2 "use_Ayache", 3 "use_Sironi" */
+  int32_t ele_analytic;              /* 1 if method_ele is "analytic" (no grid caps) */
+} pbag_limits_opts;
+
+/* Arguments of updateSockProperties (microphysics_base.h:575). */
+typedef struct pbag_shock_state {
+  double e_prime, Gamma, GammaSh, t_e, t_b, tcomov, n_prime, n_protons;
+} pbag_shock_state;
+
+/* Members after computeEleSpectrumLimits; valid = 0 when checkParams()
+ * rejected the state (beta_shock < beta_min) and nothing was recomputed. */
+typedef struct pbag_limits {
+  double B, gamma_min, gamma_max, gamma_c, accel_frac, Theta, z_cool;
+  int32_t valid, reserved;
+} pbag_limits;
+
+#define PBAG_MIN_BINS 8
+#define PBAG_MAX_BINS 1024
+
+int pbag_abi_version(void);
+/* sizeof of the ABI structs, in the order grid_desc, shock_params, step_rec,
+ * outputs, status, limits_opts, shock_state, limits (0..7); for binding checks. */
+size_t pbag_sizeof(int which);
+const char* pbag_status_string(int code);
+
+/* Electron grid gam[ngam] and photon grid freq[nfreq + 1] of one grid
+ * description (host pointers). freq[nfreq] is the next logspace point: the
+ * value used where the reference reads one past the end of its frequency
+ * vector (numeric_model.h:269-272).
+ * Replaces: Electrons::allocate + build_grid_chang_cooper (base_state.h:184-253)
+ * and Photons::allocate (base_state.h:270-285). */
+int pbag_build_grids(const pbag_grid_desc* g, double* gam, double* freq);
+
+/* Per-step shock scalars for n consecutive calls on ONE blastwave object.
+ * state[7] carries the members that persist between calls (gamma_min,
+ * gamma_max, gamma_c, accel_frac, B, Theta, z_cool); initialise it to
+ * {-1, gamma_max_param, gamma_c_param (or -1), 1, -1, -1, -1} as setBasePars
+ * leaves them. gam is the electron grid (its first and last points cap
+ * gamma_min and gamma_max). Host pointers.
+ * Replaces: updateSockProperties + computeEleSpectrumLimits
+ * (microphysics_base.h:575-605, 642-652, 808-966). */
+int pbag_shock_limits(const pbag_limits_opts* o, const double* gam, int ngam, int n,
+                      const pbag_shock_state* in, double* state, pbag_limits* out);
+
+/* ---- the GPU step ---------------------------------------------------------- */
+
+typedef struct pbag_ctx pbag_ctx;  /* opaque device context */
+
+/* Create a device context for one grid (one CommonTables entry of the
+ * reference, microphysics/common.h:93-117) on CUDA device `device`. When
+ * ssc_tables != 0 the SSC kernel K[i][j][k] (kernels.h:49-117) and its
+ * integral are built on the host and uploaded once; blastwaves with ssc_on
+ * need it. Replaces: the CommonTables grids and kernels and
+ * ElectronAndRadiation::allocateForNumericSpectra (microphysics.h:282-345). */
+int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** out);
+void pbag_destroy(pbag_ctx* ctx);
+
+/* Evolve nbw blastwaves over their whole histories and fill the requested
+ * output histories. Blastwave b owns records off[b] .. off[b+1]-1 (off has
+ * nbw+1 entries, off[0] = 0, non-decreasing), one per burster-time index in
+ * order; its state starts as a freshly allocated ElectronAndRadiation. All
+ * pointers are HOST pointers; the call copies inputs to the device, runs, and
+ * copies outputs back before returning. On a physics error the rows computed
+ * before the failing step are still returned and st names the first failure
+ * in time order, the step at which the reference would have exited.
+ * Replaces, per blastwave and step: initializeElectronDistribution
+ * (microphysics.h:347), evaluateElectronDistributionNumericMixed (:359),
+ * computeRadiationNumericMixed (:492) and storeDenseOutput (:602). */
+int pbag_run_batch(pbag_ctx* ctx, const pbag_shock_params* prm, int nbw, const int64_t* off,
+                   const pbag_step_rec* recs, const pbag_outputs* out, pbag_status* st);
+
+/* Same as pbag_run_batch with prm, recs and every output pointer in DEVICE
+ * memory of the context's device (off stays a host array). Returns after the
+ * batch has finished on the device. */
+int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
+                          const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st,
+                          void* stream);
+
+/* Number of kernels the last run launched (diagnostics). */
+int64_t pbag_last_launch_count(const pbag_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBAG_H */

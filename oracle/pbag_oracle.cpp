@@ -1,0 +1,648 @@
+// pbag_oracle.cpp - FP64 CPU restatement of the reference's comoving-radiation
+// step. TEST INFRASTRUCTURE: the checker for the GPU path in tests/, smoke()
+// and the CPU-baseline leg of bench.py; never linked by the product.
+//
+// It follows, line by line, the reference sources cited beside each function
+// (paths relative to the reference's src/ directory). Floating-point operations
+// are written in the reference's order so that results agree to rounding.
+//
+// One intentional definition: the reference reads freqs[F] (one past the end)
+// in computeSSCSpectrum (microphysics/numeric_model.h:269-272); here that
+// value is the next point of the logspace grid, freq[F-1]*base.
+#include "pbag_oracle.h"
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// utilitites/utils.h:18-60 (CGS constants)
+constexpr double c_light = 2.99792458e10;
+constexpr double pi_ = 3.141592653589793;
+constexpr double m_p = 1.6726e-24;
+constexpr double m_e = 9.1094e-28;
+constexpr double q_e = 4.803204e-10;
+constexpr double sigma_T = 6.6524e-25;
+constexpr double h_pl = 6.6260755e-27;
+constexpr double mec2 = 8.187105649650028e-07;
+const double h_by_mec2 = h_pl / m_e / c_light / c_light;
+
+// --- synchrotron kernel functions (microphysics/kernels.h) -----------------
+
+inline double nu_crit(double B, double gam) {  // kernels.h:194-197
+  return (3. * q_e * B * gam * gam) / (4. * M_PI * m_e * c_light);
+}
+inline double nu_larmor(double B) {  // kernels.h:199-202
+  return (3. * q_e * B) / (2. * pi_ * m_e * c_light);
+}
+
+double cheb_eval(const double* coeff, int order, double a, double b, double x) {  // kernels.h:158-173
+  double d = 0.0, dd = 0.0;
+  double y = (2.0 * x - a - b) / (b - a);
+  double y2 = 2.0 * y;
+  for (int j = order; j > 0; j--) {
+    double temp = d;
+    d = y2 * d - dd + coeff[j];
+    dd = temp;
+  }
+  return y * d - dd + 0.5 * coeff[0];
+}
+
+// Chebyshev series of the synchrotron function F(x) used by synchGSL
+// (kernels.h:213-279): the published GSL "synchrotron_1" expansions.
+const double syn1_cs[13] = {30.364682982501076273, 17.079395277408394574, 4.560132133545072889,
+                            0.549281246730419979, 0.372976075069301172e-01, 0.161362430201041242e-02,
+                            0.481916772120371e-04, 0.10512425288938e-05, 0.174638504670e-07,
+                            0.22815486544e-09, 0.240443082e-11, 0.2086588e-13, 0.15167e-15};
+const double syn1a_cs[23] = {2.1329305161355000985, 0.741352864954200240e-01, 0.86968099909964198e-02,
+                             0.11703826248775692e-02, 0.1645105798619192e-03, 0.240201021420640e-04,
+                             0.35827756389389e-05, 0.5447747626984e-06, 0.838802856196e-07,
+                             0.13069882684e-07, 0.2053099071e-08, 0.325187537e-09, 0.517914041e-10,
+                             0.83002988e-11, 0.13352728e-11, 0.2159150e-12, 0.349967e-13,
+                             0.56994e-14, 0.9291e-15, 0.152e-15, 0.249e-16, 0.41e-17, 0.7e-18};
+const double syn2_cs[12] = {0.4490721623532660844, 0.898353677994187218e-01, 0.81044573772151290e-02,
+                            0.4261716991089162e-03, 0.147609631270746e-04, 0.3628633615300e-06,
+                            0.66634807498e-08, 0.949077166e-10, 0.1079125e-11, 0.10022e-13, 0.77e-16,
+                            0.5e-18};
+
+double synch_gsl(double B, double nu, double gam) {  // kernels.h:211-342
+  double ec = 1.5 * B / 4.14e13;
+  double en = nu * h_by_mec2;
+  double x = en / (ec * gam * gam);
+  const double c0 = M_PI / 1.7320508075688772;
+  const double c01 = 0.2257913526447274323630976;
+  const double cond1 = 2 * M_SQRT2 * 1.4901161193847656e-08;
+  const double cond3 = -8.0 * (-7.0839641853226408e02) / 7.0;
+  double result;
+  if (x < cond1) {
+    double z = std::pow(x, 1.0 / 3.0);
+    double cf = 1 - 8.43812762813205e-01 * z * z;
+    result = 2.14952824153447863671 * z * cf;
+  } else if (x <= 4.0) {
+    double px = std::pow(x, 1.0 / 3.0);
+    double px11 = std::pow(px, 11.);
+    double t = x * x / 8.0 - 1.0;
+    double r1 = cheb_eval(syn1_cs, 12, -1.0, 1.0, t);
+    double r2 = cheb_eval(syn2_cs, 11, -1.0, 1.0, t);
+    result = px * r1 - px11 * r2 - c0 * x;
+  } else if (x < cond3) {
+    double t = (12.0 - x) / (x + 4.0);
+    double r1 = cheb_eval(syn1a_cs, 22, -1.0, 1.0, t);
+    result = std::sqrt(x) * r1 * std::exp(c01 - x);
+  } else {
+    result = 0.0;
+  }
+  result *= std::sqrt(3.) * std::pow(q_e, 3.) * B / mec2;
+  return result;
+}
+
+double synch_bessel(double B, double nu, double gam) {  // kernels.h:396-412
+  double t = nu / nu_crit(B, gam);
+  double res;
+  try {
+    double k43 = std::cyl_bessel_k(4. / 3., t);
+    double k13 = std::cyl_bessel_k(1. / 3., t);
+    res = 2 * t * t * (k43 * k13 - 3. / 5 * t * (k43 * k43 - k13 * k13));
+  } catch (...) {
+    res = 0;
+  }
+  res *= std::sqrt(3.) * std::pow(q_e, 3.) * B / (m_e * c_light * c_light);
+  return res;
+}
+
+// Aharonian+2010 eq. D7 fit to the angle-averaged synchrotron function
+// (kernels.h:420-427, 463-469).
+inline double aharonian_R(double x) {
+  double t1n = 1.808 * std::pow(x, 1. / 3.);
+  double t1d = std::sqrt(1 + 3.4 * std::pow(x, 2. / 3.));
+  double t2n = 1. + 2.21 * std::pow(x, 2. / 3.) + 0.347 * std::pow(x, 4. / 3.);
+  double t2d = 1. + 1.353 * std::pow(x, 2. / 3.) + 0.217 * std::pow(x, 4. / 3.);
+  return t1n / t1d * t2n / t2d * std::exp(-x);
+}
+
+double cyc_synch(double B, double nu, double gam) {  // kernels.h:414-437 ("CSYN")
+  double em;
+  if (gam > 2.) {
+    double x = nu / nu_crit(B, gam);
+    em = aharonian_R(x);
+    em *= std::sqrt(3.) * std::pow(q_e, 3.) * B / mec2;
+  } else {
+    double x = nu / nu_larmor(B);
+    double psq = gam * gam - 1.;
+    em = (2. * psq) / (1. + 3. * psq) * std::exp((2. * (1. - x)) / (1. + 3. * psq));
+    em *= std::sqrt(3.) * std::pow(q_e, 3.) * B / mec2;
+  }
+  return em;
+}
+
+double synch_dermer(double B, double nu, double gam) {  // kernels.h:451-473
+  double x = nu / nu_crit(B, gam);
+  double res = aharonian_R(x);
+  res *= std::sqrt(3.) * std::pow(q_e, 3.) * B / (m_e * c_light * c_light);
+  return res;
+}
+
+// Blumenthal & Gould isotropic Compton kernel, Nava form (kernels.h:96-117).
+double ssc_nava(double nu, double gam, double nu_tilde) {
+  double en = nu * h_by_mec2;
+  double en_t = nu_tilde * h_by_mec2;
+  double K = 0.;
+  if (en_t / (4. * gam * gam) < en && en <= en_t)
+    K = (en / en_t) - (1. / (4. * gam * gam));
+  else if (en_t < en && en < (4. * gam * gam * en_t / (1. + 4. * gam * en_t))) {
+    double q = en / (4. * gam * en_t * (gam - en));
+    K = 2. * q * std::log(q) + (1. + 2. * q) * (1. - q) +
+        .5 * (1. - q) * std::pow(4. * gam * en_t * q, 2.) / (1. + 4. * gam * en_t * q);
+  } else
+    K = 0;
+  return K;
+}
+
+// microphysics/microphysics.h:11-58, METHOD_TAU::iAPPROX branch
+inline double intensity_approx(double em, double dtau) {
+  if (dtau == 0) return em;
+  double u = 1. / 2. + std::exp(-dtau) / dtau - (1 - std::exp(-dtau)) / (dtau * dtau);
+  return dtau > 1.e-3 ? em * (3. * u / dtau) : em;
+}
+
+typedef double (*syn_fn)(double, double, double);
+syn_fn pick_syn(int method) {
+  switch (method) {
+    case PBAG_SYN_DER09: return synch_dermer;
+    case PBAG_SYN_GSL: return synch_gsl;
+    case PBAG_SYN_BESSEL: return synch_bessel;
+    default: return cyc_synch;
+  }
+}
+
+// Shared read-only tables for one grid (the reference's CommonTables entry).
+struct Tables {
+  int G = 0, F = 0;
+  std::vector<double> e, half, dg, dgb, nu;  // gamma grid, half grid, delta_grid[G+1], delta_grid_bar[G], nu[F+1]
+  std::vector<double> K, Kint;               // SSC kernel [F][G][F], its integral [G][F]
+  bool has_ssc = false;
+};
+
+void build_tables(const pbag_grid_desc* g, bool ssc, Tables& t) {
+  int G = g->ngam, F = g->nfreq;
+  t.G = G;
+  t.F = F;
+  t.e.assign(G, 0.);
+  t.nu.assign(F + 1, 0.);
+  orc_build_grids(g, t.e.data(), t.nu.data());
+  // base_state.h:229-250
+  double step = std::exp(std::log(g->gam2) / (double)G);
+  double sp1 = step + 1.0;
+  t.half.assign(G - 1, 0.);
+  for (int i = 0; i < G - 1; ++i) t.half[i] = .5 * t.e[i] * sp1;
+  t.dg.assign(G + 1, 0.);
+  for (int i = 0; i < G - 1; ++i) t.dg[i + 1] = t.e[i + 1] - t.e[i];
+  t.dg[0] = t.e[0] * (1 - 1.0 / step);
+  t.dg[G] = t.e[G - 1] * (step - 1);
+  t.dgb.assign(G, 0.);
+  for (int i = 0; i < G; ++i) t.dgb[i] = (t.dg[i] + t.dg[i + 1]) / 2.;
+  if (ssc) {
+    t.K.assign((size_t)F * G * F, 0.);
+    t.Kint.assign((size_t)G * F, 0.);
+    orc_ssc_kernel(t.e.data(), G, t.nu.data(), F, t.K.data(), t.Kint.data());
+    t.has_ssc = true;
+  }
+}
+
+// Per-blastwave state and scratch (ElectronAndRadiation members).
+struct BW {
+  std::vector<double> f, dfde, tmp, gsyn, gadi, gssc, heat, src, a, b, c, d, cp, dp;
+  std::vector<double> ker, sj, sa, cj, n, tj, ta, ti, spe;
+  double dr_comov = 0, vol = 0, N = -1;
+  bool init = false, syn_seen = false;
+  void alloc(int G, int F) {
+    for (auto* v : {&f, &dfde, &tmp, &gsyn, &gadi, &gssc, &heat, &src, &a, &b, &c, &d, &cp, &dp, &spe})
+      v->assign(G, 0.);
+    ker.assign((size_t)F * G, 0.);
+    for (auto* v : {&sj, &sa, &cj, &n, &tj, &ta, &ti}) v->assign(F, 0.);
+  }
+};
+
+struct Err {
+  int code = PBAG_OK;
+};
+
+// microphysics.h:228-280 powerLawElectronDistributionAnalytic
+bool power_law(const Tables& T, double gm, double gc, double gM, double p, double n_inj, double* N) {
+  bool ok = true;
+  if (gm > gc) {
+    double Kf = n_inj / (std::pow(gm, 1. - p) * (1. / gc - 1. / gm) + 1. / p * (std::pow(gm, -p) - std::pow(gM, -p)));
+    for (int i = 0; i < T.G; i++) {
+      double g = T.e[i];
+      if ((gc <= g) && (g < gm))
+        N[i] = Kf * std::pow(gm, 1. - p) * std::pow(g, -2.);
+      else if ((gm < g) && (g <= gM))
+        N[i] = Kf * std::pow(g, -p - 1.);
+      if (!std::isfinite(N[i]) || N[i] < 0.) ok = false;
+    }
+  } else {
+    double Ks = n_inj / ((1. / (1. - p)) * (std::pow(gc, 1. - p) - std::pow(gm, 1. - p)) -
+                         gc / p * (std::pow(gM, -p) - std::pow(gc, -p)));
+    for (int i = 0; i < T.G; ++i) {
+      double g = T.e[i];
+      if ((gm <= g) && (g < gc))
+        N[i] = Ks * std::pow(g, -p);
+      else if ((gc <= g) && (g <= gM))
+        N[i] = Ks * gc * std::pow(g, -p - 1.);
+      if (!std::isfinite(N[i]) || N[i] < 0.) ok = false;
+    }
+  }
+  return ok;
+}
+
+// numeric_model.h:753-801 setHeatCoolTerms (dispersion_term = 0)
+bool heat_cool(const Tables& T, BW& w, double B, double dlnVdt, bool ssc, int inner) {
+  const int G = T.G, F = T.F;
+  bool ok = true;
+  const double const_syn = sigma_T / (6. * M_PI * m_e * c_light);
+  const double const_ssc = 3. / 4. * h_pl * sigma_T / m_e / c_light;
+  (void)inner;
+#pragma omp parallel for num_threads(inner) if (inner > 1) reduction(&& : ok)
+  for (int i = 0; i < G - 1; i++) {
+    double gam = T.half[i];
+    w.gsyn[i] = const_syn * B * B * gam * gam;
+    w.gadi[i] = dlnVdt * (gam * gam - 1.) / (3. * gam);
+    if (ssc) {
+      double res = 0;
+      for (int j = 0; j < F - 1; j++)
+        res += w.n[j] / T.nu[j] * (T.nu[j + 1] - T.nu[j]) * T.Kint[(size_t)i * F + j];
+      w.gssc[i] = const_ssc * res / gam / gam;
+    }
+    w.heat[i] = w.gsyn[i] + w.gadi[i] + w.gssc[i];
+    if (!std::isfinite(w.heat[i])) ok = false;
+  }
+  w.heat[G - 1] = 0.;
+  return ok;
+}
+
+// numeric_model.h:539-675 setupVectors with dispersion = delta_j = escape = 0
+void setup_vectors(const Tables& T, BW& w, double dt) {
+  const int G = T.G;
+  for (int k = 0; k < G; ++k) w.a[k] = w.b[k] = w.c[k] = 0.;
+  for (int k = G - 2; k > 0; k--) {
+    double odgb = 1.0 / T.dgb[k];
+    double Bf = w.heat[k], Bb = w.heat[k - 1];
+    w.a[k] = odgb * (0. - 0. * Bb);              // compute_n_j_minus_one_term, C=0, delta=0
+    w.b[k] = -odgb * ((0. + 0.) + 1. * Bb - 0. * Bf);  // compute_n_j
+    w.c[k] = odgb * (1. * Bf + 0.);               // compute_n_j_plus_one
+  }
+  {  // right boundary
+    double odgb = 1.0 / T.dgb[G - 1];
+    double Hl = w.heat[G - 1];
+    w.a[G - 1] = odgb * (0. - 0. * Hl);
+    w.b[G - 1] = -odgb * ((0. + 0.) + 1. * Hl - 0.);
+    w.c[G - 1] = 0.;
+  }
+  {  // left boundary
+    double odgb = 1.0 / T.dgb[0];
+    w.a[0] = 0.0;
+    w.b[0] = -odgb * ((0. + 0.) + 0. * 0. - 0. * w.heat[0]);
+    w.c[0] = odgb * (1. * w.heat[0] + 0.);
+  }
+  for (int i = 0; i < G; i++) {
+    w.a[i] *= -dt;
+    w.b[i] = (1. - w.b[i] * dt) + 0. * dt;
+    w.c[i] *= -dt;
+  }
+}
+
+// numeric_model.h:682-708 solve -> tridiagonal_solver (:19-43)
+bool solve(const Tables& T, BW& w, double dt) {
+  const int G = T.G;
+  bool ok = true;
+  for (int i = 0; i < G; i++) {
+    w.d[i] = w.f[i] + w.src[i] * dt;
+    if (!std::isfinite(w.f[i]) || w.f[i] < 0.) ok = false;
+  }
+  for (int i = 0; i < G; i++) {
+    w.cp[i] = w.c[i] / w.b[i];
+    w.dp[i] = w.d[i] / w.b[i];
+  }
+  double sum = 0;
+  for (int i = 0; i < G; i++) sum += w.a[i];
+  if (sum > 0)
+    for (int i = 1; i < G; i++) {
+      double bm = w.b[i] - w.a[i] * w.cp[i - 1];
+      w.cp[i] = w.c[i] / bm;
+      w.dp[i] = (w.d[i] - w.a[i] * w.dp[i - 1]) / bm;
+    }
+  w.f[G - 1] = w.dp[G - 1];
+  for (int j = G - 2; j > -1; j--) w.f[j] = w.dp[j] - w.cp[j] * w.f[j + 1];
+  return ok;
+}
+
+// microphysics.h:359-489 evaluateElectronDistributionNumericMixed
+int evolve(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_rec& r, int flags,
+           int inner) {
+  const int G = T.G;
+  if ((r.B <= 0) || (r.gamma_min < 1.) || (r.gamma_max <= 1.) || (r.gamma_min >= r.gamma_max) ||
+      (r.accel_frac > 1.))
+    return PBAG_ERR_PARAM;
+  w.dr_comov = r.dr;
+  double N_tot = r.m_p1 / m_p;
+  std::fill(w.tmp.begin(), w.tmp.end(), 0.);
+  if (!power_law(T, r.gamma_min, r.gamma_c, r.gamma_max, P.p, N_tot, w.tmp.data())) return PBAG_ERR_NONFINITE;
+  double dt = r.tc_p1 - r.tc;
+  double volume = r.m / r.rho;
+  double volume_p1 = r.m_p1 / r.rho_p1;
+  double dlnVdt = P.adi_on ? 1. / dt * (1. - volume / volume_p1) : 0.;
+  if ((!std::isfinite(dlnVdt)) || (dlnVdt < 0)) return PBAG_ERR_DLNVDT;
+  // substeps (microphysics.h:412-435)
+  double dlog_gam = (T.e[1] - T.e[0]) / T.e[0];
+  double dts = sigma_T * r.gamma_max * r.B * r.B / (6. * M_PI * m_e * c_light);
+  double dta = (r.gamma_max * r.gamma_max - 1.) / (3. * r.gamma_max * r.gamma_max) * dlnVdt;
+  double delta_t = dlog_gam / (dts + dta);
+  size_t n_sub;
+  const size_t max_sub = (size_t)P.max_substeps;
+  if (delta_t >= dt / 1.) {
+    delta_t = dt / 1.;
+    n_sub = 1;
+  } else if (delta_t < dt / (double)max_sub) {
+    delta_t = dt / (double)max_sub;
+    n_sub = max_sub;
+  } else
+    n_sub = (size_t)(dt / delta_t);
+  w.vol = volume;
+  if (P.ele_method == PBAG_ELE_MIX || r.gamma_min <= 2) {
+    for (int i = 0; i < G; i++) w.f[i] = w.tmp[i];
+    return PBAG_OK;
+  }
+  w.N = (r.m_p1 - r.m) / m_p / dt;
+  // setSourceFunction (numeric_model.h:717-724)
+  double index = -P.p;
+  double norm = (1 + index) / (std::pow(r.gamma_max, index + 1) - std::pow(r.gamma_min, index + 1));
+  for (int i = 0; i < G; i++)
+    w.src[i] = ((T.e[i] > r.gamma_min) && (T.e[i] <= r.gamma_max)) ? w.N * norm * std::pow(T.e[i], index) : 0.;
+  const bool ssc = P.ssc_on && T.has_ssc;
+  if (flags & ORC_HOIST_HEATING) {
+    if (!heat_cool(T, w, r.B, dlnVdt, ssc, inner)) return PBAG_ERR_NONFINITE;
+    setup_vectors(T, w, delta_t);
+  }
+  for (size_t s = 0; s < n_sub; s++) {
+    if (!(flags & ORC_HOIST_HEATING)) {
+      if (!heat_cool(T, w, r.B, dlnVdt, ssc, inner)) return PBAG_ERR_NONFINITE;
+      setup_vectors(T, w, delta_t);
+    }
+    if (!solve(T, w, delta_t)) return PBAG_ERR_NONFINITE;
+  }
+  return PBAG_OK;
+}
+
+// base_state.h:482-536 dfdx (acc=1), stateful: only entries with f>0 are written
+void dfdx(const double* x, const double* f, double* df, int n) {
+  for (int i = 1; i < n - 1; i++)
+    if (f[i] > 0) {
+      double dx = x[i] - x[i - 1];
+      df[i] = 0.5 * (f[i + 1] - f[i - 1]) / dx;
+    }
+  if (f[0] > 0) df[0] = -1.5 * f[0] + 2. * f[1] - 0.5 * f[2];
+  int i = n - 1;
+  if (f[i] > 0) df[i] = 1.5 * f[i] - 2. * f[i - 1] + 0.5 * f[i - 2];
+}
+
+// microphysics.h:492-633 computeRadiationNumericMixed (+ storeDenseOutput)
+int radiate(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_rec& r, size_t row,
+            pbag_outputs* out, int inner) {
+  const int G = T.G, F = T.F;
+  const double B = r.B;
+  if (B < 0) return PBAG_ERR_PARAM;
+  syn_fn fn = pick_syn(P.syn_method);
+  // kernels.h:528-538 evalSynKernel
+  for (int k = 0; k < F; k++)
+    for (int j = 0; j < G; j++) w.ker[(size_t)k * G + j] = fn(B, T.nu[k], T.e[j]);
+  // numeric_model.h:148-184 computeSynSpectrum
+  std::fill(w.sj.begin(), w.sj.end(), 0.);
+  bool ok = true;
+#pragma omp parallel for num_threads(inner) if (inner > 1) reduction(&& : ok)
+  for (int i = 0; i < F - 1; i++) {
+    double res = 0.;
+    for (int j = 0; j < G - 1; j++) res += w.ker[(size_t)i * G + j] * w.f[j] * (T.e[j + 1] - T.e[j]);
+    w.sj[i] = res;
+    if (!std::isfinite(res) || res < 0.) ok = false;
+  }
+  if (!ok) return PBAG_ERR_NONFINITE;
+  // numeric_model.h:191-238 computeSSA
+  if (P.ssa_on) {
+    for (int i = 0; i < G; i++) w.tmp[i] = w.f[i] / T.e[i] / T.e[i];
+    dfdx(T.e.data(), w.tmp.data(), w.dfde.data(), G);
+    std::fill(w.sa.begin(), w.sa.end(), 0.);
+#pragma omp parallel for num_threads(inner) if (inner > 1)
+    for (int i = 0; i < F; i++) {
+      for (int j = 0; j < G - 1; j++)
+        w.sa[i] += T.e[j] * T.e[j] * (T.e[j + 1] - T.e[j]) * w.dfde[j] * w.ker[(size_t)i * G + j];
+      w.sa[i] *= -1. / (8. * M_PI * m_e * T.nu[i] * T.nu[i]);
+      w.sa[i] = std::abs(w.sa[i]);
+      if (!std::isfinite(w.sa[i])) w.sa[i] = 1e99;
+    }
+  }
+  // numeric_model.h:247-285 computeSSCSpectrum (photon field of the previous step)
+  const bool ssc = P.ssc_on && T.has_ssc;
+  if (ssc) {
+    std::fill(w.cj.begin(), w.cj.end(), 0.);
+#pragma omp parallel for num_threads(inner) if (inner > 1)
+    for (int i = 0; i < F; i++) {
+      std::vector<double> spe(G - 1, 0.);
+      const double* Ki = T.K.data() + (size_t)i * G * F;
+      for (int j = 0; j < G - 1; j++)
+        for (int k = 0; k < F; k++)
+          spe[j] += 3. / 4. * sigma_T * c_light / (T.e[j] * T.e[j]) * w.n[k] / T.nu[k] * (T.nu[k + 1] - T.nu[k]) *
+                    Ki[(size_t)j * F + k];
+      double acc = 0.;
+      for (int j = 0; j < G - 1; j++) acc += w.f[j] * h_pl * T.nu[i] * spe[j] * (T.e[j + 1] - T.e[j]);
+      w.cj[i] = acc;
+    }
+  }
+  // new photon density (microphysics.h:516-523)
+  const bool num = P.ele_method == PBAG_ELE_NUMERIC;
+  double Tesc = w.dr_comov / c_light;
+  double fac = Tesc / w.vol;
+  for (int i = 0; i < F; i++) w.n[i] = w.sj[i] * fac / (h_pl * T.nu[i]);
+  if (num && ssc)
+    for (int i = 0; i < F; i++) w.n[i] += w.cj[i] * fac / (h_pl * T.nu[i]);
+  for (int i = 0; i < F; i++) w.tj[i] = w.sj[i];
+  if (num && ssc)
+    for (int i = 0; i < F; i++) w.tj[i] += w.cj[i];
+  for (int i = 0; i < F; i++) w.ta[i] = w.sa[i];
+  // total number of electrons (microphysics.h:556-563)
+  double n_ele = 0.;
+  for (int i = 0; i < G - 1; i++) n_ele += w.f[i] * (T.e[i + 1] - T.e[i]);
+  if (n_ele <= 0) return PBAG_ERR_NELE;
+  // normalisation (microphysics.h:577-586)
+  const double acc = r.accel_frac, np = r.n_prime;
+  for (int i = 0; i < F; i++) {
+    w.ta[i] = w.ta[i] / n_ele * acc * np;
+    double dtau = w.ta[i] * w.dr_comov;
+    w.ti[i] = intensity_approx(w.tj[i] * acc, dtau);
+    w.tj[i] = w.tj[i] * acc / n_ele;
+    if (!std::isfinite(w.tj[i]) || w.tj[i] < 0.) return PBAG_ERR_NONFINITE;
+  }
+  auto put = [&](double* dst, const std::vector<double>& v, int n) {
+    if (dst) std::memcpy(dst + row * n, v.data(), sizeof(double) * n);
+  };
+  put(out->j_all, w.tj, F);
+  put(out->a_all, w.ta, F);
+  put(out->f_all, w.n, F);
+  put(out->i_all, w.ti, F);
+  // storeDenseOutput (microphysics.h:602-633)
+  if (out->syn_j_all || out->syn_a_all || out->syn_i_all) {
+    std::vector<double> j(F), a(F), in(F);
+    for (int i = 0; i < F; i++) {
+      j[i] = w.sj[i] * acc;
+      a[i] = w.sa[i] / n_ele * acc * np;
+      in[i] = intensity_approx(j[i], a[i] * w.dr_comov);
+    }
+    put(out->syn_j_all, j, F);
+    put(out->syn_a_all, a, F);
+    put(out->syn_i_all, in, F);
+  }
+  if (ssc && (out->ssc_j_all || out->ssc_i_all)) {
+    std::vector<double> j(F);
+    for (int i = 0; i < F; i++) j[i] = w.cj[i] * acc;
+    put(out->ssc_j_all, j, F);
+    put(out->ssc_i_all, j, F);  // ssc.a == 0 without pair production, so I = j
+  }
+  put(out->ele_f_all, w.f, G);
+  put(out->gdot_syn_all, w.gsyn, G);
+  put(out->gdot_adi_all, w.gadi, G);
+  put(out->gdot_ssc_all, w.gssc, G);
+  if (out->syn_j_all) {  // microphysics.h:627-631: exit if the syn history sums to 0 after step 0
+    for (int i = 0; i < F; i++)
+      if (w.sj[i] != 0.) w.syn_seen = true;
+    if (!w.syn_seen && row > 0) return PBAG_ERR_NONFINITE;
+  }
+  return PBAG_OK;
+}
+
+// microphysics.h:347-357 initializeElectronDistribution
+int initialize(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_rec& r) {
+  w.dr_comov = r.dr;
+  w.vol = r.m_p1 / r.rho_p1;
+  if (!power_law(T, r.gamma_min, r.gamma_c, r.gamma_max, P.p, r.m_p1 / m_p, w.f.data())) return PBAG_ERR_NONFINITE;
+  w.init = true;
+  for (int i = 0; i < T.G - 1; i++) w.f[i] *= r.accel_frac;
+  return PBAG_OK;
+}
+
+int run_one(const Tables& T, const pbag_shock_params& P, const pbag_step_rec* recs, size_t nr, pbag_outputs* o,
+            int flags, int inner, int* fail_step) {
+  BW w;
+  w.alloc(T.G, T.F);
+  for (size_t it = 0; it < nr; ++it) {
+    const pbag_step_rec& r = recs[it];
+    if (r.mode == PBAG_SKIP) continue;
+    int rc;
+    // blastwave_radiation.h:1160-1175: the first valid step initialises
+    if (!w.init)
+      rc = initialize(T, P, w, r);
+    else
+      rc = evolve(T, P, w, r, flags, inner);
+    if (rc == PBAG_OK) rc = radiate(T, P, w, r, it, o, inner);
+    if (rc != PBAG_OK) {
+      *fail_step = (int)it;
+      return rc;
+    }
+  }
+  return PBAG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_build_grids(const pbag_grid_desc* g, double* gam, double* freq) {
+  const int G = g->ngam, F = g->nfreq;
+  // base_state.h:229-236: e[i] = step^i, step = exp(ln(gam2)/G)
+  double step = std::exp(std::log(g->gam2) / (double)G);
+  for (int i = 0; i < G; i++) gam[i] = std::pow(step, (double)i);
+  // utils.h MakeLogspaceVec: first = 10^start, base = 10^((stop-start)/num), x *= base
+  double start = std::log10(g->freq1), stop = std::log10(g->freq2);
+  double cur = std::pow(10., start);
+  double base = std::pow(10., (stop - start) / F);
+  for (int i = 0; i <= F; i++) {
+    freq[i] = cur;
+    cur *= base;
+  }
+  return PBAG_OK;
+}
+
+double orc_syn_func(int method, double B, double nu, double gam) { return pick_syn(method)(B, nu, gam); }
+
+double orc_ssc_func(double nu, double gam, double nu_tilde) { return ssc_nava(nu, gam, nu_tilde); }
+
+int orc_ssc_kernel(const double* gam, int G, const double* freq, int F, double* K, double* Kint) {
+  std::vector<double> tmp;
+  double* KK = K;
+  if (!KK) {
+    tmp.assign((size_t)F * G * F, 0.);
+    KK = tmp.data();
+  }
+  for (int i = 0; i < F; i++)
+    for (int j = 0; j < G; j++)
+      for (int k = 0; k < F; k++) KK[((size_t)i * G + j) * F + k] = ssc_nava(freq[i], gam[j], freq[k]);
+  for (int j = 0; j < G; j++)
+    for (int k = 0; k < F; k++) {
+      double res = 0;
+      for (int i = 0; i < F - 1; i++)
+        res += KK[((size_t)i * G + j) * F + k] * freq[i + 1] * (freq[i + 1] - freq[i]);
+      Kint[(size_t)j * F + k] = res;
+    }
+  return PBAG_OK;
+}
+
+int orc_run(const pbag_grid_desc* g, const pbag_shock_params* prm, int nbw, const int64_t* offsets,
+            const pbag_step_rec* recs, pbag_outputs* out, int flags, int outer_threads, int inner_threads,
+            pbag_status* st) {
+  if (!g || !prm || !offsets || !recs || !out || nbw < 0 || g->ngam < 8 || g->nfreq < 8) return PBAG_ERR_ARG;
+  bool any_ssc = false;
+  for (int b = 0; b < nbw; ++b) any_ssc = any_ssc || prm[b].ssc_on;
+  Tables T;
+  build_tables(g, any_ssc, T);
+  // zero all output rows (skipped steps keep zero rows, like the reference's vectors)
+  const size_t nrec = (size_t)offsets[nbw];
+  for (size_t fi = 0; fi < 13; ++fi) {
+    double* p = ((double**)out)[fi];
+    size_t n = fi >= 4 && fi < 8 ? (size_t)T.G : (size_t)T.F;
+    if (p) std::memset(p, 0, sizeof(double) * nrec * n);
+  }
+  int inner = (flags & ORC_INNER_OMP) ? inner_threads : 1;
+  std::vector<int> codes(nbw, PBAG_OK), steps(nbw, -1);
+  (void)outer_threads;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(outer_threads) if (outer_threads > 1)
+  for (int b = 0; b < nbw; ++b) {
+    size_t r0 = (size_t)offsets[b], nr = (size_t)(offsets[b + 1] - offsets[b]);
+    pbag_outputs o = *out;
+    for (size_t fi = 0; fi < 13; ++fi) {
+      double** p = ((double**)&o) + fi;
+      size_t n = fi >= 4 && fi < 8 ? (size_t)T.G : (size_t)T.F;
+      if (*p) *p += r0 * n;
+    }
+    codes[b] = run_one(T, prm[b], recs + r0, nr, &o, flags, inner, &steps[b]);
+  }
+  for (int b = 0; b < nbw; ++b)
+    if (codes[b] != PBAG_OK) {
+      if (st) {
+        st->code = codes[b];
+        st->bw = b;
+        st->step = steps[b];
+      }
+      return codes[b];
+    }
+  if (st) {
+    st->code = PBAG_OK;
+    st->bw = -1;
+    st->step = -1;
+  }
+  return PBAG_OK;
+}
+
+}  // extern "C"

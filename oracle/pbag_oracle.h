@@ -1,0 +1,51 @@
+/*
+ * pbag_oracle.h - CPU restatement (FP64) of the reference's comoving-radiation
+ * step, used ONLY as the checker in tests, in smoke() and as the CPU-baseline
+ * leg of bench.py. The product path never links or calls it.
+ *
+ * Every function follows the reference source cited beside it
+ * (paths relative to the reference project's src/ directory).
+ */
+#ifndef PBAG_ORACLE_H
+#define PBAG_ORACLE_H
+
+#include "pbag.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* grids: gam[G] (base_state.h:217-253), freq[F+1] (utils.h MakeLogspaceVec;
+ * freq[F] is the next logspace point, the value the oracle defines for the
+ * one-past-the-end read in numeric_model.h:269-272). */
+int orc_build_grids(const pbag_grid_desc* g, double* gam, double* freq);
+
+/* single synchrotron kernel value K(nu; gamma, B) (kernels.h:211-522) */
+double orc_syn_func(int method, double B, double nu, double gam);
+/* single SSC kernel value (kernels.h:96-117) */
+double orc_ssc_func(double nu, double gam, double nu_tilde);
+
+/* SSC kernel tensor K[i][j][k] (may be NULL) and Kint[j][k] (kernels.h:49-94) */
+int orc_ssc_kernel(const double* gam, int G, const double* freq, int F, double* K, double* Kint);
+
+/* Flags for orc_run. */
+enum {
+  ORC_HOIST_HEATING = 1,  /* compute the (substep-invariant) cooling terms once per
+                             step instead of once per substep as the reference does;
+                             results are bitwise identical, only faster            */
+  ORC_INNER_OMP = 2       /* parallelise the inner nu loops with inner_threads, like
+                             the reference's num_threads(4) pragmas                 */
+};
+
+/* Full histories of nbw blastwaves (see pbag.h for the record and output
+ * layouts). outer_threads > 1 runs blastwaves concurrently (one per thread,
+ * private state). Returns PBAG_OK or the first error; st (may be NULL)
+ * receives the failing blastwave/step. */
+int orc_run(const pbag_grid_desc* g, const pbag_shock_params* prm, int nbw, const int64_t* offsets,
+            const pbag_step_rec* recs, pbag_outputs* out, int flags, int outer_threads,
+            int inner_threads, pbag_status* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

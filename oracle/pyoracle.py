@@ -1,0 +1,166 @@
+"""ctypes wrappers for the oracle libraries (test infrastructure only).
+
+* ``Oracle`` wraps oracle/_build/libpbag_oracle.so, the FP64 restatement of
+  the reference's comoving-radiation step (built on any machine by
+  ``make -C oracle port``).
+* ``Reference`` wraps oracle/_ref/libpbaref.so, the reference's own
+  src/microphysics headers compiled in place (``make -C oracle ref``; only
+  where the reference sources exist).
+
+Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from pyblastafterglowmag_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libpbag_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libpbaref.so")
+REF_SRC = "/root/reference/src"
+
+ORC_HOIST_HEATING = 1
+ORC_INNER_OMP = 2
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def build_reference():
+    """Build oracle/_ref/libpbaref.so when the reference sources are present."""
+    if not os.path.isdir(os.path.join(REF_SRC, "microphysics")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={REF_SRC}"], check=True)
+    return True
+
+
+def _alloc_outputs(grid, nrec, outputs):
+    arrays = {}
+    for f in outputs:
+        n = grid.ngam if f in abi.OUTPUT_ON_GAMMA else grid.nfreq
+        arrays[f] = np.zeros((nrec, n))
+    return arrays
+
+
+class Oracle:
+    def __init__(self, path=ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle()
+        lib = C.CDLL(path)
+        P = C.POINTER
+        lib.orc_build_grids.argtypes = [P(abi.GridDesc), P(C.c_double), P(C.c_double)]
+        lib.orc_syn_func.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
+        lib.orc_syn_func.restype = C.c_double
+        lib.orc_ssc_func.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.orc_ssc_func.restype = C.c_double
+        lib.orc_ssc_kernel.argtypes = [P(C.c_double), C.c_int, P(C.c_double), C.c_int,
+                                       P(C.c_double), P(C.c_double)]
+        lib.orc_run.argtypes = [P(abi.GridDesc), C.c_void_p, C.c_int, P(C.c_int64), C.c_void_p,
+                                P(abi.Outputs), C.c_int, C.c_int, C.c_int, P(abi.Status)]
+        self.lib = lib
+
+    def grids(self, grid):
+        gam = np.zeros(grid.ngam)
+        freq = np.zeros(grid.nfreq + 1)
+        self.lib.orc_build_grids(C.byref(grid), abi.dptr(gam), abi.dptr(freq))
+        return gam, freq
+
+    def syn_kernel(self, method, B, gam, freq):
+        out = np.zeros((len(freq), len(gam)))
+        for k, nu in enumerate(freq):
+            for j, g in enumerate(gam):
+                out[k, j] = self.lib.orc_syn_func(method, B, nu, g)
+        return out
+
+    def ssc_kernel(self, gam, freq_ext, full=True):
+        """K[F][G][F] (or None) and Kint[G][F]; freq_ext has F+1 points."""
+        G, F = len(gam), len(freq_ext) - 1
+        K = np.zeros((F, G, F)) if full else None
+        Kint = np.zeros((G, F))
+        self.lib.orc_ssc_kernel(abi.dptr(np.ascontiguousarray(gam)), G,
+                                abi.dptr(np.ascontiguousarray(freq_ext)), F,
+                                abi.dptr(K) if full else None, abi.dptr(Kint))
+        return K, Kint
+
+    def run(self, grid, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all"),
+            flags=ORC_HOIST_HEATING, outer_threads=1, inner_threads=1):
+        recs = np.ascontiguousarray(recs, dtype=abi.STEP_DTYPE)
+        params = np.ascontiguousarray(params, dtype=abi.SHOCK_PARAMS_DTYPE)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        arrays = _alloc_outputs(grid, int(offsets[-1]), outputs)
+        out = abi.make_outputs(arrays)
+        st = abi.Status()
+        rc = self.lib.orc_run(C.byref(grid), params.ctypes.data, len(params),
+                              offsets.ctypes.data_as(C.POINTER(C.c_int64)), recs.ctypes.data,
+                              C.byref(out), flags, outer_threads, inner_threads, C.byref(st))
+        return rc, (st.bw, st.step), arrays
+
+
+class Reference:
+    def __init__(self, path=REF_SO):
+        if not os.path.exists(path) and not build_reference():
+            raise FileNotFoundError("reference sources not available")
+        lib = C.CDLL(path)
+        P = C.POINTER
+        lib.ref_grids.argtypes = [P(abi.GridDesc), P(C.c_double), P(C.c_double), P(C.c_double)]
+        lib.ref_syn_kernel.argtypes = [C.c_int, C.c_double, P(C.c_double), C.c_int, P(C.c_double),
+                                       C.c_int, P(C.c_double)]
+        lib.ref_ssc_kernel.argtypes = [P(C.c_double), C.c_int, P(C.c_double), C.c_int, P(C.c_double),
+                                       P(C.c_double)]
+        lib.ref_ele_limits.argtypes = [P(abi.GridDesc)] + [C.c_double] * 4 + [C.c_int] * 5 + \
+            [C.c_double, C.c_double, C.c_int, P(C.c_double), P(C.c_double)]
+        lib.ref_run.argtypes = [P(abi.GridDesc), C.c_void_p, C.c_int, P(C.c_int64), C.c_void_p,
+                                P(abi.Outputs)]
+        self.lib = lib
+
+    def grids(self, grid):
+        gam = np.zeros(grid.ngam)
+        freq = np.zeros(grid.nfreq)
+        extra = C.c_double()
+        self.lib.ref_grids(C.byref(grid), abi.dptr(gam), abi.dptr(freq), C.byref(extra))
+        return gam, np.concatenate([freq, [extra.value]])
+
+    def syn_kernel(self, method, B, gam, freq):
+        gam = np.ascontiguousarray(gam)
+        freq = np.ascontiguousarray(freq)
+        out = np.zeros((len(freq), len(gam)))
+        self.lib.ref_syn_kernel(method, B, abi.dptr(gam), len(gam), abi.dptr(freq), len(freq),
+                                abi.dptr(out))
+        return out
+
+    def ssc_kernel(self, gam, freq, full=True):
+        gam = np.ascontiguousarray(gam)
+        freq = np.ascontiguousarray(freq)
+        G, F = len(gam), len(freq)
+        K = np.zeros((F, G, F)) if full else None
+        Kint = np.zeros((G, F))
+        self.lib.ref_ssc_kernel(abi.dptr(gam), G, abi.dptr(freq), F,
+                                abi.dptr(K) if full else None, abi.dptr(Kint))
+        return K, Kint
+
+    def ele_limits(self, grid, opts, states, gamma_max_const=1e7, gamma_c_const=1e5):
+        """ref_ele_limits with a LimitsOpts; returns [n][8] (B, gm, gM, gc,
+        accel, Theta, z_cool, valid)."""
+        states = np.ascontiguousarray(states, dtype=abi.SHOCK_STATE_DTYPE)
+        inp = states.view(np.float64).reshape(len(states), 8).copy()
+        out = np.zeros((len(states), 8))
+        self.lib.ref_ele_limits(C.byref(grid), opts.p, opts.eps_e, opts.eps_b, opts.eps_t,
+                                opts.method_gamma_min, opts.method_gamma_c, opts.method_gamma_max,
+                                opts.method_B, opts.method_nonrel, gamma_max_const, gamma_c_const,
+                                len(states), abi.dptr(inp), abi.dptr(out))
+        return out
+
+    def run(self, grid, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all")):
+        recs = np.ascontiguousarray(recs, dtype=abi.STEP_DTYPE)
+        params = np.ascontiguousarray(params, dtype=abi.SHOCK_PARAMS_DTYPE)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        arrays = _alloc_outputs(grid, int(offsets[-1]), outputs)
+        out = abi.make_outputs(arrays)
+        self.lib.ref_run(C.byref(grid), params.ctypes.data, len(params),
+                         offsets.ctypes.data_as(C.POINTER(C.c_int64)), recs.ctypes.data,
+                         C.byref(out))
+        return arrays

@@ -1,0 +1,145 @@
+"""Loader for the in-tree libpbag.so (the C-ABI library of include/pbag.h).
+
+The library is built in place by pyblastafterglowmag_gb300.build (called by
+__graft_entry__.build()). There is no fallback: if the shared object is
+missing, every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpbag.so")
+
+_lib = None
+
+
+class PbagError(RuntimeError):
+    def __init__(self, code, what, bw=-1, step=-1):
+        self.code, self.bw, self.step = code, bw, step
+        name = abi.STATUS_NAMES.get(code, str(code))
+        where = f" (blastwave {bw}, step {step})" if bw >= 0 else ""
+        super().__init__(f"{what}: {name} [{code}]{where}")
+
+
+def _check(rc, what, st=None):
+    if rc != abi.PBAG_OK:
+        if st is not None:
+            raise PbagError(rc, what, st.bw, st.step)
+        raise PbagError(rc, what)
+
+
+def load():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    lib.pbag_abi_version.restype = C.c_int
+    lib.pbag_sizeof.argtypes = [C.c_int]
+    lib.pbag_sizeof.restype = C.c_size_t
+    lib.pbag_status_string.argtypes = [C.c_int]
+    lib.pbag_status_string.restype = C.c_char_p
+    lib.pbag_build_grids.argtypes = [P(abi.GridDesc), P(C.c_double), P(C.c_double)]
+    lib.pbag_shock_limits.argtypes = [P(abi.LimitsOpts), P(C.c_double), C.c_int, C.c_int,
+                                      C.c_void_p, P(C.c_double), C.c_void_p]
+    lib.pbag_create.argtypes = [P(abi.GridDesc), C.c_int, C.c_int, P(C.c_void_p)]
+    lib.pbag_destroy.argtypes = [C.c_void_p]
+    lib.pbag_run_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, P(C.c_int64), C.c_void_p,
+                                   P(abi.Outputs), P(abi.Status)]
+    lib.pbag_run_batch_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, P(C.c_int64),
+                                          C.c_void_p, P(abi.Outputs), P(abi.Status), C.c_void_p]
+    lib.pbag_last_launch_count.argtypes = [C.c_void_p]
+    lib.pbag_last_launch_count.restype = C.c_int64
+    if lib.pbag_abi_version() != 1:
+        raise RuntimeError("libpbag ABI version mismatch")
+    sizes = [C.sizeof(abi.GridDesc), C.sizeof(abi.ShockParams), C.sizeof(abi.StepRec),
+             C.sizeof(abi.Outputs), C.sizeof(abi.Status), C.sizeof(abi.LimitsOpts),
+             abi.SHOCK_STATE_DTYPE.itemsize, abi.LIMITS_DTYPE.itemsize]
+    for i, s in enumerate(sizes):
+        if lib.pbag_sizeof(i) != s:
+            raise RuntimeError(f"libpbag struct {i} size {lib.pbag_sizeof(i)} != binding {s}")
+    _lib = lib
+    return lib
+
+
+def grids(grid):
+    """(gam[G], freq[F+1]) for a GridDesc."""
+    lib = load()
+    gam = np.zeros(grid.ngam)
+    freq = np.zeros(grid.nfreq + 1)
+    _check(lib.pbag_build_grids(C.byref(grid), abi.dptr(gam), abi.dptr(freq)), "pbag_build_grids")
+    return gam, freq
+
+
+def shock_limits(opts, gam, states, state=None):
+    """pbag_shock_limits over a sequence of shock states of one blastwave.
+
+    states: SHOCK_STATE_DTYPE array; returns a LIMITS_DTYPE array. state (7
+    floats, modified in place) carries the persistent members; by default it
+    starts as setBasePars leaves them."""
+    lib = load()
+    states = np.ascontiguousarray(states, dtype=abi.SHOCK_STATE_DTYPE)
+    out = np.zeros(len(states), dtype=abi.LIMITS_DTYPE)
+    if state is None:
+        state = np.array([-1.0, 1e7, -1.0, 1.0, -1.0, -1.0, -1.0])
+    gam = np.ascontiguousarray(gam, dtype=np.float64)
+    _check(lib.pbag_shock_limits(C.byref(opts), abi.dptr(gam), len(gam), len(states),
+                                 states.ctypes.data, abi.dptr(state), out.ctypes.data),
+           "pbag_shock_limits")
+    return out
+
+
+class Context:
+    """One device context: one grid (a CommonTables entry) on one GPU."""
+
+    def __init__(self, grid, device=0, ssc=True):
+        lib = load()
+        self.grid = grid
+        self._h = C.c_void_p()
+        _check(lib.pbag_create(C.byref(grid), int(device), int(bool(ssc)), C.byref(self._h)),
+               "pbag_create")
+
+    def close(self):
+        if self._h:
+            load().pbag_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_launch_count(self):
+        return int(load().pbag_last_launch_count(self._h))
+
+    def run(self, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all")):
+        """pbag_run_batch with host buffers; returns dict name -> array."""
+        lib = load()
+        recs = np.ascontiguousarray(recs, dtype=abi.STEP_DTYPE)
+        params = np.ascontiguousarray(params, dtype=abi.SHOCK_PARAMS_DTYPE)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        nrec = int(offsets[-1])
+        arrays = {}
+        for f in outputs:
+            n = self.grid.ngam if f in abi.OUTPUT_ON_GAMMA else self.grid.nfreq
+            arrays[f] = np.zeros((nrec, n))
+        out = abi.make_outputs(arrays)
+        st = abi.Status()
+        rc = lib.pbag_run_batch(self._h, params.ctypes.data, len(params),
+                                offsets.ctypes.data_as(C.POINTER(C.c_int64)), recs.ctypes.data,
+                                C.byref(out), C.byref(st))
+        _check(rc, "pbag_run_batch", st)
+        return arrays

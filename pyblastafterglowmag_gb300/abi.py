@@ -1,0 +1,122 @@
+"""ctypes mirror of include/pbag.h (structs, enums, status codes).
+
+The layouts here must match the C header field for field; tests check the
+sizes against the values the compiled library reports.
+"""
+import ctypes as C
+
+import numpy as np
+
+PBAG_OK = 0
+PBAG_ERR_ARG = -1
+PBAG_ERR_CUDA = -2
+PBAG_ERR_NONFINITE = -3
+PBAG_ERR_NELE = -4
+PBAG_ERR_PARAM = -5
+PBAG_ERR_DLNVDT = -6
+PBAG_ERR_UNSUPPORTED = -7
+PBAG_ERR_TIMEOUT = -8
+PBAG_ERR_NOMEM = -9
+
+STATUS_NAMES = {
+    PBAG_OK: "ok",
+    PBAG_ERR_ARG: "bad argument",
+    PBAG_ERR_CUDA: "CUDA error",
+    PBAG_ERR_NONFINITE: "non-finite or negative value",
+    PBAG_ERR_NELE: "total electron number <= 0",
+    PBAG_ERR_PARAM: "invalid shock parameters",
+    PBAG_ERR_DLNVDT: "invalid dlnV/dt",
+    PBAG_ERR_UNSUPPORTED: "unsupported option",
+    PBAG_ERR_TIMEOUT: "device wait timed out",
+    PBAG_ERR_NOMEM: "device allocation failed",
+}
+
+PBAG_SKIP, PBAG_INIT, PBAG_EVOLVE = 0, 1, 2
+PBAG_SYN_CSYN, PBAG_SYN_DER09, PBAG_SYN_GSL, PBAG_SYN_BESSEL = 0, 1, 2, 3
+PBAG_ELE_NUMERIC, PBAG_ELE_MIX = 1, 2
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("ngam", C.c_int32), ("nfreq", C.c_int32),
+                ("gam1", C.c_double), ("gam2", C.c_double),
+                ("freq1", C.c_double), ("freq2", C.c_double)]
+
+
+class ShockParams(C.Structure):
+    _fields_ = [("p", C.c_double), ("eps_e", C.c_double),
+                ("max_substeps", C.c_int32), ("ele_method", C.c_int32),
+                ("syn_method", C.c_int32), ("ssa_on", C.c_int32),
+                ("ssc_on", C.c_int32), ("adi_on", C.c_int32),
+                ("pp_on", C.c_int32), ("reserved", C.c_int32)]
+
+
+SHOCK_PARAMS_DTYPE = np.dtype([("p", np.float64), ("eps_e", np.float64),
+                               ("max_substeps", np.int32), ("ele_method", np.int32),
+                               ("syn_method", np.int32), ("ssa_on", np.int32),
+                               ("ssc_on", np.int32), ("adi_on", np.int32),
+                               ("pp_on", np.int32), ("reserved", np.int32)], align=True)
+assert SHOCK_PARAMS_DTYPE.itemsize == C.sizeof(ShockParams)
+
+
+class LimitsOpts(C.Structure):
+    _fields_ = [("p", C.c_double), ("eps_e", C.c_double), ("eps_b", C.c_double),
+                ("eps_t", C.c_double), ("beta_min", C.c_double), ("mu", C.c_double),
+                ("mu_e", C.c_double), ("method_B", C.c_int32),
+                ("method_gamma_min", C.c_int32), ("method_gamma_c", C.c_int32),
+                ("method_gamma_max", C.c_int32), ("method_nonrel", C.c_int32),
+                ("ele_analytic", C.c_int32)]
+
+
+SHOCK_STATE_DTYPE = np.dtype([(f, np.float64) for f in
+                              ["e_prime", "Gamma", "GammaSh", "t_e", "t_b", "tcomov",
+                               "n_prime", "n_protons"]])
+LIMITS_DTYPE = np.dtype([(f, np.float64) for f in
+                         ["B", "gamma_min", "gamma_max", "gamma_c", "accel_frac", "Theta",
+                          "z_cool"]] + [("valid", np.int32), ("reserved", np.int32)])
+
+REC_FIELDS = ["tc", "tc_p1", "m", "m_p1", "rho", "rho_p1", "dr", "dr_p1",
+              "u_p", "u_p_p1", "B", "gamma_min", "gamma_max", "gamma_c",
+              "accel_frac", "n_prime"]
+
+
+class StepRec(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("reserved", C.c_int32)] + \
+        [(f, C.c_double) for f in REC_FIELDS]
+
+
+# numpy view of an array of StepRec
+STEP_DTYPE = np.dtype([("mode", np.int32), ("reserved", np.int32)] +
+                      [(f, np.float64) for f in REC_FIELDS], align=True)
+assert STEP_DTYPE.itemsize == C.sizeof(StepRec)
+
+OUTPUT_FIELDS = ["j_all", "a_all", "f_all", "i_all",
+                 "ele_f_all", "gdot_syn_all", "gdot_adi_all", "gdot_ssc_all",
+                 "syn_j_all", "syn_a_all", "syn_i_all", "ssc_j_all", "ssc_i_all"]
+# which outputs have G (electron grid) columns rather than F
+OUTPUT_ON_GAMMA = {"ele_f_all", "gdot_syn_all", "gdot_adi_all", "gdot_ssc_all"}
+
+
+class Outputs(C.Structure):
+    _fields_ = [(f, C.POINTER(C.c_double)) for f in OUTPUT_FIELDS]
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int32), ("bw", C.c_int32),
+                ("step", C.c_int32), ("reserved", C.c_int32)]
+
+
+def dptr(a):
+    """POINTER(c_double) for a contiguous float64 numpy array (or None)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_outputs(arrays):
+    """Outputs struct from a dict name -> float64 array (missing -> NULL)."""
+    out = Outputs()
+    for f in OUTPUT_FIELDS:
+        a = arrays.get(f)
+        setattr(out, f, dptr(a) if a is not None else C.POINTER(C.c_double)())
+    return out

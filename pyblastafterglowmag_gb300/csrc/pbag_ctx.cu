@@ -1,0 +1,387 @@
+// pbag_ctx.cu - the C ABI entry points that own device memory and run a batch.
+//
+// A pbag_ctx is the device-side counterpart of one CommonTables entry of the
+// reference (microphysics/common.h:93-117): one electron grid, one photon grid
+// and the SSC kernel tables, shared read-only by every blastwave of a batch.
+// pbag_run_batch evolves the whole history of every blastwave of the batch,
+// step index by step index; at each index it launches
+//   k_evolve_radiate -> k_ssc_contract -> k_finalize
+// over all blastwaves on one stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "pbag.h"
+#include "pbag_internal.h"
+#include "pbag_kernels.h"
+
+using namespace pbag;
+
+namespace {
+
+template <typename T>
+cudaError_t dev_alloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) return cudaSuccess;
+  return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+template <typename T>
+cudaError_t upload(T** p, const T* h, size_t n, cudaStream_t st) {
+  cudaError_t e = dev_alloc(p, n);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+}  // namespace
+
+struct pbag_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  pbag_grid_desc desc{};
+  int G = 0, F = 0, Gp = 0;
+  bool ssc = false;
+  std::vector<double> gam, freq;
+  DevGrid dg{};
+  std::vector<void*> grid_mem;
+  // batch buffers, grown on demand
+  int cap_bw = 0;
+  size_t cap_rec = 0;
+  pbag_step_rec* d_recs = nullptr;
+  int64_t* d_off = nullptr;
+  pbag_shock_params* d_prm = nullptr;
+  DevState S{};
+  std::vector<void*> state_mem;
+  double* d_out = nullptr;  // output histories (host-buffer entry point)
+  size_t cap_out = 0;
+  int64_t launches = 0;
+
+  ~pbag_ctx() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : grid_mem) cudaFree(p);
+    free_state();
+    cudaFree(d_recs);
+    cudaFree(d_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void free_state() {
+    for (void* p : state_mem) cudaFree(p);
+    state_mem.clear();
+    cudaFree(d_off);
+    cudaFree(d_prm);
+    d_off = nullptr;
+    d_prm = nullptr;
+    cap_bw = 0;
+  }
+
+  template <typename T>
+  cudaError_t grid_upload(const T** dst, const std::vector<T>& h) {
+    T* p = nullptr;
+    cudaError_t e = upload(&p, h.data(), h.size(), stream);
+    if (e == cudaSuccess) grid_mem.push_back(p);
+    *dst = p;
+    return e;
+  }
+
+  template <typename T>
+  cudaError_t state_alloc(T** dst, size_t n) {
+    cudaError_t e = dev_alloc(dst, n);
+    if (e == cudaSuccess) state_mem.push_back(*dst);
+    return e;
+  }
+
+  cudaError_t reserve_bw(int nbw) {
+    if (nbw <= cap_bw) return cudaSuccess;
+    free_state();
+    int cap = std::max(nbw, 64);
+    cudaError_t e;
+    if ((e = dev_alloc(&d_off, (size_t)cap + 1)) != cudaSuccess) return e;
+    if ((e = dev_alloc(&d_prm, (size_t)cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.f, (size_t)cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.dfde, (size_t)cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.gdot, (size_t)cap * 3 * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.n, (size_t)cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.jsyn, (size_t)cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.asyn, (size_t)cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.jssc, (size_t)cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.W32, (size_t)cap * Gp)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.U32, (size_t)cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.scal, (size_t)cap * kScal)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.flags, (size_t)cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.err, (size_t)cap * 2)) != cudaSuccess) return e;
+    cap_bw = cap;
+    return cudaSuccess;
+  }
+
+  cudaError_t reset_state(int nbw) {
+    cudaError_t e;
+    const size_t n = (size_t)nbw;
+    if ((e = cudaMemsetAsync(S.f, 0, n * G * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.dfde, 0, n * G * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.gdot, 0, n * 3 * G * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.n, 0, n * F * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.jssc, 0, n * F * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.U32, 0, n * F * sizeof(float), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.W32, 0, n * Gp * sizeof(float), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.scal, 0, n * kScal * sizeof(double), stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.flags, 0, n * sizeof(int), stream)) != cudaSuccess) return e;
+    return cudaMemsetAsync(S.err, 0, n * 2 * sizeof(int), stream);
+  }
+};
+
+namespace {
+
+int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, const int64_t* off) {
+  if (nbw < 0 || !off) return PBAG_ERR_ARG;
+  if (off[0] != 0) return PBAG_ERR_ARG;
+  for (int b = 0; b < nbw; ++b)
+    if (off[b + 1] < off[b]) return PBAG_ERR_ARG;
+  if (prm_host) {
+    for (int b = 0; b < nbw; ++b) {
+      const pbag_shock_params& p = prm_host[b];
+      if (p.pp_on) return PBAG_ERR_UNSUPPORTED;
+      if (p.syn_method != PBAG_SYN_CSYN && p.syn_method != PBAG_SYN_DER09) return PBAG_ERR_UNSUPPORTED;
+      if (p.ele_method != PBAG_ELE_NUMERIC && p.ele_method != PBAG_ELE_MIX) return PBAG_ERR_ARG;
+      if (p.max_substeps < 1 || !(p.p > 0.) || !std::isfinite(p.p)) return PBAG_ERR_ARG;
+      if (p.ssc_on && !c->ssc) return PBAG_ERR_ARG;
+    }
+  }
+  return PBAG_OK;
+}
+
+// Runs every step of the batch; all pointers are device pointers except off_h.
+int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off_h,
+               const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st) {
+  cudaError_t e = c->reserve_bw(nbw);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+  const size_t nrec = (size_t)off_h[nbw];
+  if ((e = cudaMemcpyAsync(c->d_off, off_h, sizeof(int64_t) * (nbw + 1), cudaMemcpyHostToDevice, c->stream)) !=
+      cudaSuccess)
+    return PBAG_ERR_CUDA;
+  if ((e = c->reset_state(nbw)) != cudaSuccess) return PBAG_ERR_CUDA;
+  // zero rows: skipped steps keep zero output rows
+  const double* const* outp = reinterpret_cast<const double* const*>(&d_out);
+  for (int fi = 0; fi < 13; ++fi) {
+    if (!outp[fi]) continue;
+    const size_t n = (fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F;
+    if (cudaMemsetAsync((void*)outp[fi], 0, nrec * n * sizeof(double), c->stream) != cudaSuccess)
+      return PBAG_ERR_CUDA;
+  }
+  int64_t max_len = 0;
+  for (int b = 0; b < nbw; ++b) max_len = std::max<int64_t>(max_len, off_h[b + 1] - off_h[b]);
+  c->launches = 0;
+  // any blastwave with SSC on? (read from the device copy is avoided: the
+  // contraction kernel itself skips blastwaves without SSC weights)
+  for (int64_t s = 0; s < max_len; ++s) {
+    if ((e = launch_evolve_radiate(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int)s, c->stream)) != cudaSuccess)
+      return PBAG_ERR_CUDA;
+    ++c->launches;
+    if (c->ssc) {
+      if ((e = launch_ssc_contract(c->dg, c->S, nbw, c->stream)) != cudaSuccess) return PBAG_ERR_CUDA;
+      ++c->launches;
+    }
+    if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
+      return PBAG_ERR_CUDA;
+    ++c->launches;
+  }
+  std::vector<int> err((size_t)nbw * 2);
+  if (nbw > 0 && cudaMemcpyAsync(err.data(), c->S.err, err.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                 c->stream) != cudaSuccess)
+    return PBAG_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PBAG_ERR_CUDA;
+  // the reference stops at the first failure in time order (then blastwave order)
+  int code = PBAG_OK, fb = -1, fs = -1;
+  for (int b = 0; b < nbw; ++b) {
+    if (err[2 * b] != 0 && (fs < 0 || err[2 * b + 1] < fs)) {
+      code = err[2 * b];
+      fb = b;
+      fs = err[2 * b + 1];
+    }
+  }
+  if (st) {
+    st->code = code;
+    st->bw = fb;
+    st->step = fs;
+  }
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** out) {
+  if (!out) return PBAG_ERR_ARG;
+  *out = nullptr;
+  if (!g || g->ngam < PBAG_MIN_BINS || g->ngam > PBAG_MAX_BINS || g->nfreq < PBAG_MIN_BINS ||
+      g->nfreq > PBAG_MAX_BINS || !(g->gam2 > 1.) || !(g->freq1 > 0.) || !(g->freq2 > g->freq1))
+    return PBAG_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return PBAG_ERR_CUDA;
+  pbag_ctx* c = new (std::nothrow) pbag_ctx();
+  if (!c) return PBAG_ERR_NOMEM;
+  c->device = device;
+  c->desc = *g;
+  c->G = g->ngam;
+  c->F = g->nfreq;
+  c->Gp = (c->G + 15) / 16 * 16;
+  c->ssc = ssc_tables != 0;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return PBAG_ERR_CUDA;
+  }
+  const int G = c->G, F = c->F;
+  c->gam.assign(G, 0.);
+  c->freq.assign(F + 1, 0.);
+  build_grids(g, c->gam.data(), c->freq.data());
+  // derived grids (base_state.h:229-250)
+  const double step = std::exp(std::log(g->gam2) / (double)G);
+  std::vector<double> half(G - 1), de(G - 1), dg(G + 1), dgb(G), dnu(F);
+  std::vector<float> ginv2(G), psq(G);
+  for (int i = 0; i < G - 1; ++i) half[i] = .5 * c->gam[i] * (step + 1.0);
+  for (int i = 0; i < G - 1; ++i) de[i] = c->gam[i + 1] - c->gam[i];
+  for (int i = 0; i < G - 1; ++i) dg[i + 1] = c->gam[i + 1] - c->gam[i];
+  dg[0] = c->gam[0] * (1 - 1.0 / step);
+  dg[G] = c->gam[G - 1] * (step - 1);
+  for (int i = 0; i < G; ++i) dgb[i] = (dg[i] + dg[i + 1]) / 2.;
+  int n_cyc = 0;
+  for (int i = 0; i < G; ++i) {
+    ginv2[i] = (float)(1. / (c->gam[i] * c->gam[i]));
+    psq[i] = (float)(c->gam[i] * c->gam[i] - 1.);
+    if (c->gam[i] <= 2.) n_cyc = i + 1;
+  }
+  for (int k = 0; k < F; ++k) dnu[k] = (c->freq[k + 1] - c->freq[k]) / c->freq[k];
+  DevGrid& d = c->dg;
+  d.G = G;
+  d.F = F;
+  d.Gp = c->Gp;
+  d.n_cyc = n_cyc;
+  d.dlog_gam = (c->gam[1] - c->gam[0]) / c->gam[0];
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  ok(c->grid_upload(&d.e, c->gam));
+  ok(c->grid_upload(&d.half, half));
+  ok(c->grid_upload(&d.de, de));
+  ok(c->grid_upload(&d.dgb, dgb));
+  ok(c->grid_upload(&d.ginv2, ginv2));
+  ok(c->grid_upload(&d.psq32, psq));
+  ok(c->grid_upload(&d.nu, c->freq));
+  ok(c->grid_upload(&d.dnu_nu, dnu));
+  d.Kint = nullptr;
+  d.K32 = nullptr;
+  if (c->ssc) {
+    std::vector<double> Kint;
+    std::vector<float> K32;
+    build_ssc_tables(c->gam.data(), G, c->freq.data(), F, c->Gp, Kint, K32);
+    ok(c->grid_upload(&d.Kint, Kint));
+    ok(c->grid_upload(&d.K32, K32));
+    ok(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  }
+  ok(cudaStreamSynchronize(c->stream));
+  if (e != cudaSuccess) {
+    int code = e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+    delete c;
+    return code;
+  }
+  *out = c;
+  return PBAG_OK;
+}
+
+void pbag_destroy(pbag_ctx* c) { delete c; }
+
+int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int64_t* off,
+                   const pbag_step_rec* recs, const pbag_outputs* out, pbag_status* st) {
+  if (st) {
+    st->code = PBAG_ERR_ARG;
+    st->bw = st->step = -1;
+  }
+  if (!c || !out || (nbw > 0 && (!prm || !recs))) return PBAG_ERR_ARG;
+  int rc = check_batch(c, prm, nbw, off);
+  if (rc != PBAG_OK) {
+    if (st) st->code = rc;
+    return rc;
+  }
+  if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
+  const size_t nrec = (size_t)off[nbw];
+  cudaError_t e = c->reserve_bw(nbw);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+  if (nrec > c->cap_rec) {
+    cudaFree(c->d_recs);
+    c->d_recs = nullptr;
+    c->cap_rec = 0;
+    if ((e = dev_alloc(&c->d_recs, nrec)) != cudaSuccess)
+      return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+    c->cap_rec = nrec;
+  }
+  // device output buffers for the requested histories
+  const double* const* outp = reinterpret_cast<const double* const*>(out);
+  size_t need = 0;
+  for (int fi = 0; fi < 13; ++fi)
+    if (outp[fi]) need += nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+  if (need > c->cap_out) {
+    cudaFree(c->d_out);
+    c->d_out = nullptr;
+    c->cap_out = 0;
+    if ((e = dev_alloc(&c->d_out, need)) != cudaSuccess)
+      return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+    c->cap_out = need;
+  }
+  pbag_outputs dout{};
+  double** dp = reinterpret_cast<double**>(&dout);
+  size_t pos = 0;
+  for (int fi = 0; fi < 13; ++fi) {
+    if (!outp[fi]) continue;
+    dp[fi] = c->d_out + pos;
+    pos += nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+  }
+  if (nrec && cudaMemcpyAsync(c->d_recs, recs, nrec * sizeof(pbag_step_rec), cudaMemcpyHostToDevice, c->stream) !=
+                  cudaSuccess)
+    return PBAG_ERR_CUDA;
+  if (nbw && cudaMemcpyAsync(c->d_prm, prm, nbw * sizeof(pbag_shock_params), cudaMemcpyHostToDevice, c->stream) !=
+                 cudaSuccess)
+    return PBAG_ERR_CUDA;
+  rc = run_device(c, c->d_prm, nbw, off, c->d_recs, dout, st);
+  if (rc == PBAG_ERR_CUDA) return rc;
+  // copy the histories back even on a physics error (rows before the failure are valid)
+  for (int fi = 0; fi < 13; ++fi) {
+    if (!outp[fi]) continue;
+    const size_t n = nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+    if (n && cudaMemcpyAsync((void*)outp[fi], dp[fi], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream) !=
+                 cudaSuccess)
+      return PBAG_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PBAG_ERR_CUDA;
+  return rc;
+}
+
+int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
+                          const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st, void* stream) {
+  if (st) {
+    st->code = PBAG_ERR_ARG;
+    st->bw = st->step = -1;
+  }
+  if (!c || !d_out || (nbw > 0 && (!d_prm || !d_recs))) return PBAG_ERR_ARG;
+  if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
+  std::vector<pbag_shock_params> hp((size_t)std::max(nbw, 0));
+  if (nbw > 0 && cudaMemcpy(hp.data(), d_prm, hp.size() * sizeof(pbag_shock_params), cudaMemcpyDeviceToHost) !=
+                     cudaSuccess)
+    return PBAG_ERR_CUDA;
+  int rc = check_batch(c, hp.data(), nbw, off);
+  if (rc != PBAG_OK) {
+    if (st) st->code = rc;
+    return rc;
+  }
+  (void)stream;
+  return run_device(c, d_prm, nbw, off, d_recs, *d_out, st);
+}
+
+int64_t pbag_last_launch_count(const pbag_ctx* c) { return c ? c->launches : -1; }
+
+}  // extern "C"

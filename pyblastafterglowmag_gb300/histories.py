@@ -1,0 +1,310 @@
+"""Synthetic blastwave histories: the per-step scalar records that the
+reference's blastwave driver would hand to the comoving-radiation step.
+
+The reference produces these from its ODE driver (src/model_evolve.h,
+src/blastwave/) which is not part of this package. Here each jet layer follows
+a simple adiabatic thin-shell model (swept-up mass m, Lorentz factor Gamma with
+dGamma/dm = -(Gamma^2 - 1)/(M0 + 2 Gamma m), iso-equivalent radius from m),
+sampled on the reference's burster-time grid; a reverse shock exists until the
+ejecta are crossed. The shock scalars (B, gamma_min, gamma_max, gamma_c,
+accel_frac, n') come from the library's restatement of
+computeEleSpectrumLimits (microphysics_base.h:642-966), called exactly as the
+driver calls it (blastwave_radiation.h:976-1107).
+
+The value ranges (Lorentz factors, densities, cooling regimes, substep
+counts from 1 to max_substeps, the gamma_min <= 2 analytic fallback late on)
+follow the reference's configurations; the exact dynamics do not matter for the
+comoving step, whose parity is checked on identical records.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+C_LIGHT = 2.99792458e10
+M_P = 1.6726e-24
+
+
+@dataclass
+class Shock:
+    """Microphysics parameters of one shock (the *_fs / *_rs parfile keys)."""
+    eps_e: float = 0.1
+    eps_b: float = 1e-3
+    p: float = 2.2
+    ssc: bool = False
+    ssa: bool = False
+    max_substeps: int = 1000
+    ele_method: int = abi.PBAG_ELE_NUMERIC
+    syn_method: int = abi.PBAG_SYN_CSYN
+    adi: bool = True
+
+
+@dataclass
+class JetConfig:
+    """One jet: structure, energetics, ISM, grids and time grid."""
+    struct: str = "tophat"            # "tophat" or "gaussian"
+    E_iso: float = 1e52               # core isotropic energy [erg]
+    Gamma0: float = 300.0             # core initial Lorentz factor
+    theta_c: float = 0.1              # core half-opening angle [rad]
+    theta_w: float = 0.1              # wing angle [rad] (gaussian)
+    n_ism: float = 1e-2               # ISM density [cm^-3]
+    nlayers: int = 1
+    fs: Shock = field(default_factory=Shock)
+    rs: Shock = None                  # None: forward shock only
+    ngam: int = 151
+    gam1: float = 1.0
+    gam2: float = 1e8
+    nfreq: int = 96
+    freq1: float = 1e8
+    freq2: float = 1e29
+    ntb: int = 1000
+    tb1: float = 3e2
+    tb2: float = 1e14
+
+    def grid(self):
+        return abi.GridDesc(self.ngam, self.nfreq, self.gam1, self.gam2, self.freq1, self.freq2)
+
+
+def config_tophat_fs():
+    """One top-hat layer, forward shock only, synchrotron only (the
+    reference's CPU-runnable case): E_iso=1e52, Gamma0=300, theta_c=0.1,
+    n=1e-2, eps_e=0.1, eps_b=1e-3, p=2.2, 151 gamma x 96 nu, ntb=1000."""
+    return JetConfig()
+
+
+def config_gaussian_ssc():
+    """The 21-layer Gaussian jet with forward and reverse shocks, synchrotron +
+    SSC (+SSA): Eiso_c=10^54.1, Gamma0c=300, theta_c=3.5 deg, theta_w=25 deg,
+    n=10^-1.6, eps_e=10^-3.42, eps_b=10^-4.02, p=2.1, 201 gamma in [1,1e9],
+    128 nu in [1e8,1e29], ntb=1000."""
+    sh = dict(eps_e=10 ** -3.42, eps_b=10 ** -4.02, p=2.1, ssc=True, ssa=True)
+    return JetConfig(struct="gaussian", E_iso=10 ** 54.1, Gamma0=300.0,
+                     theta_c=np.deg2rad(3.5), theta_w=np.deg2rad(25.0),
+                     n_ism=10 ** -1.6, nlayers=21, fs=Shock(**sh), rs=Shock(**sh),
+                     ngam=201, gam1=1.0, gam2=1e9, nfreq=128)
+
+
+def layer_table(cfg):
+    """(theta_lo, theta_hi, E_iso, Gamma0) per layer."""
+    tw = cfg.theta_c if cfg.struct == "tophat" else cfg.theta_w
+    edges = np.linspace(0.0, tw, cfg.nlayers + 1)
+    mid = 0.5 * (edges[1:] + edges[:-1])
+    if cfg.struct == "tophat":
+        E = np.full(cfg.nlayers, cfg.E_iso)
+        G0 = np.full(cfg.nlayers, cfg.Gamma0)
+    else:
+        w = np.exp(-0.5 * (mid / cfg.theta_c) ** 2)
+        E = cfg.E_iso * w
+        G0 = 1.0 + (cfg.Gamma0 - 1.0) * w
+    G0 = np.maximum(G0, 1.5)
+    return edges[:-1], edges[1:], E, G0
+
+
+def _rk4(f, y, x0, x1, n):
+    h = (x1 - x0) / n
+    x = x0
+    out = [y.copy()]
+    for _ in range(n):
+        k1 = f(x, y)
+        k2 = f(x + h / 2, y + h / 2 * k1)
+        k3 = f(x + h / 2, y + h / 2 * k2)
+        k4 = f(x + h, y + h * k3)
+        y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        x += h
+        out.append(y.copy())
+    return np.array(out)
+
+
+def layer_dynamics(E_iso, Gamma0, n_ism, tb, omega, nsamp=4000):
+    """Thin-shell dynamics of one layer sampled at burster times tb.
+
+    Integrates in x = ln m_iso the variables (u = ln(Gamma-1), t_b, t_comov,
+    t_obs) with R = (3 m / 4 pi rho)^(1/3); returns arrays on tb."""
+    rho = n_ism * M_P
+    M0 = E_iso / ((Gamma0 - 1.0) * C_LIGHT ** 2)
+    beta0 = np.sqrt(1 - 1 / Gamma0 ** 2)
+    # start well inside the coasting phase, at the radius reached by tb[0]/10
+    R0 = beta0 * C_LIGHT * tb[0] * 0.1
+    m0 = 4 / 3 * np.pi * R0 ** 3 * rho
+    m1 = max(1e6 * M0 * Gamma0, m0 * 1e40)
+
+    def rhs(x, y):
+        m = np.exp(x)
+        gm1 = max(np.exp(y[0]), 1e-300)      # Gamma - 1, kept apart from 1 for precision
+        G = 1.0 + gm1
+        # dGamma/dm / (Gamma - 1) = -(Gamma + 1)/(M0 + 2 Gamma m)
+        dudm = -(G + 1.0) / (M0 + 2.0 * G * m)
+        R = (3 * m / (4 * np.pi * rho)) ** (1 / 3)
+        dRdx = R / 3.0                       # dR/dln m
+        beta = np.sqrt(gm1 * (2.0 + gm1)) / G
+        return np.array([dudm * m,
+                         dRdx / (beta * C_LIGHT),
+                         dRdx / (beta * G * C_LIGHT),
+                         dRdx * (1 - beta) / (beta * C_LIGHT)])
+
+    y0 = np.array([np.log(Gamma0 - 1.0), R0 / (beta0 * C_LIGHT),
+                   R0 / (beta0 * Gamma0 * C_LIGHT), R0 * (1 - beta0) / (beta0 * C_LIGHT)])
+    xs = np.linspace(np.log(m0), np.log(m1), nsamp + 1)
+    ys = _rk4(rhs, y0, xs[0], xs[-1], nsamp)
+    t_b = ys[:, 1]
+    lt = np.log(t_b)
+    lq = np.log(tb)
+    x = np.interp(lq, lt, xs)
+    u = np.interp(lq, lt, ys[:, 0])
+    tcom = np.exp(np.interp(lq, lt, np.log(ys[:, 2])))
+    tobs = np.exp(np.interp(lq, lt, np.log(ys[:, 3])))
+    m_iso = np.exp(x)
+    gm1 = np.maximum(np.exp(u), 1e-300)
+    G = 1.0 + gm1
+    beta = np.sqrt(gm1 * (2.0 + gm1)) / G
+    R = (3 * m_iso / (4 * np.pi * rho)) ** (1 / 3)
+    frac = omega / (4 * np.pi)
+    return dict(Gamma=G, beta=beta, R=R, m=m_iso * frac, m_iso=m_iso, tcomov=tcom,
+                t_obs=tobs, M0=M0 * frac, M0_iso=M0, Gamma0=Gamma0, beta0=beta0, rho=rho)
+
+
+def fs_state(d):
+    """Forward-shock downstream quantities (iso-equivalent thin shell)."""
+    G = d["Gamma"]
+    gad = (4.0 + 1.0 / G) / 3.0                               # adiabatic index
+    rho2 = (gad * G + 1.0) / (gad - 1.0) * d["rho"]           # comoving density
+    m2 = d["m"]
+    u_p = (G - 1.0) * rho2 * C_LIGHT ** 2                     # comoving energy density
+    thick = d["m_iso"] / (4 * np.pi * d["R"] ** 2 * G * rho2)  # lab-frame thickness
+    return dict(Gamma=G, GammaSh=G, rho2=rho2, m2=m2, u_p=u_p, thick=thick,
+                dr=thick * G, valid=np.ones_like(G, dtype=bool))
+
+
+def rs_state(d, shell_width=3e12):
+    """Reverse shock in the ejecta, active until the shell is crossed at the
+    deceleration radius, then until it has expanded a further factor 3."""
+    G, G0, b0 = d["Gamma"], d["Gamma0"], d["beta0"]
+    beta = d["beta"]
+    G43 = np.maximum(G0 * G * (1.0 - b0 * beta), 1.0 + 1e-9)
+    Rx = (3 * d["M0_iso"] / G0 / (4 * np.pi * d["rho"])) ** (1 / 3)  # m = M0/Gamma0
+    R = d["R"]
+    xfrac = np.minimum(1.0, (R / Rx) ** 1.5)
+    m3 = d["M0"] * np.maximum(xfrac, 1e-6)
+    rho_ej = d["M0_iso"] / (4 * np.pi * R ** 2 * shell_width * G0)
+    gad = (4.0 + 1.0 / G43) / 3.0
+    rho3 = (gad * G43 + 1.0) / (gad - 1.0) * rho_ej
+    u_p3 = (G43 - 1.0) * rho3 * C_LIGHT ** 2
+    thick = d["M0_iso"] * np.maximum(xfrac, 1e-6) / (4 * np.pi * R ** 2 * G * rho3)
+    valid = R < 3.0 * Rx
+    return dict(Gamma=G, GammaSh=G43, rho2=rho3, m2=m3, u_p=u_p3, thick=thick,
+                dr=thick * G43, valid=valid)
+
+
+def limits_opts(sh):
+    o = abi.LimitsOpts()
+    o.p, o.eps_e, o.eps_b, o.eps_t = sh.p, sh.eps_e, sh.eps_b, 0.0
+    o.beta_min, o.mu, o.mu_e = 1e-5, 0.62, 1.18
+    o.method_B = 0          # useU_b
+    o.method_gamma_min = 0  # useU_e
+    o.method_gamma_c = 0    # useTe
+    o.method_gamma_max = 0  # useB
+    o.method_nonrel = 0     # none
+    o.ele_analytic = 0
+    return o
+
+
+def shock_records(lib, st, d, sh, gam, tb):
+    """Step records of one shock: computeEleSpectrumLimits on every step, then
+    the arguments of init/evolve exactly as blastwave_radiation.h:1109-1182."""
+    n = len(tb)
+    ss = np.zeros(n, dtype=abi.SHOCK_STATE_DTYPE)
+    ss["e_prime"] = st["u_p"]
+    ss["Gamma"] = st["Gamma"]
+    ss["GammaSh"] = st["GammaSh"]
+    ss["t_e"] = d["t_obs"]
+    ss["t_b"] = tb
+    ss["tcomov"] = d["tcomov"]
+    ss["n_prime"] = st["rho2"] / M_P
+    ss["n_protons"] = st["m2"] / M_P
+    lim = lib.shock_limits(limits_opts(sh), gam, ss)
+    recs = np.zeros(n, dtype=abi.STEP_DTYPE)
+    valid = st["valid"] & (lim["valid"] == 1) & (st["u_p"] > 0) & (st["rho2"] > 0)
+    recs["mode"] = np.where(valid, abi.PBAG_EVOLVE, abi.PBAG_SKIP)
+    first = np.argmax(valid) if valid.any() else n
+    if first < n:
+        recs["mode"][first] = abi.PBAG_INIT
+    prev = lambda a: np.concatenate([a[:1], a[:-1]])
+    recs["tc"], recs["tc_p1"] = prev(d["tcomov"]), d["tcomov"]
+    recs["m"], recs["m_p1"] = prev(st["m2"]), st["m2"]
+    recs["rho"], recs["rho_p1"] = prev(st["rho2"]), st["rho2"]
+    recs["u_p"], recs["u_p_p1"] = prev(st["u_p"]), st["u_p"]
+    dr = st["dr"]
+    recs["dr"], recs["dr_p1"] = prev(dr), dr
+    # the first valid step passes the current thickness to initializeElectronDistribution
+    if first < n:
+        recs["dr"][first] = st["thick"][first]
+    for k in ("B", "gamma_min", "gamma_max", "gamma_c", "accel_frac"):
+        recs[k] = lim[k]
+    recs["n_prime"] = ss["n_prime"]
+    return recs
+
+
+def shock_params(sh):
+    p = np.zeros(1, dtype=abi.SHOCK_PARAMS_DTYPE)
+    p["p"], p["eps_e"], p["max_substeps"] = sh.p, sh.eps_e, sh.max_substeps
+    p["ele_method"], p["syn_method"] = sh.ele_method, sh.syn_method
+    p["ssa_on"], p["ssc_on"], p["adi_on"], p["pp_on"] = int(sh.ssa), int(sh.ssc), int(sh.adi), 0
+    return p[0]
+
+
+def make_batch(lib, cfg, nsteps=None):
+    """Records for every blastwave of one jet: (recs, offsets, params, grid).
+
+    Blastwaves are ordered layer by layer, forward shock then reverse shock.
+    nsteps truncates every history to its first nsteps burster times."""
+    tb = np.logspace(np.log10(cfg.tb1), np.log10(cfg.tb2), cfg.ntb)
+    if nsteps is not None:
+        tb = tb[:nsteps]
+    grid = cfg.grid()
+    gam, _ = lib.grids(grid)
+    lo, hi, E, G0 = layer_table(cfg)
+    recs, params = [], []
+    for il in range(cfg.nlayers):
+        omega = 2 * np.pi * (np.cos(lo[il]) - np.cos(hi[il])) * 2  # both hemispheres
+        d = layer_dynamics(E[il], G0[il], cfg.n_ism, tb, omega)
+        recs.append(shock_records(lib, fs_state(d), d, cfg.fs, gam, tb))
+        params.append(shock_params(cfg.fs))
+        if cfg.rs is not None:
+            recs.append(shock_records(lib, rs_state(d), d, cfg.rs, gam, tb))
+            params.append(shock_params(cfg.rs))
+    offsets = np.zeros(len(recs) + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum([len(r) for r in recs])
+    return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid
+
+
+def sweep_batch(lib, nsets, seed=3, ngam=201, nfreq=128, min_steps=200, max_steps=2000, ssc=True,
+                max_layers=41):
+    """Seeded parameter sweep: nsets jets, each a top-hat or Gaussian with
+    1..max_layers layers, log10 E_iso ~ U[50,54], log10 Gamma0 ~ U[1,3],
+    log10 n ~ U[-4,0], log10 eps_e ~ U[-3,-0.5], log10 eps_b ~ U[-5,-1],
+    p ~ U[2.05,2.8]; every blastwave keeps its first U{min_steps..max_steps}
+    steps (uneven histories)."""
+    rng = np.random.default_rng(seed)
+    all_recs, params, lens = [], [], []
+    grid = None
+    for _ in range(nsets):
+        struct = "tophat" if rng.random() < 0.5 else "gaussian"
+        nl = int(rng.integers(1, max_layers + 1))
+        sh = dict(eps_e=10 ** rng.uniform(-3, -0.5), eps_b=10 ** rng.uniform(-5, -1),
+                  p=rng.uniform(2.05, 2.8), ssc=ssc, ssa=True)
+        tc = rng.uniform(0.05, 0.15)
+        cfg = JetConfig(struct=struct, E_iso=10 ** rng.uniform(50, 54),
+                        Gamma0=10 ** rng.uniform(1, 3), theta_c=tc, theta_w=min(4 * tc, 0.6),
+                        n_ism=10 ** rng.uniform(-4, 0), nlayers=nl, fs=Shock(**sh), rs=Shock(**sh),
+                        ngam=ngam, gam1=1.0, gam2=1e9, nfreq=nfreq, ntb=max_steps)
+        recs, off, prm, grid = make_batch(lib, cfg)
+        for b in range(len(off) - 1):
+            n = int(rng.integers(min_steps, max_steps + 1))
+            r = recs[off[b]:off[b] + n]
+            all_recs.append(r)
+            lens.append(len(r))
+            params.append(prm[b])
+    offsets = np.zeros(len(lens) + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum(lens)
+    return np.concatenate(all_recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid

@@ -1,0 +1,104 @@
+"""GPU path (libpbag through its C ABI) against the FP64 oracle on identical
+seeded records. Tolerance: per-row relative L2 error <= 1e-4 for every
+history (the plain-path bar), computed over rows where the oracle is non-zero;
+rows the oracle leaves zero must be zero on the GPU too."""
+import os
+
+import numpy as np
+import pytest
+
+from pyblastafterglowmag_gb300 import abi
+from pyblastafterglowmag_gb300._lib import Context, PbagError
+import cases
+from conftest import rel_l2_rows
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+NTH = os.cpu_count() or 1
+
+
+def _compare(lib, oracle, batch, outputs=cases.ALL_OUTPUTS, tol=TOL):
+    recs, off, prm, grid = batch
+    rc, where, ref = oracle.run(grid, recs, off, prm, outputs=outputs, outer_threads=NTH)
+    assert rc == 0, (rc, where)
+    ssc = bool(np.any(prm["ssc_on"]))
+    ctx = Context(grid, device=0, ssc=ssc)
+    got = ctx.run(recs, off, prm, outputs=outputs)
+    assert ctx.last_launch_count() > 0
+    worst = {}
+    for k in outputs:
+        rel, zero_mismatch = rel_l2_rows(got[k], ref[k])
+        worst[k] = float(rel.max())
+        assert zero_mismatch == 0, f"{k}: {zero_mismatch} rows non-zero where the oracle is zero"
+        assert rel.max() <= tol, f"{k}: max rel-L2 {rel.max():.3e} (p99 {np.percentile(rel, 99):.3e})"
+    ctx.close()
+    return worst
+
+
+def test_tophat_syn(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.tophat(lib, nsteps=250))
+
+
+def test_tophat_ssa(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.tophat(lib, nsteps=250, ssa=True))
+
+
+def test_tophat_dermer_mix(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.tophat(lib, nsteps=120, ssa=True, syn_method=abi.PBAG_SYN_DER09,
+                                       ele_method=abi.PBAG_ELE_MIX))
+
+
+def test_gaussian_ssc(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
+
+
+def test_gaussian_late_window(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.gaussian_window(lib, start=380, nsteps=60))
+
+
+def test_uneven_batch(lib, oracle, cuda_device):
+    _compare(lib, oracle, cases.uneven(lib), outputs=cases.TOTALS)
+
+
+def test_error_status_matches_oracle(lib, oracle, cuda_device):
+    recs, off, prm, grid = cases.tophat(lib, nsteps=60)
+    bad = recs.copy()
+    bad["m_p1"][37] = bad["m"][37] * 0.5  # volume shrinks: dlnV/dt < 0 (microphysics.h:406-409)
+    rc, where, _ = oracle.run(grid, bad, off, prm, outputs=cases.TOTALS)
+    assert rc == abi.PBAG_ERR_DLNVDT and where == (0, 37)
+    ctx = Context(grid, device=0, ssc=False)
+    with pytest.raises(PbagError) as ei:
+        ctx.run(bad, off, prm)
+    assert ei.value.code == abi.PBAG_ERR_DLNVDT and (ei.value.bw, ei.value.step) == (0, 37)
+
+
+def test_empty_and_zero_length(lib, oracle, cuda_device):
+    recs, off, prm, grid = cases.tophat(lib, nsteps=30)
+    ctx = Context(grid, device=0, ssc=False)
+    got = ctx.run(recs[:0], np.zeros(1, dtype=np.int64), prm[:0])
+    assert all(v.shape[0] == 0 for v in got.values())
+    # a zero-length blastwave between two real ones
+    recs2 = np.concatenate([recs, recs])
+    off2 = np.array([0, 30, 30, 60], dtype=np.int64)
+    prm2 = np.concatenate([prm, prm, prm])
+    got = ctx.run(recs2, off2, prm2)
+    rc, where, ref = oracle.run(grid, recs2, off2, prm2, outputs=cases.TOTALS)
+    assert rc == 0
+    for k in cases.TOTALS:
+        rel, zm = rel_l2_rows(got[k], ref[k])
+        assert zm == 0 and rel.max() <= TOL
+
+
+def test_unsupported_options_rejected(lib, cuda_device):
+    recs, off, prm, grid = cases.tophat(lib, nsteps=10)
+    ctx = Context(grid, device=0, ssc=False)
+    p = prm.copy()
+    p["pp_on"] = 1
+    with pytest.raises(PbagError) as ei:
+        ctx.run(recs, off, p)
+    assert ei.value.code == abi.PBAG_ERR_UNSUPPORTED
+    p = prm.copy()
+    p["ssc_on"] = 1  # context built without SSC tables
+    with pytest.raises(PbagError) as ei:
+        ctx.run(recs, off, p)
+    assert ei.value.code == abi.PBAG_ERR_ARG
