@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark: blastwave-steps/s of the comoving radiation step (synchrotron +
+SSC + SSA) on the 21-layer Gaussian jet with forward and reverse shocks
+(42 blastwaves x 1000 burster times, 201 gamma x 128 nu), on one GB300.
+
+One bench "step" is one pass of the whole batch through the step: every
+blastwave evolved over its 1000-time history (all valid blastwave-steps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0). Under torchrun each rank runs its own replica
+of the jet on its own GPU (blastwaves are independent; no collective on the
+data path) and the line reports the whole-job rate over the slowest rank.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "blastwave-steps/s (sync+SSC) on 1 GB300"
+UNIT = "blastwave-steps/s"
+WORKLOAD = "gaussian-jet-21-layers-fs-rs-syn-ssc-ssa-201x128-ntb1000"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload():
+    from pyblastafterglowmag_gb300 import _lib, histories as H
+    cfg = H.config_gaussian_ssc()
+    recs, off, prm, grid = H.make_batch(_lib, cfg)
+    return cfg, recs, off, prm, grid
+
+
+def config_dict(cfg, recs, prm, extra=None):
+    d = {"workload": WORKLOAD, "blastwaves": int(len(prm)), "layers": cfg.nlayers,
+         "shocks": "forward+reverse", "ngam": cfg.ngam, "nfreq": cfg.nfreq, "ntb": cfg.ntb,
+         "valid_blastwave_steps_per_pass": int((recs["mode"] != 0).sum()),
+         "radiation": "synchrotron(CSYN)+SSA+SSC", "solve": "Chang-Cooper FP64",
+         "ssc_contraction": "FP32 accumulate, per-blastwave power-of-two scaling",
+         "l2": "flushed with a 256 MiB device write before every timed pass",
+         "inputs": "seeded synthetic blastwave histories (thin-shell dynamics)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def algorithmic_bytes(kernel, grid, active):
+    """Bytes one launch of a kernel class must move at minimum, for `active`
+    radiating blastwaves: every per-blastwave operand read or written once
+    (FP64 state and histories, FP32 scaled contraction operands) and, for the
+    SSC contraction, the shared FP32 kernel tensor read once per launch."""
+    G, F = grid.ngam, grid.nfreq
+    Gp = (G + 15) // 16 * 16
+    if kernel == "evolve":   # record, f in/out, photon field in, j_syn/a_syn out, W out, scalars
+        return active * (136 + 16 * G + 8 * F + 16 * F + 4 * Gp + 64)
+    if kernel == "ssc":      # kernel tensor + W, U in, j_ssc out
+        return 4 * F * Gp * F + active * (4 * Gp + 4 * F + 8 * F)
+    # finalize: j_syn, a_syn, j_ssc in; photon field, U out; j/a/f/i rows out; scalars
+    return active * (24 * F + 8 * F + 4 * F + 32 * F + 64)
+
+
+# ---------------------------------------------------------------- clocks ---
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.samples, self._stop = index, [], threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------- cpu baseline ---
+def cpu_sample(recs, off, prm, grid, seconds, threads):
+    """Time the oracle port on a bounded sample of the workload: windows of
+    consecutive steps spread over every blastwave's history, each window
+    re-initialised at its first step. Returns (bw-steps/s, description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from pyblastafterglowmag_gb300 import abi
+    orc = pyoracle.Oracle()
+    nbw = len(prm)
+
+    def make(nwin, wlen):
+        rr, lens, pp = [], [], []
+        for b in range(nbw):
+            n = int(off[b + 1] - off[b])
+            for s0 in np.linspace(0, n - wlen, nwin).astype(int):
+                r = recs[off[b] + s0: off[b] + s0 + wlen]
+                rr.append(r)
+                lens.append(len(r))
+                pp.append(prm[b])
+        o = np.zeros(len(lens) + 1, dtype=np.int64)
+        o[1:] = np.cumsum(lens)
+        return np.concatenate(rr), o, np.array(pp, dtype=abi.SHOCK_PARAMS_DTYPE)
+
+    # calibrate on a small sample, then size the sample to ~`seconds`
+    r, o, p = make(1, 4)
+    t0 = time.perf_counter()
+    orc.run(grid, r, o, p, flags=0, outer_threads=threads)
+    t1 = time.perf_counter() - t0
+    per_step = max(t1 / max(int((r["mode"] != 0).sum()), 1), 1e-6)
+    budget_steps = seconds / per_step
+    wlen = 8
+    nwin = int(max(1, min(40, budget_steps / (wlen * nbw))))
+    r, o, p = make(nwin, wlen)
+    t0 = time.perf_counter()
+    rc, where, _ = orc.run(grid, r, o, p, flags=0, outer_threads=threads)
+    dt = time.perf_counter() - t0
+    n = int((r["mode"] != 0).sum())
+    desc = (f"{nbw} blastwaves x {nwin} windows x {wlen} consecutive steps spread over the 1000-step "
+            f"histories ({n} valid blastwave-steps), FP64 oracle port in the reference's loop structure "
+            f"(cooling terms recomputed every substep), one blastwave per thread")
+    return n / dt, desc, dt
+
+
+def reference_arm(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    from pyblastafterglowmag_gb300 import build
+    build.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build_oracle()
+    cfg, recs, off, prm, grid = workload()
+    threads = os.cpu_count() or 1
+    per_step = max(10.0, min(60.0, 150.0 / max(args.steps + args.warmup, 1)))
+    vals, dts, desc = [], [], ""
+    for i in range(args.warmup + args.steps):
+        v, desc, dt = cpu_sample(recs, off, prm, grid, per_step, threads)
+        if i >= args.warmup:
+            vals.append(v)
+            dts.append(dt)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": config_dict(cfg, recs, prm, {"sample": desc}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- gb300 arm ---
+def gb300_arm(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from pyblastafterglowmag_gb300 import _lib, abi, build
+    build.build()
+    cfg, recs, off, prm, grid = workload()
+    nvalid = int((recs["mode"] != 0).sum())
+    nrec, nbw, F = len(recs), len(prm), grid.nfreq
+    ctx = _lib.Context(grid, device=local, ssc=True)
+    dev = torch.device("cuda", local)
+
+    # device-resident inputs and outputs
+    d_recs = torch.from_numpy(recs.view(np.uint8).copy()).to(dev)
+    d_prm = torch.from_numpy(prm.view(np.uint8).copy()).to(dev)
+    outs = ("j_all", "a_all", "f_all", "i_all")
+    d_out = {k: torch.empty((nrec, F), dtype=torch.float64, device=dev) for k in outs}
+    d_ptrs = {k: v.data_ptr() for k, v in d_out.items()}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    def one_pass():
+        ctx.run_device(d_prm.data_ptr(), nbw, off, d_recs.data_ptr(), d_ptrs)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        one_pass()
+    barrier()
+    # timed region: K passes, device time of each pass with CUDA events
+    ctx.set_timing(True)
+    launches = 0
+    ev_ms = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            one_pass()  # synchronous: returns after the batch finished on the device
+            e1.record(stream)
+            e1.synchronize()
+            ev_ms.append(e0.elapsed_time(e1))
+            launches += ctx.last_launch_count()
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    timing = ctx.timing()
+    ctx.set_timing(False)
+    total_ms = float(sum(ev_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * nvalid * args.steps / (total_ms * 1e-3)
+
+    # end to end through the host-buffer entry point (pinned host memory)
+    h_recs = torch.from_numpy(recs.view(np.uint8).copy()).pin_memory()
+    h_prm = torch.from_numpy(prm.view(np.uint8).copy()).pin_memory()
+    h_out = {k: torch.empty((nrec, F), dtype=torch.float64).pin_memory() for k in outs}
+    out_struct = abi.Outputs()
+    import ctypes as C
+    for k in abi.OUTPUT_FIELDS:
+        setattr(out_struct, k, C.cast(C.c_void_p(h_out[k].data_ptr()), C.POINTER(C.c_double))
+                if k in h_out else C.POINTER(C.c_double)())
+    lib = _lib.load()
+    off_c = np.ascontiguousarray(off, dtype=np.int64)
+
+    def e2e_pass():
+        st = abi.Status()
+        rc = lib.pbag_run_batch(ctx.handle, C.c_void_p(h_prm.data_ptr()), nbw,
+                                off_c.ctypes.data_as(C.POINTER(C.c_int64)), C.c_void_p(h_recs.data_ptr()),
+                                C.byref(out_struct), C.byref(st))
+        if rc != 0:
+            raise _lib.PbagError(rc, "pbag_run_batch", st.bw, st.step, st.site)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_pass()
+    barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e2e_pass()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_total], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * nvalid * args.steps / e2e_total
+    h2d = int(recs.nbytes + prm.nbytes + off_c.nbytes)
+    d2h = int(nrec * F * 8 * len(outs))
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel class
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    dominant = max(timing, key=lambda k: timing[k][0])
+    ms, nl = timing[dominant]
+    launches_per_pass = max(nl // max(args.steps, 1), 1)
+    active = nvalid / launches_per_pass  # blastwaves radiating per launch, on average
+    bytes_per_launch = algorithmic_bytes(dominant, grid, active)
+    achieved = bytes_per_launch / (ms / nl * 1e-3) / 1e9 if nl else None
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(dominant)
+    except Exception:
+        pass
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "bytes_per_launch": bytes_per_launch,
+                "avg_launch_us": 1e3 * ms / nl if nl else None,
+                "kernel_share": {k: v[0] / max(sum(x[0] for x in timing.values()), 1e-12) for k, v in timing.items()},
+                "kernel_ms_per_pass": {k: v[0] / args.steps for k, v in timing.items()}}
+    threads = os.cpu_count() or 1
+    cpu_v, cpu_desc, _ = cpu_sample(recs, off, prm, grid, args.cpu_sample_seconds, threads)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+            "config": config_dict(cfg, recs, prm, {"parallelism": f"replicas{world}"}),
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_desc},
+            "wall_s_timed_region": t_wall}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gb300_arm(args)
+
+
+if __name__ == "__main__":
+    main()

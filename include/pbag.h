@@ -136,7 +136,7 @@ typedef struct pbag_status {
   int32_t code;             /* pbag_status_code                                 */
   int32_t bw;               /* blastwave index of the first failure, or -1      */
   int32_t step;             /* step index within that blastwave, or -1          */
-  int32_t reserved;
+  int32_t site;             /* diagnostics: source line of the failing device check */
 } pbag_status;
 
 /* ---- per-step shock scalars (host) --------------------------------------
@@ -231,6 +231,19 @@ int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw
 
 /* Number of kernels the last run launched (diagnostics). */
 int64_t pbag_last_launch_count(const pbag_ctx* ctx);
+
+/* Kernel classes of a step, in launch order. */
+enum pbag_kernel_class {
+  PBAG_K_EVOLVE = 0,        /* Chang-Cooper evolution + synchrotron/SSA emissivity */
+  PBAG_K_SSC = 1,           /* batched SSC contraction                          */
+  PBAG_K_FINALIZE = 2       /* photon field, totals, normalisation, histories   */
+};
+/* Enable (1) or disable (0) CUDA-event timing of every kernel launch on the
+ * context's stream; resets the accumulated totals. pbag_get_timing returns,
+ * per class, the summed device time in ms and the number of timed launches
+ * since the last reset (arrays of 3). Diagnostics only. */
+int pbag_set_timing(pbag_ctx* ctx, int enable);
+int pbag_get_timing(const pbag_ctx* ctx, double* ms, int64_t* launches);
 
 #ifdef __cplusplus
 }

@@ -18,17 +18,17 @@ _lib = None
 
 
 class PbagError(RuntimeError):
-    def __init__(self, code, what, bw=-1, step=-1):
-        self.code, self.bw, self.step = code, bw, step
+    def __init__(self, code, what, bw=-1, step=-1, site=0):
+        self.code, self.bw, self.step, self.site = code, bw, step, site
         name = abi.STATUS_NAMES.get(code, str(code))
-        where = f" (blastwave {bw}, step {step})" if bw >= 0 else ""
+        where = f" (blastwave {bw}, step {step}, check {site})" if bw >= 0 else ""
         super().__init__(f"{what}: {name} [{code}]{where}")
 
 
 def _check(rc, what, st=None):
     if rc != abi.PBAG_OK:
         if st is not None:
-            raise PbagError(rc, what, st.bw, st.step)
+            raise PbagError(rc, what, st.bw, st.step, st.site)
         raise PbagError(rc, what)
 
 
@@ -58,6 +58,8 @@ def load():
                                           C.c_void_p, P(abi.Outputs), P(abi.Status), C.c_void_p]
     lib.pbag_last_launch_count.argtypes = [C.c_void_p]
     lib.pbag_last_launch_count.restype = C.c_int64
+    lib.pbag_set_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.pbag_get_timing.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64)]
     if lib.pbag_abi_version() != 1:
         raise RuntimeError("libpbag ABI version mismatch")
     sizes = [C.sizeof(abi.GridDesc), C.sizeof(abi.ShockParams), C.sizeof(abi.StepRec),
@@ -124,6 +126,30 @@ class Context:
 
     def last_launch_count(self):
         return int(load().pbag_last_launch_count(self._h))
+
+    def set_timing(self, enable):
+        _check(load().pbag_set_timing(self._h, int(bool(enable))), "pbag_set_timing")
+
+    def timing(self):
+        """{class: (ms, launches)} for evolve, ssc, finalize since set_timing."""
+        ms = (C.c_double * 3)()
+        n = (C.c_int64 * 3)()
+        _check(load().pbag_get_timing(self._h, ms, n), "pbag_get_timing")
+        return {name: (ms[i], n[i]) for i, name in enumerate(("evolve", "ssc", "finalize"))}
+
+    def run_device(self, d_params, nbw, offsets, d_recs, d_outputs):
+        """pbag_run_batch_device: d_params / d_recs are device addresses (int),
+        d_outputs a dict name -> device address; offsets a host int64 array."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        out = abi.Outputs()
+        for f in abi.OUTPUT_FIELDS:
+            a = d_outputs.get(f)
+            setattr(out, f, C.cast(C.c_void_p(a), C.POINTER(C.c_double)) if a else C.POINTER(C.c_double)())
+        st = abi.Status()
+        rc = load().pbag_run_batch_device(self._h, C.c_void_p(d_params), int(nbw),
+                                          offsets.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          C.c_void_p(d_recs), C.byref(out), C.byref(st), None)
+        _check(rc, "pbag_run_batch_device", st)
 
     def run(self, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all")):
         """pbag_run_batch with host buffers; returns dict name -> array."""

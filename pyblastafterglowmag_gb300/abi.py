@@ -102,7 +102,7 @@ class Outputs(C.Structure):
 
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("bw", C.c_int32),
-                ("step", C.c_int32), ("reserved", C.c_int32)]
+                ("step", C.c_int32), ("site", C.c_int32)]
 
 
 def dptr(a):

@@ -59,10 +59,17 @@ struct pbag_ctx {
   double* d_out = nullptr;  // output histories (host-buffer entry point)
   size_t cap_out = 0;
   int64_t launches = 0;
+  // optional per-kernel-class timing with CUDA events on the launch stream
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;           // 2 events per timed launch
+  std::vector<int> ev_class;             // kernel class of each event pair
+  double class_ms[kKernelClasses] = {0, 0, 0};
+  int64_t class_launches[kKernelClasses] = {0, 0, 0};
 
   ~pbag_ctx() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
     for (void* p : grid_mem) cudaFree(p);
     free_state();
     cudaFree(d_recs);
@@ -97,7 +104,7 @@ struct pbag_ctx {
   }
 
   cudaError_t reserve_bw(int nbw) {
-    if (nbw <= cap_bw) return cudaSuccess;
+    if (nbw <= cap_bw && cap_bw > 0) return cudaSuccess;
     free_state();
     int cap = std::max(nbw, 64);
     cudaError_t e;
@@ -114,7 +121,7 @@ struct pbag_ctx {
     if ((e = state_alloc(&S.U32, (size_t)cap * F)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.scal, (size_t)cap * kScal)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.flags, (size_t)cap)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.err, (size_t)cap * 2)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.err, (size_t)cap * 4)) != cudaSuccess) return e;
     cap_bw = cap;
     return cudaSuccess;
   }
@@ -131,7 +138,7 @@ struct pbag_ctx {
     if ((e = cudaMemsetAsync(S.W32, 0, n * Gp * sizeof(float), stream)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(S.scal, 0, n * kScal * sizeof(double), stream)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(S.flags, 0, n * sizeof(int), stream)) != cudaSuccess) return e;
-    return cudaMemsetAsync(S.err, 0, n * 2 * sizeof(int), stream);
+    return cudaMemsetAsync(S.err, 0, n * 4 * sizeof(int), stream);
   }
 };
 
@@ -176,38 +183,63 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   int64_t max_len = 0;
   for (int b = 0; b < nbw; ++b) max_len = std::max<int64_t>(max_len, off_h[b + 1] - off_h[b]);
   c->launches = 0;
-  // any blastwave with SSC on? (read from the device copy is avoided: the
-  // contraction kernel itself skips blastwaves without SSC weights)
+  size_t nev = 0;
+  auto mark = [&](int cls, bool start) -> bool {
+    if (!c->timing) return true;
+    if (nev >= c->ev.size()) {
+      cudaEvent_t x;
+      if (cudaEventCreate(&x) != cudaSuccess) return false;
+      c->ev.push_back(x);
+      c->ev_class.push_back(0);
+    }
+    if (start) c->ev_class[nev / 2] = cls;
+    return cudaEventRecord(c->ev[nev++], c->stream) == cudaSuccess;
+  };
+  // the contraction kernel skips blastwaves without SSC weights itself
   for (int64_t s = 0; s < max_len; ++s) {
+    if (!mark(kClassEvolve, true)) return PBAG_ERR_CUDA;
     if ((e = launch_evolve_radiate(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int)s, c->stream)) != cudaSuccess)
       return PBAG_ERR_CUDA;
+    if (!mark(kClassEvolve, false)) return PBAG_ERR_CUDA;
     ++c->launches;
     if (c->ssc) {
+      if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
       if ((e = launch_ssc_contract(c->dg, c->S, nbw, c->stream)) != cudaSuccess) return PBAG_ERR_CUDA;
+      if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
       ++c->launches;
     }
+    if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
     if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
       return PBAG_ERR_CUDA;
+    if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
     ++c->launches;
   }
-  std::vector<int> err((size_t)nbw * 2);
+  std::vector<int> err((size_t)nbw * 4);
   if (nbw > 0 && cudaMemcpyAsync(err.data(), c->S.err, err.size() * sizeof(int), cudaMemcpyDeviceToHost,
                                  c->stream) != cudaSuccess)
     return PBAG_ERR_CUDA;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PBAG_ERR_CUDA;
+  for (size_t k = 0; k + 1 < nev; k += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]) != cudaSuccess) return PBAG_ERR_CUDA;
+    c->class_ms[c->ev_class[k / 2]] += ms;
+    c->class_launches[c->ev_class[k / 2]] += 1;
+  }
   // the reference stops at the first failure in time order (then blastwave order)
-  int code = PBAG_OK, fb = -1, fs = -1;
+  int code = PBAG_OK, fb = -1, fs = -1, site = 0;
   for (int b = 0; b < nbw; ++b) {
-    if (err[2 * b] != 0 && (fs < 0 || err[2 * b + 1] < fs)) {
-      code = err[2 * b];
+    if (err[4 * b] != 0 && (fs < 0 || err[4 * b + 1] < fs)) {
+      code = err[4 * b];
       fb = b;
-      fs = err[2 * b + 1];
+      fs = err[4 * b + 1];
+      site = err[4 * b + 2];
     }
   }
   if (st) {
     st->code = code;
     st->bw = fb;
     st->step = fs;
+    st->site = site;
   }
   return code;
 }
@@ -301,6 +333,7 @@ int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int
   if (st) {
     st->code = PBAG_ERR_ARG;
     st->bw = st->step = -1;
+    st->site = 0;
   }
   if (!c || !out || (nbw > 0 && (!prm || !recs))) return PBAG_ERR_ARG;
   int rc = check_batch(c, prm, nbw, off);
@@ -366,6 +399,7 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
   if (st) {
     st->code = PBAG_ERR_ARG;
     st->bw = st->step = -1;
+    st->site = 0;
   }
   if (!c || !d_out || (nbw > 0 && (!d_prm || !d_recs))) return PBAG_ERR_ARG;
   if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
@@ -383,5 +417,24 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
 }
 
 int64_t pbag_last_launch_count(const pbag_ctx* c) { return c ? c->launches : -1; }
+
+int pbag_set_timing(pbag_ctx* c, int enable) {
+  if (!c) return PBAG_ERR_ARG;
+  c->timing = enable != 0;
+  for (int k = 0; k < kKernelClasses; ++k) {
+    c->class_ms[k] = 0.;
+    c->class_launches[k] = 0;
+  }
+  return PBAG_OK;
+}
+
+int pbag_get_timing(const pbag_ctx* c, double* ms, int64_t* launches) {
+  if (!c || !ms || !launches) return PBAG_ERR_ARG;
+  for (int k = 0; k < kKernelClasses; ++k) {
+    ms[k] = c->class_ms[k];
+    launches[k] = c->class_launches[k];
+  }
+  return PBAG_OK;
+}
 
 }  // extern "C"

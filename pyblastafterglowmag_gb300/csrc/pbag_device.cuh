@@ -11,6 +11,8 @@
 namespace pbag {
 
 constexpr int kStepThreads = 128;     // threads per blastwave in the step kernels
+constexpr int kKernelClasses = 3;     // evolve, ssc, finalize (pbag_kernel_class)
+constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 constexpr int kMaxPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // gamma bins per thread
 
 // Read-only tables of one grid (one CommonTables entry), device pointers.
@@ -43,7 +45,7 @@ struct DevState {
   float* U32;      // [nbw][F]   SSC seed-photon weights, scaled to FP32
   double* scal;    // [nbw][kScal] per-step scalars handed between kernels
   int* flags;      // [nbw]      kFlag* bits
-  int* err;        // [nbw][2]   first error code and step index
+  int* err;        // [nbw][4]   first error: code, step index, check site, unused
 };
 
 enum : int {
@@ -77,8 +79,11 @@ __host__ __device__ inline double pow2_scale(double maxabs) {
 // All return the dimensionless shape R; the caller multiplies by the FP64
 // prefactor sqrt(3) q^3 B / (m_e c^2) of kernels.h:427,434,471.
 
-// Aharonian+2010 eq. D7 fit (kernels.h:420-427), x = nu / nu_crit.
+// Aharonian+2010 eq. D7 fit (kernels.h:420-427), x = nu / nu_crit. Beyond
+// x = 150 the factor exp(-x) is below the smallest FP32 subnormal, so the
+// value is 0 (this also keeps x^(4/3) from overflowing for huge x).
 __device__ __forceinline__ float aharonian_R32(float x) {
+  if (!(x <= 150.f)) return x > 150.f ? 0.f : x;  // NaN propagates
   float y = cbrtf(x);
   float y2 = y * y;
   float y4 = y2 * y2;

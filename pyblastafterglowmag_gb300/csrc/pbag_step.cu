@@ -30,8 +30,11 @@ __device__ __forceinline__ bool bad_value(double v) {  // !isfinite(v) || v < 0
 }
 
 // Record the first error of a blastwave (later ones are ignored).
-__device__ void set_error(const DevState& S, int b, int code, int step) {
-  if (atomicCAS(&S.err[2 * b], 0, code) == 0) S.err[2 * b + 1] = step;
+__device__ void set_error(const DevState& S, int b, int code, int step, int site) {
+  if (atomicCAS(&S.err[4 * b], 0, code) == 0) {
+    S.err[4 * b + 1] = step;
+    S.err[4 * b + 2] = site;
+  }
 }
 
 // microphysics.h:228-280: coefficient of the analytic broken power law,
@@ -110,7 +113,7 @@ k_evolve_radiate(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, 
 
   int flags = S.flags[b];
   const int64_t r0 = off[b], len = off[b + 1] - off[b];
-  bool active = S.err[2 * b] == 0 && step < len;
+  bool active = S.err[4 * b] == 0 && step < len;
   pbag_step_rec r;
   if (active) {
     r = recs[r0 + step];
@@ -126,7 +129,7 @@ k_evolve_radiate(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, 
 
 #define PBAG_FAIL(code)                                 \
   do {                                                  \
-    if (tid == 0) set_error(S, b, (code), step);        \
+    if (tid == 0) set_error(S, b, (code), step, __LINE__); \
     return;                                             \
   } while (0)
 
@@ -509,9 +512,9 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
     }
     S.flags[b] = fl;
     if (any_bad)
-      set_error(S, b, PBAG_ERR_NONFINITE, step);
+      set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
     else if (dense_syn && !(fl & kFlagSynSeen) && step > 0)
-      set_error(S, b, PBAG_ERR_NONFINITE, step);  // microphysics.h:627-631
+      set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);  // microphysics.h:627-631
   }
 }
 
