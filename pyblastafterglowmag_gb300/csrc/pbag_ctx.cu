@@ -3,9 +3,9 @@
 // A pbag_ctx is the device-side counterpart of one CommonTables entry of the
 // reference (microphysics/common.h:93-117): one electron grid, one photon grid
 // and the SSC kernel tables, shared read-only by every blastwave of a batch.
-// pbag_run_batch evolves the whole history of every blastwave of the batch,
-// step index by step index; at each index it launches
-//   k_evolve_radiate -> k_ssc_contract -> k_finalize
+// pbag_run_batch evolves the whole history of every blastwave of the batch:
+// one preparation pass over all records, then, step index by step index,
+//   k_evolve -> k_rad_ssc -> k_finalize
 // over all blastwaves on one stream.
 #include <cuda_runtime.h>
 
@@ -37,6 +37,11 @@ cudaError_t upload(T** p, const T* h, size_t n, cudaStream_t st) {
   return cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, st);
 }
 
+int cuda_code(cudaError_t e) { return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA; }
+
+constexpr int kOutputs = 13;  // pointers in pbag_outputs
+inline bool output_on_gamma(int fi) { return fi >= 4 && fi < 8; }
+
 }  // namespace
 
 struct pbag_ctx {
@@ -51,8 +56,10 @@ struct pbag_ctx {
   // batch buffers, grown on demand
   int cap_bw = 0;
   size_t cap_rec = 0;
-  pbag_step_rec* d_recs = nullptr;
+  pbag_step_rec* d_recs = nullptr;  // records (host-buffer entry point)
+  StepScal* d_ss = nullptr;         // per-record scalars
   int64_t* d_off = nullptr;
+  int64_t* d_first = nullptr;
   pbag_shock_params* d_prm = nullptr;
   DevState S{};
   std::vector<void*> state_mem;
@@ -61,8 +68,8 @@ struct pbag_ctx {
   int64_t launches = 0;
   // optional per-kernel-class timing with CUDA events on the launch stream
   bool timing = false;
-  std::vector<cudaEvent_t> ev;           // 2 events per timed launch
-  std::vector<int> ev_class;             // kernel class of each event pair
+  std::vector<cudaEvent_t> ev;  // 2 events per timed launch
+  std::vector<int> ev_class;    // kernel class of each event pair
   double class_ms[kKernelClasses] = {0, 0, 0};
   int64_t class_launches[kKernelClasses] = {0, 0, 0};
 
@@ -73,6 +80,7 @@ struct pbag_ctx {
     for (void* p : grid_mem) cudaFree(p);
     free_state();
     cudaFree(d_recs);
+    cudaFree(d_ss);
     cudaFree(d_out);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -80,11 +88,10 @@ struct pbag_ctx {
   void free_state() {
     for (void* p : state_mem) cudaFree(p);
     state_mem.clear();
-    cudaFree(d_off);
-    cudaFree(d_prm);
-    d_off = nullptr;
-    d_prm = nullptr;
     cap_bw = 0;
+    d_off = nullptr;
+    d_first = nullptr;
+    d_prm = nullptr;
   }
 
   template <typename T>
@@ -106,39 +113,62 @@ struct pbag_ctx {
   cudaError_t reserve_bw(int nbw) {
     if (nbw <= cap_bw && cap_bw > 0) return cudaSuccess;
     free_state();
-    int cap = std::max(nbw, 64);
+    const size_t cap = (size_t)std::max(nbw, 64);
     cudaError_t e;
-    if ((e = dev_alloc(&d_off, (size_t)cap + 1)) != cudaSuccess) return e;
-    if ((e = dev_alloc(&d_prm, (size_t)cap)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.f, (size_t)cap * G)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.dfde, (size_t)cap * G)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.gdot, (size_t)cap * 3 * G)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.n, (size_t)cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.jsyn, (size_t)cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.asyn, (size_t)cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.jssc, (size_t)cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.W32, (size_t)cap * Gp)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.U32, (size_t)cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.scal, (size_t)cap * kScal)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.flags, (size_t)cap)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.err, (size_t)cap * 4)) != cudaSuccess) return e;
-    cap_bw = cap;
+    if ((e = state_alloc(&d_off, cap + 1)) != cudaSuccess) return e;
+    if ((e = state_alloc(&d_first, cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&d_prm, cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.f, cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.dfde, cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.powp, cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.gdot, cap * 3 * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.n, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.jsyn, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.asyn, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.jssc, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.W32, cap * Gp)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.U32, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.w32, cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.v32, cap * G)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.scal, cap * kScal)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.flags, cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.err, cap * 4)) != cudaSuccess) return e;
+    cap_bw = (int)cap;
+    return cudaSuccess;
+  }
+
+  cudaError_t reserve_rec(size_t nrec, bool host_records) {
+    if (nrec > cap_rec) {
+      cudaFree(d_recs);
+      cudaFree(d_ss);
+      d_recs = nullptr;
+      d_ss = nullptr;
+      cap_rec = 0;
+      cudaError_t e;
+      if ((e = dev_alloc(&d_ss, nrec)) != cudaSuccess) return e;
+      if ((e = dev_alloc(&d_recs, nrec)) != cudaSuccess) return e;
+      cap_rec = nrec;
+    }
+    (void)host_records;
     return cudaSuccess;
   }
 
   cudaError_t reset_state(int nbw) {
     cudaError_t e;
     const size_t n = (size_t)nbw;
-    if ((e = cudaMemsetAsync(S.f, 0, n * G * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.dfde, 0, n * G * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.gdot, 0, n * 3 * G * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.n, 0, n * F * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.jssc, 0, n * F * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.U32, 0, n * F * sizeof(float), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.W32, 0, n * Gp * sizeof(float), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.scal, 0, n * kScal * sizeof(double), stream)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(S.flags, 0, n * sizeof(int), stream)) != cudaSuccess) return e;
-    return cudaMemsetAsync(S.err, 0, n * 4 * sizeof(int), stream);
+    auto z = [&](void* p, size_t bytes) {
+      return bytes ? cudaMemsetAsync(p, 0, bytes, stream) : cudaSuccess;
+    };
+    if ((e = z(S.f, n * G * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.dfde, n * G * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.gdot, n * 3 * G * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.n, n * F * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.jssc, n * F * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.U32, n * F * sizeof(float))) != cudaSuccess) return e;
+    if ((e = z(S.W32, n * Gp * sizeof(float))) != cudaSuccess) return e;
+    if ((e = z(S.scal, n * kScal * sizeof(double))) != cudaSuccess) return e;
+    if ((e = z(S.flags, n * sizeof(int))) != cudaSuccess) return e;
+    return z(S.err, n * 4 * sizeof(int));
   }
 };
 
@@ -149,6 +179,9 @@ int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, c
   if (off[0] != 0) return PBAG_ERR_ARG;
   for (int b = 0; b < nbw; ++b)
     if (off[b + 1] < off[b]) return PBAG_ERR_ARG;
+  if (nbw > 0 && off[nbw] > (int64_t)1 << 40) return PBAG_ERR_ARG;
+  for (int b = 0; b < nbw; ++b)
+    if (off[b + 1] - off[b] > (int64_t)1 << 30) return PBAG_ERR_ARG;
   if (prm_host) {
     for (int b = 0; b < nbw; ++b) {
       const pbag_shock_params& p = prm_host[b];
@@ -166,23 +199,30 @@ int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, c
 int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off_h,
                const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st) {
   cudaError_t e = c->reserve_bw(nbw);
-  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+  if (e != cudaSuccess) return cuda_code(e);
   const size_t nrec = (size_t)off_h[nbw];
+  if ((e = c->reserve_rec(nrec, false)) != cudaSuccess) return cuda_code(e);
   if ((e = cudaMemcpyAsync(c->d_off, off_h, sizeof(int64_t) * (nbw + 1), cudaMemcpyHostToDevice, c->stream)) !=
       cudaSuccess)
     return PBAG_ERR_CUDA;
   if ((e = c->reset_state(nbw)) != cudaSuccess) return PBAG_ERR_CUDA;
   // zero rows: skipped steps keep zero output rows
   const double* const* outp = reinterpret_cast<const double* const*>(&d_out);
-  for (int fi = 0; fi < 13; ++fi) {
-    if (!outp[fi]) continue;
-    const size_t n = (fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F;
+  for (int fi = 0; fi < kOutputs; ++fi) {
+    if (!outp[fi] || !nrec) continue;
+    const size_t n = output_on_gamma(fi) ? (size_t)c->G : (size_t)c->F;
     if (cudaMemsetAsync((void*)outp[fi], 0, nrec * n * sizeof(double), c->stream) != cudaSuccess)
       return PBAG_ERR_CUDA;
   }
   int64_t max_len = 0;
   for (int b = 0; b < nbw; ++b) max_len = std::max<int64_t>(max_len, off_h[b + 1] - off_h[b]);
   c->launches = 0;
+  if (nbw > 0) {
+    if ((e = launch_prepare(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int64_t)nrec, c->d_first, c->d_ss,
+                            c->stream)) != cudaSuccess)
+      return PBAG_ERR_CUDA;
+    c->launches += nrec > 0 ? 3 : 2;
+  }
   size_t nev = 0;
   auto mark = [&](int cls, bool start) -> bool {
     if (!c->timing) return true;
@@ -195,24 +235,20 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
     if (start) c->ev_class[nev / 2] = cls;
     return cudaEventRecord(c->ev[nev++], c->stream) == cudaSuccess;
   };
-  // the contraction kernel skips blastwaves without SSC weights itself
   for (int64_t s = 0; s < max_len; ++s) {
     if (!mark(kClassEvolve, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_evolve_radiate(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int)s, c->stream)) != cudaSuccess)
+    if ((e = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, c->stream)) != cudaSuccess)
       return PBAG_ERR_CUDA;
     if (!mark(kClassEvolve, false)) return PBAG_ERR_CUDA;
-    ++c->launches;
-    if (c->ssc) {
-      if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
-      if ((e = launch_ssc_contract(c->dg, c->S, nbw, c->stream)) != cudaSuccess) return PBAG_ERR_CUDA;
-      if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
-      ++c->launches;
-    }
+    if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
+    if ((e = launch_rad_ssc(c->dg, c->S, d_prm, nbw, c->ssc, (int)s, c->stream)) != cudaSuccess)
+      return PBAG_ERR_CUDA;
+    if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
     if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
     if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
       return PBAG_ERR_CUDA;
     if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
-    ++c->launches;
+    c->launches += 3;
   }
   std::vector<int> err((size_t)nbw * 4);
   if (nbw > 0 && cudaMemcpyAsync(err.data(), c->S.err, err.size() * sizeof(int), cudaMemcpyDeviceToHost,
@@ -244,6 +280,13 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   return code;
 }
 
+void reset_status(pbag_status* st) {
+  if (!st) return;
+  st->code = PBAG_ERR_ARG;
+  st->bw = st->step = -1;
+  st->site = 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -255,6 +298,7 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
       g->nfreq > PBAG_MAX_BINS || !(g->gam2 > 1.) || !(g->freq1 > 0.) || !(g->freq2 > g->freq1))
     return PBAG_ERR_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return PBAG_ERR_CUDA;
+  if (configure_kernels() != cudaSuccess) return PBAG_ERR_CUDA;
   pbag_ctx* c = new (std::nothrow) pbag_ctx();
   if (!c) return PBAG_ERR_NOMEM;
   c->device = device;
@@ -271,54 +315,83 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   c->gam.assign(G, 0.);
   c->freq.assign(F + 1, 0.);
   build_grids(g, c->gam.data(), c->freq.data());
-  // derived grids (base_state.h:229-250)
+  const std::vector<double>& e = c->gam;
+  const std::vector<double>& nu = c->freq;
+  // derived tables (base_state.h:229-250 and the per-step products of
+  // numeric_model.h / microphysics.h, tabulated once)
   const double step = std::exp(std::log(g->gam2) / (double)G);
-  std::vector<double> half(G - 1), de(G - 1), dg(G + 1), dgb(G), dnu(F);
+  std::vector<double> inv_e(G), inv_e2(G), de(G - 1), e2de(G - 1), inv_dxm(G, 0.), half2(G - 1), hadi(G - 1),
+      ihalf2(G - 1), dg(G + 1), inv_dgb(G), dnu(F), inv_hnu(F), ssa_nu(F);
   std::vector<float> ginv2(G), psq(G);
-  for (int i = 0; i < G - 1; ++i) half[i] = .5 * c->gam[i] * (step + 1.0);
-  for (int i = 0; i < G - 1; ++i) de[i] = c->gam[i + 1] - c->gam[i];
-  for (int i = 0; i < G - 1; ++i) dg[i + 1] = c->gam[i + 1] - c->gam[i];
-  dg[0] = c->gam[0] * (1 - 1.0 / step);
-  dg[G] = c->gam[G - 1] * (step - 1);
-  for (int i = 0; i < G; ++i) dgb[i] = (dg[i] + dg[i + 1]) / 2.;
+  for (int i = 0; i < G; ++i) {
+    inv_e[i] = 1. / e[i];
+    inv_e2[i] = 1. / e[i] / e[i];
+    if (i > 0) inv_dxm[i] = 1. / (e[i] - e[i - 1]);
+  }
+  for (int i = 0; i < G - 1; ++i) {
+    de[i] = e[i + 1] - e[i];
+    e2de[i] = e[i] * e[i] * (e[i + 1] - e[i]);
+    const double h = .5 * e[i] * (step + 1.0);
+    half2[i] = h * h;
+    hadi[i] = (h * h - 1.) / (3. * h);
+    ihalf2[i] = 1. / h / h;
+    dg[i + 1] = e[i + 1] - e[i];
+  }
+  dg[0] = e[0] * (1 - 1.0 / step);
+  dg[G] = e[G - 1] * (step - 1);
+  for (int i = 0; i < G; ++i) inv_dgb[i] = 1.0 / ((dg[i] + dg[i + 1]) / 2.);
   int n_cyc = 0;
   for (int i = 0; i < G; ++i) {
-    ginv2[i] = (float)(1. / (c->gam[i] * c->gam[i]));
-    psq[i] = (float)(c->gam[i] * c->gam[i] - 1.);
-    if (c->gam[i] <= 2.) n_cyc = i + 1;
+    ginv2[i] = (float)(1. / (e[i] * e[i]));
+    psq[i] = (float)(e[i] * e[i] - 1.);
+    if (e[i] <= 2.) n_cyc = i + 1;
   }
-  for (int k = 0; k < F; ++k) dnu[k] = (c->freq[k + 1] - c->freq[k]) / c->freq[k];
+  for (int k = 0; k < F; ++k) {
+    dnu[k] = (nu[k + 1] - nu[k]) / nu[k];
+    inv_hnu[k] = 1. / (cgs::h_pl * nu[k]);
+    ssa_nu[k] = -1. / (8. * M_PI * cgs::m_e * nu[k] * nu[k]);
+  }
   DevGrid& d = c->dg;
   d.G = G;
   d.F = F;
   d.Gp = c->Gp;
   d.n_cyc = n_cyc;
-  d.dlog_gam = (c->gam[1] - c->gam[0]) / c->gam[0];
-  cudaError_t e = cudaSuccess;
+  d.dlog_gam = (e[1] - e[0]) / e[0];
+  cudaError_t err = cudaSuccess;
   auto ok = [&](cudaError_t x) {
-    if (e == cudaSuccess) e = x;
+    if (err == cudaSuccess) err = x;
   };
-  ok(c->grid_upload(&d.e, c->gam));
-  ok(c->grid_upload(&d.half, half));
+  ok(c->grid_upload(&d.e, e));
+  ok(c->grid_upload(&d.inv_e, inv_e));
+  ok(c->grid_upload(&d.inv_e2, inv_e2));
   ok(c->grid_upload(&d.de, de));
-  ok(c->grid_upload(&d.dgb, dgb));
+  ok(c->grid_upload(&d.e2de, e2de));
+  ok(c->grid_upload(&d.inv_dxm, inv_dxm));
+  ok(c->grid_upload(&d.half2, half2));
+  ok(c->grid_upload(&d.hadi, hadi));
+  ok(c->grid_upload(&d.ihalf2, ihalf2));
+  ok(c->grid_upload(&d.inv_dgb, inv_dgb));
   ok(c->grid_upload(&d.ginv2, ginv2));
   ok(c->grid_upload(&d.psq32, psq));
-  ok(c->grid_upload(&d.nu, c->freq));
+  ok(c->grid_upload(&d.nu, nu));
   ok(c->grid_upload(&d.dnu_nu, dnu));
-  d.Kint = nullptr;
+  ok(c->grid_upload(&d.inv_hnu, inv_hnu));
+  ok(c->grid_upload(&d.ssa_nu, ssa_nu));
+  d.Kint32 = nullptr;
+  d.kscale = nullptr;
   d.K32 = nullptr;
   if (c->ssc) {
-    std::vector<double> Kint;
-    std::vector<float> K32;
-    build_ssc_tables(c->gam.data(), G, c->freq.data(), F, c->Gp, Kint, K32);
-    ok(c->grid_upload(&d.Kint, Kint));
+    std::vector<float> Kint32, K32;
+    std::vector<double> kscale;
+    build_ssc_tables(e.data(), G, nu.data(), F, c->Gp, Kint32, kscale, K32);
+    ok(c->grid_upload(&d.Kint32, Kint32));
+    ok(c->grid_upload(&d.kscale, kscale));
     ok(c->grid_upload(&d.K32, K32));
-    ok(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+    ok(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
   }
   ok(cudaStreamSynchronize(c->stream));
-  if (e != cudaSuccess) {
-    int code = e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+  if (err != cudaSuccess) {
+    const int code = cuda_code(err);
     delete c;
     return code;
   }
@@ -330,11 +403,7 @@ void pbag_destroy(pbag_ctx* c) { delete c; }
 
 int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int64_t* off,
                    const pbag_step_rec* recs, const pbag_outputs* out, pbag_status* st) {
-  if (st) {
-    st->code = PBAG_ERR_ARG;
-    st->bw = st->step = -1;
-    st->site = 0;
-  }
+  reset_status(st);
   if (!c || !out || (nbw > 0 && (!prm || !recs))) return PBAG_ERR_ARG;
   int rc = check_batch(c, prm, nbw, off);
   if (rc != PBAG_OK) {
@@ -344,35 +413,27 @@ int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int
   if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
   const size_t nrec = (size_t)off[nbw];
   cudaError_t e = c->reserve_bw(nbw);
-  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
-  if (nrec > c->cap_rec) {
-    cudaFree(c->d_recs);
-    c->d_recs = nullptr;
-    c->cap_rec = 0;
-    if ((e = dev_alloc(&c->d_recs, nrec)) != cudaSuccess)
-      return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
-    c->cap_rec = nrec;
-  }
+  if (e != cudaSuccess) return cuda_code(e);
+  if ((e = c->reserve_rec(nrec, true)) != cudaSuccess) return cuda_code(e);
   // device output buffers for the requested histories
   const double* const* outp = reinterpret_cast<const double* const*>(out);
   size_t need = 0;
-  for (int fi = 0; fi < 13; ++fi)
-    if (outp[fi]) need += nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+  for (int fi = 0; fi < kOutputs; ++fi)
+    if (outp[fi]) need += nrec * (output_on_gamma(fi) ? (size_t)c->G : (size_t)c->F);
   if (need > c->cap_out) {
     cudaFree(c->d_out);
     c->d_out = nullptr;
     c->cap_out = 0;
-    if ((e = dev_alloc(&c->d_out, need)) != cudaSuccess)
-      return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+    if ((e = dev_alloc(&c->d_out, need)) != cudaSuccess) return cuda_code(e);
     c->cap_out = need;
   }
   pbag_outputs dout{};
   double** dp = reinterpret_cast<double**>(&dout);
   size_t pos = 0;
-  for (int fi = 0; fi < 13; ++fi) {
+  for (int fi = 0; fi < kOutputs; ++fi) {
     if (!outp[fi]) continue;
     dp[fi] = c->d_out + pos;
-    pos += nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+    pos += nrec * (output_on_gamma(fi) ? (size_t)c->G : (size_t)c->F);
   }
   if (nrec && cudaMemcpyAsync(c->d_recs, recs, nrec * sizeof(pbag_step_rec), cudaMemcpyHostToDevice, c->stream) !=
                   cudaSuccess)
@@ -381,11 +442,11 @@ int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int
                  cudaSuccess)
     return PBAG_ERR_CUDA;
   rc = run_device(c, c->d_prm, nbw, off, c->d_recs, dout, st);
-  if (rc == PBAG_ERR_CUDA) return rc;
+  if (rc == PBAG_ERR_CUDA || rc == PBAG_ERR_NOMEM) return rc;
   // copy the histories back even on a physics error (rows before the failure are valid)
-  for (int fi = 0; fi < 13; ++fi) {
+  for (int fi = 0; fi < kOutputs; ++fi) {
     if (!outp[fi]) continue;
-    const size_t n = nrec * ((fi >= 4 && fi < 8) ? (size_t)c->G : (size_t)c->F);
+    const size_t n = nrec * (output_on_gamma(fi) ? (size_t)c->G : (size_t)c->F);
     if (n && cudaMemcpyAsync((void*)outp[fi], dp[fi], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream) !=
                  cudaSuccess)
       return PBAG_ERR_CUDA;
@@ -396,11 +457,7 @@ int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int
 
 int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
                           const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st, void* stream) {
-  if (st) {
-    st->code = PBAG_ERR_ARG;
-    st->bw = st->step = -1;
-    st->site = 0;
-  }
+  reset_status(st);
   if (!c || !d_out || (nbw > 0 && (!d_prm || !d_recs))) return PBAG_ERR_ARG;
   if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
   std::vector<pbag_shock_params> hp((size_t)std::max(nbw, 0));

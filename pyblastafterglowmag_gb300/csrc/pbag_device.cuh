@@ -10,32 +10,72 @@
 
 namespace pbag {
 
-constexpr int kStepThreads = 128;     // threads per blastwave in the step kernels
-constexpr int kKernelClasses = 3;     // evolve, ssc, finalize (pbag_kernel_class)
-constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
+constexpr int kStepThreads = 128;     // threads per blastwave in the evolve / finalize kernels
 constexpr int kMaxPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // gamma bins per thread
+constexpr int kRadThreads = 128;      // threads of one radiation CTA
+constexpr int kRadFreqs = 32;         // frequencies per radiation CTA (4 threads per frequency)
+constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
+constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 
 // Read-only tables of one grid (one CommonTables entry), device pointers.
+// Products and reciprocals the reference recomputes every step are tabulated
+// once in FP64 so that the per-step kernels use multiplications only.
 struct DevGrid {
   int G, F, Gp;          // Gp: G rounded up to a multiple of 16 (padded SSC operand)
   int n_cyc;             // number of bins with e[j] <= 2 (cyclotron branch of cycSynch)
   double dlog_gam;       // (e[1]-e[0])/e[0] (microphysics.h:413)
-  const float* psq32;    // [G]   e[j]^2 - 1 in FP32 (cyclotron branch)
   const double* e;       // [G]   gamma grid e[i] = step^i
-  const double* half;    // [G-1] half grid (base_state.h:237)
+  const double* inv_e;   // [G]   1/e
+  const double* inv_e2;  // [G]   1/e^2 (f/e/e of computeSSA, numeric_model.h:195)
   const double* de;      // [G-1] e[j+1]-e[j]
-  const double* dgb;     // [G]   delta_grid_bar (base_state.h:248-250)
+  const double* e2de;    // [G-1] e_j^2 (e_{j+1}-e_j) (numeric_model.h:208)
+  const double* inv_dxm; // [G]   1/(e_i - e_{i-1}) (base_state.h:492), 0 at i=0
+  const double* half2;   // [G-1] half grid squared (numeric_model.h:374)
+  const double* hadi;    // [G-1] (half^2-1)/(3 half) (numeric_model.h:383)
+  const double* ihalf2;  // [G-1] 1/half^2 (numeric_model.h:400)
+  const double* inv_dgb; // [G]   1/delta_grid_bar (numeric_model.h:556)
   const float* ginv2;    // [G]   1/e[j]^2 (FP32, synchrotron argument)
+  const float* psq32;    // [G]   e[j]^2 - 1 in FP32 (cyclotron branch)
   const double* nu;      // [F+1] frequency grid, nu[F] = next logspace point
   const double* dnu_nu;  // [F]   (nu[k+1]-nu[k])/nu[k]
-  const double* Kint;    // [G][F] SSC kernel integral (kernels.h:79-91), FP64
+  const double* inv_hnu; // [F]   1/(h nu) (microphysics.h:520)
+  const double* ssa_nu;  // [F]   -1/(8 pi m_e nu^2) (numeric_model.h:211)
+  const float* Kint32;   // [G][F] SSC kernel integral / kscale[k] (kernels.h:79-91)
+  const double* kscale;  // [F]   power-of-two column scales of Kint32
   const float* K32;      // [F][Gp][F] SSC kernel (i, j, k) in FP32, j >= G zero
+};
+
+// Per-record scalars of one step, computed once for the whole batch by
+// k_prep (the reference recomputes them inside each step).
+struct StepScal {
+  double K;          // power-law normalisation K_s / K_f (microphysics.h:237-263)
+  double c_fast;     // gamma_min^(1-p) (fast-cooling lower branch)
+  double Ns;         // N_inj * norm: source amplitude (numeric_model.h:718-721)
+  double dt_sub;     // substep length (microphysics.h:416-431)
+  double dlnVdt;     // (microphysics.h:405)
+  double dr, vol;    // dr_comov and source.vol of this step
+  double pref;       // synchrotron prefactor sqrt(3) q^3 B / (m_e c^2) (kernels.h:427,471)
+  float inv_ncrit;   // 1 / nu_crit(B, gamma=1) (kernels.h:194-197)
+  float inv_nlar;    // 1 / nu_larmor(B) (kernels.h:199-202)
+  int n_sub;         // Chang-Cooper substeps; 0 = analytic distribution this step
+  int flags;         // kRec* bits
+  int err, site;     // error the record alone triggers (0 = none) and its check site
+  int ia0, ia1;      // first branch of the analytic distribution: bins [ia0, ia1)
+  int ib0, ib1;      // second branch: bins [ib0, ib1)
+  int iq0, iq1;      // injection (source) bins [iq0, iq1)
+};
+
+enum : int {
+  kRecValid = 1,     // the blastwave is valid at this step
+  kRecInit = 2,      // first valid step: initializeElectronDistribution
+  kRecFast = 4,      // fast-cooling branch (gamma_min > gamma_c)
 };
 
 // Per-blastwave state that lives across steps (structure of arrays).
 struct DevState {
   double* f;       // [nbw][G]   N(gamma) (ele.f)
   double* dfde;    // [nbw][G]   d(f/gamma^2)/dgamma, stateful (base_state.h:482-536)
+  double* powp;    // [nbw][G]   e^-p of the blastwave's injection index
   double* gdot;    // [nbw][3][G] gam_dot_syn, _adi, _ssc (last substep)
   double* n;       // [nbw][F]   photon density total_rad.f of the previous step
   double* jsyn;    // [nbw][F]   synchrotron emissivity of this step
@@ -43,6 +83,8 @@ struct DevState {
   double* jssc;    // [nbw][F]   SSC emissivity of this step
   float* W32;      // [nbw][Gp]  SSC electron weights, scaled to FP32
   float* U32;      // [nbw][F]   SSC seed-photon weights, scaled to FP32
+  float* w32;      // [nbw][G]   synchrotron weights f_j (e_{j+1}-e_j), scaled
+  float* v32;      // [nbw][G]   SSA weights e_j^2 (e_{j+1}-e_j) dfde_j, scaled
   double* scal;    // [nbw][kScal] per-step scalars handed between kernels
   int* flags;      // [nbw]      kFlag* bits
   int* err;        // [nbw][4]   first error: code, step index, check site, unused
@@ -57,7 +99,12 @@ enum : int {
   kScalAcc = 5,    // accel_frac of this step
   kScalNp = 6,     // n_prime of this step
   kScalNsub = 7,   // substeps taken (diagnostic)
-  kScal = 8
+  kScalSw = 8,     // scale of w32
+  kScalSv = 9,     // scale of v32
+  kScalPref = 10,  // synchrotron prefactor of this step
+  kScalIncrit = 11,  // 1/nu_crit(B,1) of this step
+  kScalInlar = 12,   // 1/nu_larmor(B) of this step
+  kScal = 16
 };
 
 enum : int {
@@ -67,9 +114,10 @@ enum : int {
   kFlagUValid = 8    // U32/sU hold the previous step's photon field
 };
 
-// Power of two close to 1/max|x| (exact rescaling); 1 when max is 0 or not finite.
+// Power of two close to 1/max|x| (exact rescaling); 1 when max is 0, not
+// finite, or so small that the inverse would overflow.
 __host__ __device__ inline double pow2_scale(double maxabs) {
-  if (!(maxabs > 0.) || !(maxabs < 1.e308)) return 1.;
+  if (!(maxabs > 1.e-300) || !(maxabs < 1.e300)) return 1.;
   int ex;
   frexp(maxabs, &ex);
   return ldexp(1., -ex);
@@ -89,18 +137,12 @@ __device__ __forceinline__ float aharonian_R32(float x) {
   float y4 = y2 * y2;
   float num = fmaf(0.347f, y4, fmaf(2.21f, y2, 1.f));
   float den = fmaf(0.217f, y4, fmaf(1.353f, y2, 1.f));
-  return 1.808f * y * rsqrtf(fmaf(3.4f, y2, 1.f)) * num / den * expf(-x);
+  return 1.808f * y * rsqrtf(fmaf(3.4f, y2, 1.f)) * __fdividef(num, den) * expf(-x);
 }
 
-// Chebyshev recurrence (kernels.h:158-173) on [-1,1].
-__device__ __forceinline__ float cheb32(const float* c, int order, float t) {
-  float d = 0.f, dd = 0.f, y2 = 2.f * t;
-  for (int j = order; j > 0; j--) {
-    float tmp = d;
-    d = fmaf(y2, d, -dd) + c[j];
-    dd = tmp;
-  }
-  return fmaf(t, d, -dd) + 0.5f * c[0];
+// Cyclotron branch of cycSynch (kernels.h:428-435) for gamma <= 2.
+__device__ __forceinline__ float cyclotron_R32(float psq, float xl) {
+  return (2.f * psq) / (1.f + 3.f * psq) * expf((2.f * (1.f - xl)) / (1.f + 3.f * psq));
 }
 
 }  // namespace pbag

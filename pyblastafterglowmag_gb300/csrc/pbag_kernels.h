@@ -10,16 +10,25 @@
 
 namespace pbag {
 
-cudaError_t launch_evolve_radiate(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
-                                  const pbag_shock_params* prm, int nbw, int step, cudaStream_t st);
+// once per batch: init steps, e^-p tables, per-record scalars
+cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
+                           const pbag_shock_params* prm, int nbw, int64_t nrec, int64_t* first, StepScal* ss,
+                           cudaStream_t st);
+// every step
+cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
+                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step, cudaStream_t st);
+cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
+                           int step, cudaStream_t st);
 cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* off, const pbag_shock_params* prm,
                             int nbw, int step, const pbag_outputs& out, cudaStream_t st);
-cudaError_t launch_ssc_contract(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st);
+// kernel attributes (dynamic shared memory limits); call once per device
+cudaError_t configure_kernels();
 
-// SSC kernel tables on the host (kernels.h:49-117): Kint[G][F] in FP64 and
-// K32[F][Gp][F] (i, j, k) in FP32, j >= G zero-padded.
-void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, std::vector<double>& Kint,
-                      std::vector<float>& K32);
+// SSC kernel tables on the host (kernels.h:49-117): Kint32[G][F] = Kint / kscale[k]
+// with power-of-two column scales, and K32[F][Gp][F] (i, j, k) in FP32,
+// j >= G zero-padded.
+void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, std::vector<float>& Kint32,
+                      std::vector<double>& kscale, std::vector<float>& K32);
 
 }  // namespace pbag
 

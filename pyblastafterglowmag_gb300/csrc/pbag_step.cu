@@ -1,23 +1,28 @@
-// pbag_step.cu - per-blastwave kernels of one comoving-radiation step.
+// pbag_step.cu - the kernels of one comoving-radiation step.
 //
-//   k_evolve_radiate : evaluateElectronDistributionNumericMixed (microphysics.h:359-489)
-//                      or initializeElectronDistribution (microphysics.h:347-357),
-//                      then the synchrotron part of computeRadiationNumericMixed
-//                      (microphysics.h:498-506): kernel, j_syn, SSA, N_e, SSC weights.
-//   k_finalize       : the rest of computeRadiationNumericMixed (microphysics.h:516-599)
-//                      and storeDenseOutput (:602-633): photon field, totals,
-//                      normalisation, intensity, history rows.
-// The SSC contraction between them lives in pbag_ssc.cu.
-//
-// One CTA of 128 threads (4 warps, one per SM sub-partition) owns one
-// blastwave. The Chang-Cooper substeps run as a systolic pipeline: thread t
-// owns c = ceil(G/128) consecutive gamma bins and processes substep m at tick
-// m + (T-1-t), one tick after the thread above it produced the bin it needs.
-// The recurrence stays in FP64.
+// Once per batch:
+//   k_first_valid : first valid record of every blastwave (its init step)
+//   k_powp        : e_i^-p per blastwave (injection index p is per blastwave)
+//   k_prep        : every per-record scalar of evaluateElectronDistributionNumericMixed
+//                   (microphysics.h:359-489) and initializeElectronDistribution
+//                   (:347-357) that depends on the record alone, all records in
+//                   parallel: power-law normalisation and bin ranges, dlnV/dt,
+//                   substep count and length, injection amplitude, synchrotron
+//                   prefactors, and the exit conditions those lines check.
+// Every step (one launch each over all blastwaves):
+//   k_evolve      : the state-dependent part of the evolution - analytic
+//                   distribution, or cooling terms (numeric_model.h:753-801) and
+//                   the Chang-Cooper substeps (:539-708) - then N_e and the FP32
+//                   weights of the synchrotron, SSA and SSC sums.
+//   k_rad_ssc     : the O(F G) synchrotron and SSA sums (numeric_model.h:148-238)
+//                   and the O(F^2 G) SSC contraction (pbag_ssc.cu), in one launch.
+//   k_finalize    : photon field, totals, normalisation, intensity and history
+//                   rows (microphysics.h:516-633).
 #include <cuda_runtime.h>
 
 #include "pbag_device.cuh"
 #include "pbag_kernels.h"
+#include "pbag_ssc.cuh"
 
 namespace pbag {
 
@@ -37,37 +42,22 @@ __device__ void set_error(const DevState& S, int b, int code, int step, int site
   }
 }
 
-// microphysics.h:228-280: coefficient of the analytic broken power law,
-// K_f (fast cooling, gm > gc) or K_s (slow cooling).
-__device__ double power_law_norm(double gm, double gc, double gM, double p, double n_inj) {
-  if (gm > gc)
-    return n_inj / (pow(gm, 1. - p) * (1. / gc - 1. / gm) + 1. / p * (pow(gm, -p) - pow(gM, -p)));
-  return n_inj / ((1. / (1. - p)) * (pow(gc, 1. - p) - pow(gm, 1. - p)) - gc / p * (pow(gM, -p) - pow(gc, -p)));
-}
-
-// Entry of the analytic distribution at gamma g; false when the reference
-// leaves the entry untouched (neither branch applies).
-__device__ bool power_law_at(double g, double gm, double gc, double gM, double p, double K, double& v) {
-  if (gm > gc) {
-    if ((gc <= g) && (g < gm)) {
-      v = K * pow(gm, 1. - p) * pow(g, -2.);
-      return true;
-    }
-    if ((gm < g) && (g <= gM)) {
-      v = K * pow(g, -p - 1.);
-      return true;
-    }
-  } else {
-    if ((gm <= g) && (g < gc)) {
-      v = K * pow(g, -p);
-      return true;
-    }
-    if ((gc <= g) && (g <= gM)) {
-      v = K * gc * pow(g, -p - 1.);
-      return true;
-    }
+// first index with e[i] >= x (lower bound) / e[i] > x (upper bound)
+__device__ int lower_bound_e(const double* e, int G, double x) {
+  int lo = 0, hi = G;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (e[mid] < x) lo = mid + 1; else hi = mid;
   }
-  return false;
+  return lo;
+}
+__device__ int upper_bound_e(const double* e, int G, double x) {
+  int lo = 0, hi = G;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (e[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
 }
 
 template <typename T>
@@ -94,19 +84,181 @@ __device__ T block_max(T v, T* red) {
   return r;
 }
 
+// Error-free transformation a + b = s + e (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
+__global__ void k_first_valid(const pbag_step_rec* __restrict__ recs, const int64_t* __restrict__ off, int nbw,
+                              int64_t* __restrict__ first) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbw) return;
+  int64_t r = off[b];
+  const int64_t end = off[b + 1];
+  while (r < end && recs[r].mode == PBAG_SKIP) ++r;
+  first[b] = r;  // == end when the blastwave is never valid
+}
+
+__global__ void k_powp(DevGrid g, const pbag_shock_params* __restrict__ prm, int nbw, double* __restrict__ powp) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nbw * g.G) return;
+  const int b = (int)(idx / g.G), i = (int)(idx - (int64_t)b * g.G);
+  powp[idx] = pow(g.e[i], -prm[b].p);
+}
+
+// Value of the analytic distribution (microphysics.h:237-278) at bin i, given
+// that i lies in branch a (first) or b (second).
+__device__ __forceinline__ double pl_branch_a(const DevGrid& g, const StepScal& s, const double* pp, int i) {
+  return (s.flags & kRecFast) ? s.K * s.c_fast * g.inv_e2[i] : s.K * pp[i];
+}
+__device__ __forceinline__ double pl_branch_b(const DevGrid& g, const StepScal& s, const double* pp, int i,
+                                              double Kb) {
+  return Kb * pp[i] * g.inv_e[i];
+}
+
+__global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const int64_t* __restrict__ off,
+                       const pbag_shock_params* __restrict__ prm, int nbw, int64_t nrec,
+                       const int64_t* __restrict__ first, const double* __restrict__ powp,
+                       StepScal* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  int lo = 0, hi = nbw;  // blastwave owning record r: last b with off[b] <= r
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= r) lo = mid; else hi = mid;
+  }
+  const int b = lo;
+  const pbag_step_rec q = recs[r];
+  StepScal s = {};
+  if (q.mode == PBAG_SKIP) {
+    out[r] = s;
+    return;
+  }
+  const pbag_shock_params P = prm[b];
+  const int G = g.G;
+  const double* pp = powp + (size_t)b * G;
+  s.flags = kRecValid;
+  const bool init = r == first[b];
+  if (init) s.flags |= kRecInit;
+  const double gm = q.gamma_min, gc = q.gamma_c, gM = q.gamma_max, p = P.p;
+  // powerLawElectronDistributionAnalytic (microphysics.h:228-280), n_inj = m/m_p
+  const double n_inj = q.m_p1 / m_p;
+  const bool fast = gm > gc;
+  double Kb;
+  if (fast) {
+    s.flags |= kRecFast;
+    s.K = n_inj / (pow(gm, 1. - p) * (1. / gc - 1. / gm) + 1. / p * (pow(gm, -p) - pow(gM, -p)));
+    s.c_fast = pow(gm, 1. - p);
+    s.ia0 = lower_bound_e(g.e, G, gc);  // gc <= gamma < gm
+    s.ia1 = lower_bound_e(g.e, G, gm);
+    s.ib0 = upper_bound_e(g.e, G, gm);  // gm < gamma <= gM
+    s.ib1 = upper_bound_e(g.e, G, gM);
+    Kb = s.K;
+  } else {
+    s.K = n_inj / ((1. / (1. - p)) * (pow(gc, 1. - p) - pow(gm, 1. - p)) - gc / p * (pow(gM, -p) - pow(gc, -p)));
+    s.c_fast = 0.;
+    s.ia0 = lower_bound_e(g.e, G, gm);  // gm <= gamma < gc
+    s.ia1 = lower_bound_e(g.e, G, gc);
+    s.ib0 = lower_bound_e(g.e, G, gc);  // gc <= gamma <= gM
+    s.ib1 = upper_bound_e(g.e, G, gM);
+    Kb = s.K * gc;
+  }
+  if (s.ia1 < s.ia0) s.ia1 = s.ia0;
+  if (s.ib1 < s.ib0) s.ib1 = s.ib0;
+  // the reference exits when an assigned entry is not finite or negative; the
+  // entries of each branch decrease with gamma, so its first entry decides
+  bool pl_bad = (s.ia1 > s.ia0 && bad_value(pl_branch_a(g, s, pp, s.ia0))) ||
+                (s.ib1 > s.ib0 && bad_value(pl_branch_b(g, s, pp, s.ib0, Kb)));
+  // synchrotron kernel constants (kernels.h:194-202, 427, 471)
+  const double B = q.B;
+  const bool dermer = P.syn_method == PBAG_SYN_DER09;
+  s.pref = dermer ? sqrt3 * pow(q_e, 3.) * B / (m_e * c_light * c_light) : sqrt3 * pow(q_e, 3.) * B / mec2;
+  s.inv_ncrit = (float)((4. * M_PI * m_e * c_light) / (3. * q_e * B));
+  s.inv_nlar = (float)((2. * pi_ * m_e * c_light) / (3. * q_e * B));
+  s.dr = q.dr;
+  if (init) {
+    s.vol = q.m_p1 / q.rho_p1;
+    if (pl_bad) {
+      s.err = PBAG_ERR_NONFINITE;
+      s.site = __LINE__;
+    } else if (B < 0) {  // evalSynKernel (kernels.h:529-532)
+      s.err = PBAG_ERR_PARAM;
+      s.site = __LINE__;
+    }
+    out[r] = s;
+    return;
+  }
+  // evaluateElectronDistributionNumericMixed (microphysics.h:372-435)
+  if ((B <= 0) || (gm < 1.) || (gM <= 1.) || (gm >= gM) || (q.accel_frac > 1.)) {
+    s.err = PBAG_ERR_PARAM;
+    s.site = __LINE__;
+    out[r] = s;
+    return;
+  }
+  if (pl_bad) {
+    s.err = PBAG_ERR_NONFINITE;
+    s.site = __LINE__;
+    out[r] = s;
+    return;
+  }
+  const double dt = q.tc_p1 - q.tc;
+  const double volume = q.m / q.rho;
+  const double volume_p1 = q.m_p1 / q.rho_p1;
+  const double dlnVdt = P.adi_on ? 1. / dt * (1. - volume / volume_p1) : 0.;
+  if ((!isfinite(dlnVdt)) || (dlnVdt < 0)) {
+    s.err = PBAG_ERR_DLNVDT;
+    s.site = __LINE__;
+    out[r] = s;
+    return;
+  }
+  s.dlnVdt = dlnVdt;
+  const double dts = sigma_T * gM * B * B / (6. * M_PI * m_e * c_light);
+  const double dta = (gM * gM - 1.) / (3. * gM * gM) * dlnVdt;
+  double delta_t = g.dlog_gam / (dts + dta);
+  int n_sub;
+  const int max_sub = P.max_substeps;
+  if (delta_t >= dt / 1.) {
+    delta_t = dt / 1.;
+    n_sub = 1;
+  } else if (delta_t < dt / (double)max_sub) {
+    delta_t = dt / (double)max_sub;
+    n_sub = max_sub;
+  } else {
+    n_sub = (int)(dt / delta_t);
+  }
+  s.vol = volume;
+  if (P.ele_method == PBAG_ELE_MIX || gm <= 2) {
+    s.n_sub = 0;  // analytic distribution replaces the evolution (microphysics.h:446-448)
+  } else {
+    s.n_sub = n_sub;
+    s.dt_sub = delta_t;
+    const double Nsrc = (q.m_p1 - q.m) / m_p / dt;
+    const double index = -p;
+    const double norm = (1 + index) / (pow(gM, index + 1) - pow(gm, index + 1));
+    s.Ns = Nsrc * norm;
+    s.iq0 = upper_bound_e(g.e, G, gm);  // gm < gamma <= gM (numeric_model.h:720)
+    s.iq1 = upper_bound_e(g.e, G, gM);
+    if (s.iq1 < s.iq0) s.iq1 = s.iq0;
+  }
+  out[r] = s;
+}
+
+// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kStepThreads)
-k_evolve_radiate(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const int64_t* __restrict__ off,
-                 const pbag_shock_params* __restrict__ prm, int step) {
+k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const StepScal* __restrict__ ss,
+         const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step) {
   const int b = blockIdx.x;
   const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
   __shared__ double sh_f[PBAG_MAX_BINS];   // heating term, then N(gamma)
-  __shared__ double sh_u[PBAG_MAX_BINS];   // seed-photon weights (FP64)
-  __shared__ double sh_v[PBAG_MAX_BINS];   // SSA weights
-  __shared__ float sh_w[PBAG_MAX_BINS];    // synchrotron weights (FP32, scaled)
+  __shared__ double sh_t[PBAG_MAX_BINS];   // f / gamma^2
+  __shared__ double sh_vd[PBAG_MAX_BINS];  // SSA weights
+  __shared__ float sh_v[PBAG_MAX_BINS];    // seed-photon weights for the SSC cooling GEMV
   __shared__ double red_d[kStepThreads / 32];
   __shared__ double xfer[2][kStepThreads / 32];
   __shared__ int sh_bad;
@@ -114,314 +266,314 @@ k_evolve_radiate(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, 
   int flags = S.flags[b];
   const int64_t r0 = off[b], len = off[b + 1] - off[b];
   bool active = S.err[4 * b] == 0 && step < len;
-  pbag_step_rec r;
+  StepScal sc;
   if (active) {
-    r = recs[r0 + step];
-    active = r.mode != PBAG_SKIP;
+    sc = ss[r0 + step];
+    active = (sc.flags & kRecValid) != 0;
   }
   if (tid == 0) sh_bad = 0;
   __syncthreads();  // every thread has read flags before thread 0 rewrites them
   if (tid == 0) S.flags[b] = flags & ~kFlagActive;
   if (!active) return;
-  const pbag_shock_params P = prm[b];
-  double* f = S.f + (size_t)b * G;
-  double* scal = S.scal + (size_t)b * kScal;
 
-#define PBAG_FAIL(code)                                 \
-  do {                                                  \
-    if (tid == 0) set_error(S, b, (code), step, __LINE__); \
-    return;                                             \
+#define PBAG_FAIL(code, site)                            \
+  do {                                                   \
+    if (tid == 0) set_error(S, b, (code), step, (site)); \
+    return;                                              \
   } while (0)
 
-  double dr_comov, vol;
-  int nsub_taken = 0;
-  if (!(flags & kFlagInit)) {
-    // ---- initializeElectronDistribution (microphysics.h:347-357)
-    dr_comov = r.dr;
-    vol = r.m_p1 / r.rho_p1;
-    const double K = power_law_norm(r.gamma_min, r.gamma_c, r.gamma_max, P.p, r.m_p1 / m_p);
-    bool bad = false;
+  if (sc.err) PBAG_FAIL(sc.err, sc.site);
+  const pbag_step_rec& r = recs[r0 + step];
+  const double accel = r.accel_frac, B = r.B;
+  const pbag_shock_params P = prm[b];
+  double* f = S.f + (size_t)b * G;
+  const double* pp = S.powp + (size_t)b * G;
+  const double Kb = (sc.flags & kRecFast) ? sc.K : sc.K * r.gamma_c;
+
+  if (sc.flags & kRecInit) {
+    // ---- initializeElectronDistribution (microphysics.h:347-357): untouched
+    // entries keep their value, then all but the last bin scale by accel_frac
     for (int i = tid; i < G; i += kStepThreads) {
-      double v;
-      double fi = power_law_at(g.e[i], r.gamma_min, r.gamma_c, r.gamma_max, P.p, K, v) ? v : f[i];
-      if (bad_value(fi)) bad = true;
-      if (i < G - 1) fi *= r.accel_frac;
-      f[i] = fi;
+      double v = f[i];
+      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(g, sc, pp, i);
+      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
+      if (i < G - 1) v *= accel;
+      f[i] = v;
     }
-    if (bad) atomicOr(&sh_bad, 1);
-    __syncthreads();
-    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE);
     flags |= kFlagInit;
-  } else {
-    // ---- evaluateElectronDistributionNumericMixed (microphysics.h:359-489)
-    if ((r.B <= 0) || (r.gamma_min < 1.) || (r.gamma_max <= 1.) || (r.gamma_min >= r.gamma_max) ||
-        (r.accel_frac > 1.))
-      PBAG_FAIL(PBAG_ERR_PARAM);
-    dr_comov = r.dr;
-    const double gm = r.gamma_min, gM = r.gamma_max, gc = r.gamma_c, p = P.p;
-    const double K = power_law_norm(gm, gc, gM, p, r.m_p1 / m_p);
-    const double dt = r.tc_p1 - r.tc;
-    const double volume = r.m / r.rho;
-    const double volume_p1 = r.m_p1 / r.rho_p1;
-    const double dlnVdt = P.adi_on ? 1. / dt * (1. - volume / volume_p1) : 0.;
-    const bool analytic = P.ele_method == PBAG_ELE_MIX || gm <= 2;
-    // the analytic distribution is always evaluated (microphysics.h:389-390)
-    // and the reference exits if an assigned entry is not finite or negative
-    bool bad = false;
+  } else if (sc.n_sub == 0) {
+    // ---- analytic distribution (microphysics.h:446-448)
     for (int i = tid; i < G; i += kStepThreads) {
       double v = 0.;
-      const bool set = power_law_at(g.e[i], gm, gc, gM, p, K, v);
-      if (set && bad_value(v)) bad = true;
-      if (analytic) f[i] = set ? v : 0.;
+      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(g, sc, pp, i);
+      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
+      f[i] = v;
     }
-    if (bad) atomicOr(&sh_bad, 1);
+  } else {
+    // ---- Chang-Cooper evolution (microphysics.h:451-480)
+    const bool ssc = P.ssc_on && g.K32 != nullptr;
+    const double delta_t = sc.dt_sub;
+    const int n_sub = sc.n_sub;
+    double sv = 1.;
+    if (ssc) {  // seed-photon weights n_k dnu_k / nu_k, scaled by the kernel-integral columns
+      const double* n = S.n + (size_t)b * F;
+      double vmax = 0.;
+      for (int k = tid; k < F - 1; k += kStepThreads) vmax = fmax(vmax, n[k] * g.dnu_nu[k] * g.kscale[k]);
+      vmax = block_max(vmax, red_d);
+      sv = pow2_scale(vmax);
+      for (int k = tid; k < F; k += kStepThreads)
+        sh_v[k] = k < F - 1 ? (float)(n[k] * g.dnu_nu[k] * g.kscale[k] * sv) : 0.f;
+    }
     __syncthreads();
-    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE);
-    if ((!isfinite(dlnVdt)) || (dlnVdt < 0)) PBAG_FAIL(PBAG_ERR_DLNVDT);
-    // substep count (microphysics.h:412-435)
-    const double dts = sigma_T * gM * r.B * r.B / (6. * M_PI * m_e * c_light);
-    const double dta = (gM * gM - 1.) / (3. * gM * gM) * dlnVdt;
-    double delta_t = g.dlog_gam / (dts + dta);
-    int n_sub;
-    const int max_sub = P.max_substeps;
-    if (delta_t >= dt / 1.) {
-      delta_t = dt / 1.;
-      n_sub = 1;
-    } else if (delta_t < dt / (double)max_sub) {
-      delta_t = dt / (double)max_sub;
-      n_sub = max_sub;
-    } else {
-      n_sub = (int)(dt / delta_t);
-    }
-    vol = volume;
-    if (!analytic) {
-      nsub_taken = n_sub;
-      const double Nsrc = (r.m_p1 - r.m) / m_p / dt;
-      const double index = -p;
-      const double norm = (1 + index) / (pow(gM, index + 1) - pow(gm, index + 1));
-      const bool ssc = P.ssc_on && g.K32 != nullptr;
-      // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k of the previous step
+    // heating / cooling terms at the half grid (numeric_model.h:753-801);
+    // constant over the substeps, so evaluated once per step
+    const double c_syn = sigma_T / (6. * M_PI * m_e * c_light) * B * B;
+    const double c_ssc = 3. / 4. * h_pl * sigma_T / m_e / c_light / sv;
+    double* gsyn = S.gdot + (size_t)b * 3 * G;
+    double* gadi = gsyn + G;
+    double* gssc = gadi + G;
+    bool hbad = false;
+    for (int i = tid; i < G - 1; i += kStepThreads) {
+      const double vs = c_syn * g.half2[i];
+      const double va = sc.dlnVdt * g.hadi[i];
+      double vc = gssc[i];
       if (ssc) {
-        const double* n = S.n + (size_t)b * F;
-        for (int k = tid; k < F; k += kStepThreads) sh_u[k] = n[k] / g.nu[k] * (g.nu[k + 1] - g.nu[k]);
+        const float* kr = g.Kint32 + (size_t)i * F;
+        float acc = 0.f;
+        for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], __ldg(kr + k), acc);
+        vc = c_ssc * (double)acc * g.ihalf2[i];
+        gssc[i] = vc;
       }
-      __syncthreads();
-      // heating / cooling terms at the half grid (numeric_model.h:753-801);
-      // constant over the substeps, so evaluated once per step
-      const double c_syn = sigma_T / (6. * M_PI * m_e * c_light);
-      const double c_ssc = 3. / 4. * h_pl * sigma_T / m_e / c_light;
-      double* gsyn = S.gdot + (size_t)b * 3 * G;
-      double* gadi = gsyn + G;
-      double* gssc = gadi + G;
-      bool hbad = false;
-      for (int i = tid; i < G - 1; i += kStepThreads) {
-        const double ga = g.half[i];
-        const double vs = c_syn * r.B * r.B * ga * ga;
-        const double va = dlnVdt * (ga * ga - 1.) / (3. * ga);
-        double vc = gssc[i];
-        if (ssc) {
-          const double* kr = g.Kint + (size_t)i * F;
-          double res = 0;
-          for (int k = 0; k < F - 1; k++) res = fma(sh_u[k], kr[k], res);
-          vc = c_ssc * res / ga / ga;
-          gssc[i] = vc;
-        }
-        gsyn[i] = vs;
-        gadi[i] = va;
-        const double H = vs + va + vc;
-        if (!isfinite(H)) hbad = true;
-        sh_f[i] = H;
-      }
-      if (tid == 0) sh_f[G - 1] = 0.;  // heating_term[G-1] is never set (numeric_model.h:761)
-      if (hbad) atomicOr(&sh_bad, 1);
-      __syncthreads();
-      if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE);
-      // tridiagonal coefficients (numeric_model.h:539-675 with dispersion = 0,
-      // delta_j = 0): a = 0, b_k = 1 + dt H_{k-1}/dgb_k (b_0 = b_{G-1} = 1),
-      // c_k = -dt H_k/dgb_k (c_{G-1} = 0). Each substep is the back
-      // substitution f_k = (f_k + Q_k dt)/b_k - (c_k/b_k) f_{k+1}
-      // (numeric_model.h:19-43, 682-708).
-      const int c = (G + kStepThreads - 1) / kStepThreads;
-      const int T = (G + c - 1) / c;  // threads that own bins
-      double fr[kMaxPerThread], ib[kMaxPerThread], qb[kMaxPerThread], bt[kMaxPerThread];
-#pragma unroll
-      for (int q = 0; q < kMaxPerThread; ++q) {
-        const int j = tid * c + q;
-        fr[q] = ib[q] = qb[q] = bt[q] = 0.;
-        if (q < c && j < G) {
-          const double odgb = 1.0 / g.dgb[j];
-          double braw, craw;
-          if (j == 0) {
-            braw = -odgb * ((0. + 0.) + 0. * 0. - 0. * sh_f[0]);
-            craw = odgb * (1. * sh_f[0] + 0.);
-          } else if (j == G - 1) {
-            braw = -odgb * ((0. + 0.) + 1. * sh_f[G - 1] - 0.);
-            craw = 0.;
-          } else {
-            braw = -odgb * ((0. + 0.) + 1. * sh_f[j - 1] - 0. * sh_f[j]);
-            craw = odgb * (1. * sh_f[j] + 0.);
-          }
-          const double bb = (1. - braw * delta_t) + 0. * delta_t;
-          const double cc = craw * -delta_t;
-          const double Q = ((g.e[j] > gm) && (g.e[j] <= gM)) ? Nsrc * norm * pow(g.e[j], index) : 0.;
-          ib[q] = 1. / bb;
-          bt[q] = -(cc / bb);
-          qb[q] = (Q * delta_t) / bb;
-          fr[q] = f[j];
-        }
-      }
-      // systolic substeps: thread t handles substep m = tau - (T-1-t)
-      const int lane = tid & 31, warp = tid >> 5;
-      if (tid < 2 * (kStepThreads / 32)) (&xfer[0][0])[tid] = 0.;
-      __syncthreads();
-      double low = 0.;
-      bool sbad = false;
-      const int ticks = n_sub + T - 1;
-      for (int tau = 0; tau < ticks; ++tau) {
-        double up = __shfl_down_sync(0xffffffffu, low, 1);
-        if (lane == 31) up = warp + 1 < kStepThreads / 32 ? xfer[tau & 1][warp + 1] : 0.;
-        const int m = tau - (T - 1 - tid);
-        if (tid < T && m >= 0 && m < n_sub) {
-          double fn = up;
-#pragma unroll
-          for (int q = kMaxPerThread - 1; q >= 0; --q) {
-            if (q < c) {
-              sbad |= bad_value(fr[q]);  // solve() checks f before each substep (numeric_model.h:688)
-              const double a = fma(fr[q], ib[q], qb[q]);
-              fr[q] = fma(bt[q], fn, a);
-              fn = fr[q];
-            }
-          }
-          low = fr[0];
-        }
-        if (lane == 0) xfer[(tau + 1) & 1][warp] = low;
-        __syncthreads();
-      }
-      if (sbad) atomicOr(&sh_bad, 1);
-#pragma unroll
-      for (int q = 0; q < kMaxPerThread; ++q) {
-        const int j = tid * c + q;
-        if (q < c && j < G) f[j] = fr[q];
-      }
-      __syncthreads();
-      if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE);
+      gsyn[i] = vs;
+      gadi[i] = va;
+      const double H = vs + va + vc;
+      if (!isfinite(H)) hbad = true;
+      sh_f[i] = H;
     }
+    if (tid == 0) sh_f[G - 1] = 0.;  // heating_term[G-1] is never set (numeric_model.h:761)
+    if (hbad) atomicOr(&sh_bad, 1);
+    __syncthreads();
+    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
+    // tridiagonal coefficients (numeric_model.h:539-675 with dispersion = 0,
+    // delta_j = 0): a = 0, b_k = 1 + dt H_{k-1}/dgb_k (b_0 = b_{G-1} = 1),
+    // c_k = -dt H_k/dgb_k (c_{G-1} = 0). Each substep is the back
+    // substitution f_k = (f_k + Q_k dt)/b_k - (c_k/b_k) f_{k+1}
+    // (numeric_model.h:19-43, 682-708).
+    const int c = (G + kStepThreads - 1) / kStepThreads;
+    const int T = (G + c - 1) / c;  // threads that own bins
+    double fr[kMaxPerThread], ib[kMaxPerThread], qb[kMaxPerThread], bt[kMaxPerThread];
+#pragma unroll
+    for (int q = 0; q < kMaxPerThread; ++q) {
+      const int j = tid * c + q;
+      fr[q] = ib[q] = qb[q] = bt[q] = 0.;
+      if (q < c && j < G) {
+        const double odgb = g.inv_dgb[j];
+        const double Hb = (j > 0 && j < G - 1) ? sh_f[j - 1] : 0.;  // b_0 and b_{G-1} see no inflow
+        const double Hf = j < G - 1 ? sh_f[j] : 0.;
+        const double bb = 1. + (odgb * Hb) * delta_t;
+        const double cc = (odgb * Hf) * -delta_t;
+        const double Q = (j >= sc.iq0 && j < sc.iq1) ? sc.Ns * pp[j] : 0.;
+        ib[q] = 1. / bb;
+        bt[q] = -(cc * ib[q]);
+        qb[q] = (Q * delta_t) * ib[q];
+        fr[q] = f[j];
+      }
+    }
+    // systolic substeps: thread t handles substep m = tau - (T-1-t)
+    const int lane = tid & 31, warp = tid >> 5;
+    if (tid < 2 * (kStepThreads / 32)) (&xfer[0][0])[tid] = 0.;
+    __syncthreads();
+    double low = 0.;
+    bool sbad = false;
+    const int ticks = n_sub + T - 1;
+    for (int tau = 0; tau < ticks; ++tau) {
+      double up = __shfl_down_sync(0xffffffffu, low, 1);
+      if (lane == 31) up = warp + 1 < kStepThreads / 32 ? xfer[tau & 1][warp + 1] : 0.;
+      const int m = tau - (T - 1 - tid);
+      if (tid < T && m >= 0 && m < n_sub) {
+        double fn = up;
+#pragma unroll
+        for (int q = kMaxPerThread - 1; q >= 0; --q) {
+          if (q < c) {
+            sbad |= bad_value(fr[q]);  // solve() checks f before each substep (numeric_model.h:688)
+            const double a = fma(fr[q], ib[q], qb[q]);
+            fr[q] = fma(bt[q], fn, a);
+            fn = fr[q];
+          }
+        }
+        low = fr[0];
+      }
+      if (lane == 0) xfer[(tau + 1) & 1][warp] = low;
+      __syncthreads();
+    }
+    if (sbad) atomicOr(&sh_bad, 1);
+#pragma unroll
+    for (int q = 0; q < kMaxPerThread; ++q) {
+      const int j = tid * c + q;
+      if (q < c && j < G) f[j] = fr[q];
+    }
+    __syncthreads();
+    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
   }
   __syncthreads();
 
-  // ---- computeRadiationNumericMixed, synchrotron part (microphysics.h:498-506)
-  const double B = r.B;
-  if (B < 0) PBAG_FAIL(PBAG_ERR_PARAM);  // evalSynKernel (kernels.h:529-532)
-  for (int i = tid; i < G; i += kStepThreads) sh_f[i] = f[i];
+  // ---- per-step weights of the radiation sums (microphysics.h:498-558)
+  for (int i = tid; i < G; i += kStepThreads) {
+    const double fi = f[i];
+    sh_f[i] = fi;
+    sh_t[i] = fi * g.inv_e2[i];  // f / e / e (numeric_model.h:194-195)
+  }
   __syncthreads();
-  // N_e (microphysics.h:556-558) and the weights f_j (e_{j+1}-e_j)
-  double ne = 0., wmax = 0.;
+  double ne = 0., wmax = 0., Wmax = 0.;
   for (int i = tid; i < G - 1; i += kStepThreads) {
     const double w = sh_f[i] * g.de[i];
-    ne += w;
+    ne += w;  // N_e (microphysics.h:556-558)
     wmax = fmax(wmax, w);
+    Wmax = fmax(Wmax, w * g.inv_e2[i]);
   }
   ne = block_sum(ne, red_d);
   wmax = block_max(wmax, red_d);
+  Wmax = block_max(Wmax, red_d);
   const double sw = pow2_scale(wmax);
-  // SSA: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501, numeric_model.h:193-196)
-  double* dfde = S.dfde + (size_t)b * G;
+  float* w32 = S.w32 + (size_t)b * G;
+  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
+  // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
+  double sv = 1.;
   if (P.ssa_on) {
+    double* dfde = S.dfde + (size_t)b * G;
+    double vmax = 0.;
     for (int i = tid; i < G; i += kStepThreads) {
-      const double t = sh_f[i] / g.e[i] / g.e[i];
+      const double t = sh_t[i];
+      double d = dfde[i];
       if (t > 0) {
-        double d;
-        if (i == 0) {
-          const double t1 = sh_f[1] / g.e[1] / g.e[1], t2 = sh_f[2] / g.e[2] / g.e[2];
-          d = -1.5 * t + 2. * t1 - 0.5 * t2;
-        } else if (i == G - 1) {
-          const double t1 = sh_f[G - 2] / g.e[G - 2] / g.e[G - 2], t2 = sh_f[G - 3] / g.e[G - 3] / g.e[G - 3];
-          d = 1.5 * t - 2. * t1 + 0.5 * t2;
-        } else {
-          const double tp = sh_f[i + 1] / g.e[i + 1] / g.e[i + 1], tm = sh_f[i - 1] / g.e[i - 1] / g.e[i - 1];
-          d = 0.5 * (tp - tm) / (g.e[i] - g.e[i - 1]);
-        }
+        if (i == 0)
+          d = -1.5 * t + 2. * sh_t[1] - 0.5 * sh_t[2];
+        else if (i == G - 1)
+          d = 1.5 * t - 2. * sh_t[G - 2] + 0.5 * sh_t[G - 3];
+        else
+          d = 0.5 * (sh_t[i + 1] - sh_t[i - 1]) * g.inv_dxm[i];
         dfde[i] = d;
       }
-    }
-  }
-  __syncthreads();
-  for (int i = tid; i < G; i += kStepThreads) {
-    sh_w[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
-    sh_v[i] = (P.ssa_on && i < G - 1) ? g.e[i] * g.e[i] * (g.e[i + 1] - g.e[i]) * dfde[i] : 0.;
-  }
-  __syncthreads();
-  // kernel prefactor (kernels.h:427 CSYN, :471 Dermer09) and nu / nu_crit
-  const bool dermer = P.syn_method == PBAG_SYN_DER09;
-  const double pref = dermer ? sqrt3 * pow(q_e, 3.) * B / (m_e * c_light * c_light) : sqrt3 * pow(q_e, 3.) * B / mec2;
-  const double inv_ncrit = (4. * M_PI * m_e * c_light) / (3. * q_e * B);  // 1/nu_crit(B, 1) (kernels.h:194-197)
-  const double inv_nlar = (2. * pi_ * m_e * c_light) / (3. * q_e * B);    // 1/nu_larmor(B) (kernels.h:199-202)
-  const int jcyc = dermer ? 0 : g.n_cyc;  // bins with gamma <= 2 use the cyclotron branch (CSYN only)
-  double* jsyn = S.jsyn + (size_t)b * F;
-  double* asyn = S.asyn + (size_t)b * F;
-  bool jbad = false;
-  for (int k = tid; k < F; k += kStepThreads) {
-    const double nu = g.nu[k];
-    const float a_k = (float)(nu * inv_ncrit);
-    const float xl = (float)(nu * inv_nlar);
-    float acc = 0.f;
-    double acca = 0.;
-    for (int j = 0; j < G - 1; ++j) {
-      float R;
-      if (j >= jcyc) {
-        R = aharonian_R32(a_k * g.ginv2[j]);
-      } else {  // cyclotron branch of cycSynch (kernels.h:428-435)
-        const float psq = g.psq32[j];
-        R = (2.f * psq) / (1.f + 3.f * psq) * expf((2.f * (1.f - xl)) / (1.f + 3.f * psq));
+      if (i < G - 1) {
+        const double v = g.e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
+        sh_vd[i] = v;
+        vmax = fmax(vmax, fabs(v));
       }
-      acc = fmaf(R, sh_w[j], acc);
-      if (P.ssa_on) acca = fma((double)R, sh_v[j], acca);
     }
-    const double js = k < F - 1 ? pref * ((double)acc / sw) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
-    if (!isfinite(js) || js < 0.) jbad = true;
-    jsyn[k] = js;
-    if (P.ssa_on) {
-      double a = pref * acca;
-      a *= -1. / (8. * M_PI * m_e * nu * nu);
-      a = fabs(a);
-      if (!isfinite(a)) a = 1e99;
-      asyn[k] = a;
-    } else {
-      asyn[k] = 0.;
-    }
+    vmax = block_max(vmax, red_d);  // (its barriers also publish sh_vd)
+    sv = pow2_scale(vmax);
+    float* v32 = S.v32 + (size_t)b * G;
+    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? (float)(sh_vd[i] * sv) : 0.f;
   }
-  if (jbad) atomicOr(&sh_bad, 1);
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   if (P.ssc_on && g.K32 != nullptr) {
-    double wm = 0.;
-    for (int j = tid; j < G - 1; j += kStepThreads)
-      wm = fmax(wm, sh_f[j] * g.de[j] * (3. / 4. * sigma_T * c_light / (g.e[j] * g.e[j])));
-    wm = block_max(wm, red_d);
-    const double s = pow2_scale(wm);
+    const double sW = pow2_scale(Wmax);
     float* W = S.W32 + (size_t)b * g.Gp;
     for (int j = tid; j < g.Gp; j += kStepThreads)
-      W[j] = j < G - 1 ? (float)(sh_f[j] * g.de[j] * (3. / 4. * sigma_T * c_light / (g.e[j] * g.e[j])) * s) : 0.f;
-    if (tid == 0) scal[kScalSW] = 1. / s;
+      W[j] = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
+    if (tid == 0) S.scal[(size_t)b * kScal + kScalSW] = 3. / 4. * sigma_T * c_light / sW;
   }
-  __syncthreads();
-  if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE);
-  if (ne <= 0) PBAG_FAIL(PBAG_ERR_NELE);  // microphysics.h:560-563
+  if (ne <= 0) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // microphysics.h:560-563
   if (tid == 0) {
-    scal[kScalDr] = dr_comov;
-    scal[kScalVol] = vol;
+    double* scal = S.scal + (size_t)b * kScal;
+    scal[kScalDr] = sc.dr;
+    scal[kScalVol] = sc.vol;
     scal[kScalNele] = ne;
-    scal[kScalAcc] = r.accel_frac;
+    scal[kScalAcc] = accel;
     scal[kScalNp] = r.n_prime;
-    scal[kScalNsub] = (double)nsub_taken;
+    scal[kScalNsub] = (double)sc.n_sub;
+    scal[kScalSw] = 1. / sw;
+    scal[kScalSv] = 1. / sv;
+    scal[kScalPref] = sc.pref;
+    scal[kScalIncrit] = (double)sc.inv_ncrit;
+    scal[kScalInlar] = (double)sc.inv_nlar;
     S.flags[b] = flags | kFlagActive;
   }
 #undef PBAG_FAIL
 }
 
 // ---------------------------------------------------------------------------
+// Synchrotron emissivity and SSA absorption of one blastwave for kRadFreqs
+// frequencies: 4 threads per frequency split the gamma sum; the synchrotron
+// kernel values are generated in FP32 on the fly and never stored.
+__device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk,
+                              int step) {
+  const int tid = threadIdx.x;
+  const int G = g.G, F = g.F;
+  __shared__ float sw_[PBAG_MAX_BINS];
+  __shared__ float sv_[PBAG_MAX_BINS];
+  if (!(S.flags[b] & kFlagActive)) return;
+  const bool ssa = prm[b].ssa_on != 0;
+  const bool dermer = prm[b].syn_method == PBAG_SYN_DER09;
+  for (int i = tid; i < G; i += kRadThreads) {
+    sw_[i] = S.w32[(size_t)b * G + i];
+    sv_[i] = ssa ? S.v32[(size_t)b * G + i] : 0.f;
+  }
+  __syncthreads();
+  const double* scal = S.scal + (size_t)b * kScal;
+  const float incrit = (float)scal[kScalIncrit], inlar = (float)scal[kScalInlar];
+  const int kq = tid >> 2, jl = tid & 3;
+  const int k = kblk * kRadFreqs + kq;
+  const int kk = k < F ? k : F - 1;
+  const double nu = g.nu[kk];
+  const float a_k = (float)nu * incrit;
+  const float xl = (float)nu * inlar;
+  const int jcyc = dermer ? 0 : g.n_cyc;
+  float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
+  for (int j = jl; j < G - 1; j += 4) {
+    const float R = j >= jcyc ? aharonian_R32(a_k * g.ginv2[j]) : cyclotron_R32(g.psq32[j], xl);
+    acc = fmaf(R, sw_[j], acc);
+    if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
+      const float x = R * sv_[j];
+      const float t = as + x;
+      ac += fabsf(as) >= fabsf(x) ? (as - t) + x : (x - t) + as;
+      as = t;
+    }
+  }
+  // combine the 4 partial sums of each frequency (adjacent lanes)
+#pragma unroll
+  for (int o = 1; o <= 2; o <<= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const float os = __shfl_xor_sync(0xffffffffu, as, o);
+    const float oc = __shfl_xor_sync(0xffffffffu, ac, o);
+    float s, e;
+    two_sum(as, os, s, e);
+    as = s;
+    ac = ac + oc + e;
+  }
+  if (jl == 0 && k < F) {
+    const double pref = scal[kScalPref];
+    const double js = k < F - 1 ? pref * ((double)acc * scal[kScalSw]) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
+    if (!isfinite(js) || js < 0.) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
+    S.jsyn[(size_t)b * F + k] = js;
+    double a = 0.;
+    if (ssa) {
+      a = pref * (((double)as + (double)ac) * scal[kScalSv]) * g.ssa_nu[k];  // numeric_model.h:206-211
+      a = fabs(a);
+      if (!isfinite(a)) a = 1e99;
+    }
+    S.asyn[(size_t)b * F + k] = a;
+  }
+}
+
+template <int KPT>
+__global__ void __launch_bounds__(kRadThreads)
+k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int step) {
+  static_assert(kRadThreads == kSscThreads, "radiation and SSC tiles share the launch shape");
+  const int blk = blockIdx.x;
+  const int rc = (g.F + kRadFreqs - 1) / kRadFreqs;
+  if (blk < rad_blocks) {
+    radiate_block(g, S, prm, blk / rc, blk % rc, step);
+  } else {
+    ssc_block<KPT>(g, S, nbw, blk - rad_blocks);
+  }
+}
+
+// ---------------------------------------------------------------------------
 __device__ __forceinline__ double intensity_approx(double em, double dtau) {  // microphysics.h:11-58, iAPPROX
   if (dtau == 0) return em;
-  const double u = 1. / 2. + exp(-dtau) / dtau - (1 - exp(-dtau)) / (dtau * dtau);
+  const double e = exp(-dtau);
+  const double u = 1. / 2. + e / dtau - (1 - e) / (dtau * dtau);
   return dtau > 1.e-3 ? em * (3. * u / dtau) : em;
 }
 
@@ -432,7 +584,7 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
   const int G = g.G, F = g.F;
   __shared__ double red_d[kStepThreads / 32];
   const int flags = S.flags[b];
-  if (!(flags & kFlagActive)) return;
+  if (!(flags & kFlagActive) || S.err[4 * b] != 0) return;
   const pbag_shock_params P = prm[b];
   const double* scal = S.scal + (size_t)b * kScal;
   const double dr = scal[kScalDr], vol = scal[kScalVol], ne = scal[kScalNele];
@@ -446,24 +598,20 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
   const double* asyn = S.asyn + (size_t)b * F;
   const double* jssc = S.jssc + (size_t)b * F;
   // new photon density (microphysics.h:516-523)
-  const double Tesc = dr / c_light;
-  const double fac = Tesc / vol;
+  const double fac = dr / c_light / vol;
+  const double acc_ne = acc / ne, anp_ne = acc * np / ne;
   bool bad = false, seen = false;
   double umax = 0.;
   for (int k = tid; k < F; k += kStepThreads) {
-    const double nu = g.nu[k];
-    double nk = jsyn[k] * fac / (h_pl * nu);
-    if (num && ssc) nk += jssc[k] * fac / (h_pl * nu);
+    const double js = jsyn[k], cs = (num && ssc) ? jssc[k] : 0.;
+    const double nk = js * fac * g.inv_hnu[k] + cs * fac * g.inv_hnu[k];
     n[k] = nk;
-    umax = fmax(umax, nk / nu * (g.nu[k + 1] - nu));
+    umax = fmax(umax, nk * g.dnu_nu[k]);
     // totals and normalisation (microphysics.h:540-586)
-    double tj = jsyn[k];
-    if (num && ssc) tj += jssc[k];
-    double ta = asyn[k];
-    ta = ta / ne * acc * np;
-    const double dtau = ta * dr;
-    const double ti = intensity_approx(tj * acc, dtau);
-    tj = tj * acc / ne;
+    const double tj0 = js + cs;
+    const double ta = asyn[k] * anp_ne;
+    const double ti = intensity_approx(tj0 * acc, ta * dr);
+    const double tj = tj0 * acc_ne;
     if (!isfinite(tj) || tj < 0.) bad = true;
     if (out.j_all) out.j_all[row * F + k] = tj;
     if (out.a_all) out.a_all[row * F + k] = ta;
@@ -471,8 +619,8 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
     if (out.i_all) out.i_all[row * F + k] = ti;
     // storeDenseOutput (microphysics.h:602-633)
     if (dense_syn) {
-      const double sj = jsyn[k] * acc;
-      const double sa = asyn[k] / ne * acc * np;
+      const double sj = js * acc;
+      const double sa = asyn[k] * anp_ne;
       if (out.syn_j_all) out.syn_j_all[row * F + k] = sj;
       if (out.syn_a_all) out.syn_a_all[row * F + k] = sa;
       if (out.syn_i_all) out.syn_i_all[row * F + k] = intensity_approx(sj, sa * dr);
@@ -494,12 +642,12 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
       if (out.gdot_ssc_all) out.gdot_ssc_all[row * G + i] = gd[2 * G + i];
     }
   }
-  // seed-photon weights of this step for the next step's SSC contraction
+  // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k for the next step's SSC contraction
   umax = block_max(umax, red_d);
   const double su = pow2_scale(umax);
   if (ssc) {
     float* U = S.U32 + (size_t)b * F;
-    for (int k = tid; k < F; k += kStepThreads) U[k] = (float)(n[k] / g.nu[k] * (g.nu[k + 1] - g.nu[k]) * su);
+    for (int k = tid; k < F; k += kStepThreads) U[k] = (float)(n[k] * g.dnu_nu[k] * su);
   }
   const int any_bad = __syncthreads_or(bad ? 1 : 0);
   const int any_seen = __syncthreads_or(seen ? 1 : 0);
@@ -519,9 +667,41 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
 }
 
 // ---------------------------------------------------------------------------
-cudaError_t launch_evolve_radiate(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
-                                  const pbag_shock_params* prm, int nbw, int step, cudaStream_t st) {
-  k_evolve_radiate<<<nbw, kStepThreads, 0, st>>>(g, S, recs, off, prm, step);
+cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
+                           const pbag_shock_params* prm, int nbw, int64_t nrec, int64_t* first, StepScal* ss,
+                           cudaStream_t st) {
+  if (nbw <= 0) return cudaSuccess;
+  k_first_valid<<<(nbw + 127) / 128, 128, 0, st>>>(recs, off, nbw, first);
+  const int64_t npw = (int64_t)nbw * g.G;
+  k_powp<<<(unsigned)((npw + 255) / 256), 256, 0, st>>>(g, prm, nbw, S.powp);
+  if (nrec > 0)
+    k_prep<<<(unsigned)((nrec + 127) / 128), 128, 0, st>>>(g, recs, off, prm, nbw, nrec, first, S.powp, ss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
+                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step, cudaStream_t st) {
+  k_evolve<<<nbw, kStepThreads, 0, st>>>(g, S, recs, ss, off, prm, step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
+                           int step, cudaStream_t st) {
+  const int rc = (g.F + kRadFreqs - 1) / kRadFreqs;
+  const int rad_blocks = nbw * rc;
+  const int ssc_blocks = ssc ? ssc_block_count(g, nbw) : 0;
+  const int total = rad_blocks + ssc_blocks;
+  if (total <= 0) return cudaSuccess;
+  const int kpt = (g.F + kSscThreads - 1) / kSscThreads;
+  const size_t smem = ssc ? (size_t)ssc_smem_bytes(g) : 0;
+  if (kpt <= 1)
+    k_rad_ssc<1><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+  else if (kpt <= 2)
+    k_rad_ssc<2><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+  else if (kpt <= 4)
+    k_rad_ssc<4><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+  else
+    k_rad_ssc<8><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
   return cudaGetLastError();
 }
 
@@ -529,6 +709,18 @@ cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* 
                             int nbw, int step, const pbag_outputs& out, cudaStream_t st) {
   k_finalize<<<nbw, kStepThreads, 0, st>>>(g, S, off, prm, step, out);
   return cudaGetLastError();
+}
+
+cudaError_t configure_kernels() {
+  const int smem = ssc_smem_max_bytes();
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_rad_ssc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rad_ssc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rad_ssc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(k_rad_ssc<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 }  // namespace pbag
