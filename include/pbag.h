@@ -229,6 +229,27 @@ int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw
                           const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st,
                           void* stream);
 
+/* Allocation-free variant of pbag_run_batch_device. No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory while
+ * they run the step - code recording into a CUDA graph, hosts that only hand
+ * out memory from their own pool, latency-critical loops that must not pay an
+ * allocation - and keeps every intermediate buffer in one fixed __device__
+ * array of PBAG_NOALLOC_SCRATCH_BYTES inside the library instead of memory the
+ * context allocates. It calls no cudaMalloc/cudaFree; inputs and outputs are
+ * the caller's device buffers exactly as for pbag_run_batch_device, on a
+ * context created beforehand (pbag_create allocates the grid tables).
+ * Limit: the batch needs about 17 KiB per blastwave of 201 x 128 bins plus
+ * 112 B per record (all rounded to 256 B blocks); a larger batch returns
+ * PBAG_ERR_ARG with st->site set to the KiB it would need.
+ * The first call on a device looks up the array's device address (once per
+ * device); make that first call before any stream capture. Every call shares
+ * the array and it keeps the last call's contents (the call clears what must
+ * start at zero): calls that overlap on the GPU race, so issue them one at a
+ * time. Every GPU that loads the library holds the array until exit. */
+#define PBAG_NOALLOC_SCRATCH_BYTES (16u << 20)
+int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
+                           const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st);
+
 /* Number of kernels the last run launched (diagnostics). */
 int64_t pbag_last_launch_count(const pbag_ctx* ctx);
 

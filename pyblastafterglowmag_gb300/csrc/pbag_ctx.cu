@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "pbag.h"
+#include "pbag_ctx_view.h"
 #include "pbag_internal.h"
 #include "pbag_kernels.h"
 
@@ -495,3 +496,19 @@ int pbag_get_timing(const pbag_ctx* c, double* ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+namespace pbag {
+
+bool ctx_view(const pbag_ctx* c, CtxView* v) {
+  if (!c || !v) return false;
+  v->device = c->device;
+  v->stream = c->stream;
+  v->dg = c->dg;
+  v->ssc = c->ssc;
+  v->G = c->G;
+  v->F = c->F;
+  v->Gp = c->Gp;
+  return true;
+}
+
+}  // namespace pbag
