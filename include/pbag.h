@@ -239,7 +239,7 @@ int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw
  * the caller's device buffers exactly as for pbag_run_batch_device, on a
  * context created beforehand (pbag_create allocates the grid tables).
  * Limit: the batch needs about 17 KiB per blastwave of 201 x 128 bins plus
- * 112 B per record (all rounded to 256 B blocks); a larger batch returns
+ * 120 B per record (all rounded to 256 B blocks); a larger batch returns
  * PBAG_ERR_ARG with st->site set to the KiB it would need.
  * The first call on a device looks up the array's device address (once per
  * device); make that first call before any stream capture. Every call shares
@@ -252,6 +252,18 @@ int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nb
 
 /* Number of kernels the last run launched (diagnostics). */
 int64_t pbag_last_launch_count(const pbag_ctx* ctx);
+
+/* How the SSC spectrum (numeric_model.h:247-285) is contracted. AUTO uses
+ * the tensor cores with split-BF16 operands (FP32 accumulation, relative
+ * error ~1e-5) when nfreq is 128 or 256, and FP32 CUDA cores otherwise.
+ * TC_BF16 (one BF16 product, ~1e-3) exists for precision studies only. */
+enum pbag_ssc_path {
+  PBAG_SSC_AUTO = 0,
+  PBAG_SSC_CUDA_FP32 = 1,
+  PBAG_SSC_TC_SPLIT_BF16 = 2,
+  PBAG_SSC_TC_BF16 = 3
+};
+int pbag_set_ssc_path(pbag_ctx* ctx, int path);
 
 /* Kernel classes of a step, in launch order. */
 enum pbag_kernel_class {

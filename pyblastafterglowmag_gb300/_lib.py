@@ -59,6 +59,7 @@ def load():
     lib.pbag_last_launch_count.argtypes = [C.c_void_p]
     lib.pbag_last_launch_count.restype = C.c_int64
     lib.pbag_set_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.pbag_set_ssc_path.argtypes = [C.c_void_p, C.c_int]
     lib.pbag_get_timing.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64)]
     if lib.pbag_abi_version() != 1:
         raise RuntimeError("libpbag ABI version mismatch")
@@ -126,6 +127,10 @@ class Context:
 
     def last_launch_count(self):
         return int(load().pbag_last_launch_count(self._h))
+
+    def set_ssc_path(self, path):
+        """abi.PBAG_SSC_AUTO / _CUDA_FP32 / _TC_SPLIT_BF16 / _TC_BF16."""
+        _check(load().pbag_set_ssc_path(self._h, int(path)), "pbag_set_ssc_path")
 
     def set_timing(self, enable):
         _check(load().pbag_set_timing(self._h, int(bool(enable))), "pbag_set_timing")

@@ -43,6 +43,29 @@ int cuda_code(cudaError_t e) { return e == cudaErrorMemoryAllocation ? PBAG_ERR_
 constexpr int kOutputs = 13;  // pointers in pbag_outputs
 inline bool output_on_gamma(int fi) { return fi >= 4 && fi < 8; }
 
+// Everything a captured step loop depends on: replaying the graph is only
+// valid while all of it is unchanged.
+struct GraphKey {
+  int nbw;
+  int64_t max_len;
+  size_t nrec;
+  const void* recs;
+  const void* prm;
+  const void* state;
+  const void* ss;
+  bool ssc;
+  int ssc_path;
+  const void* out[kOutputs];
+  bool operator==(const GraphKey& o) const {
+    if (nbw != o.nbw || max_len != o.max_len || nrec != o.nrec || recs != o.recs || prm != o.prm ||
+        state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path)
+      return false;
+    for (int k = 0; k < kOutputs; ++k)
+      if (out[k] != o.out[k]) return false;
+    return true;
+  }
+};
+
 }  // namespace
 
 struct pbag_ctx {
@@ -51,9 +74,33 @@ struct pbag_ctx {
   pbag_grid_desc desc{};
   int G = 0, F = 0, Gp = 0;
   bool ssc = false;
+  int ssc_path = PBAG_SSC_AUTO;
   std::vector<double> gam, freq;
   DevGrid dg{};
   std::vector<void*> grid_mem;
+
+  // which SSC contraction runs: tensor cores when the grid allows it, unless
+  // the caller pinned a path
+  bool ssc_on_tensor_cores() const {
+    return ssc && dg.Bt && (ssc_path == PBAG_SSC_AUTO || ssc_path == PBAG_SSC_TC_SPLIT_BF16 ||
+                            ssc_path == PBAG_SSC_TC_BF16);
+  }
+
+  // radiation sums + SSC contraction of one step; the tensor-core contraction
+  // runs on a second stream next to the synchrotron sums (both read only what
+  // k_evolve wrote) and joins the main stream before the next step
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaError_t launch_radiation(const pbag_shock_params* d_prm, int nbw, int s) {
+    if (!ssc_on_tensor_cores()) return launch_rad_ssc(dg, S, d_prm, nbw, ssc, s, stream);
+    cudaError_t e;
+    if ((e = cudaEventRecord(ev_fork, stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
+    if ((e = launch_ssc_tc(dg, S, dg.Bt, nbw, ssc_path != PBAG_SSC_TC_BF16, side)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
+    if ((e = launch_rad_ssc(dg, S, d_prm, nbw, false, s, stream)) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(stream, ev_join, 0);
+  }
   // batch buffers, grown on demand
   int cap_bw = 0;
   size_t cap_rec = 0;
@@ -73,10 +120,18 @@ struct pbag_ctx {
   std::vector<int> ev_class;    // kernel class of each event pair
   double class_ms[kKernelClasses] = {0, 0, 0};
   int64_t class_launches[kKernelClasses] = {0, 0, 0};
+  // captured step loop of the last batch shape
+  cudaGraphExec_t graph_exec = nullptr;
+  GraphKey graph_key{};
 
   ~pbag_ctx() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (side) cudaStreamSynchronize(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     for (void* p : grid_mem) cudaFree(p);
     free_state();
@@ -236,20 +291,57 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
     if (start) c->ev_class[nev / 2] = cls;
     return cudaEventRecord(c->ev[nev++], c->stream) == cudaSuccess;
   };
+  // Without timing, the step loop (3 launches per step index) is captured once
+  // into a CUDA graph per batch shape and buffer set, and replayed.
+  if (!c->timing && max_len > 0) {
+    GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, {}};
+    std::memcpy(key.out, &d_out, sizeof(d_out));
+    if (!c->graph_exec || !(key == c->graph_key)) {
+      if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+      c->graph_exec = nullptr;
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBAG_ERR_CUDA;
+      cudaError_t ce = cudaSuccess;
+      for (int64_t s = 0; s < max_len && ce == cudaSuccess; ++s) {
+        ce = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream);
+        if (ce == cudaSuccess) ce = c->launch_radiation(d_prm, nbw, (int)s);
+      }
+      if (ce == cudaSuccess)
+        ce = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)(max_len - 1), d_out, c->stream);
+      cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+      if (ce != cudaSuccess || ee != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        return PBAG_ERR_CUDA;
+      }
+      ee = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ee != cudaSuccess) {
+        c->graph_exec = nullptr;
+        return PBAG_ERR_CUDA;
+      }
+      c->graph_key = key;
+    }
+    if (cudaGraphLaunch(c->graph_exec, c->stream) != cudaSuccess) return PBAG_ERR_CUDA;
+    c->launches += (c->ssc_on_tensor_cores() ? 3 : 2) * max_len + 1;
+    max_len = 0;  // the loop below has nothing left to launch
+  }
   for (int64_t s = 0; s < max_len; ++s) {
     if (!mark(kClassEvolve, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, c->stream)) != cudaSuccess)
+    if ((e = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) !=
+        cudaSuccess)
       return PBAG_ERR_CUDA;
     if (!mark(kClassEvolve, false)) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_rad_ssc(c->dg, c->S, d_prm, nbw, c->ssc, (int)s, c->stream)) != cudaSuccess)
-      return PBAG_ERR_CUDA;
+    if ((e = c->launch_radiation(d_prm, nbw, (int)s)) != cudaSuccess) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
-    if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
-      return PBAG_ERR_CUDA;
-    if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
-    c->launches += 3;
+    c->launches += c->ssc_on_tensor_cores() ? 3 : 2;
+    if (s == max_len - 1) {
+      if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
+      if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
+        return PBAG_ERR_CUDA;
+      if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
+      c->launches += 1;
+    }
   }
   std::vector<int> err((size_t)nbw * 4);
   if (nbw > 0 && cudaMemcpyAsync(err.data(), c->S.err, err.size() * sizeof(int), cudaMemcpyDeviceToHost,
@@ -308,7 +400,10 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   c->F = g->nfreq;
   c->Gp = (c->G + 15) / 16 * 16;
   c->ssc = ssc_tables != 0;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return PBAG_ERR_CUDA;
   }
@@ -381,13 +476,19 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   d.Kint32 = nullptr;
   d.kscale = nullptr;
   d.K32 = nullptr;
+  d.Bt = nullptr;
   if (c->ssc) {
     std::vector<float> Kint32, K32;
     std::vector<double> kscale;
+    std::vector<uint16_t> Bt;
     build_ssc_tables(e.data(), G, nu.data(), F, c->Gp, Kint32, kscale, K32);
     ok(c->grid_upload(&d.Kint32, Kint32));
     ok(c->grid_upload(&d.kscale, kscale));
     ok(c->grid_upload(&d.K32, K32));
+    if (ssc_tc_supported(F)) {
+      build_ssc_tc_operand(K32, F, c->Gp, Bt);
+      ok(c->grid_upload(&d.Bt, Bt));
+    }
     ok(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
   }
   ok(cudaStreamSynchronize(c->stream));
@@ -475,6 +576,13 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
 }
 
 int64_t pbag_last_launch_count(const pbag_ctx* c) { return c ? c->launches : -1; }
+
+int pbag_set_ssc_path(pbag_ctx* c, int path) {
+  if (!c || path < PBAG_SSC_AUTO || path > PBAG_SSC_TC_BF16) return PBAG_ERR_ARG;
+  if ((path == PBAG_SSC_TC_SPLIT_BF16 || path == PBAG_SSC_TC_BF16) && !c->dg.Bt) return PBAG_ERR_UNSUPPORTED;
+  c->ssc_path = path;
+  return PBAG_OK;
+}
 
 int pbag_set_timing(pbag_ctx* c, int enable) {
   if (!c) return PBAG_ERR_ARG;

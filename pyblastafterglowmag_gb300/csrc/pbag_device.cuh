@@ -13,7 +13,8 @@ namespace pbag {
 constexpr int kStepThreads = 128;     // threads per blastwave in the evolve / finalize kernels
 constexpr int kMaxPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // gamma bins per thread
 constexpr int kRadThreads = 128;      // threads of one radiation CTA
-constexpr int kRadFreqs = 32;         // frequencies per radiation CTA (4 threads per frequency)
+constexpr int kRadLanes = 8;          // threads per frequency in a radiation CTA
+constexpr int kRadFreqs = kRadThreads / kRadLanes;  // frequencies per radiation CTA
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
 constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 
@@ -43,6 +44,7 @@ struct DevGrid {
   const float* Kint32;   // [G][F] SSC kernel integral / kscale[k] (kernels.h:79-91)
   const double* kscale;  // [F]   power-of-two column scales of Kint32
   const float* K32;      // [F][Gp][F] SSC kernel (i, j, k) in FP32, j >= G zero
+  const uint16_t* Bt;    // SSC kernel as BF16 hi/lo tensor-core operand slabs (pbag_ssc_tc.cu), or null
 };
 
 // Per-record scalars of one step, computed once for the whole batch by
@@ -54,6 +56,7 @@ struct StepScal {
   double dt_sub;     // substep length (microphysics.h:416-431)
   double dlnVdt;     // (microphysics.h:405)
   double dr, vol;    // dr_comov and source.vol of this step
+  double fac;        // (dr/c)/vol: photon-field factor (microphysics.h:517-518)
   double pref;       // synchrotron prefactor sqrt(3) q^3 B / (m_e c^2) (kernels.h:427,471)
   float inv_ncrit;   // 1 / nu_crit(B, gamma=1) (kernels.h:194-197)
   float inv_nlar;    // 1 / nu_larmor(B) (kernels.h:199-202)
@@ -104,6 +107,9 @@ enum : int {
   kScalPref = 10,  // synchrotron prefactor of this step
   kScalIncrit = 11,  // 1/nu_crit(B,1) of this step
   kScalInlar = 12,   // 1/nu_larmor(B) of this step
+  kScalFac = 13,     // photon escape factor (dr/c)/vol (microphysics.h:517-518)
+  kScalAccNe = 14,   // accel_frac / N_e
+  kScalAnpNe = 15,   // accel_frac n' / N_e
   kScal = 16
 };
 
@@ -121,6 +127,41 @@ __host__ __device__ inline double pow2_scale(double maxabs) {
   int ex;
   frexp(maxabs, &ex);
   return ldexp(1., -ex);
+}
+
+// ---- FP64 predicates and scales on the integer pipe -------------------------
+// FP64 compares, max/min, frexp/ldexp and divisions cost hundreds of cycles
+// per warp instruction on this part; these helpers read the bit pattern.
+
+// !isfinite(v) || v < 0, as the reference's checks (-0.0 passes)
+__device__ __forceinline__ bool bad_value(double v) {
+  const int hi = __double2hiint(v);
+  if ((hi & 0x7ff00000) == 0x7ff00000) return true;  // inf or NaN
+  return hi < 0 && ((hi & 0x7fffffff) | __double2loint(v)) != 0;
+}
+// v > 0 for a non-NaN v
+__device__ __forceinline__ bool positive(double v) {
+  const int hi = __double2hiint(v);
+  if ((hi & 0x7ff00000) == 0x7ff00000 && (((hi & 0xfffff) | __double2loint(v)) != 0)) return false;  // NaN
+  return hi > 0 || (hi == 0 && __double2loint(v) != 0);
+}
+// !isfinite(v)
+__device__ __forceinline__ bool not_finite(double v) { return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000; }
+// isnan(v)
+__device__ __forceinline__ bool is_nan(double v) {
+  const int hi = __double2hiint(v);
+  return (hi & 0x7ff00000) == 0x7ff00000 && (((hi & 0xfffff) | __double2loint(v)) != 0);
+}
+// biased exponent field of |v| (0 for zero and subnormals)
+__device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >> 20) & 0x7ff; }
+// pow2_scale(max) given the biased exponent E of max: 2^-(E-1022), or 1 outside
+// the range where the scaled values and the inverse stay normal
+__device__ __forceinline__ double scale_from_exp(int E) {
+  return (E <= 26 || E >= 2019) ? 1. : __hiloint2double((2045 - E) << 20, 0);
+}
+// the exact inverse of scale_from_exp(E)
+__device__ __forceinline__ double unscale_from_exp(int E) {
+  return (E <= 26 || E >= 2019) ? 1. : __hiloint2double((E + 1) << 20, 0);
 }
 
 // ---- synchrotron kernel functions in FP32 (kernels.h) ---------------------

@@ -14,15 +14,23 @@ namespace pbag {
 cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
                            const pbag_shock_params* prm, int nbw, int64_t nrec, int64_t* first, StepScal* ss,
                            cudaStream_t st);
-// every step
+// every step: k_evolve(step) first completes step-1 (photon field, totals,
+// history rows); after the last step launch_finalize completes it
 cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
-                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step, cudaStream_t st);
+                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step,
+                          const pbag_outputs& out, cudaStream_t st);
 cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
                            int step, cudaStream_t st);
 cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* off, const pbag_shock_params* prm,
                             int nbw, int step, const pbag_outputs& out, cudaStream_t st);
 // kernel attributes (dynamic shared memory limits); call once per device
 cudaError_t configure_kernels();
+
+// tensor-core SSC contraction (pbag_ssc_tc.cu), for F = 128 or 256
+bool ssc_tc_supported(int F);
+void build_ssc_tc_operand(const std::vector<float>& K32, int F, int Gp, std::vector<uint16_t>& Bt);
+cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
+                          cudaStream_t st);
 
 // SSC kernel tables on the host (kernels.h:49-117): Kint32[G][F] = Kint / kscale[k]
 // with power-of-two column scales, and K32[F][Gp][F] (i, j, k) in FP32,

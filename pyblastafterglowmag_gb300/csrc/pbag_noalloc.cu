@@ -215,10 +215,10 @@ extern "C" int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_
   if (nbw > 0) {
     ok(launch_prepare(v.dg, S, d_recs, d_off, d_prm, nbw, (int64_t)nrec, d_first, d_ss, s));
     for (int64_t step = 0; step < max_len && e == cudaSuccess; ++step) {
-      ok(launch_evolve(v.dg, S, d_recs, d_ss, d_off, d_prm, nbw, (int)step, s));
+      ok(launch_evolve(v.dg, S, d_recs, d_ss, d_off, d_prm, nbw, (int)step, *d_out, s));
       ok(launch_rad_ssc(v.dg, S, d_prm, nbw, v.ssc, (int)step, s));
-      ok(launch_finalize(v.dg, S, d_off, d_prm, nbw, (int)step, *d_out, s));
     }
+    if (max_len > 0) ok(launch_finalize(v.dg, S, d_off, d_prm, nbw, (int)(max_len - 1), *d_out, s));
   }
   int fail[4] = {PBAG_OK, -1, -1, 0};
   if (nbw > 0) {

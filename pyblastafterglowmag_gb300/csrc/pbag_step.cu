@@ -30,8 +30,16 @@ using namespace cgs;
 
 namespace {
 
-__device__ __forceinline__ bool bad_value(double v) {  // !isfinite(v) || v < 0
-  return !(v >= 0.) || !(v <= 1.7976931348623157e308);
+// Block-wide max of a non-negative int (exponent fields), on the integer pipe.
+__device__ int block_max_int(int v, int* red) {
+  v = __reduce_max_sync(0xffffffffu, v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  int r = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = max(r, red[i]);
+  return r;
 }
 
 // Record the first error of a blastwave (later ones are ignored).
@@ -183,6 +191,7 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   s.dr = q.dr;
   if (init) {
     s.vol = q.m_p1 / q.rho_p1;
+    s.fac = s.dr / c_light / s.vol;
     if (pl_bad) {
       s.err = PBAG_ERR_NONFINITE;
       s.site = __LINE__;
@@ -232,6 +241,7 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
     n_sub = (int)(dt / delta_t);
   }
   s.vol = volume;
+  s.fac = s.dr / c_light / s.vol;
   if (P.ele_method == PBAG_ELE_MIX || gm <= 2) {
     s.n_sub = 0;  // analytic distribution replaces the evolution (microphysics.h:446-448)
   } else {
@@ -248,18 +258,27 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   out[r] = s;
 }
 
+__device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* __restrict__ off,
+                            const pbag_shock_params* __restrict__ prm, int b, int step, const pbag_outputs& out);
+
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kStepThreads)
 k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const StepScal* __restrict__ ss,
-         const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step) {
+         const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step, pbag_outputs out) {
   const int b = blockIdx.x;
   const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
+  // the previous step's photon field, totals and history rows (same CTA shape)
+  if (step > 0) {
+    finalize_bw(g, S, off, prm, b, step - 1, out);
+    __syncthreads();  // its flag and error updates are visible below
+  }
   __shared__ double sh_f[PBAG_MAX_BINS];   // heating term, then N(gamma)
   __shared__ double sh_t[PBAG_MAX_BINS];   // f / gamma^2
   __shared__ double sh_vd[PBAG_MAX_BINS];  // SSA weights
   __shared__ float sh_v[PBAG_MAX_BINS];    // seed-photon weights for the SSC cooling GEMV
   __shared__ double red_d[kStepThreads / 32];
+  __shared__ int red_i[kStepThreads / 32];
   __shared__ double xfer[2][kStepThreads / 32];
   __shared__ int sh_bad;
 
@@ -314,21 +333,25 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     const bool ssc = P.ssc_on && g.K32 != nullptr;
     const double delta_t = sc.dt_sub;
     const int n_sub = sc.n_sub;
-    double sv = 1.;
+    double sv = 1., usv = 1.;
     if (ssc) {  // seed-photon weights n_k dnu_k / nu_k, scaled by the kernel-integral columns
       const double* n = S.n + (size_t)b * F;
-      double vmax = 0.;
-      for (int k = tid; k < F - 1; k += kStepThreads) vmax = fmax(vmax, n[k] * g.dnu_nu[k] * g.kscale[k]);
-      vmax = block_max(vmax, red_d);
-      sv = pow2_scale(vmax);
-      for (int k = tid; k < F; k += kStepThreads)
-        sh_v[k] = k < F - 1 ? (float)(n[k] * g.dnu_nu[k] * g.kscale[k] * sv) : 0.f;
+      int vexp = 0;
+      for (int k = tid; k < F - 1; k += kStepThreads) {
+        const double v = n[k] * g.dnu_nu[k] * g.kscale[k];
+        sh_t[k] = v;  // (sh_t is free until the weights below)
+        vexp = max(vexp, exp_field(v));
+      }
+      vexp = block_max_int(vexp, red_i);
+      sv = scale_from_exp(vexp);
+      usv = unscale_from_exp(vexp);
+      for (int k = tid; k < F; k += kStepThreads) sh_v[k] = k < F - 1 ? (float)(sh_t[k] * sv) : 0.f;
     }
     __syncthreads();
     // heating / cooling terms at the half grid (numeric_model.h:753-801);
     // constant over the substeps, so evaluated once per step
     const double c_syn = sigma_T / (6. * M_PI * m_e * c_light) * B * B;
-    const double c_ssc = 3. / 4. * h_pl * sigma_T / m_e / c_light / sv;
+    const double c_ssc = 3. / 4. * h_pl * sigma_T / m_e / c_light * usv;
     double* gsyn = S.gdot + (size_t)b * 3 * G;
     double* gadi = gsyn + G;
     double* gssc = gadi + G;
@@ -347,7 +370,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       gsyn[i] = vs;
       gadi[i] = va;
       const double H = vs + va + vc;
-      if (!isfinite(H)) hbad = true;
+      if (not_finite(H)) hbad = true;
       sh_f[i] = H;
     }
     if (tid == 0) sh_f[G - 1] = 0.;  // heating_term[G-1] is never set (numeric_model.h:761)
@@ -424,28 +447,29 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     sh_t[i] = fi * g.inv_e2[i];  // f / e / e (numeric_model.h:194-195)
   }
   __syncthreads();
-  double ne = 0., wmax = 0., Wmax = 0.;
+  // the power-of-two scales come from the largest exponent field
+  double ne = 0.;
+  int wexp = 0, Wexp = 0;
   for (int i = tid; i < G - 1; i += kStepThreads) {
     const double w = sh_f[i] * g.de[i];
     ne += w;  // N_e (microphysics.h:556-558)
-    wmax = fmax(wmax, w);
-    Wmax = fmax(Wmax, w * g.inv_e2[i]);
+    wexp = max(wexp, exp_field(w));
+    Wexp = max(Wexp, exp_field(w * g.inv_e2[i]));
   }
   ne = block_sum(ne, red_d);
-  wmax = block_max(wmax, red_d);
-  Wmax = block_max(Wmax, red_d);
-  const double sw = pow2_scale(wmax);
+  wexp = block_max_int(wexp, red_i);
+  Wexp = block_max_int(Wexp, red_i);
+  const double sw = scale_from_exp(wexp);
   float* w32 = S.w32 + (size_t)b * G;
   for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
   // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
-  double sv = 1.;
+  int vexp = 0;
   if (P.ssa_on) {
     double* dfde = S.dfde + (size_t)b * G;
-    double vmax = 0.;
     for (int i = tid; i < G; i += kStepThreads) {
       const double t = sh_t[i];
       double d = dfde[i];
-      if (t > 0) {
+      if (positive(t)) {
         if (i == 0)
           d = -1.5 * t + 2. * sh_t[1] - 0.5 * sh_t[2];
         else if (i == G - 1)
@@ -457,33 +481,37 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       if (i < G - 1) {
         const double v = g.e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
         sh_vd[i] = v;
-        vmax = fmax(vmax, fabs(v));
+        vexp = max(vexp, exp_field(v));
       }
     }
-    vmax = block_max(vmax, red_d);  // (its barriers also publish sh_vd)
-    sv = pow2_scale(vmax);
+    vexp = block_max_int(vexp, red_i);  // (its barriers also publish sh_vd)
+    const double sv = scale_from_exp(vexp);
     float* v32 = S.v32 + (size_t)b * G;
     for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? (float)(sh_vd[i] * sv) : 0.f;
   }
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   if (P.ssc_on && g.K32 != nullptr) {
-    const double sW = pow2_scale(Wmax);
+    const double sW = scale_from_exp(Wexp);
     float* W = S.W32 + (size_t)b * g.Gp;
     for (int j = tid; j < g.Gp; j += kStepThreads)
       W[j] = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
-    if (tid == 0) S.scal[(size_t)b * kScal + kScalSW] = 3. / 4. * sigma_T * c_light / sW;
+    if (tid == 0) S.scal[(size_t)b * kScal + kScalSW] = 3. / 4. * sigma_T * c_light * unscale_from_exp(Wexp);
   }
-  if (ne <= 0) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // microphysics.h:560-563
+  if (!positive(ne) && !is_nan(ne)) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // n_ele <= 0 (microphysics.h:560-563)
   if (tid == 0) {
     double* scal = S.scal + (size_t)b * kScal;
     scal[kScalDr] = sc.dr;
     scal[kScalVol] = sc.vol;
     scal[kScalNele] = ne;
+    scal[kScalFac] = sc.fac;
+    const double acc_ne = accel / ne;
+    scal[kScalAccNe] = acc_ne;
+    scal[kScalAnpNe] = accel * r.n_prime / ne;
     scal[kScalAcc] = accel;
     scal[kScalNp] = r.n_prime;
     scal[kScalNsub] = (double)sc.n_sub;
-    scal[kScalSw] = 1. / sw;
-    scal[kScalSv] = 1. / sv;
+    scal[kScalSw] = unscale_from_exp(wexp);
+    scal[kScalSv] = unscale_from_exp(vexp);
     scal[kScalPref] = sc.pref;
     scal[kScalIncrit] = (double)sc.inv_ncrit;
     scal[kScalInlar] = (double)sc.inv_nlar;
@@ -494,7 +522,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 
 // ---------------------------------------------------------------------------
 // Synchrotron emissivity and SSA absorption of one blastwave for kRadFreqs
-// frequencies: 4 threads per frequency split the gamma sum; the synchrotron
+// frequencies: kRadLanes threads per frequency split the gamma sum; the synchrotron
 // kernel values are generated in FP32 on the fly and never stored.
 __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk,
                               int step) {
@@ -512,7 +540,7 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   __syncthreads();
   const double* scal = S.scal + (size_t)b * kScal;
   const float incrit = (float)scal[kScalIncrit], inlar = (float)scal[kScalInlar];
-  const int kq = tid >> 2, jl = tid & 3;
+  const int kq = tid / kRadLanes, jl = tid % kRadLanes;
   const int k = kblk * kRadFreqs + kq;
   const int kk = k < F ? k : F - 1;
   const double nu = g.nu[kk];
@@ -520,7 +548,7 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   const float xl = (float)nu * inlar;
   const int jcyc = dermer ? 0 : g.n_cyc;
   float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
-  for (int j = jl; j < G - 1; j += 4) {
+  for (int j = jl; j < G - 1; j += kRadLanes) {
     const float R = j >= jcyc ? aharonian_R32(a_k * g.ginv2[j]) : cyclotron_R32(g.psq32[j], xl);
     acc = fmaf(R, sw_[j], acc);
     if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
@@ -530,9 +558,9 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
       as = t;
     }
   }
-  // combine the 4 partial sums of each frequency (adjacent lanes)
+  // combine the kRadLanes partial sums of each frequency (adjacent lanes)
 #pragma unroll
-  for (int o = 1; o <= 2; o <<= 1) {
+  for (int o = 1; o < kRadLanes; o <<= 1) {
     acc += __shfl_xor_sync(0xffffffffu, acc, o);
     const float os = __shfl_xor_sync(0xffffffffu, as, o);
     const float oc = __shfl_xor_sync(0xffffffffu, ac, o);
@@ -544,13 +572,13 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   if (jl == 0 && k < F) {
     const double pref = scal[kScalPref];
     const double js = k < F - 1 ? pref * ((double)acc * scal[kScalSw]) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
-    if (!isfinite(js) || js < 0.) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
+    if (bad_value(js)) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
     S.jsyn[(size_t)b * F + k] = js;
     double a = 0.;
     if (ssa) {
       a = pref * (((double)as + (double)ac) * scal[kScalSv]) * g.ssa_nu[k];  // numeric_model.h:206-211
       a = fabs(a);
-      if (!isfinite(a)) a = 1e99;
+      if (not_finite(a)) a = 1e99;
     }
     S.asyn[(size_t)b * F + k] = a;
   }
@@ -570,25 +598,30 @@ k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int 
 }
 
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double intensity_approx(double em, double dtau) {  // microphysics.h:11-58, iAPPROX
-  if (dtau == 0) return em;
+// microphysics.h:11-58, METHOD_TAU::iAPPROX; one reciprocal instead of three divisions
+__device__ __forceinline__ double intensity_approx(double em, double dtau) {
+  if (((__double2hiint(dtau) & 0x7fffffff) | __double2loint(dtau)) == 0) return em;  // dtau == 0
+  if (!(dtau > 1.e-3)) return em;
   const double e = exp(-dtau);
-  const double u = 1. / 2. + e / dtau - (1 - e) / (dtau * dtau);
-  return dtau > 1.e-3 ? em * (3. * u / dtau) : em;
+  const double r = 1. / dtau;
+  const double u = 1. / 2. + e * r - (1 - e) * (r * r);
+  return em * (3. * u * r);
 }
 
-__global__ void __launch_bounds__(kStepThreads)
-k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm,
-           int step, pbag_outputs out) {
-  const int b = blockIdx.x, tid = threadIdx.x;
+// The rest of computeRadiationNumericMixed for blastwave b at `step`, once its
+// synchrotron and SSC emissivities are in place; a no-op unless the
+// blastwave radiated at that step. Runs at the start of the next step's
+// k_evolve (same CTA shape), and as k_finalize after the last step.
+__device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* __restrict__ off,
+                            const pbag_shock_params* __restrict__ prm, int b, int step, const pbag_outputs& out) {
+  const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
-  __shared__ double red_d[kStepThreads / 32];
+  __shared__ int red_i[kStepThreads / 32];
   const int flags = S.flags[b];
   if (!(flags & kFlagActive) || S.err[4 * b] != 0) return;
   const pbag_shock_params P = prm[b];
   const double* scal = S.scal + (size_t)b * kScal;
-  const double dr = scal[kScalDr], vol = scal[kScalVol], ne = scal[kScalNele];
-  const double acc = scal[kScalAcc], np = scal[kScalNp];
+  const double dr = scal[kScalDr], acc = scal[kScalAcc];
   const bool num = P.ele_method == PBAG_ELE_NUMERIC;
   const bool ssc = P.ssc_on && g.K32 != nullptr;
   const bool dense_syn = out.syn_j_all || out.syn_a_all || out.syn_i_all;
@@ -598,21 +631,21 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
   const double* asyn = S.asyn + (size_t)b * F;
   const double* jssc = S.jssc + (size_t)b * F;
   // new photon density (microphysics.h:516-523)
-  const double fac = dr / c_light / vol;
-  const double acc_ne = acc / ne, anp_ne = acc * np / ne;
+  const double fac = scal[kScalFac];
+  const double acc_ne = scal[kScalAccNe], anp_ne = scal[kScalAnpNe];
   bool bad = false, seen = false;
-  double umax = 0.;
+  int uexp = 0;
   for (int k = tid; k < F; k += kStepThreads) {
     const double js = jsyn[k], cs = (num && ssc) ? jssc[k] : 0.;
     const double nk = js * fac * g.inv_hnu[k] + cs * fac * g.inv_hnu[k];
     n[k] = nk;
-    umax = fmax(umax, nk * g.dnu_nu[k]);
+    uexp = max(uexp, exp_field(nk * g.dnu_nu[k]));
     // totals and normalisation (microphysics.h:540-586)
     const double tj0 = js + cs;
     const double ta = asyn[k] * anp_ne;
     const double ti = intensity_approx(tj0 * acc, ta * dr);
     const double tj = tj0 * acc_ne;
-    if (!isfinite(tj) || tj < 0.) bad = true;
+    if (bad_value(tj)) bad = true;
     if (out.j_all) out.j_all[row * F + k] = tj;
     if (out.a_all) out.a_all[row * F + k] = ta;
     if (out.f_all) out.f_all[row * F + k] = nk;
@@ -643,8 +676,8 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
     }
   }
   // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k for the next step's SSC contraction
-  umax = block_max(umax, red_d);
-  const double su = pow2_scale(umax);
+  uexp = block_max_int(uexp, red_i);
+  const double su = scale_from_exp(uexp);
   if (ssc) {
     float* U = S.U32 + (size_t)b * F;
     for (int k = tid; k < F; k += kStepThreads) U[k] = (float)(n[k] * g.dnu_nu[k] * su);
@@ -655,7 +688,7 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
     int fl = flags;
     if (any_seen) fl |= kFlagSynSeen;
     if (ssc) {
-      S.scal[(size_t)b * kScal + kScalSU] = 1. / su;
+      S.scal[(size_t)b * kScal + kScalSU] = unscale_from_exp(uexp);
       fl |= kFlagUValid;
     }
     S.flags[b] = fl;
@@ -664,6 +697,12 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
     else if (dense_syn && !(fl & kFlagSynSeen) && step > 0)
       set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);  // microphysics.h:627-631
   }
+}
+
+__global__ void __launch_bounds__(kStepThreads)
+k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm,
+           int step, pbag_outputs out) {
+  finalize_bw(g, S, off, prm, blockIdx.x, step, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -680,8 +719,9 @@ cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_
 }
 
 cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
-                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step, cudaStream_t st) {
-  k_evolve<<<nbw, kStepThreads, 0, st>>>(g, S, recs, ss, off, prm, step);
+                          const int64_t* off, const pbag_shock_params* prm, int nbw, int step,
+                          const pbag_outputs& out, cudaStream_t st) {
+  k_evolve<<<nbw, kStepThreads, 0, st>>>(g, S, recs, ss, off, prm, step, out);
   return cudaGetLastError();
 }
 
