@@ -473,16 +473,20 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.dnu_nu, dnu));
   ok(c->grid_upload(&d.inv_hnu, inv_hnu));
   ok(c->grid_upload(&d.ssa_nu, ssa_nu));
-  d.Kint32 = nullptr;
+  d.Gs = (G + 3) / 4 * 4;
+  d.kint_stage = 0;
+  d.KintT = nullptr;
   d.kscale = nullptr;
   d.K32 = nullptr;
   d.Bt = nullptr;
   if (c->ssc) {
-    std::vector<float> Kint32, K32;
+    std::vector<float> KintT, K32;
     std::vector<double> kscale;
     std::vector<uint16_t> Bt;
-    build_ssc_tables(e.data(), G, nu.data(), F, c->Gp, Kint32, kscale, K32);
-    ok(c->grid_upload(&d.Kint32, Kint32));
+    build_ssc_tables(e.data(), G, nu.data(), F, c->Gp, d.Gs, KintT, kscale, K32);
+    ok(c->grid_upload(&d.KintT, KintT));
+    const size_t kbytes = KintT.size() * sizeof(float);
+    d.kint_stage = kbytes <= kKintStageMax ? (int)kbytes : 0;
     ok(c->grid_upload(&d.kscale, kscale));
     ok(c->grid_upload(&d.K32, K32));
     if (ssc_tc_supported(F)) {

@@ -15,6 +15,9 @@ constexpr int kMaxPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;
 constexpr int kRadThreads = 128;      // threads of one radiation CTA
 constexpr int kRadLanes = 8;          // threads per frequency in a radiation CTA
 constexpr int kRadFreqs = kRadThreads / kRadLanes;  // frequencies per radiation CTA
+constexpr int kStepWarps = kStepThreads / 32;
+constexpr int kKintStageMax = 112 * 1024;  // largest SSC kernel-integral table staged in shared memory
+constexpr int kScanMaxSub = 96;       // below this many substeps the solve is a parallel scan
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
 constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 
@@ -41,8 +44,10 @@ struct DevGrid {
   const double* dnu_nu;  // [F]   (nu[k+1]-nu[k])/nu[k]
   const double* inv_hnu; // [F]   1/(h nu) (microphysics.h:520)
   const double* ssa_nu;  // [F]   -1/(8 pi m_e nu^2) (numeric_model.h:211)
-  const float* Kint32;   // [G][F] SSC kernel integral / kscale[k] (kernels.h:79-91)
-  const double* kscale;  // [F]   power-of-two column scales of Kint32
+  int Gs;                // G rounded up to a multiple of 4 (row stride of KintT)
+  int kint_stage;        // bytes of KintT the evolve kernel stages in shared memory (0: read from L2)
+  const float* KintT;    // [F][Gs] SSC kernel integral / kscale[k] (kernels.h:79-91), k-major
+  const double* kscale;  // [F]   power-of-two column scales of KintT
   const float* K32;      // [F][Gp][F] SSC kernel (i, j, k) in FP32, j >= G zero
   const uint16_t* Bt;    // SSC kernel as BF16 hi/lo tensor-core operand slabs (pbag_ssc_tc.cu), or null
 };

@@ -32,11 +32,14 @@ void build_ssc_tc_operand(const std::vector<float>& K32, int F, int Gp, std::vec
 cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
                           cudaStream_t st);
 
-// SSC kernel tables on the host (kernels.h:49-117): Kint32[G][F] = Kint / kscale[k]
-// with power-of-two column scales, and K32[F][Gp][F] (i, j, k) in FP32,
-// j >= G zero-padded.
-void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, std::vector<float>& Kint32,
+// SSC kernel tables on the host (kernels.h:49-117): KintT[F][Gs] = Kint[j][k] /
+// kscale[k] stored k-major (row k, column j < G, zero beyond) with power-of-two
+// column scales, and K32[F][Gp][F] (i, j, k) in FP32, j >= G zero-padded.
+void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, int Gs, std::vector<float>& KintT,
                       std::vector<double>& kscale, std::vector<float>& K32);
+// dynamic shared memory of k_evolve for this grid, and the largest for any grid
+size_t evolve_smem_bytes(const DevGrid& g);
+size_t evolve_smem_max_bytes();
 
 }  // namespace pbag
 

@@ -34,7 +34,7 @@ double ssc_nava(double nu, double gam, double nu_tilde) {
 
 }  // namespace
 
-void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, std::vector<float>& Kint32,
+void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, int Gs, std::vector<float>& KintT,
                       std::vector<double>& kscale, std::vector<float>& K32) {
   std::vector<double> K((size_t)F * G * F);
   const unsigned hw = std::thread::hardware_concurrency();
@@ -65,9 +65,9 @@ void build_ssc_tables(const double* gam, int G, const double* freq, int F, int G
       kscale[k] = std::ldexp(1., ex);  // >= m, so the scaled column is <= 1
     }
   }
-  Kint32.assign((size_t)G * F, 0.f);
+  KintT.assign((size_t)F * Gs, 0.f);
   for (int j = 0; j < G; j++)
-    for (int k = 0; k < F; k++) Kint32[(size_t)j * F + k] = (float)(Kint[(size_t)j * F + k] / kscale[k]);
+    for (int k = 0; k < F; k++) KintT[(size_t)k * Gs + j] = (float)(Kint[(size_t)j * F + k] / kscale[k]);
   K32.assign((size_t)F * Gp * F, 0.f);
   for (int i = 0; i < F; i++)
     for (int j = 0; j < G; j++)

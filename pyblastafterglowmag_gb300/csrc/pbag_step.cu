@@ -262,25 +262,164 @@ __device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* 
                             const pbag_shock_params* __restrict__ prm, int b, int step, const pbag_outputs& out);
 
 // ---------------------------------------------------------------------------
+// Chang-Cooper substeps (numeric_model.h:19-43, 682-708) of one blastwave-step.
+// With dispersion 0 the system is upper bidiagonal and each substep is
+//   f_j <- a_j + beta_j f_{j+1},  a_j = f_j / b_j + Q_j dt / b_j,  beta_j = -c_j / b_j,
+// with a, b, c the same in every substep of a step. Thread t owns bins
+// t*C .. t*C+C-1 in registers (fr, ib = 1/b, qb = Q dt / b, bt = beta).
+// Both solvers below return whether a value checked before a substep was
+// negative or not finite (solve() checks f first, numeric_model.h:688).
+
+// Parallel suffix scan over the threads: the composition of the affine maps
+// x -> A_t + P_t x of all threads to the right gives every thread the value of
+// its right neighbour's first bin; the products P (the betas) are the same in
+// every substep and are formed once. Cost per substep: C + 5 + (warps) + C
+// dependent FMAs, so it wins for few substeps.
+template <int C>
+__device__ bool cc_scan(double (&fr)[C], const double (&ib)[C], const double (&qb)[C], const double (&bt)[C],
+                        int n_sub, double (*xs)[kStepWarps], double* pw0) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double P = 1.;
+#pragma unroll
+  for (int q = 0; q < C; ++q) P *= bt[q];
+  double pk[5];
+  double Pc = P;
+#pragma unroll
+  for (int lev = 0; lev < 5; ++lev) {
+    const int d = 1 << lev;
+    const double Po = __shfl_down_sync(0xffffffffu, Pc, d);
+    pk[lev] = Pc;
+    if (lane + d < 32) Pc *= Po;
+  }
+  // Pc: product of the betas from this thread to the end of its warp
+  double Pwn = __shfl_down_sync(0xffffffffu, Pc, 1);
+  if (lane == 31) Pwn = 1.;
+  if (lane == 0) pw0[warp] = Pc;
+  __syncthreads();
+  double pwr[kStepWarps];
+#pragma unroll
+  for (int v = 0; v < kStepWarps; ++v) pwr[v] = pw0[v];
+  bool bad = false;
+  for (int m = 0; m < n_sub; ++m) {
+    double a[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      bad |= bad_value(fr[q]);
+      a[q] = fma(fr[q], ib[q], qb[q]);
+    }
+    double A = a[C - 1];
+#pragma unroll
+    for (int q = C - 2; q >= 0; --q) A = fma(bt[q], A, a[q]);
+    double Sx = A;
+#pragma unroll
+    for (int lev = 0; lev < 5; ++lev) {
+      const int d = 1 << lev;
+      const double So = __shfl_down_sync(0xffffffffu, Sx, d);
+      if (lane + d < 32) Sx = fma(pk[lev], So, Sx);
+    }
+    double Sn = __shfl_down_sync(0xffffffffu, Sx, 1);
+    if (lane == 31) Sn = 0.;
+    if (lane == 0) xs[m & 1][warp] = Sx;
+    __syncthreads();
+    // value of the first bin of the next warp
+    double carry = 0.;
+#pragma unroll
+    for (int v = kStepWarps - 1; v > 0; --v)
+      if (v > warp) carry = fma(pwr[v], carry, xs[m & 1][v]);
+    double fn = fma(Pwn, carry, Sn);  // first bin of the right neighbour
+#pragma unroll
+    for (int q = C - 1; q >= 0; --q) {
+      fr[q] = fma(bt[q], fn, a[q]);
+      fn = fr[q];
+    }
+  }
+  return bad;
+}
+
+// Systolic pipeline: thread t runs substep m at tick m + (T-1-t), taking the
+// right neighbour's new first bin of the same substep from the tick before.
+// n_sub + T - 1 ticks of C dependent FMAs: it wins for many substeps.
+template <int C>
+__device__ bool cc_systolic(double (&fr)[C], const double (&ib)[C], const double (&qb)[C], const double (&bt)[C],
+                            int n_sub, int T, double (*xs)[kStepWarps]) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < 2 * kStepWarps) (&xs[0][0])[tid] = 0.;
+  __syncthreads();
+  double low = 0.;
+  bool bad = false;
+  const int ticks = n_sub + T - 1;
+  for (int tau = 0; tau < ticks; ++tau) {
+    double up = __shfl_down_sync(0xffffffffu, low, 1);
+    if (lane == 31) up = warp + 1 < kStepWarps ? xs[tau & 1][warp + 1] : 0.;
+    const int m = tau - (T - 1 - tid);
+    if (tid < T && m >= 0 && m < n_sub) {
+      double fn = up;
+#pragma unroll
+      for (int q = C - 1; q >= 0; --q) {
+        bad |= bad_value(fr[q]);
+        const double a = fma(fr[q], ib[q], qb[q]);
+        fr[q] = fma(bt[q], fn, a);
+        fn = fr[q];
+      }
+      low = fr[0];
+    }
+    if (lane == 0) xs[(tau + 1) & 1][warp] = low;
+    __syncthreads();
+  }
+  return bad;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// bounded wait on phase `parity` of an mbarrier
+__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (it > 16) __nanosleep(32);
+  }
+  return false;
+}
+
+// Dynamic shared memory of k_evolve: [staged KintT][N(gamma) | f/gamma^2 | SSA
+// weights (G doubles each)][seed-photon weights (F floats)].
+__host__ __device__ inline size_t evolve_stage_bytes(const DevGrid& g) { return ((size_t)g.kint_stage + 127) / 128 * 128; }
+__host__ __device__ inline size_t evolve_bytes(const DevGrid& g) {
+  return evolve_stage_bytes(g) + 3 * (size_t)g.G * sizeof(double) + (size_t)g.F * sizeof(float);
+}
+
+// ---------------------------------------------------------------------------
+// One step of every blastwave, one CTA each, C gamma bins per thread in the solve.
+template <int C>
 __global__ void __launch_bounds__(kStepThreads)
 k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const StepScal* __restrict__ ss,
          const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step, pbag_outputs out) {
   const int b = blockIdx.x;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = g.G, F = g.F;
   // the previous step's photon field, totals and history rows (same CTA shape)
   if (step > 0) {
     finalize_bw(g, S, off, prm, b, step - 1, out);
     __syncthreads();  // its flag and error updates are visible below
   }
-  __shared__ double sh_f[PBAG_MAX_BINS];   // heating term, then N(gamma)
-  __shared__ double sh_t[PBAG_MAX_BINS];   // f / gamma^2
-  __shared__ double sh_vd[PBAG_MAX_BINS];  // SSA weights
-  __shared__ float sh_v[PBAG_MAX_BINS];    // seed-photon weights for the SSC cooling GEMV
-  __shared__ double red_d[kStepThreads / 32];
-  __shared__ int red_i[kStepThreads / 32];
-  __shared__ double xfer[2][kStepThreads / 32];
-  __shared__ int sh_bad;
+  extern __shared__ __align__(128) unsigned char evo_smem[];
+  float* sh_k = reinterpret_cast<float*>(evo_smem);  // staged KintT
+  double* sh_f = reinterpret_cast<double*>(evo_smem + evolve_stage_bytes(g));  // heating term, then N(gamma)
+  double* sh_t = sh_f + G;                                                      // f / gamma^2
+  double* sh_vd = sh_t + G;                                                     // SSA weights
+  float* sh_v = reinterpret_cast<float*>(sh_vd + G);  // seed-photon weights of the SSC cooling GEMV
+  __shared__ double red_d[kStepWarps];
+  __shared__ int red_i[3][kStepWarps];
+  __shared__ double xs[2][kStepWarps];
+  __shared__ double pw0[kStepWarps];
+  __shared__ __align__(8) uint64_t kbar;
 
   int flags = S.flags[b];
   const int64_t r0 = off[b], len = off[b + 1] - off[b];
@@ -290,7 +429,6 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     sc = ss[r0 + step];
     active = (sc.flags & kRecValid) != 0;
   }
-  if (tid == 0) sh_bad = 0;
   __syncthreads();  // every thread has read flags before thread 0 rewrites them
   if (tid == 0) S.flags[b] = flags & ~kFlagActive;
   if (!active) return;
@@ -308,6 +446,14 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   double* f = S.f + (size_t)b * G;
   const double* pp = S.powp + (size_t)b * G;
   const double Kb = (sc.flags & kRecFast) ? sc.K : sc.K * r.gamma_c;
+  // the stateful SSA derivative of the last step, needed at the end
+  double* dfde = S.dfde + (size_t)b * G;
+  double dpre[C];
+#pragma unroll
+  for (int k = 0; k < C; ++k) {
+    const int i = tid + k * kStepThreads;
+    dpre[k] = (P.ssa_on && i < G) ? dfde[i] : 0.;
+  }
 
   if (sc.flags & kRecInit) {
     // ---- initializeElectronDistribution (microphysics.h:347-357): untouched
@@ -318,6 +464,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
       if (i < G - 1) v *= accel;
       f[i] = v;
+      sh_f[i] = v;
     }
     flags |= kFlagInit;
   } else if (sc.n_sub == 0) {
@@ -327,12 +474,42 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(g, sc, pp, i);
       else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
       f[i] = v;
+      sh_f[i] = v;
     }
   } else {
     // ---- Chang-Cooper evolution (microphysics.h:451-480)
-    const bool ssc = P.ssc_on && g.K32 != nullptr;
+    const bool ssc = P.ssc_on && g.KintT != nullptr;
+    const bool staged = ssc && g.kint_stage > 0;
+    if (staged && tid == 0) {
+      // the kernel-integral table streams into shared memory while the
+      // seed-photon weights are formed
+      const uint32_t bar = smem_addr(&kbar);
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)g.kint_stage)
+                   : "memory");
+      const unsigned char* src = reinterpret_cast<const unsigned char*>(g.KintT);
+      for (int o = 0; o < g.kint_stage; o += 32768) {
+        const uint32_t n = (uint32_t)min(32768, g.kint_stage - o);
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(evo_smem + o)),
+            "l"(src + o), "r"(n), "r"(bar)
+            : "memory");
+      }
+    }
     const double delta_t = sc.dt_sub;
     const int n_sub = sc.n_sub;
+    // this thread's bins j = tid*C + q: state and per-bin tables, loaded early
+    double fr[C], ppq[C], odg[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int j = tid * C + q;
+      const bool in = j < G;
+      fr[q] = in ? f[j] : 0.;
+      ppq[q] = in ? pp[j] : 0.;
+      odg[q] = in ? g.inv_dgb[j] : 0.;
+    }
     double sv = 1., usv = 1.;
     if (ssc) {  // seed-photon weights n_k dnu_k / nu_k, scaled by the kernel-integral columns
       const double* n = S.n + (size_t)b * F;
@@ -342,12 +519,22 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
         sh_t[k] = v;  // (sh_t is free until the weights below)
         vexp = max(vexp, exp_field(v));
       }
-      vexp = block_max_int(vexp, red_i);
+      vexp = block_max_int(vexp, red_i[0]);
       sv = scale_from_exp(vexp);
       usv = unscale_from_exp(vexp);
       for (int k = tid; k < F; k += kStepThreads) sh_v[k] = k < F - 1 ? (float)(sh_t[k] * sv) : 0.f;
     }
     __syncthreads();
+    if (staged) {
+      const int miss = __syncthreads_or(mbar_wait_bounded(smem_addr(&kbar), 0) ? 0 : 1);
+      if (miss) {
+        if (tid == 0) {
+          set_error(S, b, PBAG_ERR_TIMEOUT, step, __LINE__);
+          mbar_wait_bounded(smem_addr(&kbar), 0);  // the copy must land before the CTA exits
+        }
+        return;
+      }
+    }
     // heating / cooling terms at the half grid (numeric_model.h:753-801);
     // constant over the substeps, so evaluated once per step
     const double c_syn = sigma_T / (6. * M_PI * m_e * c_light) * B * B;
@@ -355,15 +542,23 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     double* gsyn = S.gdot + (size_t)b * 3 * G;
     double* gadi = gsyn + G;
     double* gssc = gadi + G;
+    const int Gs = g.Gs;
     bool hbad = false;
     for (int i = tid; i < G - 1; i += kStepThreads) {
       const double vs = c_syn * g.half2[i];
       const double va = sc.dlnVdt * g.hadi[i];
       double vc = gssc[i];
       if (ssc) {
-        const float* kr = g.Kint32 + (size_t)i * F;
         float acc = 0.f;
-        for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], __ldg(kr + k), acc);
+        if (staged) {
+          const float* kc = sh_k + i;
+#pragma unroll 8
+          for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], kc[(size_t)k * Gs], acc);
+        } else {
+          const float* kc = g.KintT + i;
+#pragma unroll 16
+          for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], __ldg(kc + (size_t)k * Gs), acc);
+        }
         vc = c_ssc * (double)acc * g.ihalf2[i];
         gssc[i] = vc;
       }
@@ -374,132 +569,129 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       sh_f[i] = H;
     }
     if (tid == 0) sh_f[G - 1] = 0.;  // heating_term[G-1] is never set (numeric_model.h:761)
-    if (hbad) atomicOr(&sh_bad, 1);
-    __syncthreads();
-    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
+    if (__syncthreads_or(hbad ? 1 : 0)) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
     // tridiagonal coefficients (numeric_model.h:539-675 with dispersion = 0,
     // delta_j = 0): a = 0, b_k = 1 + dt H_{k-1}/dgb_k (b_0 = b_{G-1} = 1),
-    // c_k = -dt H_k/dgb_k (c_{G-1} = 0). Each substep is the back
-    // substitution f_k = (f_k + Q_k dt)/b_k - (c_k/b_k) f_{k+1}
-    // (numeric_model.h:19-43, 682-708).
-    const int c = (G + kStepThreads - 1) / kStepThreads;
-    const int T = (G + c - 1) / c;  // threads that own bins
-    double fr[kMaxPerThread], ib[kMaxPerThread], qb[kMaxPerThread], bt[kMaxPerThread];
+    // c_k = -dt H_k/dgb_k (c_{G-1} = 0)
+    double ib[C], qb[C], bt[C];
 #pragma unroll
-    for (int q = 0; q < kMaxPerThread; ++q) {
-      const int j = tid * c + q;
-      fr[q] = ib[q] = qb[q] = bt[q] = 0.;
-      if (q < c && j < G) {
-        const double odgb = g.inv_dgb[j];
+    for (int q = 0; q < C; ++q) {
+      const int j = tid * C + q;
+      ib[q] = qb[q] = bt[q] = 0.;
+      if (j < G) {
         const double Hb = (j > 0 && j < G - 1) ? sh_f[j - 1] : 0.;  // b_0 and b_{G-1} see no inflow
         const double Hf = j < G - 1 ? sh_f[j] : 0.;
-        const double bb = 1. + (odgb * Hb) * delta_t;
-        const double cc = (odgb * Hf) * -delta_t;
-        const double Q = (j >= sc.iq0 && j < sc.iq1) ? sc.Ns * pp[j] : 0.;
+        const double bb = 1. + (odg[q] * Hb) * delta_t;
+        const double cc = (odg[q] * Hf) * -delta_t;
+        const double Q = (j >= sc.iq0 && j < sc.iq1) ? sc.Ns * ppq[q] : 0.;
         ib[q] = 1. / bb;
         bt[q] = -(cc * ib[q]);
         qb[q] = (Q * delta_t) * ib[q];
-        fr[q] = f[j];
       }
     }
-    // systolic substeps: thread t handles substep m = tau - (T-1-t)
-    const int lane = tid & 31, warp = tid >> 5;
-    if (tid < 2 * (kStepThreads / 32)) (&xfer[0][0])[tid] = 0.;
-    __syncthreads();
-    double low = 0.;
-    bool sbad = false;
-    const int ticks = n_sub + T - 1;
-    for (int tau = 0; tau < ticks; ++tau) {
-      double up = __shfl_down_sync(0xffffffffu, low, 1);
-      if (lane == 31) up = warp + 1 < kStepThreads / 32 ? xfer[tau & 1][warp + 1] : 0.;
-      const int m = tau - (T - 1 - tid);
-      if (tid < T && m >= 0 && m < n_sub) {
-        double fn = up;
+    const int T = (G + C - 1) / C;  // threads that own bins
+    const bool sbad = n_sub < kScanMaxSub ? cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0)
+                                          : cc_systolic<C>(fr, ib, qb, bt, n_sub, T, xs);
+    __syncthreads();  // every heating value has been read: sh_f takes N(gamma)
 #pragma unroll
-        for (int q = kMaxPerThread - 1; q >= 0; --q) {
-          if (q < c) {
-            sbad |= bad_value(fr[q]);  // solve() checks f before each substep (numeric_model.h:688)
-            const double a = fma(fr[q], ib[q], qb[q]);
-            fr[q] = fma(bt[q], fn, a);
-            fn = fr[q];
-          }
-        }
-        low = fr[0];
+    for (int q = 0; q < C; ++q) {
+      const int j = tid * C + q;
+      if (j < G) {
+        f[j] = fr[q];
+        sh_f[j] = fr[q];
       }
-      if (lane == 0) xfer[(tau + 1) & 1][warp] = low;
-      __syncthreads();
     }
-    if (sbad) atomicOr(&sh_bad, 1);
-#pragma unroll
-    for (int q = 0; q < kMaxPerThread; ++q) {
-      const int j = tid * c + q;
-      if (q < c && j < G) f[j] = fr[q];
-    }
-    __syncthreads();
-    if (sh_bad) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
+    if (__syncthreads_or(sbad ? 1 : 0)) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
   }
   __syncthreads();
 
-  // ---- per-step weights of the radiation sums (microphysics.h:498-558)
-  for (int i = tid; i < G; i += kStepThreads) {
-    const double fi = f[i];
-    sh_f[i] = fi;
-    sh_t[i] = fi * g.inv_e2[i];  // f / e / e (numeric_model.h:194-195)
-  }
-  __syncthreads();
-  // the power-of-two scales come from the largest exponent field
+  // ---- per-step weights of the radiation sums (microphysics.h:498-558):
+  // N_e and the power-of-two scales in one block reduction
   double ne = 0.;
   int wexp = 0, Wexp = 0;
-  for (int i = tid; i < G - 1; i += kStepThreads) {
-    const double w = sh_f[i] * g.de[i];
-    ne += w;  // N_e (microphysics.h:556-558)
-    wexp = max(wexp, exp_field(w));
-    Wexp = max(Wexp, exp_field(w * g.inv_e2[i]));
+#pragma unroll
+  for (int k = 0; k < C; ++k) {
+    const int i = tid + k * kStepThreads;
+    if (i < G) {
+      const double fi = sh_f[i];
+      sh_t[i] = fi * g.inv_e2[i];  // f / e / e (numeric_model.h:194-195)
+      if (i < G - 1) {
+        const double w = fi * g.de[i];
+        ne += w;  // N_e (microphysics.h:556-558)
+        wexp = max(wexp, exp_field(w));
+        Wexp = max(Wexp, exp_field(w * g.inv_e2[i]));
+      }
+    }
   }
-  ne = block_sum(ne, red_d);
-  wexp = block_max_int(wexp, red_i);
-  Wexp = block_max_int(Wexp, red_i);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ne += __shfl_down_sync(0xffffffffu, ne, o);
+  wexp = __reduce_max_sync(0xffffffffu, wexp);
+  Wexp = __reduce_max_sync(0xffffffffu, Wexp);
+  if (lane == 0) {
+    red_d[warp] = ne;
+    red_i[1][warp] = wexp;
+    red_i[2][warp] = Wexp;
+  }
+  __syncthreads();  // publishes sh_t and the partial results
+  ne = 0.;
+  wexp = Wexp = 0;
+#pragma unroll
+  for (int v = 0; v < kStepWarps; ++v) {
+    ne += red_d[v];
+    wexp = max(wexp, red_i[1][v]);
+    Wexp = max(Wexp, red_i[2][v]);
+  }
   const double sw = scale_from_exp(wexp);
   float* w32 = S.w32 + (size_t)b * G;
   for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
-  // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
-  int vexp = 0;
-  if (P.ssa_on) {
-    double* dfde = S.dfde + (size_t)b * G;
-    for (int i = tid; i < G; i += kStepThreads) {
-      const double t = sh_t[i];
-      double d = dfde[i];
-      if (positive(t)) {
-        if (i == 0)
-          d = -1.5 * t + 2. * sh_t[1] - 0.5 * sh_t[2];
-        else if (i == G - 1)
-          d = 1.5 * t - 2. * sh_t[G - 2] + 0.5 * sh_t[G - 3];
-        else
-          d = 0.5 * (sh_t[i + 1] - sh_t[i - 1]) * g.inv_dxm[i];
-        dfde[i] = d;
-      }
-      if (i < G - 1) {
-        const double v = g.e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
-        sh_vd[i] = v;
-        vexp = max(vexp, exp_field(v));
-      }
-    }
-    vexp = block_max_int(vexp, red_i);  // (its barriers also publish sh_vd)
-    const double sv = scale_from_exp(vexp);
-    float* v32 = S.v32 + (size_t)b * G;
-    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? (float)(sh_vd[i] * sv) : 0.f;
-  }
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   if (P.ssc_on && g.K32 != nullptr) {
     const double sW = scale_from_exp(Wexp);
     float* W = S.W32 + (size_t)b * g.Gp;
     for (int j = tid; j < g.Gp; j += kStepThreads)
       W[j] = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
-    if (tid == 0) S.scal[(size_t)b * kScal + kScalSW] = 3. / 4. * sigma_T * c_light * unscale_from_exp(Wexp);
+  }
+  // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
+  int vexp = 0;
+  if (P.ssa_on) {
+#pragma unroll
+    for (int k = 0; k < C; ++k) {
+      const int i = tid + k * kStepThreads;
+      if (i < G) {
+        const double t = sh_t[i];
+        double d = dpre[k];
+        if (positive(t)) {
+          if (i == 0)
+            d = -1.5 * t + 2. * sh_t[1] - 0.5 * sh_t[2];
+          else if (i == G - 1)
+            d = 1.5 * t - 2. * sh_t[G - 2] + 0.5 * sh_t[G - 3];
+          else
+            d = 0.5 * (sh_t[i + 1] - sh_t[i - 1]) * g.inv_dxm[i];
+          dfde[i] = d;
+        }
+        if (i < G - 1) {
+          const double v = g.e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
+          sh_vd[i] = v;
+          vexp = max(vexp, exp_field(v));
+        }
+      }
+    }
+    vexp = __reduce_max_sync(0xffffffffu, vexp);
+    if (lane == 0) red_i[0][warp] = vexp;
+  }
+  __syncthreads();  // publishes sh_vd and the SSA scale
+  if (P.ssa_on) {
+    vexp = 0;
+#pragma unroll
+    for (int v = 0; v < kStepWarps; ++v) vexp = max(vexp, red_i[0][v]);
+    const double svd = scale_from_exp(vexp);
+    float* v32 = S.v32 + (size_t)b * G;
+    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? (float)(sh_vd[i] * svd) : 0.f;
   }
   if (!positive(ne) && !is_nan(ne)) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // n_ele <= 0 (microphysics.h:560-563)
   if (tid == 0) {
     double* scal = S.scal + (size_t)b * kScal;
+    if (P.ssc_on && g.K32 != nullptr) scal[kScalSW] = 3. / 4. * sigma_T * c_light * unscale_from_exp(Wexp);
     scal[kScalDr] = sc.dr;
     scal[kScalVol] = sc.vol;
     scal[kScalNele] = ne;
@@ -721,7 +913,16 @@ cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_
 cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
                           const int64_t* off, const pbag_shock_params* prm, int nbw, int step,
                           const pbag_outputs& out, cudaStream_t st) {
-  k_evolve<<<nbw, kStepThreads, 0, st>>>(g, S, recs, ss, off, prm, step, out);
+  const size_t smem = evolve_bytes(g);
+  const int c = (g.G + kStepThreads - 1) / kStepThreads;
+  if (c <= 1)
+    k_evolve<1><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
+  else if (c <= 2)
+    k_evolve<2><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
+  else if (c <= 4)
+    k_evolve<4><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
+  else
+    k_evolve<8><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
   return cudaGetLastError();
 }
 
@@ -751,9 +952,24 @@ cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* 
   return cudaGetLastError();
 }
 
+size_t evolve_smem_bytes(const DevGrid& g) { return evolve_bytes(g); }
+size_t evolve_smem_max_bytes() {
+  return ((size_t)kKintStageMax + 127) / 128 * 128 + 3 * (size_t)PBAG_MAX_BINS * sizeof(double) +
+         (size_t)PBAG_MAX_BINS * sizeof(float);
+}
+
 cudaError_t configure_kernels() {
   const int smem = ssc_smem_max_bytes();
+  const int esmem = (int)evolve_smem_max_bytes();
   cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_evolve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_evolve<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_evolve<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_evolve<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
+    return e;
   if ((e = cudaFuncSetAttribute(k_rad_ssc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(k_rad_ssc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
