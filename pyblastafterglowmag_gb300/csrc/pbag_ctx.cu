@@ -144,6 +144,7 @@ struct pbag_ctx {
   void free_state() {
     for (void* p : state_mem) cudaFree(p);
     state_mem.clear();
+    S.Abf = nullptr;
     cap_bw = 0;
     d_off = nullptr;
     d_first = nullptr;
@@ -179,10 +180,13 @@ struct pbag_ctx {
     if ((e = state_alloc(&S.powp, cap * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.gdot, cap * 3 * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.n, cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.jsyn, cap * F)) != cudaSuccess) return e;
-    if ((e = state_alloc(&S.asyn, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.syn32, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.ssa32, cap * F)) != cudaSuccess) return e;
+    if ((e = state_alloc(&S.rad32, cap * 4)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.jssc, cap * F)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.W32, cap * Gp)) != cudaSuccess) return e;
+    if (dg.Bt && (e = state_alloc(&S.Abf, (cap + kTcCols - 1) / kTcCols * tc_tile_elems(kTcCols, Gp))) != cudaSuccess)
+      return e;
     if ((e = state_alloc(&S.U32, cap * F)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.w32, cap * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.v32, cap * G)) != cudaSuccess) return e;
@@ -222,6 +226,9 @@ struct pbag_ctx {
     if ((e = z(S.jssc, n * F * sizeof(double))) != cudaSuccess) return e;
     if ((e = z(S.U32, n * F * sizeof(float))) != cudaSuccess) return e;
     if ((e = z(S.W32, n * Gp * sizeof(float))) != cudaSuccess) return e;
+    if (S.Abf && (e = z(S.Abf, (n + kTcCols - 1) / kTcCols * tc_tile_elems(kTcCols, Gp) * sizeof(uint16_t))) !=
+                     cudaSuccess)
+      return e;
     if ((e = z(S.scal, n * kScal * sizeof(double))) != cudaSuccess) return e;
     if ((e = z(S.flags, n * sizeof(int))) != cudaSuccess) return e;
     return z(S.err, n * 4 * sizeof(int));
@@ -418,7 +425,7 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   const double step = std::exp(std::log(g->gam2) / (double)G);
   std::vector<double> inv_e(G), inv_e2(G), de(G - 1), e2de(G - 1), inv_dxm(G, 0.), half2(G - 1), hadi(G - 1),
       ihalf2(G - 1), dg(G + 1), inv_dgb(G), dnu(F), inv_hnu(F), ssa_nu(F);
-  std::vector<float> ginv2(G), psq(G);
+  std::vector<float> ginv2(G), psq(G), ginv23(G), nu13(F), nu32(F);
   for (int i = 0; i < G; ++i) {
     inv_e[i] = 1. / e[i];
     inv_e2[i] = 1. / e[i] / e[i];
@@ -440,10 +447,13 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   for (int i = 0; i < G; ++i) {
     ginv2[i] = (float)(1. / (e[i] * e[i]));
     psq[i] = (float)(e[i] * e[i] - 1.);
+    ginv23[i] = (float)std::pow(e[i], -2. / 3.);
     if (e[i] <= 2.) n_cyc = i + 1;
   }
   for (int k = 0; k < F; ++k) {
     dnu[k] = (nu[k + 1] - nu[k]) / nu[k];
+    nu13[k] = (float)std::cbrt(nu[k]);
+    nu32[k] = (float)nu[k];
     inv_hnu[k] = 1. / (cgs::h_pl * nu[k]);
     ssa_nu[k] = -1. / (8. * M_PI * cgs::m_e * nu[k] * nu[k]);
   }
@@ -469,6 +479,9 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.inv_dgb, inv_dgb));
   ok(c->grid_upload(&d.ginv2, ginv2));
   ok(c->grid_upload(&d.psq32, psq));
+  ok(c->grid_upload(&d.ginv23, ginv23));
+  ok(c->grid_upload(&d.nu13, nu13));
+  ok(c->grid_upload(&d.nu32, nu32));
   ok(c->grid_upload(&d.nu, nu));
   ok(c->grid_upload(&d.dnu_nu, dnu));
   ok(c->grid_upload(&d.inv_hnu, inv_hnu));

@@ -13,9 +13,10 @@ namespace pbag {
 constexpr int kStepThreads = 128;     // threads per blastwave in the evolve / finalize kernels
 constexpr int kMaxPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // gamma bins per thread
 constexpr int kRadThreads = 128;      // threads of one radiation CTA
-constexpr int kRadLanes = 8;          // threads per frequency in a radiation CTA
+constexpr int kRadLanes = 32;         // threads per frequency in a radiation CTA (one warp)
 constexpr int kRadFreqs = kRadThreads / kRadLanes;  // frequencies per radiation CTA
 constexpr int kStepWarps = kStepThreads / 32;
+constexpr int kFinalPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // frequencies per thread in finalize
 constexpr int kKintStageMax = 112 * 1024;  // largest SSC kernel-integral table staged in shared memory
 constexpr int kScanMaxSub = 96;       // below this many substeps the solve is a parallel scan
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
@@ -40,7 +41,10 @@ struct DevGrid {
   const double* inv_dgb; // [G]   1/delta_grid_bar (numeric_model.h:556)
   const float* ginv2;    // [G]   1/e[j]^2 (FP32, synchrotron argument)
   const float* psq32;    // [G]   e[j]^2 - 1 in FP32 (cyclotron branch)
+  const float* ginv23;   // [G]   e[j]^(-2/3): cube root of the 1/e^2 factor of the synchrotron argument
   const double* nu;      // [F+1] frequency grid, nu[F] = next logspace point
+  const float* nu13;     // [F]   cube root of nu
+  const float* nu32;     // [F]   nu in FP32
   const double* dnu_nu;  // [F]   (nu[k+1]-nu[k])/nu[k]
   const double* inv_hnu; // [F]   1/(h nu) (microphysics.h:520)
   const double* ssa_nu;  // [F]   -1/(8 pi m_e nu^2) (numeric_model.h:211)
@@ -86,10 +90,12 @@ struct DevState {
   double* powp;    // [nbw][G]   e^-p of the blastwave's injection index
   double* gdot;    // [nbw][3][G] gam_dot_syn, _adi, _ssc (last substep)
   double* n;       // [nbw][F]   photon density total_rad.f of the previous step
-  double* jsyn;    // [nbw][F]   synchrotron emissivity of this step
-  double* asyn;    // [nbw][F]   SSA absorption of this step
+  float* syn32;    // [nbw][F]   FP32 synchrotron sum of this step (scaled by the w32 scale)
+  float2* ssa32;   // [nbw][F]   FP32 SSA sum and its compensation (scaled by the v32 scale)
+  float* rad32;    // [nbw][4]   FP32 scalars of the radiation kernel: 1/nu_crit(B,1), 1/nu_larmor(B), cbrt(1/nu_crit)
   double* jssc;    // [nbw][F]   SSC emissivity of this step
   float* W32;      // [nbw][Gp]  SSC electron weights, scaled to FP32
+  uint16_t* Abf;   // [ceil(nbw/256)][2*256*Gp] the same weights as BF16 hi/lo tensor-core operand tiles
   float* U32;      // [nbw][F]   SSC seed-photon weights, scaled to FP32
   float* w32;      // [nbw][G]   synchrotron weights f_j (e_{j+1}-e_j), scaled
   float* v32;      // [nbw][G]   SSA weights e_j^2 (e_{j+1}-e_j) dfde_j, scaled
@@ -110,8 +116,7 @@ enum : int {
   kScalSw = 8,     // scale of w32
   kScalSv = 9,     // scale of v32
   kScalPref = 10,  // synchrotron prefactor of this step
-  kScalIncrit = 11,  // 1/nu_crit(B,1) of this step
-  kScalInlar = 12,   // 1/nu_larmor(B) of this step
+  // 11, 12 unused
   kScalFac = 13,     // photon escape factor (dr/c)/vol (microphysics.h:517-518)
   kScalAccNe = 14,   // accel_frac / N_e
   kScalAnpNe = 15,   // accel_frac n' / N_e
@@ -124,6 +129,24 @@ enum : int {
   kFlagSynSeen = 4,  // a non-zero synchrotron emissivity was produced (dense check)
   kFlagUValid = 8    // U32/sU hold the previous step's photon field
 };
+
+// ---- tensor-core operand layout (pbag_ssc_tc.cu) ----------------------------
+// A K-major BF16 operand of `rows` rows (output columns k of one SSC kernel
+// slab, or the blastwaves of one tile) and Gp columns (gamma, a multiple of 16)
+// is stored in chunks of kTcChunk columns; chunk c (kc8 = its number of
+// 8-column groups) holds the hi part, then the lo part, each as rows/8 x kc8
+// core matrices of 8 rows x 16 bytes, row group major. The first n rows of a
+// part are therefore its first n/8 row groups, contiguous.
+constexpr int kTcCols = 256;  // blastwaves per tensor-core tile (MMA N at most)
+constexpr int kTcChunk = 32;  // K columns per chunk
+__host__ __device__ inline size_t tc_operand_offset(int row, int col, int rows, int Gp, bool lo) {
+  const int c = col / kTcChunk, kl = col % kTcChunk;
+  const int left = Gp / 8 - c * (kTcChunk / 8);
+  const int kc8 = left < kTcChunk / 8 ? left : kTcChunk / 8;
+  return (size_t)2 * rows * kTcChunk * c + (lo ? (size_t)rows * kc8 * 8 : 0) +
+         (size_t)((row >> 3) * kc8 + (kl >> 3)) * 64 + (row & 7) * 8 + (kl & 7);
+}
+__host__ __device__ inline size_t tc_tile_elems(int rows, int Gp) { return (size_t)2 * rows * Gp; }
 
 // Power of two close to 1/max|x| (exact rescaling); 1 when max is 0, not
 // finite, or so small that the inverse would overflow.
@@ -173,12 +196,12 @@ __device__ __forceinline__ double unscale_from_exp(int E) {
 // All return the dimensionless shape R; the caller multiplies by the FP64
 // prefactor sqrt(3) q^3 B / (m_e c^2) of kernels.h:427,434,471.
 
-// Aharonian+2010 eq. D7 fit (kernels.h:420-427), x = nu / nu_crit. Beyond
-// x = 150 the factor exp(-x) is below the smallest FP32 subnormal, so the
-// value is 0 (this also keeps x^(4/3) from overflowing for huge x).
-__device__ __forceinline__ float aharonian_R32(float x) {
+// Aharonian+2010 eq. D7 fit (kernels.h:420-427), x = nu / nu_crit, y = x^(1/3)
+// (the caller forms y as a product of tabulated cube roots). Beyond x = 150
+// the factor exp(-x) is below the smallest FP32 subnormal, so the value is 0
+// (this also keeps x^(4/3) from overflowing for huge x).
+__device__ __forceinline__ float aharonian_R32(float x, float y) {
   if (!(x <= 150.f)) return x > 150.f ? 0.f : x;  // NaN propagates
-  float y = cbrtf(x);
   float y2 = y * y;
   float y4 = y2 * y2;
   float num = fmaf(0.347f, y4, fmaf(2.21f, y2, 1.f));

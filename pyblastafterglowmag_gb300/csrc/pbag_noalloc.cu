@@ -71,7 +71,11 @@ size_t scratch_need(int nbw, size_t nrec, int G, int F, int Gp) {
   c.take<int64_t>(n);
   for (int k = 0; k < 3; ++k) c.take<double>(n * G);  // f, dfde, powp
   c.take<double>(n * 3 * G);                          // gdot
-  for (int k = 0; k < 4; ++k) c.take<double>(n * F);  // n, jsyn, asyn, jssc
+  c.take<double>(n * F);                              // n
+  c.take<float>(n * F);                               // syn32
+  c.take<float2>(n * F);                              // ssa32
+  c.take<float>(n * 4);                               // rad32
+  c.take<double>(n * F);                              // jssc
   c.take<float>(n * Gp);                              // W32
   c.take<float>(n * F);                               // U32
   c.take<float>(n * G);                               // w32
@@ -177,8 +181,9 @@ extern "C" int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_
   S.powp = cv.take<double>(n * v.G);
   S.gdot = cv.take<double>(n * 3 * v.G);
   S.n = cv.take<double>(n * v.F);
-  S.jsyn = cv.take<double>(n * v.F);
-  S.asyn = cv.take<double>(n * v.F);
+  S.syn32 = cv.take<float>(n * v.F);
+  S.ssa32 = cv.take<float2>(n * v.F);
+  S.rad32 = cv.take<float>(n * 4);
   S.jssc = cv.take<double>(n * v.F);
   S.W32 = cv.take<float>(n * v.Gp);
   S.U32 = cv.take<float>(n * v.F);

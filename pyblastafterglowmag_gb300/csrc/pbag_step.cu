@@ -18,6 +18,7 @@
 //                   and the O(F^2 G) SSC contraction (pbag_ssc.cu), in one launch.
 //   k_finalize    : photon field, totals, normalisation, intensity and history
 //                   rows (microphysics.h:516-633).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "pbag_device.cuh"
@@ -645,11 +646,22 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   float* w32 = S.w32 + (size_t)b * G;
   for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
+  // (FP32 for the CUDA-core contraction, BF16 hi + lo tiles for the tensor cores)
   if (P.ssc_on && g.K32 != nullptr) {
     const double sW = scale_from_exp(Wexp);
     float* W = S.W32 + (size_t)b * g.Gp;
-    for (int j = tid; j < g.Gp; j += kStepThreads)
-      W[j] = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
+    uint16_t* A = S.Abf ? S.Abf + (size_t)(b / kTcCols) * tc_tile_elems(kTcCols, g.Gp) : nullptr;
+    const int m = b % kTcCols;
+    for (int j = tid; j < g.Gp; j += kStepThreads) {
+      const float w = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
+      W[j] = w;
+      if (A) {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(w - __bfloat162float(hi));
+        A[tc_operand_offset(m, j, kTcCols, g.Gp, false)] = __bfloat16_as_ushort(hi);
+        A[tc_operand_offset(m, j, kTcCols, g.Gp, true)] = __bfloat16_as_ushort(lo);
+      }
+    }
   }
   // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
   int vexp = 0;
@@ -705,52 +717,53 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     scal[kScalSw] = unscale_from_exp(wexp);
     scal[kScalSv] = unscale_from_exp(vexp);
     scal[kScalPref] = sc.pref;
-    scal[kScalIncrit] = (double)sc.inv_ncrit;
-    scal[kScalInlar] = (double)sc.inv_nlar;
+    float* rp = S.rad32 + (size_t)b * 4;
+    rp[0] = sc.inv_ncrit;
+    rp[1] = sc.inv_nlar;
+    rp[2] = cbrtf(sc.inv_ncrit);
+    rp[3] = 0.f;
     S.flags[b] = flags | kFlagActive;
   }
 #undef PBAG_FAIL
 }
 
 // ---------------------------------------------------------------------------
-// Synchrotron emissivity and SSA absorption of one blastwave for kRadFreqs
-// frequencies: kRadLanes threads per frequency split the gamma sum; the synchrotron
-// kernel values are generated in FP32 on the fly and never stored.
-__device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk,
-                              int step) {
+// Synchrotron and SSA sums of one blastwave for kRadFreqs frequencies: one warp
+// per frequency splits the gamma sum over its lanes; the synchrotron kernel
+// values are generated in FP32 on the fly and never stored. The kernel has no
+// FP64 instruction (each costs a warp 64 cycles of its SM sub-partition's
+// FP64 unit on this part): the FP64 prefactors are applied by finalize_bw.
+__device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk) {
   const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
-  __shared__ float sw_[PBAG_MAX_BINS];
-  __shared__ float sv_[PBAG_MAX_BINS];
   if (!(S.flags[b] & kFlagActive)) return;
   const bool ssa = prm[b].ssa_on != 0;
   const bool dermer = prm[b].syn_method == PBAG_SYN_DER09;
-  for (int i = tid; i < G; i += kRadThreads) {
-    sw_[i] = S.w32[(size_t)b * G + i];
-    sv_[i] = ssa ? S.v32[(size_t)b * G + i] : 0.f;
-  }
-  __syncthreads();
-  const double* scal = S.scal + (size_t)b * kScal;
-  const float incrit = (float)scal[kScalIncrit], inlar = (float)scal[kScalInlar];
+  const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);
+  const float incrit = rp.x, inlar = rp.y;
   const int kq = tid / kRadLanes, jl = tid % kRadLanes;
   const int k = kblk * kRadFreqs + kq;
   const int kk = k < F ? k : F - 1;
-  const double nu = g.nu[kk];
-  const float a_k = (float)nu * incrit;
-  const float xl = (float)nu * inlar;
+  const float nu = g.nu32[kk];
+  const float a_k = nu * incrit;          // x = a_k / e_j^2
+  const float y_k = g.nu13[kk] * rp.z;    // x^(1/3) = y_k e_j^(-2/3)
+  const float xl = nu * inlar;
   const int jcyc = dermer ? 0 : g.n_cyc;
+  const float* w = S.w32 + (size_t)b * G;
+  const float* v = S.v32 + (size_t)b * G;
   float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
   for (int j = jl; j < G - 1; j += kRadLanes) {
-    const float R = j >= jcyc ? aharonian_R32(a_k * g.ginv2[j]) : cyclotron_R32(g.psq32[j], xl);
-    acc = fmaf(R, sw_[j], acc);
+    const float R = j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
+                              : cyclotron_R32(__ldg(g.psq32 + j), xl);
+    acc = fmaf(R, __ldg(w + j), acc);
     if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
-      const float x = R * sv_[j];
+      const float x = R * __ldg(v + j);
       const float t = as + x;
       ac += fabsf(as) >= fabsf(x) ? (as - t) + x : (x - t) + as;
       as = t;
     }
   }
-  // combine the kRadLanes partial sums of each frequency (adjacent lanes)
+  // combine the kRadLanes partial sums of each frequency
 #pragma unroll
   for (int o = 1; o < kRadLanes; o <<= 1) {
     acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -762,17 +775,8 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
     ac = ac + oc + e;
   }
   if (jl == 0 && k < F) {
-    const double pref = scal[kScalPref];
-    const double js = k < F - 1 ? pref * ((double)acc * scal[kScalSw]) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
-    if (bad_value(js)) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
-    S.jsyn[(size_t)b * F + k] = js;
-    double a = 0.;
-    if (ssa) {
-      a = pref * (((double)as + (double)ac) * scal[kScalSv]) * g.ssa_nu[k];  // numeric_model.h:206-211
-      a = fabs(a);
-      if (not_finite(a)) a = 1e99;
-    }
-    S.asyn[(size_t)b * F + k] = a;
+    S.syn32[(size_t)b * F + k] = acc;
+    S.ssa32[(size_t)b * F + k] = ssa ? make_float2(as, ac) : make_float2(0.f, 0.f);
   }
 }
 
@@ -780,10 +784,11 @@ template <int KPT>
 __global__ void __launch_bounds__(kRadThreads)
 k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int step) {
   static_assert(kRadThreads == kSscThreads, "radiation and SSC tiles share the launch shape");
+  (void)step;
   const int blk = blockIdx.x;
   const int rc = (g.F + kRadFreqs - 1) / kRadFreqs;
   if (blk < rad_blocks) {
-    radiate_block(g, S, prm, blk / rc, blk % rc, step);
+    radiate_block(g, S, prm, blk / rc, blk % rc);
   } else {
     ssc_block<KPT>(g, S, nbw, blk - rad_blocks);
   }
@@ -819,22 +824,50 @@ __device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* 
   const bool dense_syn = out.syn_j_all || out.syn_a_all || out.syn_i_all;
   const size_t row = (size_t)(off[b] + step);
   double* n = S.n + (size_t)b * F;
-  const double* jsyn = S.jsyn + (size_t)b * F;
-  const double* asyn = S.asyn + (size_t)b * F;
+  const float* syn32 = S.syn32 + (size_t)b * F;
+  const float2* ssa32 = S.ssa32 + (size_t)b * F;
   const double* jssc = S.jssc + (size_t)b * F;
+  // synchrotron emissivity and SSA absorption from the FP32 sums
+  // (numeric_model.h:148-238): the prefactor and the power-of-two scales
+  const double pref = scal[kScalPref], ssw = scal[kScalSw], ssv = scal[kScalSv];
+  double jsv[kFinalPerThread], asv[kFinalPerThread];
+  bool jbad = false;
+#pragma unroll
+  for (int q = 0; q < kFinalPerThread; ++q) {
+    const int k = tid + q * kStepThreads;
+    jsv[q] = asv[q] = 0.;
+    if (k < F) {
+      const double js = k < F - 1 ? pref * ((double)syn32[k] * ssw) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
+      if (bad_value(js)) jbad = true;
+      jsv[q] = js;
+      if (P.ssa_on) {
+        const float2 sa = ssa32[k];
+        double a = fabs(pref * (((double)sa.x + (double)sa.y) * ssv) * g.ssa_nu[k]);  // numeric_model.h:206-211
+        if (not_finite(a)) a = 1e99;
+        asv[q] = a;
+      }
+    }
+  }
+  if (__syncthreads_or(jbad ? 1 : 0)) {
+    if (tid == 0) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
+    return;
+  }
   // new photon density (microphysics.h:516-523)
   const double fac = scal[kScalFac];
   const double acc_ne = scal[kScalAccNe], anp_ne = scal[kScalAnpNe];
   bool bad = false, seen = false;
   int uexp = 0;
-  for (int k = tid; k < F; k += kStepThreads) {
-    const double js = jsyn[k], cs = (num && ssc) ? jssc[k] : 0.;
+#pragma unroll
+  for (int q = 0; q < kFinalPerThread; ++q) {
+    const int k = tid + q * kStepThreads;
+    if (k >= F) continue;
+    const double js = jsv[q], cs = (num && ssc) ? jssc[k] : 0.;
     const double nk = js * fac * g.inv_hnu[k] + cs * fac * g.inv_hnu[k];
     n[k] = nk;
     uexp = max(uexp, exp_field(nk * g.dnu_nu[k]));
     // totals and normalisation (microphysics.h:540-586)
     const double tj0 = js + cs;
-    const double ta = asyn[k] * anp_ne;
+    const double ta = asv[q] * anp_ne;
     const double ti = intensity_approx(tj0 * acc, ta * dr);
     const double tj = tj0 * acc_ne;
     if (bad_value(tj)) bad = true;
@@ -845,7 +878,7 @@ __device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* 
     // storeDenseOutput (microphysics.h:602-633)
     if (dense_syn) {
       const double sj = js * acc;
-      const double sa = asyn[k] * anp_ne;
+      const double sa = asv[q] * anp_ne;
       if (out.syn_j_all) out.syn_j_all[row * F + k] = sj;
       if (out.syn_a_all) out.syn_a_all[row * F + k] = sa;
       if (out.syn_i_all) out.syn_i_all[row * F + k] = intensity_approx(sj, sa * dr);
