@@ -187,7 +187,10 @@ struct pbag_ctx {
     if ((e = state_alloc(&S.W32, cap * Gp)) != cudaSuccess) return e;
     if (dg.Bt && (e = state_alloc(&S.Abf, (cap + kTcCols - 1) / kTcCols * tc_tile_elems(kTcCols, Gp))) != cudaSuccess)
       return e;
-    if ((e = state_alloc(&S.U32, cap * F)) != cudaSuccess) return e;
+    // whole tensor-core tiles of rows: the SSC kernel copies U a tile at a time
+    const size_t urows = dg.Bt ? (cap + kTcCols - 1) / kTcCols * kTcCols : cap;
+    if ((e = state_alloc(&S.U32, urows * F)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.U32, 0, urows * F * sizeof(float), stream)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.w32, cap * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.v32, cap * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.scal, cap * kScal)) != cudaSuccess) return e;
@@ -486,6 +489,20 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.dnu_nu, dnu));
   ok(c->grid_upload(&d.inv_hnu, inv_hnu));
   ok(c->grid_upload(&d.ssa_nu, ssa_nu));
+  // the evolve kernel's tables in one block (GridTab layout)
+  d.Ge = (G + 1) / 2 * 2;
+  d.Fe = (F + 1) / 2 * 2;
+  d.etab_doubles = kTabG * d.Ge + kTabF * d.Fe;
+  std::vector<double> etab((size_t)d.etab_doubles, 0.);
+  {
+    const std::vector<double>* gsrc[kTabG] = {&inv_e, &inv_e2, &de, &e2de, &inv_dxm, &half2, &hadi, &ihalf2, &inv_dgb};
+    for (int t = 0; t < kTabG; ++t) std::copy(gsrc[t]->begin(), gsrc[t]->end(), etab.begin() + (size_t)t * d.Ge);
+    const size_t fb = (size_t)kTabG * d.Ge;
+    std::copy(dnu.begin(), dnu.end(), etab.begin() + fb + (size_t)kTabDnuNu * d.Fe);
+    std::copy(inv_hnu.begin(), inv_hnu.end(), etab.begin() + fb + (size_t)kTabInvHnu * d.Fe);
+    std::fill(etab.begin() + fb + (size_t)kTabKscale * d.Fe, etab.begin() + fb + (size_t)kTabKscale * d.Fe + F, 1.);
+    std::copy(ssa_nu.begin(), ssa_nu.end(), etab.begin() + fb + (size_t)kTabSsaNu * d.Fe);
+  }
   d.Gs = (G + 3) / 4 * 4;
   d.kint_stage = 0;
   d.KintT = nullptr;
@@ -501,6 +518,7 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     const size_t kbytes = KintT.size() * sizeof(float);
     d.kint_stage = kbytes <= kKintStageMax ? (int)kbytes : 0;
     ok(c->grid_upload(&d.kscale, kscale));
+    std::copy(kscale.begin(), kscale.end(), etab.begin() + (size_t)kTabG * d.Ge + (size_t)kTabKscale * d.Fe);
     ok(c->grid_upload(&d.K32, K32));
     if (ssc_tc_supported(F)) {
       build_ssc_tc_operand(K32, F, c->Gp, Bt);
@@ -508,6 +526,7 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     }
     ok(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
   }
+  ok(c->grid_upload(&d.etab, etab));
   ok(cudaStreamSynchronize(c->stream));
   if (err != cudaSuccess) {
     const int code = cuda_code(err);

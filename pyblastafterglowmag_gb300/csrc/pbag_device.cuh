@@ -54,6 +54,21 @@ struct DevGrid {
   const double* kscale;  // [F]   power-of-two column scales of KintT
   const float* K32;      // [F][Gp][F] SSC kernel (i, j, k) in FP32, j >= G zero
   const uint16_t* Bt;    // SSC kernel as BF16 hi/lo tensor-core operand slabs (pbag_ssc_tc.cu), or null
+  const double* etab;    // the FP64 tables of the evolve kernel in one block (GridTab), staged by one bulk copy
+  int Ge, Fe;            // G and F rounded up to even (sub-table strides of etab)
+  int etab_doubles;      // size of etab: kTabG * Ge + kTabF * Fe
+};
+
+// Layout of DevGrid::etab: G tables at t * Ge, then F tables at kTabG * Ge + u * Fe.
+enum : int {
+  kTabInvE = 0, kTabInvE2, kTabDe, kTabE2de, kTabInvDxm, kTabHalf2, kTabHadi, kTabIhalf2, kTabInvDgb, kTabG
+};
+enum : int { kTabDnuNu = 0, kTabInvHnu, kTabKscale, kTabSsaNu, kTabF };
+struct GridTab {
+  const double* p;  // etab in global or shared memory
+  int Ge, Fe;
+  __host__ __device__ const double* gt(int t) const { return p + t * Ge; }
+  __host__ __device__ const double* ft(int u) const { return p + kTabG * Ge + u * Fe; }
 };
 
 // Per-record scalars of one step, computed once for the whole batch by

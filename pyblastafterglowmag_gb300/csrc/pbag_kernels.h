@@ -37,8 +37,7 @@ cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* B
 // column scales, and K32[F][Gp][F] (i, j, k) in FP32, j >= G zero-padded.
 void build_ssc_tables(const double* gam, int G, const double* freq, int F, int Gp, int Gs, std::vector<float>& KintT,
                       std::vector<double>& kscale, std::vector<float>& K32);
-// dynamic shared memory of k_evolve for this grid, and the largest for any grid
-size_t evolve_smem_bytes(const DevGrid& g);
+// the largest dynamic shared memory of k_evolve for any grid
 size_t evolve_smem_max_bytes();
 
 }  // namespace pbag

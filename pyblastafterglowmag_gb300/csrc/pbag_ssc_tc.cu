@@ -39,17 +39,37 @@ namespace pbag {
 namespace {
 
 constexpr int kTcThreads = 128;
-constexpr int kTcK = 128;        // accumulator rows (output columns k) per half of the frequency grid
-constexpr int kTcStages = 3;
+constexpr int kTcK = 128;          // accumulator rows (output columns k) per half of the frequency grid
+constexpr int kTcMaxStages = 8;    // ring of chunk stages (all chunks of a small problem at once)
 constexpr int kK8 = kTcChunk / 8;  // 16-byte K columns of a full chunk
 constexpr int kWaitLimit = 1 << 21;
 constexpr int kPStride = kTcK + 1;  // row stride (floats) of the epilogue's product table
+constexpr size_t kTcBodyMax = 200 * 1024;  // stages (or product table) + U tile
+constexpr size_t kTcUSmemMax = 64 * 1024;  // largest U tile staged in shared memory
 
-// dynamic shared memory of one launch: stages of [A hi | A lo (F rows each) | B hi | B lo (N rows each)]
+// Dynamic shared memory of one launch: [body: ring of stages of [A hi | A lo (F
+// rows each) | B hi | B lo (N rows each)], reused by the product table][U tile
+// (N x F floats) when it fits][barriers].
 __host__ __device__ constexpr uint32_t tc_a_region(int F) { return 2u * F * kK8 * 16; }
 __host__ __device__ constexpr uint32_t tc_stage_bytes(int F, int N) { return tc_a_region(F) + 2u * N * kK8 * 16; }
-__host__ __device__ constexpr size_t tc_smem_bytes(int F, int N) {
-  return 1024 + (size_t)kTcStages * tc_stage_bytes(F, N) + 8 * 2 * kTcStages + 16;
+struct TcPlan {
+  int S;            // stages
+  uint32_t body;    // bytes of the stage ring / product table
+  uint32_t ubytes;  // bytes of the U tile in shared memory (0: read from global)
+  size_t smem;      // dynamic shared memory
+};
+inline TcPlan tc_plan(int F, int N, int Gp) {
+  TcPlan p;
+  const int nchunks = (Gp / 8 + kK8 - 1) / kK8;
+  const uint32_t stage = tc_stage_bytes(F, N);
+  const size_t ub = (size_t)N * F * sizeof(float);
+  p.ubytes = ub <= kTcUSmemMax ? (uint32_t)ub : 0u;
+  const size_t room = kTcBodyMax - p.ubytes;
+  p.S = std::max(2, std::min({nchunks, kTcMaxStages, (int)(room / stage)}));
+  p.body = std::max<uint32_t>((uint32_t)p.S * stage, (uint32_t)(N * kPStride * sizeof(float)));
+  p.body = (p.body + 1023) / 1024 * 1024;
+  p.smem = 1024 + (size_t)p.body + p.ubytes + 16 * kTcMaxStages + 16;
+  return p;
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -96,15 +116,17 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
 
 // One CTA: output frequency i = blockIdx.x, blastwaves kTcCols*blockIdx.y + [0, N).
 // Thread 0 streams the chunks of the kernel slab (A, F rows) and of the weight
-// tile (B, N rows) through a ring of stages and issues the MMAs; all threads
-// run the epilogue. H = F / 128 accumulator halves.
+// tile (B, N rows) through a ring of S stages and issues the MMAs; all threads
+// run the epilogue. H = F / 128 accumulator halves. Every load that does not
+// depend on another is issued first, the copies before the tensor-memory
+// allocation.
 template <int H, bool kSplit>
 __global__ void __launch_bounds__(kTcThreads)
-k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int Gp, int nrows, int N,
-         const int* __restrict__ flags, const float* __restrict__ U32, const double* __restrict__ scal,
-         const double* __restrict__ nu, double* __restrict__ out, int* __restrict__ err) {
+k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int Gp, int nrows, int N, int S,
+         uint32_t body, uint32_t ubytes, const int* __restrict__ flags, const float* __restrict__ U32,
+         const double* __restrict__ scal, const double* __restrict__ nu, double* __restrict__ out,
+         int* __restrict__ err) {
   constexpr int F = kTcK * H;
-  constexpr int S = kTcStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
@@ -112,22 +134,77 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
   const uint32_t stage_bytes = tc_stage_bytes(F, N);
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + (size_t)S * stage_bytes);  // full[S], empty[S]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S);
+  float* Us = reinterpret_cast<float*>(base + body);                   // U tile [N][F]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + body + ubytes);  // full[S], empty[S], U
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kTcMaxStages + 1);
   __shared__ int fail;
+  auto stage_ptr = [&](int st) { return base + (size_t)st * stage_bytes; };
 
-  // the blastwaves this thread finishes (columns tid and tid + 128) and their
-  // FP64 factors, loaded while the MMAs run
+  const int nk8 = Gp / 8;
+  const int nchunks = (nk8 + kK8 - 1) / kK8;
+  const uint16_t* Ai = Bt + (size_t)i * tc_tile_elems(F, Gp);                  // kernel slab of frequency i
+  const uint16_t* Bw = Abf + (size_t)blockIdx.y * tc_tile_elems(kTcCols, Gp);  // weight tile
+  auto load = [&](int c, int st) {
+    const int kc8 = min(kK8, nk8 - c * kK8);
+    const uint32_t ab = (kSplit ? 2u : 1u) * F * kc8 * 16;  // hi (+ lo), contiguous
+    const uint32_t bp = (uint32_t)N * kc8 * 16;              // first N rows of one part
+    const uint32_t bar = smem_u32(&bars[st]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(ab + (kSplit ? 2u : 1u) * bp)
+                 : "memory");
+    const uint16_t* bsrc = Bw + (size_t)2 * kTcCols * kTcChunk * c;
+    unsigned char* bdst = stage_ptr(st) + tc_a_region(F);
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(stage_ptr(st))),
+        "l"(Ai + (size_t)2 * F * kTcChunk * c), "r"(ab), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(bdst)),
+        "l"(bsrc), "r"(bp), "r"(bar)
+        : "memory");
+    if (kSplit)
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_u32(bdst + bp)),
+          "l"(bsrc + (size_t)kTcCols * kc8 * 8), "r"(bp), "r"(bar)
+          : "memory");
+  };
+  const int pre = min(S, nchunks);
+  const uint32_t ubar = smem_u32(&bars[2 * kTcMaxStages]);
+  if (tid == 0) {
+    fail = 0;
+    for (int s = 0; s < 2 * S; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int c = 0; c < pre; ++c) load(c, c);
+    if (ubytes) {  // the tile's seed-photon weights, rows as in global memory
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ubar), "r"(ubytes) : "memory");
+      const unsigned char* usrc = reinterpret_cast<const unsigned char*>(U32 + (size_t)row0 * F);
+      for (uint32_t o = 0; o < ubytes; o += 32768u)
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(reinterpret_cast<unsigned char*>(Us) + o)),
+            "l"(usrc + o), "r"(min(32768u, ubytes - o)), "r"(ubar)
+            : "memory");
+    }
+  }
+  // the blastwaves this thread finishes (columns tid and tid + 128) and their FP64 factors
   bool live[2];
   double fac[2];
   const double hnu = cgs::h_pl * nu[i];
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
     const int col = tid + q * kTcThreads, r = row0 + col;
-    live[q] = col < N && r < nrows && (flags[r] & kFlagActive);
-    fac[q] = live[q] ? hnu * scal[(size_t)r * kScal + kScalSW] * scal[(size_t)r * kScal + kScalSU] : 0.;
+    const bool in = col < N && r < nrows;
+    const int fl = in ? flags[r] : 0;
+    const double sw = in ? scal[(size_t)r * kScal + kScalSW] : 0.;
+    const double su = in ? scal[(size_t)r * kScal + kScalSU] : 0.;
+    live[q] = (fl & kFlagActive) != 0;
+    fac[q] = hnu * sw * su;
   }
-  // seed-photon weights U[b][k] of this thread's rows k (= tid + 128 h) for the first 16 columns
+  // without a staged U tile: this thread's U[b][k] (k = tid + 128 h) for the first 16 columns
   float u[H][16];
   auto load_u = [&](int cb, float (&dst)[H][16]) {
 #pragma unroll
@@ -138,15 +215,10 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
         dst[h][c] = r < nrows ? __ldg(U32 + (size_t)r * F + tid + kTcK * h) : 0.f;
       }
   };
-  load_u(0, u);
+  if (!ubytes) load_u(0, u);
 
   uint32_t ncols = 32;
   while (ncols < (uint32_t)(H * N)) ncols <<= 1;
-  if (tid == 0) {
-    fail = 0;
-    for (int s = 0; s < 2 * S; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(ncols));
@@ -157,94 +229,66 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  const int nk8 = Gp / 8;
-  const int nchunks = (nk8 + kK8 - 1) / kK8;
-  if (any && tid == 0) {
-    const uint16_t* Ai = Bt + (size_t)i * tc_tile_elems(F, Gp);                     // kernel slab of frequency i
-    const uint16_t* Bw = Abf + (size_t)blockIdx.y * tc_tile_elems(kTcCols, Gp);     // weight tile
-    auto stage_ptr = [&](int st) { return base + (size_t)st * stage_bytes; };
-    auto load = [&](int c, int st) {
-      const int kc8 = min(kK8, nk8 - c * kK8);
-      const uint32_t ab = (kSplit ? 2u : 1u) * F * kc8 * 16;  // hi (+ lo), contiguous
-      const uint32_t bp = (uint32_t)N * kc8 * 16;              // first N rows of one part
-      const uint32_t bar = smem_u32(&bars[st]);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                   "r"(ab + (kSplit ? 2u : 1u) * bp)
-                   : "memory");
-      const uint16_t* bsrc = Bw + (size_t)2 * kTcCols * kTcChunk * c;
-      unsigned char* bdst = stage_ptr(st) + tc_a_region(F);
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_u32(stage_ptr(st))),
-          "l"(Ai + (size_t)2 * F * kTcChunk * c), "r"(ab), "r"(bar)
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_u32(bdst)),
-          "l"(bsrc), "r"(bp), "r"(bar)
-          : "memory");
-      if (kSplit)
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(bdst + bp)),
-            "l"(bsrc + (size_t)kTcCols * kc8 * 8), "r"(bp), "r"(bar)
-            : "memory");
-    };
-    const uint32_t idesc = idesc_bf16(kTcK, N);
-    const int pre = min(S, nchunks);
-    for (int c = 0; c < pre; ++c) load(c, c);
+  if (tid == 0) {
     int loaded = pre;  // chunks whose copies were issued
     int next = 0;      // next chunk to consume
     bool ok = true;
-    for (; next < nchunks; ++next) {
-      const int c = next, st = c % S;
-      if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)(c / S) & 1)) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int kc8 = min(kK8, nk8 - c * kK8);
-      const uint32_t sbo = (uint32_t)kc8 * 128;
-      const uint32_t a_hi = smem_u32(stage_ptr(st)), a_lo = a_hi + (uint32_t)F * kc8 * 16;
-      const uint32_t b_hi = a_hi + tc_a_region(F), b_lo = b_hi + (uint32_t)N * kc8 * 16;
-#pragma unroll
-      for (int h = 0; h < H; ++h) {
-        const uint32_t ah = (uint32_t)h * kTcK * kc8 * 16;  // rows k of half h: row groups 16h ...
-        const uint32_t d = tmem + (uint32_t)(h * N);
-        for (int s2 = 0; s2 < kc8 / 2; ++s2) {
-          const uint32_t ko = (uint32_t)s2 * 256;  // two 16-byte K columns per MMA (K = 16)
-          mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc,
-                   (c > 0 || s2 > 0) ? 1u : 0u);
-          if (kSplit) {
-            mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_lo + ko, 128, sbo), idesc, 1);
-            mma_bf16(d, smem_desc(a_lo + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc, 1);
-          }
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&bars[S + st]))
-                   : "memory");
-      // refill the stage of the previous chunk once its MMAs are done (they
-      // complete while this chunk's MMAs run)
-      if (c >= 1 && loaded < nchunks) {
-        const int pc = c - 1, pst = pc % S;
-        if (!mbar_wait(smem_u32(&bars[S + pst]), (uint32_t)(pc / S) & 1)) {
+    if (any) {
+      const uint32_t idesc = idesc_bf16(kTcK, N);
+      for (; next < nchunks; ++next) {
+        const int c = next, st = c % S;
+        if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)(c / S) & 1)) {
           ok = false;
-          ++next;
           break;
         }
-        load(loaded, pst);
-        ++loaded;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int kc8 = min(kK8, nk8 - c * kK8);
+        const uint32_t sbo = (uint32_t)kc8 * 128;
+        const uint32_t a_hi = smem_u32(stage_ptr(st)), a_lo = a_hi + (uint32_t)F * kc8 * 16;
+        const uint32_t b_hi = a_hi + tc_a_region(F), b_lo = b_hi + (uint32_t)N * kc8 * 16;
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+          const uint32_t ah = (uint32_t)h * kTcK * kc8 * 16;  // rows k of half h: row groups 16h ...
+          const uint32_t d = tmem + (uint32_t)(h * N);
+          for (int s2 = 0; s2 < kc8 / 2; ++s2) {
+            const uint32_t ko = (uint32_t)s2 * 256;  // two 16-byte K columns per MMA (K = 16)
+            mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc,
+                     (c > 0 || s2 > 0) ? 1u : 0u);
+            if (kSplit) {
+              mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_lo + ko, 128, sbo), idesc, 1);
+              mma_bf16(d, smem_desc(a_lo + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc, 1);
+            }
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&bars[S + st]))
+                     : "memory");
+        // refill the stage of the previous chunk once its MMAs are done (they
+        // complete while this chunk's MMAs run)
+        if (c >= 1 && loaded < nchunks) {
+          const int pc = c - 1, pst = pc % S;
+          if (!mbar_wait(smem_u32(&bars[S + pst]), (uint32_t)(pc / S) & 1)) {
+            ok = false;
+            ++next;
+            break;
+          }
+          load(loaded, pst);
+          ++loaded;
+        }
+      }
+      if (ok) {
+        // the last commit completes after every earlier MMA of this thread
+        const int c = nchunks - 1;
+        ok = mbar_wait(smem_u32(&bars[S + c % S]), (uint32_t)(c / S) & 1);
       }
     }
-    if (ok) {
-      // the last commit completes after every earlier MMA of this thread
-      const int c = nchunks - 1;
-      ok = mbar_wait(smem_u32(&bars[S + c % S]), (uint32_t)(c / S) & 1);
-    } else {
-      // a bounded wait ran out: give the copies and MMAs in flight one more bounded wait each
+    if (ubytes && !mbar_wait(ubar, 0)) ok = false;
+    if (!any || !ok) {
+      // nothing to compute, or a bounded wait ran out: the copies and MMAs in
+      // flight get one more bounded wait each before the CTA exits
       for (int c = next; c < loaded; ++c) mbar_wait(smem_u32(&bars[c % S]), (uint32_t)(c / S) & 1);
       if (next > 0) mbar_wait(smem_u32(&bars[S + (next - 1) % S]), (uint32_t)((next - 1) / S) & 1);
+      if (ubytes) mbar_wait(ubar, 0);
     }
     if (!ok) {
       fail = 1;
@@ -263,7 +307,14 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
     const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
     for (int cb = 0; cb < N / 16; ++cb) {
       float un[H][16];
-      if (cb + 1 < N / 16) load_u(cb + 1, un);
+      if (ubytes) {
+#pragma unroll
+        for (int h = 0; h < H; ++h)
+#pragma unroll
+          for (int c = 0; c < 16; ++c) u[h][c] = Us[(size_t)(cb * 16 + c) * F + tid + kTcK * h];
+      } else if (cb + 1 < N / 16) {
+        load_u(cb + 1, un);
+      }
       float p[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) p[c] = 0.f;
@@ -281,7 +332,7 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
       }
 #pragma unroll
       for (int c = 0; c < 16; ++c) P[(size_t)(cb * 16 + c) * kPStride + tid] = p[c];
-      if (cb + 1 < N / 16) {
+      if (!ubytes && cb + 1 < N / 16) {
 #pragma unroll
         for (int h = 0; h < H; ++h)
 #pragma unroll
@@ -289,16 +340,21 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
       }
     }
     __syncthreads();
-    // sum over k for blastwaves tid and tid + 128
+    // sum over k for blastwaves tid and tid + 128 (four partial sums)
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       if (!live[q]) continue;
       const int col = tid + q * kTcThreads;
       const float* row = P + (size_t)col * kPStride;
-      float acc = 0.f;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
 #pragma unroll 8
-      for (int k = 0; k < kTcK; ++k) acc += row[k];
-      out[(size_t)(row0 + col) * F + i] = fac[q] * (double)acc;
+      for (int k = 0; k < kTcK; k += 4) {
+        a0 += row[k];
+        a1 += row[k + 1];
+        a2 += row[k + 2];
+        a3 += row[k + 3];
+      }
+      out[(size_t)(row0 + col) * F + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -314,16 +370,18 @@ cudaError_t launch_tc(const uint16_t* Abf, const uint16_t* Bt, int Gp, int nrows
                       const double* scal, const double* nu, double* out, int* err, cudaStream_t st) {
   constexpr int F = kTcK * H;
   const int N = std::min(kTcCols, (nrows + 15) / 16 * 16);
+  const TcPlan plan = tc_plan(F, N, Gp);
+  if (plan.smem > 2048 + kTcBodyMax + 16 * kTcMaxStages + 16) return cudaErrorInvalidConfiguration;
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_ssc_tc<H, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tc_smem_bytes(F, kTcCols));
+                                         (int)(2048 + kTcBodyMax + 16 * kTcMaxStages + 16));
     if (e != cudaSuccess) return e;
     attr = true;
   }
   dim3 grid(F, (nrows + kTcCols - 1) / kTcCols);
-  k_ssc_tc<H, kSplit><<<grid, kTcThreads, tc_smem_bytes(F, N), st>>>(Abf, Bt, Gp, nrows, N, flags, U32, scal, nu,
-                                                                       out, err);
+  k_ssc_tc<H, kSplit><<<grid, kTcThreads, plan.smem, st>>>(Abf, Bt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
+                                                             flags, U32, scal, nu, out, err);
   return cudaGetLastError();
 }
 

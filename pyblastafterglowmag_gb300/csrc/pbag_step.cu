@@ -122,12 +122,12 @@ __global__ void k_powp(DevGrid g, const pbag_shock_params* __restrict__ prm, int
 
 // Value of the analytic distribution (microphysics.h:237-278) at bin i, given
 // that i lies in branch a (first) or b (second).
-__device__ __forceinline__ double pl_branch_a(const DevGrid& g, const StepScal& s, const double* pp, int i) {
-  return (s.flags & kRecFast) ? s.K * s.c_fast * g.inv_e2[i] : s.K * pp[i];
+__device__ __forceinline__ double pl_branch_a(const GridTab& T, const StepScal& s, const double* pp, int i) {
+  return (s.flags & kRecFast) ? s.K * s.c_fast * T.gt(kTabInvE2)[i] : s.K * pp[i];
 }
-__device__ __forceinline__ double pl_branch_b(const DevGrid& g, const StepScal& s, const double* pp, int i,
+__device__ __forceinline__ double pl_branch_b(const GridTab& T, const StepScal& s, const double* pp, int i,
                                               double Kb) {
-  return Kb * pp[i] * g.inv_e[i];
+  return Kb * pp[i] * T.gt(kTabInvE)[i];
 }
 
 __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const int64_t* __restrict__ off,
@@ -181,8 +181,9 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   if (s.ib1 < s.ib0) s.ib1 = s.ib0;
   // the reference exits when an assigned entry is not finite or negative; the
   // entries of each branch decrease with gamma, so its first entry decides
-  bool pl_bad = (s.ia1 > s.ia0 && bad_value(pl_branch_a(g, s, pp, s.ia0))) ||
-                (s.ib1 > s.ib0 && bad_value(pl_branch_b(g, s, pp, s.ib0, Kb)));
+  const GridTab T{g.etab, g.Ge, g.Fe};
+  bool pl_bad = (s.ia1 > s.ia0 && bad_value(pl_branch_a(T, s, pp, s.ia0))) ||
+                (s.ib1 > s.ib0 && bad_value(pl_branch_b(T, s, pp, s.ib0, Kb)));
   // synchrotron kernel constants (kernels.h:194-202, 427, 471)
   const double B = q.B;
   const bool dermer = P.syn_method == PBAG_SYN_DER09;
@@ -259,8 +260,10 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   out[r] = s;
 }
 
-__device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* __restrict__ off,
-                            const pbag_shock_params* __restrict__ prm, int b, int step, const pbag_outputs& out);
+template <int FQ>
+__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
+                           const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
+                           float* sh_v, double* sh_usv, int* sh_state);
 
 // ---------------------------------------------------------------------------
 // Chang-Cooper substeps (numeric_model.h:19-43, 682-708) of one blastwave-step.
@@ -389,50 +392,172 @@ __device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-// Dynamic shared memory of k_evolve: [staged KintT][N(gamma) | f/gamma^2 | SSA
-// weights (G doubles each)][seed-photon weights (F floats)].
-__host__ __device__ inline size_t evolve_stage_bytes(const DevGrid& g) { return ((size_t)g.kint_stage + 127) / 128 * 128; }
-__host__ __device__ inline size_t evolve_bytes(const DevGrid& g) {
-  return evolve_stage_bytes(g) + 3 * (size_t)g.G * sizeof(double) + (size_t)g.F * sizeof(float);
+// bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) into
+// shared memory, completing on `bar`, in pieces of at most 32 KiB
+__device__ void bulk_to_smem(void* dst, const void* src, int bytes, uint32_t bar) {
+  for (int o = 0; o < bytes; o += 32768) {
+    const uint32_t n = (uint32_t)min(32768, bytes - o);
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(static_cast<unsigned char*>(dst) + o)),
+        "l"(static_cast<const unsigned char*>(src) + o), "r"(n), "r"(bar)
+        : "memory");
+  }
+}
+
+// Dynamic shared memory of k_evolve: [staged KintT (kstage bytes)][tables
+// (etab)][N(gamma) | f/gamma^2 | SSA weights (G doubles each)][seed-photon
+// weights (F floats)].
+__host__ __device__ inline size_t evolve_kint_bytes(int kstage) { return ((size_t)kstage + 127) / 128 * 128; }
+__host__ __device__ inline size_t evolve_bytes(const DevGrid& g, int kstage) {
+  return evolve_kint_bytes(kstage) + (size_t)g.etab_doubles * sizeof(double) + 3 * (size_t)g.G * sizeof(double) +
+         (size_t)g.F * sizeof(float);
+}
+
+// Largest dynamic shared memory of k_evolve. The kernel-integral table is
+// staged only for batches small enough to run with few CTAs per SM (larger
+// batches keep more CTAs per SM instead) and only when it fits.
+constexpr size_t kEvolveSmemMax = 220 * 1024;
+constexpr int kStageMaxBw = 304;
+inline int evolve_kint_stage(const DevGrid& g, int nbw) {
+  if (g.kint_stage <= 0 || nbw > kStageMaxBw) return 0;
+  return evolve_bytes(g, g.kint_stage) <= kEvolveSmemMax ? g.kint_stage : 0;
 }
 
 // ---------------------------------------------------------------------------
-// One step of every blastwave, one CTA each, C gamma bins per thread in the solve.
-template <int C>
-__global__ void __launch_bounds__(kStepThreads)
+// One step of every blastwave, one CTA each, C gamma bins per thread in the solve,
+// FQ frequencies per thread in the completion of the previous step.
+// Every global load that does not depend on another is issued at the start
+// (grid tables by one bulk copy into shared memory, the blastwave's state into
+// registers), so that the step pays few dependent memory round trips.
+template <int C, int FQ>
+__global__ void __launch_bounds__(kStepThreads, 1)
 k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const StepScal* __restrict__ ss,
-         const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step, pbag_outputs out) {
+         const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step, pbag_outputs out,
+         int kstage) {
   const int b = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = g.G, F = g.F;
-  // the previous step's photon field, totals and history rows (same CTA shape)
-  if (step > 0) {
-    finalize_bw(g, S, off, prm, b, step - 1, out);
-    __syncthreads();  // its flag and error updates are visible below
-  }
   extern __shared__ __align__(128) unsigned char evo_smem[];
   float* sh_k = reinterpret_cast<float*>(evo_smem);  // staged KintT
-  double* sh_f = reinterpret_cast<double*>(evo_smem + evolve_stage_bytes(g));  // heating term, then N(gamma)
-  double* sh_t = sh_f + G;                                                      // f / gamma^2
-  double* sh_vd = sh_t + G;                                                     // SSA weights
+  double* sh_tab = reinterpret_cast<double*>(evo_smem + evolve_kint_bytes(kstage));
+  double* sh_f = sh_tab + g.etab_doubles;  // heating term, then N(gamma)
+  double* sh_t = sh_f + G;                 // f / gamma^2; photon field of the previous step
+  double* sh_vd = sh_t + G;                // SSA weights
   float* sh_v = reinterpret_cast<float*>(sh_vd + G);  // seed-photon weights of the SSC cooling GEMV
   __shared__ double red_d[kStepWarps];
   __shared__ int red_i[3][kStepWarps];
   __shared__ double xs[2][kStepWarps];
   __shared__ double pw0[kStepWarps];
-  __shared__ __align__(8) uint64_t kbar;
+  __shared__ __align__(8) uint64_t bars[2];  // tables, kernel integral
+  __shared__ int sh_state[2];                // flags and error code after the previous step's completion
+  __shared__ double sh_usv;                  // inverse scale of sh_v
+  const GridTab T{sh_tab, g.Ge, g.Fe};
 
-  int flags = S.flags[b];
-  const int64_t r0 = off[b], len = off[b + 1] - off[b];
-  bool active = S.err[4 * b] == 0 && step < len;
-  StepScal sc;
-  if (active) {
-    sc = ss[r0 + step];
-    active = (sc.flags & kRecValid) != 0;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const int tb = g.etab_doubles * (int)sizeof(double);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bars[0])), "r"(tb)
+                 : "memory");
+    bulk_to_smem(sh_tab, g.etab, tb, smem_addr(&bars[0]));
   }
-  __syncthreads();  // every thread has read flags before thread 0 rewrites them
+  // independent loads of this blastwave
+  const int flags0 = S.flags[b];
+  const int err0 = S.err[4 * b];
+  const int64_t r0 = off[b], len = off[b + 1] - r0;
+  const pbag_shock_params P = prm[b];
+  double* f = S.f + (size_t)b * G;
+  const double* pp = S.powp + (size_t)b * G;
+  double* dfde = S.dfde + (size_t)b * G;
+  double fr[C], ppq[C], dpre[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    const int j = tid * C + q;  // solve: contiguous bins per thread
+    fr[q] = j < G ? f[j] : 0.;
+    ppq[q] = j < G ? pp[j] : 0.;
+    const int i = tid + q * kStepThreads;  // everything else: strided bins
+    dpre[q] = (P.ssa_on && i < G) ? dfde[i] : 0.;
+  }
+  // gamma-grid history rows of the previous step, written once it completes
+  const bool hist_g = step > 0 && (out.ele_f_all || out.gdot_syn_all || out.gdot_adi_all || out.gdot_ssc_all);
+  double hf[C], hgs[C], hga[C], hgc[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    const int i = tid + q * kStepThreads;
+    const bool in = hist_g && i < G;
+    const double* gd = S.gdot + (size_t)b * 3 * G;
+    hf[q] = in ? f[i] : 0.;
+    hgs[q] = in ? gd[i] : 0.;
+    hga[q] = in ? gd[G + i] : 0.;
+    hgc[q] = in ? gd[2 * G + i] : 0.;
+  }
+  const bool in_range = step < len;
+  StepScal sc{};
+  double accel = 0., B = 0., gamma_c = 0., n_prime = 0.;
+  if (in_range) {
+    sc = ss[r0 + step];
+    const pbag_step_rec& r = recs[r0 + step];
+    accel = r.accel_frac;
+    B = r.B;
+    gamma_c = r.gamma_c;
+    n_prime = r.n_prime;
+  }
+  const bool ssc = P.ssc_on && g.KintT != nullptr;
+  // the kernel-integral table streams into shared memory while the previous
+  // step completes, when this step runs the Chang-Cooper substeps with SSC
+  const bool staged = kstage > 0 && ssc && in_range && err0 == 0 && (sc.flags & kRecValid) && !sc.err &&
+                      !(sc.flags & kRecInit) && sc.n_sub > 0;
+  if (staged && tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bars[1])), "r"(kstage)
+                 : "memory");
+    bulk_to_smem(sh_k, g.KintT, kstage, smem_addr(&bars[1]));
+  }
+  __syncthreads();  // the barriers are initialised
+  auto drain = [&]() {  // copies must land before the CTA exits
+    if (tid == 0 && staged) mbar_wait_bounded(smem_addr(&bars[1]), 0);
+  };
+  if (__syncthreads_or(mbar_wait_bounded(smem_addr(&bars[0]), 0) ? 0 : 1)) {
+    if (tid == 0) {
+      set_error(S, b, PBAG_ERR_TIMEOUT, step, __LINE__);
+      mbar_wait_bounded(smem_addr(&bars[0]), 0);
+    }
+    drain();
+    return;
+  }
+
+  // the previous step's photon field, totals and history rows (same CTA shape);
+  // its photon field and seed-photon weights stay in shared memory
+  int flags = flags0, errc = err0;
+  bool have_v = false;
+  if (step > 0) {
+    const int fin = finalize_bw<FQ>(g, T, S, off, P, b, step - 1, out, flags0, err0, sh_v, &sh_usv, sh_state);
+    if (fin) {
+      __syncthreads();
+      flags = sh_state[0];
+      errc = sh_state[1];
+      have_v = fin == 1 && errc == 0;
+    }
+    if (fin == 1 && hist_g) {
+      const size_t row = (size_t)(r0 + step - 1);
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        const int i = tid + q * kStepThreads;
+        if (i >= G) continue;
+        if (out.ele_f_all) out.ele_f_all[row * G + i] = hf[q];
+        if (out.gdot_syn_all) out.gdot_syn_all[row * G + i] = hgs[q];
+        if (out.gdot_adi_all) out.gdot_adi_all[row * G + i] = hga[q];
+        if (out.gdot_ssc_all) out.gdot_ssc_all[row * G + i] = hgc[q];
+      }
+    }
+  }
+  const bool active = errc == 0 && in_range && (sc.flags & kRecValid);
   if (tid == 0) S.flags[b] = flags & ~kFlagActive;
-  if (!active) return;
+  if (!active) {
+    drain();
+    return;
+  }
 
 #define PBAG_FAIL(code, site)                            \
   do {                                                   \
@@ -441,28 +566,15 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   } while (0)
 
   if (sc.err) PBAG_FAIL(sc.err, sc.site);
-  const pbag_step_rec& r = recs[r0 + step];
-  const double accel = r.accel_frac, B = r.B;
-  const pbag_shock_params P = prm[b];
-  double* f = S.f + (size_t)b * G;
-  const double* pp = S.powp + (size_t)b * G;
-  const double Kb = (sc.flags & kRecFast) ? sc.K : sc.K * r.gamma_c;
-  // the stateful SSA derivative of the last step, needed at the end
-  double* dfde = S.dfde + (size_t)b * G;
-  double dpre[C];
-#pragma unroll
-  for (int k = 0; k < C; ++k) {
-    const int i = tid + k * kStepThreads;
-    dpre[k] = (P.ssa_on && i < G) ? dfde[i] : 0.;
-  }
+  const double Kb = (sc.flags & kRecFast) ? sc.K : sc.K * gamma_c;
 
   if (sc.flags & kRecInit) {
     // ---- initializeElectronDistribution (microphysics.h:347-357): untouched
     // entries keep their value, then all but the last bin scale by accel_frac
     for (int i = tid; i < G; i += kStepThreads) {
       double v = f[i];
-      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(g, sc, pp, i);
-      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
+      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(T, sc, pp, i);
+      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(T, sc, pp, i, Kb);
       if (i < G - 1) v *= accel;
       f[i] = v;
       sh_f[i] = v;
@@ -472,68 +584,38 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     // ---- analytic distribution (microphysics.h:446-448)
     for (int i = tid; i < G; i += kStepThreads) {
       double v = 0.;
-      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(g, sc, pp, i);
-      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(g, sc, pp, i, Kb);
+      if (i >= sc.ia0 && i < sc.ia1) v = pl_branch_a(T, sc, pp, i);
+      else if (i >= sc.ib0 && i < sc.ib1) v = pl_branch_b(T, sc, pp, i, Kb);
       f[i] = v;
       sh_f[i] = v;
     }
   } else {
     // ---- Chang-Cooper evolution (microphysics.h:451-480)
-    const bool ssc = P.ssc_on && g.KintT != nullptr;
-    const bool staged = ssc && g.kint_stage > 0;
-    if (staged && tid == 0) {
-      // the kernel-integral table streams into shared memory while the
-      // seed-photon weights are formed
-      const uint32_t bar = smem_addr(&kbar);
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)g.kint_stage)
-                   : "memory");
-      const unsigned char* src = reinterpret_cast<const unsigned char*>(g.KintT);
-      for (int o = 0; o < g.kint_stage; o += 32768) {
-        const uint32_t n = (uint32_t)min(32768, g.kint_stage - o);
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_addr(evo_smem + o)),
-            "l"(src + o), "r"(n), "r"(bar)
-            : "memory");
-      }
-    }
     const double delta_t = sc.dt_sub;
     const int n_sub = sc.n_sub;
-    // this thread's bins j = tid*C + q: state and per-bin tables, loaded early
-    double fr[C], ppq[C], odg[C];
-#pragma unroll
-    for (int q = 0; q < C; ++q) {
-      const int j = tid * C + q;
-      const bool in = j < G;
-      fr[q] = in ? f[j] : 0.;
-      ppq[q] = in ? pp[j] : 0.;
-      odg[q] = in ? g.inv_dgb[j] : 0.;
-    }
-    double sv = 1., usv = 1.;
-    if (ssc) {  // seed-photon weights n_k dnu_k / nu_k, scaled by the kernel-integral columns
-      const double* n = S.n + (size_t)b * F;
-      int vexp = 0;
-      for (int k = tid; k < F - 1; k += kStepThreads) {
-        const double v = n[k] * g.dnu_nu[k] * g.kscale[k];
-        sh_t[k] = v;  // (sh_t is free until the weights below)
-        vexp = max(vexp, exp_field(v));
+    double usv = 1.;
+    if (ssc) {
+      if (have_v) {
+        usv = sh_usv;
+      } else {  // the photon field of an earlier step, from global memory
+        const double* n = S.n + (size_t)b * F;
+        const double* dnu = T.ft(kTabDnuNu);
+        const double* ksc = T.ft(kTabKscale);
+        int vexp = 0;
+        for (int k = tid; k < F - 1; k += kStepThreads) vexp = max(vexp, exp_field(n[k] * dnu[k] * ksc[k]));
+        vexp = block_max_int(vexp, red_i[0]);
+        const double sv = scale_from_exp(vexp);
+        usv = unscale_from_exp(vexp);
+        for (int k = tid; k < F; k += kStepThreads) sh_v[k] = k < F - 1 ? (float)(n[k] * dnu[k] * ksc[k] * sv) : 0.f;
+        __syncthreads();
       }
-      vexp = block_max_int(vexp, red_i[0]);
-      sv = scale_from_exp(vexp);
-      usv = unscale_from_exp(vexp);
-      for (int k = tid; k < F; k += kStepThreads) sh_v[k] = k < F - 1 ? (float)(sh_t[k] * sv) : 0.f;
     }
-    __syncthreads();
-    if (staged) {
-      const int miss = __syncthreads_or(mbar_wait_bounded(smem_addr(&kbar), 0) ? 0 : 1);
+    const bool kint_smem = staged;
+    if (kint_smem) {
+      const int miss = __syncthreads_or(mbar_wait_bounded(smem_addr(&bars[1]), 0) ? 0 : 1);
       if (miss) {
-        if (tid == 0) {
-          set_error(S, b, PBAG_ERR_TIMEOUT, step, __LINE__);
-          mbar_wait_bounded(smem_addr(&kbar), 0);  // the copy must land before the CTA exits
-        }
-        return;
+        if (tid == 0) mbar_wait_bounded(smem_addr(&bars[1]), 0);
+        PBAG_FAIL(PBAG_ERR_TIMEOUT, __LINE__);
       }
     }
     // heating / cooling terms at the half grid (numeric_model.h:753-801);
@@ -546,12 +628,12 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     const int Gs = g.Gs;
     bool hbad = false;
     for (int i = tid; i < G - 1; i += kStepThreads) {
-      const double vs = c_syn * g.half2[i];
-      const double va = sc.dlnVdt * g.hadi[i];
-      double vc = gssc[i];
+      const double vs = c_syn * T.gt(kTabHalf2)[i];
+      const double va = sc.dlnVdt * T.gt(kTabHadi)[i];
+      double vc = 0.;
       if (ssc) {
         float acc = 0.f;
-        if (staged) {
+        if (kint_smem) {
           const float* kc = sh_k + i;
 #pragma unroll 8
           for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], kc[(size_t)k * Gs], acc);
@@ -560,8 +642,10 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 #pragma unroll 16
           for (int k = 0; k < F - 1; k++) acc = fmaf(sh_v[k], __ldg(kc + (size_t)k * Gs), acc);
         }
-        vc = c_ssc * (double)acc * g.ihalf2[i];
+        vc = c_ssc * (double)acc * T.gt(kTabIhalf2)[i];
         gssc[i] = vc;
+      } else {
+        vc = gssc[i];  // stays as the last SSC step left it
       }
       gsyn[i] = vs;
       gadi[i] = va;
@@ -580,19 +664,20 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       const int j = tid * C + q;
       ib[q] = qb[q] = bt[q] = 0.;
       if (j < G) {
+        const double odg = T.gt(kTabInvDgb)[j];
         const double Hb = (j > 0 && j < G - 1) ? sh_f[j - 1] : 0.;  // b_0 and b_{G-1} see no inflow
         const double Hf = j < G - 1 ? sh_f[j] : 0.;
-        const double bb = 1. + (odg[q] * Hb) * delta_t;
-        const double cc = (odg[q] * Hf) * -delta_t;
+        const double bb = 1. + (odg * Hb) * delta_t;
+        const double cc = (odg * Hf) * -delta_t;
         const double Q = (j >= sc.iq0 && j < sc.iq1) ? sc.Ns * ppq[q] : 0.;
         ib[q] = 1. / bb;
         bt[q] = -(cc * ib[q]);
         qb[q] = (Q * delta_t) * ib[q];
       }
     }
-    const int T = (G + C - 1) / C;  // threads that own bins
+    const int Tn = (G + C - 1) / C;  // threads that own bins
     const bool sbad = n_sub < kScanMaxSub ? cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0)
-                                          : cc_systolic<C>(fr, ib, qb, bt, n_sub, T, xs);
+                                          : cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
     __syncthreads();  // every heating value has been read: sh_f takes N(gamma)
 #pragma unroll
     for (int q = 0; q < C; ++q) {
@@ -608,6 +693,8 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 
   // ---- per-step weights of the radiation sums (microphysics.h:498-558):
   // N_e and the power-of-two scales in one block reduction
+  const double* t_inv_e2 = T.gt(kTabInvE2);
+  const double* t_de = T.gt(kTabDe);
   double ne = 0.;
   int wexp = 0, Wexp = 0;
 #pragma unroll
@@ -615,12 +702,12 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     const int i = tid + k * kStepThreads;
     if (i < G) {
       const double fi = sh_f[i];
-      sh_t[i] = fi * g.inv_e2[i];  // f / e / e (numeric_model.h:194-195)
+      sh_t[i] = fi * t_inv_e2[i];  // f / e / e (numeric_model.h:194-195)
       if (i < G - 1) {
-        const double w = fi * g.de[i];
+        const double w = fi * t_de[i];
         ne += w;  // N_e (microphysics.h:556-558)
         wexp = max(wexp, exp_field(w));
-        Wexp = max(Wexp, exp_field(w * g.inv_e2[i]));
+        Wexp = max(Wexp, exp_field(w * t_inv_e2[i]));
       }
     }
   }
@@ -644,7 +731,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   }
   const double sw = scale_from_exp(wexp);
   float* w32 = S.w32 + (size_t)b * G;
-  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * g.de[i] * sw) : 0.f;
+  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * t_de[i] * sw) : 0.f;
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   // (FP32 for the CUDA-core contraction, BF16 hi + lo tiles for the tensor cores)
   if (P.ssc_on && g.K32 != nullptr) {
@@ -653,7 +740,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     uint16_t* A = S.Abf ? S.Abf + (size_t)(b / kTcCols) * tc_tile_elems(kTcCols, g.Gp) : nullptr;
     const int m = b % kTcCols;
     for (int j = tid; j < g.Gp; j += kStepThreads) {
-      const float w = j < G - 1 ? (float)(sh_f[j] * g.de[j] * g.inv_e2[j] * sW) : 0.f;
+      const float w = j < G - 1 ? (float)(sh_f[j] * t_de[j] * t_inv_e2[j] * sW) : 0.f;
       W[j] = w;
       if (A) {
         const __nv_bfloat16 hi = __float2bfloat16_rn(w);
@@ -666,6 +753,8 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   // SSA weights: dfde = d(f/gamma^2)/dgamma, stateful (base_state.h:482-501)
   int vexp = 0;
   if (P.ssa_on) {
+    const double* t_dxm = T.gt(kTabInvDxm);
+    const double* t_e2de = T.gt(kTabE2de);
 #pragma unroll
     for (int k = 0; k < C; ++k) {
       const int i = tid + k * kStepThreads;
@@ -678,11 +767,11 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
           else if (i == G - 1)
             d = 1.5 * t - 2. * sh_t[G - 2] + 0.5 * sh_t[G - 3];
           else
-            d = 0.5 * (sh_t[i + 1] - sh_t[i - 1]) * g.inv_dxm[i];
+            d = 0.5 * (sh_t[i + 1] - sh_t[i - 1]) * t_dxm[i];
           dfde[i] = d;
         }
         if (i < G - 1) {
-          const double v = g.e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
+          const double v = t_e2de[i] * d;  // e_j^2 (e_{j+1}-e_j) dfde_j (numeric_model.h:208)
           sh_vd[i] = v;
           vexp = max(vexp, exp_field(v));
         }
@@ -710,9 +799,9 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     scal[kScalFac] = sc.fac;
     const double acc_ne = accel / ne;
     scal[kScalAccNe] = acc_ne;
-    scal[kScalAnpNe] = accel * r.n_prime / ne;
+    scal[kScalAnpNe] = accel * n_prime / ne;
     scal[kScalAcc] = accel;
-    scal[kScalNp] = r.n_prime;
+    scal[kScalNp] = n_prime;
     scal[kScalNsub] = (double)sc.n_sub;
     scal[kScalSw] = unscale_from_exp(wexp);
     scal[kScalSv] = unscale_from_exp(vexp);
@@ -806,67 +895,96 @@ __device__ __forceinline__ double intensity_approx(double em, double dtau) {
 }
 
 // The rest of computeRadiationNumericMixed for blastwave b at `step`, once its
-// synchrotron and SSC emissivities are in place; a no-op unless the
-// blastwave radiated at that step. Runs at the start of the next step's
-// k_evolve (same CTA shape), and as k_finalize after the last step.
-__device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* __restrict__ off,
-                            const pbag_shock_params* __restrict__ prm, int b, int step, const pbag_outputs& out) {
-  const int tid = threadIdx.x;
-  const int G = g.G, F = g.F;
-  __shared__ int red_i[kStepThreads / 32];
-  const int flags = S.flags[b];
-  if (!(flags & kFlagActive) || S.err[4 * b] != 0) return;
-  const pbag_shock_params P = prm[b];
+// synchrotron and SSC sums are in place: synchrotron emissivity and SSA
+// absorption, photon field, totals, the frequency-grid history rows, the
+// seed-photon weights U of the step's SSC contraction and, when sh_v is given,
+// the SSC cooling weights of the next step. A no-op returning false unless the
+// blastwave radiated at `step` without error. The gamma-grid history rows
+// (ele_f_all, gdot_*) are the caller's. Thread 0 leaves the blastwave's new
+// flags and error code in sh_state; the caller synchronises before reading.
+// Returns 0 (nothing to do), 1 (rows written) or 2 (a synchrotron value failed
+// its check; nothing written). FQ frequencies per thread (F <= 128 FQ).
+template <int FQ>
+__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
+                            const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
+                            float* sh_v, double* sh_usv, int* sh_state) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int F = g.F;
+  __shared__ int red_f[3][kStepWarps];
+  if (!(flags & kFlagActive) || err != 0) return 0;
   const double* scal = S.scal + (size_t)b * kScal;
-  const double dr = scal[kScalDr], acc = scal[kScalAcc];
   const bool num = P.ele_method == PBAG_ELE_NUMERIC;
   const bool ssc = P.ssc_on && g.K32 != nullptr;
   const bool dense_syn = out.syn_j_all || out.syn_a_all || out.syn_i_all;
   const size_t row = (size_t)(off[b] + step);
-  double* n = S.n + (size_t)b * F;
   const float* syn32 = S.syn32 + (size_t)b * F;
   const float2* ssa32 = S.ssa32 + (size_t)b * F;
   const double* jssc = S.jssc + (size_t)b * F;
+  // every load first
+  const double dr = scal[kScalDr], acc = scal[kScalAcc];
+  const double pref = scal[kScalPref], ssw = scal[kScalSw], ssv = scal[kScalSv];
+  const double fac = scal[kScalFac], acc_ne = scal[kScalAccNe], anp_ne = scal[kScalAnpNe];
+  float s32[FQ];
+  float2 a32[FQ];
+  double cs[FQ];
+#pragma unroll
+  for (int q = 0; q < FQ; ++q) {
+    const int k = tid + q * kStepThreads;
+    const bool in = k < F;
+    s32[q] = in ? syn32[k] : 0.f;
+    a32[q] = (in && P.ssa_on) ? ssa32[k] : make_float2(0.f, 0.f);
+    cs[q] = (in && ssc) ? jssc[k] : 0.;
+  }
   // synchrotron emissivity and SSA absorption from the FP32 sums
   // (numeric_model.h:148-238): the prefactor and the power-of-two scales
-  const double pref = scal[kScalPref], ssw = scal[kScalSw], ssv = scal[kScalSv];
-  double jsv[kFinalPerThread], asv[kFinalPerThread];
+  double jsv[FQ], asv[FQ];
   bool jbad = false;
 #pragma unroll
-  for (int q = 0; q < kFinalPerThread; ++q) {
+  for (int q = 0; q < FQ; ++q) {
     const int k = tid + q * kStepThreads;
     jsv[q] = asv[q] = 0.;
     if (k < F) {
-      const double js = k < F - 1 ? pref * ((double)syn32[k] * ssw) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
+      const double js = k < F - 1 ? pref * ((double)s32[q] * ssw) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
       if (bad_value(js)) jbad = true;
       jsv[q] = js;
       if (P.ssa_on) {
-        const float2 sa = ssa32[k];
-        double a = fabs(pref * (((double)sa.x + (double)sa.y) * ssv) * g.ssa_nu[k]);  // numeric_model.h:206-211
+        double a = fabs(pref * (((double)a32[q].x + (double)a32[q].y) * ssv) * T.ft(kTabSsaNu)[k]);  // :206-211
         if (not_finite(a)) a = 1e99;
         asv[q] = a;
       }
     }
   }
   if (__syncthreads_or(jbad ? 1 : 0)) {
-    if (tid == 0) set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
-    return;
+    if (tid == 0) {
+      set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
+      if (sh_state) {
+        sh_state[0] = flags;
+        sh_state[1] = PBAG_ERR_NONFINITE;
+      }
+    }
+    return 2;
   }
-  // new photon density (microphysics.h:516-523)
-  const double fac = scal[kScalFac];
-  const double acc_ne = scal[kScalAccNe], anp_ne = scal[kScalAnpNe];
+  // new photon density (microphysics.h:516-523), totals and normalisation (:540-586)
+  double* n = S.n + (size_t)b * F;
+  const double* inv_hnu = T.ft(kTabInvHnu);
+  const double* dnu = T.ft(kTabDnuNu);
+  const double* ksc = T.ft(kTabKscale);
   bool bad = false, seen = false;
-  int uexp = 0;
+  int uexp = 0, vexp = 0;
+  double un[FQ];
 #pragma unroll
-  for (int q = 0; q < kFinalPerThread; ++q) {
+  for (int q = 0; q < FQ; ++q) {
     const int k = tid + q * kStepThreads;
+    un[q] = 0.;
     if (k >= F) continue;
-    const double js = jsv[q], cs = (num && ssc) ? jssc[k] : 0.;
-    const double nk = js * fac * g.inv_hnu[k] + cs * fac * g.inv_hnu[k];
+    const double js = jsv[q], c = num ? cs[q] : 0.;
+    const double nk = js * fac * inv_hnu[k] + c * fac * inv_hnu[k];
     n[k] = nk;
-    uexp = max(uexp, exp_field(nk * g.dnu_nu[k]));
-    // totals and normalisation (microphysics.h:540-586)
-    const double tj0 = js + cs;
+    const double u = nk * dnu[k];
+    un[q] = u;
+    uexp = max(uexp, exp_field(u));
+    if (k < F - 1) vexp = max(vexp, exp_field(u * ksc[k]));
+    const double tj0 = js + c;
     const double ta = asv[q] * anp_ne;
     const double ti = intensity_approx(tj0 * acc, ta * dr);
     const double tj = tj0 * acc_ne;
@@ -885,49 +1003,99 @@ __device__ void finalize_bw(const DevGrid& g, const DevState& S, const int64_t* 
       if (sj != 0.) seen = true;
     }
     if (ssc) {
-      const double cj = jssc[k] * acc;
+      const double cj = cs[q] * acc;
       if (out.ssc_j_all) out.ssc_j_all[row * F + k] = cj;
       if (out.ssc_i_all) out.ssc_i_all[row * F + k] = cj;  // ssc.a = 0 without pair production
     }
   }
-  if (out.ele_f_all || out.gdot_syn_all || out.gdot_adi_all || out.gdot_ssc_all) {
-    const double* f = S.f + (size_t)b * G;
-    const double* gd = S.gdot + (size_t)b * 3 * G;
-    for (int i = tid; i < G; i += kStepThreads) {
-      if (out.ele_f_all) out.ele_f_all[row * G + i] = f[i];
-      if (out.gdot_syn_all) out.gdot_syn_all[row * G + i] = gd[i];
-      if (out.gdot_adi_all) out.gdot_adi_all[row * G + i] = gd[G + i];
-      if (out.gdot_ssc_all) out.gdot_ssc_all[row * G + i] = gd[2 * G + i];
+  // one reduction: the scales of U and of the cooling weights, the checks
+  uexp = __reduce_max_sync(0xffffffffu, uexp);
+  vexp = __reduce_max_sync(0xffffffffu, vexp);
+  const unsigned bits = __reduce_or_sync(0xffffffffu, (bad ? 1u : 0u) | (seen ? 2u : 0u));
+  if (lane == 0) {
+    red_f[0][warp] = uexp;
+    red_f[1][warp] = vexp;
+    red_f[2][warp] = (int)bits;
+  }
+  __syncthreads();
+  uexp = vexp = 0;
+  unsigned any = 0;
+#pragma unroll
+  for (int v = 0; v < kStepWarps; ++v) {
+    uexp = max(uexp, red_f[0][v]);
+    vexp = max(vexp, red_f[1][v]);
+    any |= (unsigned)red_f[2][v];
+  }
+  if (ssc) {
+    // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k of this step's SSC contraction
+    const double su = scale_from_exp(uexp);
+    float* U = S.U32 + (size_t)b * F;
+    // cooling weights n_k dnu_k/nu_k kscale_k of the next step (numeric_model.h:395-400)
+    const double sv = scale_from_exp(vexp);
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+      const int k = tid + q * kStepThreads;
+      if (k >= F) continue;
+      U[k] = (float)(un[q] * su);
+      if (sh_v) sh_v[k] = k < F - 1 ? (float)(un[q] * ksc[k] * sv) : 0.f;
     }
   }
-  // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k for the next step's SSC contraction
-  uexp = block_max_int(uexp, red_i);
-  const double su = scale_from_exp(uexp);
-  if (ssc) {
-    float* U = S.U32 + (size_t)b * F;
-    for (int k = tid; k < F; k += kStepThreads) U[k] = (float)(n[k] * g.dnu_nu[k] * su);
-  }
-  const int any_bad = __syncthreads_or(bad ? 1 : 0);
-  const int any_seen = __syncthreads_or(seen ? 1 : 0);
   if (tid == 0) {
     int fl = flags;
-    if (any_seen) fl |= kFlagSynSeen;
+    if (any & 2u) fl |= kFlagSynSeen;
     if (ssc) {
       S.scal[(size_t)b * kScal + kScalSU] = unscale_from_exp(uexp);
       fl |= kFlagUValid;
+      if (sh_usv) *sh_usv = unscale_from_exp(vexp);
     }
     S.flags[b] = fl;
-    if (any_bad)
-      set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);
+    int e = 0;
+    if (any & 1u)
+      e = PBAG_ERR_NONFINITE;
     else if (dense_syn && !(fl & kFlagSynSeen) && step > 0)
-      set_error(S, b, PBAG_ERR_NONFINITE, step, __LINE__);  // microphysics.h:627-631
+      e = PBAG_ERR_NONFINITE;  // microphysics.h:627-631
+    if (e) set_error(S, b, e, step, __LINE__);
+    if (sh_state) {
+      sh_state[0] = fl;
+      sh_state[1] = e;
+    }
+  }
+  return 1;
+}
+
+// gamma-grid history rows of blastwave b at `step` (storeDenseOutput, microphysics.h:602-633)
+__device__ void history_rows_g(const DevGrid& g, const DevState& S, size_t row, int b, const pbag_outputs& out) {
+  if (!(out.ele_f_all || out.gdot_syn_all || out.gdot_adi_all || out.gdot_ssc_all)) return;
+  const int G = g.G;
+  const double* f = S.f + (size_t)b * G;
+  const double* gd = S.gdot + (size_t)b * 3 * G;
+  for (int i = threadIdx.x; i < G; i += kStepThreads) {
+    if (out.ele_f_all) out.ele_f_all[row * G + i] = f[i];
+    if (out.gdot_syn_all) out.gdot_syn_all[row * G + i] = gd[i];
+    if (out.gdot_adi_all) out.gdot_adi_all[row * G + i] = gd[G + i];
+    if (out.gdot_ssc_all) out.gdot_ssc_all[row * G + i] = gd[2 * G + i];
   }
 }
 
 __global__ void __launch_bounds__(kStepThreads)
 k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm,
            int step, pbag_outputs out) {
-  finalize_bw(g, S, off, prm, blockIdx.x, step, out);
+  const int b = blockIdx.x;
+  const int flags = S.flags[b], err = S.err[4 * b];
+  if (step >= off[b + 1] - off[b]) return;
+  const pbag_shock_params P = prm[b];
+  const GridTab T{g.etab, g.Ge, g.Fe};
+  const int fq = (g.F + kStepThreads - 1) / kStepThreads;
+  int fin;
+  if (fq <= 1)
+    fin = finalize_bw<1>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+  else if (fq <= 2)
+    fin = finalize_bw<2>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+  else if (fq <= 4)
+    fin = finalize_bw<4>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+  else
+    fin = finalize_bw<8>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+  if (fin == 1) history_rows_g(g, S, (size_t)(off[b] + step), b, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -946,16 +1114,26 @@ cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_
 cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
                           const int64_t* off, const pbag_shock_params* prm, int nbw, int step,
                           const pbag_outputs& out, cudaStream_t st) {
-  const size_t smem = evolve_bytes(g);
+  const int kstage = evolve_kint_stage(g, nbw);
+  const size_t smem = evolve_bytes(g, kstage);
   const int c = (g.G + kStepThreads - 1) / kStepThreads;
-  if (c <= 1)
-    k_evolve<1><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
-  else if (c <= 2)
-    k_evolve<2><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
-  else if (c <= 4)
-    k_evolve<4><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
-  else
-    k_evolve<8><<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out);
+  const int fq = (g.F + kStepThreads - 1) / kStepThreads;
+  auto go = [&](auto kern) { kern<<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out, kstage); };
+#define PBAG_EVOLVE_FQ(CC)                 \
+  if (fq <= 1) go(k_evolve<CC, 1>);        \
+  else if (fq <= 2) go(k_evolve<CC, 2>);   \
+  else if (fq <= 4) go(k_evolve<CC, 4>);   \
+  else go(k_evolve<CC, 8>);
+  if (c <= 1) {
+    PBAG_EVOLVE_FQ(1)
+  } else if (c <= 2) {
+    PBAG_EVOLVE_FQ(2)
+  } else if (c <= 4) {
+    PBAG_EVOLVE_FQ(4)
+  } else {
+    PBAG_EVOLVE_FQ(8)
+  }
+#undef PBAG_EVOLVE_FQ
   return cudaGetLastError();
 }
 
@@ -985,30 +1163,29 @@ cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* 
   return cudaGetLastError();
 }
 
-size_t evolve_smem_bytes(const DevGrid& g) { return evolve_bytes(g); }
-size_t evolve_smem_max_bytes() {
-  return ((size_t)kKintStageMax + 127) / 128 * 128 + 3 * (size_t)PBAG_MAX_BINS * sizeof(double) +
-         (size_t)PBAG_MAX_BINS * sizeof(float);
-}
+size_t evolve_smem_max_bytes() { return kEvolveSmemMax; }
 
 cudaError_t configure_kernels() {
   const int smem = ssc_smem_max_bytes();
   const int esmem = (int)evolve_smem_max_bytes();
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_evolve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_evolve<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_evolve<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_evolve<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, esmem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rad_ssc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rad_ssc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rad_ssc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
-    return e;
+  cudaError_t e = cudaSuccess;
+  auto attr = [&](const void* k, int bytes) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  };
+#define PBAG_EVOLVE_ATTR(CC)                                   \
+  attr((const void*)k_evolve<CC, 1>, esmem);                   \
+  attr((const void*)k_evolve<CC, 2>, esmem);                   \
+  attr((const void*)k_evolve<CC, 4>, esmem);                   \
+  attr((const void*)k_evolve<CC, 8>, esmem);
+  PBAG_EVOLVE_ATTR(1)
+  PBAG_EVOLVE_ATTR(2)
+  PBAG_EVOLVE_ATTR(4)
+  PBAG_EVOLVE_ATTR(8)
+#undef PBAG_EVOLVE_ATTR
+  attr((const void*)k_rad_ssc<1>, smem);
+  attr((const void*)k_rad_ssc<2>, smem);
+  attr((const void*)k_rad_ssc<4>, smem);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_rad_ssc<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
