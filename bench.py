@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--profile", type=int, default=0,
+                    help="run this many device passes of the workload and exit (for ncu captures)")
     return ap.parse_args()
 
 
@@ -69,19 +71,20 @@ def config_dict(cfg, recs, prm, extra=None):
     return d
 
 
-def algorithmic_bytes(kernel, grid, active):
-    """Bytes one launch of a kernel class must move at minimum, for `active`
-    radiating blastwaves: every per-blastwave operand read or written once
-    (FP64 state and histories, FP32 scaled contraction operands) and, for the
-    SSC contraction, the shared FP32 kernel tensor read once per launch."""
+def algorithmic_bytes_per_bw_step(grid, outputs):
+    """Bytes one blastwave-step must move at minimum (FP64): N(gamma) in and
+    out (2G), photon field in and out (2F), ~20 step scalars, and the history
+    rows the caller asked for (F values each; j and a are the totals). The
+    evolve kernel does all of it (it completes the previous step too)."""
     G, F = grid.ngam, grid.nfreq
-    Gp = (G + 15) // 16 * 16
-    if kernel == "evolve":   # record, f in/out, photon field in, j_syn/a_syn out, W out, scalars
-        return active * (136 + 16 * G + 8 * F + 16 * F + 4 * Gp + 64)
-    if kernel == "ssc":      # kernel tensor + W, U in, j_ssc out
-        return 4 * F * Gp * F + active * (4 * Gp + 4 * F + 8 * F)
-    # finalize: j_syn, a_syn, j_ssc in; photon field, U out; j/a/f/i rows out; scalars
-    return active * (24 * F + 8 * F + 4 * F + 32 * F + 64)
+    return 8 * (2 * G + 2 * F + 20 + len(outputs) * F)
+
+
+def contraction_flops_per_bw_step(grid):
+    """Algorithmic FLOPs of the emissivity contractions of one blastwave-step:
+    the SSC bilinear form 2 F^2 G and the synchrotron quadrature 2 F G."""
+    G, F = grid.ngam, grid.nfreq
+    return 2 * F * F * G + 2 * F * G
 
 
 # ---------------------------------------------------------------- clocks ---
@@ -232,6 +235,12 @@ def gb300_arm(args):
     def one_pass():
         ctx.run_device(d_prm.data_ptr(), nbw, off, d_recs.data_ptr(), d_ptrs)
 
+    if args.profile:
+        for _ in range(args.profile):
+            one_pass()
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_passes": args.profile, "launches_per_pass": ctx.last_launch_count()}))
+        return
     for _ in range(args.warmup):
         flush.zero_()
         one_pass()
@@ -319,26 +328,40 @@ def gb300_arm(args):
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
     dominant = max(timing, key=lambda k: timing[k][0])
-    ms, nl = timing[dominant]
-    launches_per_pass = max(nl // prof_passes, 1)
-    active = nvalid / launches_per_pass  # blastwaves radiating per launch, on average
-    bytes_per_launch = algorithmic_bytes(dominant, grid, active)
-    achieved = bytes_per_launch / (ms / nl * 1e-3) / 1e9 if nl else None
-    traffic = None
+    share = {k: v[0] / max(sum(x[0] for x in timing.values()), 1e-12) for k, v in timing.items()}
+    traffic = {}
     try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = tr.get(dominant)
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except Exception:
         pass
-    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak if achieved else None, "traffic": traffic,
+    # the evolve kernel (Chang-Cooper solve + completion of the previous step): HBM roofline
+    ms_e, nl_e = timing["evolve"]
+    bw_steps_per_launch = nvalid / max(nl_e, 1)
+    bytes_per_launch = bw_steps_per_launch * algorithmic_bytes_per_bw_step(grid, outs)
+    achieved = bytes_per_launch / (ms_e / nl_e * 1e-3) / 1e9 if nl_e else None
+    roofline = {"bound": "hbm", "kernel": "evolve", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None,
+                "traffic": traffic.get("evolve_bytes_per_launch"),
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "bytes_per_launch": bytes_per_launch,
-                "avg_launch_us": 1e3 * ms / nl if nl else None,
-                "kernel_share": {k: v[0] / max(sum(x[0] for x in timing.values()), 1e-12) for k, v in timing.items()},
+                "bytes_per_blastwave_step": algorithmic_bytes_per_bw_step(grid, outs),
+                "avg_launch_us": 1e3 * ms_e / nl_e if nl_e else None,
+                "dominant_kernel_class": dominant,
+                "kernel_share": share,
                 "kernel_ms_per_pass": {k: v[0] / prof_passes for k, v in timing.items()},
                 "kernel_timing": "CUDA events around every launch on the library stream, one extra pass of the same workload with direct launches"}
+    # the emissivity contractions (tensor-core SSC + synchrotron/SSA): tensor roofline
+    ms_c, nl_c = timing["ssc"]
+    flops_per_launch = nvalid / max(nl_c, 1) * contraction_flops_per_bw_step(grid)
+    tflops = flops_per_launch / (ms_c / nl_c * 1e-3) / 1e12 if nl_c else None
+    roofline_c = {"bound": "tensor", "kernel": "ssc+radiation", "achieved": tflops, "peak": tc_peak,
+                  "unit": "TFLOP/s", "frac": tflops / tc_peak if tflops else None,
+                  "traffic": traffic.get("ssc_bytes_per_launch"),
+                  "flops_per_blastwave_step": contraction_flops_per_bw_step(grid),
+                  "avg_launch_us": 1e3 * ms_c / nl_c if nl_c else None,
+                  "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
     threads = os.cpu_count() or 1
     cpu_v, cpu_desc, _ = cpu_sample(recs, off, prm, grid, args.cpu_sample_seconds, threads)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -349,6 +372,7 @@ def gb300_arm(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "roofline": roofline,
+            "roofline_contraction": roofline_c,
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_desc},
             "wall_s_timed_region": t_wall}
     print(json.dumps(line), flush=True)
