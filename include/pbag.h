@@ -278,6 +278,30 @@ enum pbag_kernel_class {
 int pbag_set_timing(pbag_ctx* ctx, int enable);
 int pbag_get_timing(const pbag_ctx* ctx, double* ms, int64_t* launches);
 
+/* Emissivity contractions of n comoving states, without the Chang-Cooper
+ * evolution (the contraction microbenchmark, and a building block for callers
+ * that hold N(gamma) themselves). For state s, with the electron spectrum
+ * f[s][G] on the context's gamma grid, the field B[s] and the seed photon
+ * density nph[s][F] (total_rad.f of the previous step):
+ *   jsyn[s][k]: computeSynSpectrum (numeric_model.h:148-184) with the kernel of
+ *               SynKernel::evalSynKernel (kernels.h:528-538) at B[s];
+ *   jssc[s][i]: computeSSCSpectrum(nph[s]) (numeric_model.h:247-285).
+ * The synchrotron sums run in FP32 on CUDA cores; `precision` selects the SSC
+ * contraction. Device pointers on the context's device, row-major [n][F] /
+ * [n][G]; jsyn or jssc may be NULL (then B or nph may be too). Needs a context
+ * created with ssc_tables = 1 for jssc; the tensor-core precisions need
+ * nfreq = 128 or 256 (else PBAG_ERR_UNSUPPORTED). Synchronous. A negative or
+ * non-finite j_syn value (the reference's exit in computeSynSpectrum) returns
+ * PBAG_ERR_NONFINITE with st->bw = the first failing state. */
+enum pbag_precision {
+  PBAG_PREC_FP32 = 0,        /* CUDA cores, FP32 with power-of-two scaling       */
+  PBAG_PREC_BF16 = 1,        /* tensor cores, BF16 operands, FP32 accumulation   */
+  PBAG_PREC_SPLIT_BF16 = 2,  /* tensor cores, hi+lo BF16 (3 products), FP32 acc. */
+  PBAG_PREC_TF32 = 3         /* tensor cores, TF32 operands, FP32 accumulation   */
+};
+int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph, int syn_method,
+                  int precision, double* d_jsyn, double* d_jssc, pbag_status* st);
+
 #ifdef __cplusplus
 }
 #endif

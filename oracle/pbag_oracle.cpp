@@ -645,4 +645,54 @@ int orc_run(const pbag_grid_desc* g, const pbag_shock_params* prm, int nbw, cons
   return PBAG_OK;
 }
 
+int orc_contract(const pbag_grid_desc* g, int n, const double* f, const double* B, const double* nph, int syn_method,
+                 double* jsyn, double* jssc, int threads) {
+  if (!g || n < 0 || !f || g->ngam < 8 || g->nfreq < 8) return PBAG_ERR_ARG;
+  const int G = g->ngam, F = g->nfreq;
+  std::vector<double> e(G), nu(F + 1);
+  orc_build_grids(g, e.data(), nu.data());
+  std::vector<double> K;
+  if (jssc) {
+    if (!nph) return PBAG_ERR_ARG;
+    K.assign((size_t)F * G * F, 0.);
+    for (int i = 0; i < F; i++)
+      for (int j = 0; j < G; j++)
+        for (int k = 0; k < F; k++) K[((size_t)i * G + j) * F + k] = ssc_nava(nu[i], e[j], nu[k]);
+  }
+  if (jsyn && !B) return PBAG_ERR_ARG;
+  const auto syn = pick_syn(syn_method);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads) if (threads > 1)
+  for (int s = 0; s < n; ++s) {
+    const double* fs = f + (size_t)s * G;
+    if (jsyn) {
+      // computeSynSpectrum (numeric_model.h:148-184) with the kernel of SynKernel::evalSynKernel
+      // (kernels.h:528-538) at this state's field
+      double* js = jsyn + (size_t)s * F;
+      for (int i = 0; i < F; ++i) js[i] = 0.;
+      for (int i = 0; i < F - 1; ++i) {
+        double res = 0.;
+        for (int j = 0; j < G - 1; ++j) res += syn(B[s], nu[i], e[j]) * fs[j] * (e[j + 1] - e[j]);
+        js[i] = res;
+      }
+    }
+    if (jssc) {
+      // computeSSCSpectrum (numeric_model.h:247-285), photon_density = nph[s]
+      const double* ph = nph + (size_t)s * F;
+      double* jc = jssc + (size_t)s * F;
+      std::vector<double> scat(G - 1);
+      for (int i = 0; i < F; ++i) {
+        for (int j = 0; j < G - 1; ++j) scat[j] = 0.;
+        for (int j = 0; j < G - 1; ++j)
+          for (int k = 0; k < F; ++k)
+            scat[j] += 3. / 4. * sigma_T * c_light / (e[j] * e[j]) * ph[k] / nu[k] * (nu[k + 1] - nu[k]) *
+                       K[((size_t)i * G + j) * F + k];
+        double r = 0.;
+        for (int j = 0; j < G - 1; ++j) r += fs[j] * h_pl * nu[i] * scat[j] * (e[j + 1] - e[j]);
+        jc[i] = r;
+      }
+    }
+  }
+  return PBAG_OK;
+}
+
 }  // extern "C"

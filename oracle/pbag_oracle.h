@@ -28,6 +28,14 @@ double orc_ssc_func(double nu, double gam, double nu_tilde);
 /* SSC kernel tensor K[i][j][k] (may be NULL) and Kint[j][k] (kernels.h:49-94) */
 int orc_ssc_kernel(const double* gam, int G, const double* freq, int F, double* K, double* Kint);
 
+/* Emissivity contractions of n comoving states on the grid g: jsyn[s][k]
+ * (computeSynSpectrum, numeric_model.h:148-184, kernel at field B[s]) and
+ * jssc[s][i] (computeSSCSpectrum, numeric_model.h:247-285, seed photon
+ * density nph[s]) from the electron spectra f[s][G]. jsyn or jssc may be
+ * NULL. threads > 1 runs states concurrently. */
+int orc_contract(const pbag_grid_desc* g, int n, const double* f, const double* B, const double* nph, int syn_method,
+                 double* jsyn, double* jssc, int threads);
+
 /* Flags for orc_run. */
 enum {
   ORC_HOIST_HEATING = 1,  /* compute the (substep-invariant) cooling terms once per

@@ -61,6 +61,8 @@ class Oracle:
                                        P(C.c_double), P(C.c_double)]
         lib.orc_run.argtypes = [P(abi.GridDesc), C.c_void_p, C.c_int, P(C.c_int64), C.c_void_p,
                                 P(abi.Outputs), C.c_int, C.c_int, C.c_int, P(abi.Status)]
+        lib.orc_contract.argtypes = [P(abi.GridDesc), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_int]
         self.lib = lib
 
     def grids(self, grid):
@@ -85,6 +87,23 @@ class Oracle:
                                 abi.dptr(np.ascontiguousarray(freq_ext)), F,
                                 abi.dptr(K) if full else None, abi.dptr(Kint))
         return K, Kint
+
+    def contract(self, grid, f, B=None, nph=None, syn_method=abi.PBAG_SYN_CSYN, syn=True, ssc=True, threads=1):
+        """FP64 j_syn and j_ssc [n][F] of n states (orc_contract)."""
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        n = f.shape[0]
+        jsyn = np.zeros((n, grid.nfreq)) if syn else None
+        jssc = np.zeros((n, grid.nfreq)) if ssc else None
+        Bv = np.ascontiguousarray(B, dtype=np.float64) if B is not None else None
+        nv = np.ascontiguousarray(nph, dtype=np.float64) if nph is not None else None
+        rc = self.lib.orc_contract(C.byref(grid), n, f.ctypes.data,
+                                   Bv.ctypes.data if Bv is not None else None,
+                                   nv.ctypes.data if nv is not None else None, int(syn_method),
+                                   jsyn.ctypes.data if syn else None, jssc.ctypes.data if ssc else None,
+                                   int(threads))
+        if rc != 0:
+            raise RuntimeError(f"orc_contract failed: {rc}")
+        return jsyn, jssc
 
     def run(self, grid, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all"),
             flags=ORC_HOIST_HEATING, outer_threads=1, inner_threads=1):
@@ -153,6 +172,23 @@ class Reference:
                                 opts.method_B, opts.method_nonrel, gamma_max_const, gamma_c_const,
                                 len(states), abi.dptr(inp), abi.dptr(out))
         return out
+
+    def contract(self, grid, f, B=None, nph=None, syn_method=abi.PBAG_SYN_CSYN, syn=True, ssc=True, threads=1):
+        """FP64 j_syn and j_ssc [n][F] of n states (orc_contract)."""
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        n = f.shape[0]
+        jsyn = np.zeros((n, grid.nfreq)) if syn else None
+        jssc = np.zeros((n, grid.nfreq)) if ssc else None
+        Bv = np.ascontiguousarray(B, dtype=np.float64) if B is not None else None
+        nv = np.ascontiguousarray(nph, dtype=np.float64) if nph is not None else None
+        rc = self.lib.orc_contract(C.byref(grid), n, f.ctypes.data,
+                                   Bv.ctypes.data if Bv is not None else None,
+                                   nv.ctypes.data if nv is not None else None, int(syn_method),
+                                   jsyn.ctypes.data if syn else None, jssc.ctypes.data if ssc else None,
+                                   int(threads))
+        if rc != 0:
+            raise RuntimeError(f"orc_contract failed: {rc}")
+        return jsyn, jssc
 
     def run(self, grid, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all")):
         recs = np.ascontiguousarray(recs, dtype=abi.STEP_DTYPE)

@@ -60,6 +60,8 @@ def load():
     lib.pbag_last_launch_count.restype = C.c_int64
     lib.pbag_set_timing.argtypes = [C.c_void_p, C.c_int]
     lib.pbag_set_ssc_path.argtypes = [C.c_void_p, C.c_int]
+    lib.pbag_contract.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                  C.c_void_p, C.c_void_p, P(abi.Status)]
     lib.pbag_get_timing.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64)]
     if lib.pbag_abi_version() != 1:
         raise RuntimeError("libpbag ABI version mismatch")
@@ -127,6 +129,15 @@ class Context:
 
     def last_launch_count(self):
         return int(load().pbag_last_launch_count(self._h))
+
+    def contract_device(self, n, d_f, d_B, d_nph, syn_method, precision, d_jsyn, d_jssc):
+        """pbag_contract on device addresses (int, or 0 for NULL): f [n][G],
+        B [n], nph [n][F] in; jsyn, jssc [n][F] out."""
+        st = abi.Status()
+        rc = load().pbag_contract(self._h, int(n), C.c_void_p(d_f or None), C.c_void_p(d_B or None),
+                                  C.c_void_p(d_nph or None), int(syn_method), int(precision),
+                                  C.c_void_p(d_jsyn or None), C.c_void_p(d_jssc or None), C.byref(st))
+        _check(rc, "pbag_contract", st)
 
     def set_ssc_path(self, path):
         """abi.PBAG_SSC_AUTO / _CUDA_FP32 / _TC_SPLIT_BF16 / _TC_BF16."""

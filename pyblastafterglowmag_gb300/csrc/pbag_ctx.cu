@@ -123,10 +123,16 @@ struct pbag_ctx {
   // captured step loop of the last batch shape
   cudaGraphExec_t graph_exec = nullptr;
   GraphKey graph_key{};
+  // workspaces of other entry points (pbag_contract)
+  CtxExtension* ext[kExtSlots] = {};
 
   ~pbag_ctx() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    for (CtxExtension*& x : ext) {
+      delete x;
+      x = nullptr;
+    }
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (side) cudaStreamSynchronize(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
@@ -642,6 +648,15 @@ int pbag_get_timing(const pbag_ctx* c, double* ms, int64_t* launches) {
 }  // extern "C"
 
 namespace pbag {
+
+CtxExtension* ctx_get_extension(pbag_ctx* c, int slot) {
+  return c && slot >= 0 && slot < kExtSlots ? c->ext[slot] : nullptr;
+}
+void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* x) {
+  if (!c || slot < 0 || slot >= kExtSlots) return;
+  delete c->ext[slot];
+  c->ext[slot] = x;
+}
 
 bool ctx_view(const pbag_ctx* c, CtxView* v) {
   if (!c || !v) return false;

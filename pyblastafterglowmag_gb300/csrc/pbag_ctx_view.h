@@ -20,6 +20,15 @@ struct CtxView {
 // Fills *v from c; false when c is null.
 bool ctx_view(const pbag_ctx* c, CtxView* v);
 
+// A per-context workspace owned by an entry point of another translation
+// unit: created on first use, destroyed with the context.
+struct CtxExtension {
+  virtual ~CtxExtension() = default;
+};
+enum : int { kExtContract = 0, kExtSlots = 2 };
+CtxExtension* ctx_get_extension(pbag_ctx* c, int slot);
+void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* ext);
+
 }  // namespace pbag
 
 #endif

@@ -146,21 +146,28 @@ enum : int {
 };
 
 // ---- tensor-core operand layout (pbag_ssc_tc.cu) ----------------------------
-// A K-major BF16 operand of `rows` rows (output columns k of one SSC kernel
-// slab, or the blastwaves of one tile) and Gp columns (gamma, a multiple of 16)
-// is stored in chunks of kTcChunk columns; chunk c (kc8 = its number of
-// 8-column groups) holds the hi part, then the lo part, each as rows/8 x kc8
-// core matrices of 8 rows x 16 bytes, row group major. The first n rows of a
-// part are therefore its first n/8 row groups, contiguous.
-constexpr int kTcCols = 256;  // blastwaves per tensor-core tile (MMA N at most)
-constexpr int kTcChunk = 32;  // K columns per chunk
-__host__ __device__ inline size_t tc_operand_offset(int row, int col, int rows, int Gp, bool lo) {
-  const int c = col / kTcChunk, kl = col % kTcChunk;
-  const int left = Gp / 8 - c * (kTcChunk / 8);
-  const int kc8 = left < kTcChunk / 8 ? left : kTcChunk / 8;
-  return (size_t)2 * rows * kTcChunk * c + (lo ? (size_t)rows * kc8 * 8 : 0) +
-         (size_t)((row >> 3) * kc8 + (kl >> 3)) * 64 + (row & 7) * 8 + (kl & 7);
+// A K-major operand of `rows` rows (output columns k of one SSC kernel slab, or
+// the blastwaves of one tile) and Gp columns (gamma, a multiple of 16), with
+// elements of esize bytes (2: BF16, 4: TF32), is stored in chunks of
+// kTcChunk16 16-byte columns; chunk c (kc = its number of 16-byte columns)
+// holds the hi part, then the lo part, each as rows/8 x kc core matrices of 8
+// rows x 16 bytes, row-group major. The first n rows of a part are therefore
+// its first n/8 row groups, contiguous.
+constexpr int kTcCols = 256;   // blastwaves per tensor-core tile (MMA N at most)
+constexpr int kTcChunk16 = 4;  // 16-byte K columns per chunk
+constexpr int kTcChunk = kTcChunk16 * 8;  // BF16 K columns per chunk
+__host__ __device__ inline size_t tc_operand_byte_offset(int row, int col, int rows, int Gp, int esize, bool lo) {
+  const int epc = 16 / esize;  // elements per 16-byte column
+  const int c = col / (kTcChunk16 * epc), kl = col % (kTcChunk16 * epc);
+  const int left = Gp / epc - c * kTcChunk16;
+  const int kc = left < kTcChunk16 ? left : kTcChunk16;
+  return (size_t)2 * rows * kTcChunk16 * 16 * c + (lo ? (size_t)rows * kc * 16 : 0) +
+         (size_t)((row >> 3) * kc + kl / epc) * 128 + (row & 7) * 16 + (kl % epc) * esize;
 }
+__host__ __device__ inline size_t tc_operand_offset(int row, int col, int rows, int Gp, bool lo) {
+  return tc_operand_byte_offset(row, col, rows, Gp, 2, lo) / 2;
+}
+__host__ __device__ inline size_t tc_tile_bytes(int rows, int Gp, int esize) { return (size_t)2 * rows * Gp * esize; }
 __host__ __device__ inline size_t tc_tile_elems(int rows, int Gp) { return (size_t)2 * rows * Gp; }
 
 // Power of two close to 1/max|x| (exact rescaling); 1 when max is 0, not

@@ -31,6 +31,15 @@ bool ssc_tc_supported(int F);
 void build_ssc_tc_operand(const std::vector<float>& K32, int F, int Gp, std::vector<uint16_t>& Bt);
 cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
                           cudaStream_t st);
+// the same contraction on explicit operands: mode kTcBf16 / kTcSplit (BF16
+// tiles) or kTcTf32 (FP32 tiles in the 4-byte layout), Wt the weight tiles,
+// Kt the kernel slabs
+enum : int { kTcBf16 = 0, kTcSplit = 1, kTcTf32 = 2 };
+cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
+                               const int* flags, const float* U32, const double* scal, const double* nu, double* out,
+                               int* err, cudaStream_t st);
+// K slabs as TF32 operands (FP32 values rounded to TF32, 4-byte layout, lo parts zero)
+void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32);
 
 // SSC kernel tables on the host (kernels.h:49-117): KintT[F][Gs] = Kint[j][k] /
 // kscale[k] stored k-major (row k, column j < G, zero beyond) with power-of-two

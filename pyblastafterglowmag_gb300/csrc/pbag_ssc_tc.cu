@@ -41,7 +41,7 @@ namespace {
 constexpr int kTcThreads = 128;
 constexpr int kTcK = 128;          // accumulator rows (output columns k) per half of the frequency grid
 constexpr int kTcMaxStages = 8;    // ring of chunk stages (all chunks of a small problem at once)
-constexpr int kK8 = kTcChunk / 8;  // 16-byte K columns of a full chunk
+constexpr int kK8 = kTcChunk16;   // 16-byte K columns of a full chunk
 constexpr int kWaitLimit = 1 << 21;
 constexpr int kPStride = kTcK + 1;  // row stride (floats) of the epilogue's product table
 constexpr size_t kTcBodyMax = 200 * 1024;  // stages (or product table) + U tile
@@ -87,9 +87,11 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;               // base offset 0, relative LBO, no swizzle
 }
 
-// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor, D = F32, both operands K-major: kind::f16 with A = B =
+// BF16 (type 1), or kind::tf32 with A = B = TF32 (type 2).
+__host__ __device__ constexpr uint32_t idesc_mma(int M, int N, bool tf32) {
+  return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
@@ -106,27 +108,39 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
-      : "memory");
+template <bool kTf32>
+__device__ __forceinline__ void mma_issue(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  if (kTf32)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
 }
 
 // One CTA: output frequency i = blockIdx.x, blastwaves kTcCols*blockIdx.y + [0, N).
 // Thread 0 streams the chunks of the kernel slab (A, F rows) and of the weight
 // tile (B, N rows) through a ring of S stages and issues the MMAs; all threads
-// run the epilogue. H = F / 128 accumulator halves. Every load that does not
-// depend on another is issued first, the copies before the tensor-memory
-// allocation.
-template <int H, bool kSplit>
+// run the epilogue. H = F / 128 accumulator halves; MODE is kTcBf16, kTcSplit
+// (three MMAs per K step) or kTcTf32 (4-byte operands, kind::tf32). Every load
+// that does not depend on another is issued first, the copies before the
+// tensor-memory allocation.
+template <int H, int MODE>
 __global__ void __launch_bounds__(kTcThreads)
-k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int Gp, int nrows, int N, int S,
+k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int N, int S,
          uint32_t body, uint32_t ubytes, const int* __restrict__ flags, const float* __restrict__ U32,
          const double* __restrict__ scal, const double* __restrict__ nu, double* __restrict__ out,
          int* __restrict__ err) {
   constexpr int F = kTcK * H;
+  constexpr bool kSplit = MODE == kTcSplit;
+  constexpr bool kTf32 = MODE == kTcTf32;
+  constexpr int kEs = kTf32 ? 4 : 2;  // operand element size
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
@@ -140,10 +154,10 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
   __shared__ int fail;
   auto stage_ptr = [&](int st) { return base + (size_t)st * stage_bytes; };
 
-  const int nk8 = Gp / 8;
+  const int nk8 = Gp * kEs / 16;  // 16-byte K columns
   const int nchunks = (nk8 + kK8 - 1) / kK8;
-  const uint16_t* Ai = Bt + (size_t)i * tc_tile_elems(F, Gp);                  // kernel slab of frequency i
-  const uint16_t* Bw = Abf + (size_t)blockIdx.y * tc_tile_elems(kTcCols, Gp);  // weight tile
+  const unsigned char* Ai = Kt + (size_t)i * tc_tile_bytes(F, Gp, kEs);                  // kernel slab of frequency i
+  const unsigned char* Bw = Wt + (size_t)blockIdx.y * tc_tile_bytes(kTcCols, Gp, kEs);  // weight tile
   auto load = [&](int c, int st) {
     const int kc8 = min(kK8, nk8 - c * kK8);
     const uint32_t ab = (kSplit ? 2u : 1u) * F * kc8 * 16;  // hi (+ lo), contiguous
@@ -152,12 +166,12 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
                  "r"(ab + (kSplit ? 2u : 1u) * bp)
                  : "memory");
-    const uint16_t* bsrc = Bw + (size_t)2 * kTcCols * kTcChunk * c;
+    const unsigned char* bsrc = Bw + (size_t)2 * kTcCols * kK8 * 16 * c;
     unsigned char* bdst = stage_ptr(st) + tc_a_region(F);
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_u32(stage_ptr(st))),
-        "l"(Ai + (size_t)2 * F * kTcChunk * c), "r"(ab), "r"(bar)
+        "l"(Ai + (size_t)2 * F * kK8 * 16 * c), "r"(ab), "r"(bar)
         : "memory");
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -168,7 +182,7 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
       asm volatile(
           "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
               smem_u32(bdst + bp)),
-          "l"(bsrc + (size_t)kTcCols * kc8 * 8), "r"(bp), "r"(bar)
+          "l"(bsrc + (size_t)kTcCols * kc8 * 16), "r"(bp), "r"(bar)
           : "memory");
   };
   const int pre = min(S, nchunks);
@@ -234,7 +248,7 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
     int next = 0;      // next chunk to consume
     bool ok = true;
     if (any) {
-      const uint32_t idesc = idesc_bf16(kTcK, N);
+      const uint32_t idesc = idesc_mma(kTcK, N, kTf32);
       for (; next < nchunks; ++next) {
         const int c = next, st = c % S;
         if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)(c / S) & 1)) {
@@ -251,12 +265,12 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
           const uint32_t ah = (uint32_t)h * kTcK * kc8 * 16;  // rows k of half h: row groups 16h ...
           const uint32_t d = tmem + (uint32_t)(h * N);
           for (int s2 = 0; s2 < kc8 / 2; ++s2) {
-            const uint32_t ko = (uint32_t)s2 * 256;  // two 16-byte K columns per MMA (K = 16)
-            mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc,
-                     (c > 0 || s2 > 0) ? 1u : 0u);
+            const uint32_t ko = (uint32_t)s2 * 256;  // two 16-byte K columns per MMA (K = 16 BF16 or 8 TF32)
+            mma_issue<kTf32>(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc,
+                             (c > 0 || s2 > 0) ? 1u : 0u);
             if (kSplit) {
-              mma_bf16(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_lo + ko, 128, sbo), idesc, 1);
-              mma_bf16(d, smem_desc(a_lo + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc, 1);
+              mma_issue<kTf32>(d, smem_desc(a_hi + ah + ko, 128, sbo), smem_desc(b_lo + ko, 128, sbo), idesc, 1);
+              mma_issue<kTf32>(d, smem_desc(a_lo + ah + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc, 1);
             }
           }
         }
@@ -365,23 +379,24 @@ k_ssc_tc(const uint16_t* __restrict__ Abf, const uint16_t* __restrict__ Bt, int 
   }
 }
 
-template <int H, bool kSplit>
-cudaError_t launch_tc(const uint16_t* Abf, const uint16_t* Bt, int Gp, int nrows, const int* flags, const float* U32,
-                      const double* scal, const double* nu, double* out, int* err, cudaStream_t st) {
+template <int H, int MODE>
+cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
+                      const float* U32, const double* scal, const double* nu, double* out, int* err,
+                      cudaStream_t st) {
   constexpr int F = kTcK * H;
   const int N = std::min(kTcCols, (nrows + 15) / 16 * 16);
-  const TcPlan plan = tc_plan(F, N, Gp);
+  const TcPlan plan = tc_plan(F, N, Gp * (MODE == kTcTf32 ? 2 : 1));
   if (plan.smem > 2048 + kTcBodyMax + 16 * kTcMaxStages + 16) return cudaErrorInvalidConfiguration;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_ssc_tc<H, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_ssc_tc<H, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2048 + kTcBodyMax + 16 * kTcMaxStages + 16));
     if (e != cudaSuccess) return e;
     attr = true;
   }
   dim3 grid(F, (nrows + kTcCols - 1) / kTcCols);
-  k_ssc_tc<H, kSplit><<<grid, kTcThreads, plan.smem, st>>>(Abf, Bt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
-                                                             flags, U32, scal, nu, out, err);
+  k_ssc_tc<H, MODE><<<grid, kTcThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
+                                                           flags, U32, scal, nu, out, err);
   return cudaGetLastError();
 }
 
@@ -417,17 +432,55 @@ void build_ssc_tc_operand(const std::vector<float>& K32, int F, int Gp, std::vec
   }
 }
 
+float tf32_round(float x) {  // round to nearest even at TF32 precision (finite inputs)
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  u += 0xFFFu + ((u >> 13) & 1u);
+  u &= ~0x1FFFu;
+  float y;
+  std::memcpy(&y, &u, 4);
+  return y;
+}
+
+void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32) {
+  const int N = F;
+  Bt32.assign(tc_tile_bytes(N, Gp, 4) / 4 * F, 0.f);
+  for (int i = 0; i < F; ++i) {
+    float* Bi = Bt32.data() + tc_tile_bytes(N, Gp, 4) / 4 * i;
+    for (int n = 0; n < N; ++n)
+      for (int j = 0; j < Gp; ++j)
+        Bi[tc_operand_byte_offset(n, j, N, Gp, 4, false) / 4] = tf32_round(K32[((size_t)i * Gp + j) * F + n]);
+  }
+}
+
+cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
+                               const int* flags, const float* U32, const double* scal, const double* nu, double* out,
+                               int* err, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
+  const auto* w = static_cast<const unsigned char*>(Wt);
+  const auto* k = static_cast<const unsigned char*>(Kt);
+#define PBAG_TC_CASE(HH, MM) \
+  return launch_tc<HH, MM>(w, k, Gp, nrows, flags, U32, scal, nu, out, err, st)
+  if (F == 128) {
+    if (mode == kTcSplit) PBAG_TC_CASE(1, kTcSplit);
+    if (mode == kTcBf16) PBAG_TC_CASE(1, kTcBf16);
+    if (mode == kTcTf32) PBAG_TC_CASE(1, kTcTf32);
+  }
+  if (F == 256) {
+    if (mode == kTcSplit) PBAG_TC_CASE(2, kTcSplit);
+    if (mode == kTcBf16) PBAG_TC_CASE(2, kTcBf16);
+    if (mode == kTcTf32) PBAG_TC_CASE(2, kTcTf32);
+  }
+#undef PBAG_TC_CASE
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
                           cudaStream_t st) {
-  if (nbw <= 0) return cudaSuccess;
-  if (!S.Abf || !Bt || g.Gp % 16 != 0) return cudaErrorInvalidValue;
-  if (g.F == 128)
-    return split ? launch_tc<1, true>(S.Abf, Bt, g.Gp, nbw, S.flags, S.U32, S.scal, g.nu, S.jssc, S.err, st)
-                 : launch_tc<1, false>(S.Abf, Bt, g.Gp, nbw, S.flags, S.U32, S.scal, g.nu, S.jssc, S.err, st);
-  if (g.F == 256)
-    return split ? launch_tc<2, true>(S.Abf, Bt, g.Gp, nbw, S.flags, S.U32, S.scal, g.nu, S.jssc, S.err, st)
-                 : launch_tc<2, false>(S.Abf, Bt, g.Gp, nbw, S.flags, S.U32, S.scal, g.nu, S.jssc, S.err, st);
-  return cudaErrorInvalidValue;
+  if (!S.Abf || !Bt) return cudaErrorInvalidValue;
+  return launch_ssc_tc_mode(split ? kTcSplit : kTcBf16, g.F, g.Gp, S.Abf, Bt, nbw, S.flags, S.U32, S.scal, g.nu,
+                            S.jssc, S.err, st);
 }
 
 }  // namespace pbag
