@@ -39,6 +39,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction"],
+                    help="gaussian-jet: the step benchmark (default); contraction: the emissivity-"
+                         "contraction microbenchmark (65536 states, 256 gamma x 256 nu)")
+    ap.add_argument("--states", type=int, default=65536)
+    ap.add_argument("--fp32-states", type=int, default=4096,
+                    help="states of the FP32 CUDA-core variant of the contraction benchmark")
+    ap.add_argument("--check-states", type=int, default=64,
+                    help="states checked against the FP64 oracle in the contraction benchmark")
     ap.add_argument("--profile", type=int, default=0,
                     help="run this many device passes of the workload and exit (for ncu captures)")
     return ap.parse_args()
@@ -378,9 +386,145 @@ def gb300_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------ contraction arm ---
+def contraction_arm(args):
+    """Emissivity-contraction microbenchmark: pbag_contract (synchrotron sums
+    in FP32 + SSC contraction) on seeded states, for every SSC precision, each
+    checked against the FP64 oracle on a sample of states."""
+    import ctypes as C
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pyblastafterglowmag_gb300 import _lib, abi, build, contraction as CT
+    build.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    dev = torch.device("cuda", local)
+    n = args.states
+    g = CT.grid_desc(256, 256)
+    G, F = g.ngam, g.nfreq
+    gam, freq = _lib.grids(g)
+    f, B = CT.states(gam, n)
+    ctx = _lib.Context(g, local, ssc=True)
+    d_f = torch.from_numpy(f).to(dev)
+    d_B = torch.from_numpy(B).to(dev)
+    d_js = torch.zeros((n, F), dtype=torch.float64, device=dev)
+    d_jc = torch.zeros((n, F), dtype=torch.float64, device=dev)
+    # seed photons: the states' own synchrotron spectra
+    ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), 0, abi.PBAG_SYN_CSYN, abi.PBAG_PREC_FP32,
+                        d_js.data_ptr(), 0)
+    nu = torch.from_numpy(np.asarray(freq[:F])).to(dev)
+    d_n = (d_js / (CT.H_PL * nu[None, :])).contiguous()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    flops_state = 2 * F * F * G + 2 * F * G
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    orc = pyoracle.Oracle()
+    ns = min(args.check_states, n)
+    sample = np.linspace(0, n - 1, ns).astype(int)
+    threads = os.cpu_count() or 1
+    variants = {}
+    with ClockSampler(local) as clk:
+        for prec in (abi.PBAG_PREC_SPLIT_BF16, abi.PBAG_PREC_BF16, abi.PBAG_PREC_TF32, abi.PBAG_PREC_FP32):
+            nn = n if prec != abi.PBAG_PREC_FP32 else min(n, args.fp32_states)
+
+            def run(ssc_only=False):
+                ctx.contract_device(nn, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN, prec,
+                                    0 if ssc_only else d_js.data_ptr(), d_jc.data_ptr())
+
+            def timed(ssc_only):
+                for _ in range(args.warmup):
+                    flush.zero_()
+                    run(ssc_only)
+                ms = []
+                for _ in range(args.steps):
+                    flush.zero_()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    torch.cuda.synchronize(dev)
+                    e0.record()
+                    run(ssc_only)
+                    e1.record()
+                    e1.synchronize()
+                    ms.append(e0.elapsed_time(e1))
+                return statistics.median(ms)
+
+            ms_all = timed(False)
+            ms_ssc = timed(True)
+            run(False)
+            js = d_js[sample[sample < nn]].cpu().numpy()
+            jc = d_jc[sample[sample < nn]].cpu().numpy()
+            idx = sample[sample < nn]
+            ojs, ojc = orc.contract(g, f[idx], B=B[idx], nph=d_n[idx].cpu().numpy(), threads=threads)
+
+            def rel(x, y):
+                num = np.sqrt(((x - y) ** 2).sum(axis=1))
+                den = np.sqrt((y ** 2).sum(axis=1))
+                r = num[den > 0] / den[den > 0]
+                return float(r.max()), float(np.percentile(r, 99))
+
+            es, ec = rel(js, ojs), rel(jc, ojc)
+            tflops = nn * flops_state / (ms_all * 1e-3) / 1e12
+            variants[abi.PRECISION_NAMES[prec]] = {
+                "states": int(nn), "ms_per_pass": ms_all, "states_per_s": nn / (ms_all * 1e-3),
+                "ssc_only_ms_per_pass": ms_ssc,
+                "tflops_algorithmic": tflops, "frac_of_bf16_peak": tflops / tc_peak,
+                "ssc_tflops_algorithmic": nn * 2 * F * F * G / (ms_ssc * 1e-3) / 1e12,
+                "rel_l2_jsyn_max": es[0], "rel_l2_jssc_max": ec[0], "rel_l2_jssc_p99": ec[1],
+                "checked_states": int(len(idx))}
+    best = variants["split-bf16"]
+    # end to end through the C ABI with host buffers: states in, spectra out
+    h_f = torch.from_numpy(f).pin_memory()
+    h_B = torch.from_numpy(B).pin_memory()
+    h_n = d_n.cpu().pin_memory()
+    h_js = torch.empty((n, F), dtype=torch.float64).pin_memory()
+    h_jc = torch.empty((n, F), dtype=torch.float64).pin_memory()
+
+    def e2e():
+        d_f.copy_(h_f, non_blocking=True)
+        d_B.copy_(h_B, non_blocking=True)
+        d_n.copy_(h_n, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+        ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN,
+                            abi.PBAG_PREC_SPLIT_BF16, d_js.data_ptr(), d_jc.data_ptr())
+        h_js.copy_(d_js)
+        h_jc.copy_(d_jc)
+
+    e2e()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if rank != 0:
+        return
+    line = {"metric": "contraction states/s (synchrotron + SSC, split-BF16) on 1 GB300", "value": best["states_per_s"],
+            "unit": "states/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": best["ms_per_pass"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3/f32", "data": "synthetic",
+            "config": {"workload": "contraction-microbench-65536-states-256x256", "states": n, "ngam": G, "nfreq": F,
+                       "inputs": "seeded power laws with exponential cutoff; seed photons = own synchrotron spectra",
+                       "l2": "flushed with a 256 MiB device write before every timed pass"},
+            "clocks": clk.summary(),
+            "e2e": {"value": n / e2e_s, "unit": "states/s", "h2d_bytes_per_step": int(f.nbytes + B.nbytes + h_n.numel() * 8),
+                    "d2h_bytes_per_step": int(2 * n * F * 8)},
+            "roofline": {"bound": "tensor", "kernel": "k_ssc_tc (split-bf16) + prep + synchrotron sums",
+                         "achieved": best["tflops_algorithmic"], "peak": tc_peak, "unit": "TFLOP/s",
+                         "frac": best["frac_of_bf16_peak"], "traffic": None,
+                         "flops_per_state": flops_state,
+                         "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"},
+            "variants": variants}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "contraction":
+        contraction_arm(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gb300_arm(args)

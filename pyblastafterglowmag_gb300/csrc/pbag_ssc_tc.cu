@@ -44,18 +44,22 @@ constexpr int kTcMaxStages = 8;    // ring of chunk stages (all chunks of a smal
 constexpr int kK8 = kTcChunk16;   // 16-byte K columns of a full chunk
 constexpr int kWaitLimit = 1 << 21;
 constexpr int kPStride = kTcK + 1;  // row stride (floats) of the epilogue's product table
-constexpr size_t kTcBodyMax = 200 * 1024;  // stages (or product table) + U tile
-constexpr size_t kTcUSmemMax = 64 * 1024;  // largest U tile staged in shared memory
+constexpr size_t kTcDynMax = 231424;       // dynamic shared memory of a CTA (227 KiB less the static part)
+constexpr size_t kTcFixed = 1024 + 256;   // alignment slack, barriers and the tensor-memory slot
+constexpr size_t kTcUSmemMax = 64 * 1024; // largest U tile staged whole in shared memory
+constexpr int kTcURing = 2;               // otherwise: ring of U column blocks (16 blastwaves each)
 
 // Dynamic shared memory of one launch: [body: ring of stages of [A hi | A lo (F
-// rows each) | B hi | B lo (N rows each)], reused by the product table][U tile
-// (N x F floats) when it fits][barriers].
+// rows each) | B hi | B lo (N rows each)], reused by the product table][U: the
+// whole tile (N x F floats) when it fits, else a ring of kTcURing blocks of 16
+// rows][barriers].
 __host__ __device__ constexpr uint32_t tc_a_region(int F) { return 2u * F * kK8 * 16; }
 __host__ __device__ constexpr uint32_t tc_stage_bytes(int F, int N) { return tc_a_region(F) + 2u * N * kK8 * 16; }
 struct TcPlan {
   int S;            // stages
   uint32_t body;    // bytes of the stage ring / product table
-  uint32_t ubytes;  // bytes of the U tile in shared memory (0: read from global)
+  uint32_t ubytes;  // bytes of the whole U tile in shared memory (0: the ring instead)
+  uint32_t uring;   // bytes of the U block ring (0 when the whole tile is staged)
   size_t smem;      // dynamic shared memory
 };
 inline TcPlan tc_plan(int F, int N, int Gp) {
@@ -64,12 +68,20 @@ inline TcPlan tc_plan(int F, int N, int Gp) {
   const uint32_t stage = tc_stage_bytes(F, N);
   const size_t ub = (size_t)N * F * sizeof(float);
   p.ubytes = ub <= kTcUSmemMax ? (uint32_t)ub : 0u;
-  const size_t room = kTcBodyMax - p.ubytes;
+  p.uring = p.ubytes ? 0u : (uint32_t)(kTcURing * 16 * F * sizeof(float));
+  const size_t room = kTcDynMax - kTcFixed - p.ubytes - p.uring;
   p.S = std::max(2, std::min({nchunks, kTcMaxStages, (int)(room / stage)}));
   p.body = std::max<uint32_t>((uint32_t)p.S * stage, (uint32_t)(N * kPStride * sizeof(float)));
   p.body = (p.body + 1023) / 1024 * 1024;
-  p.smem = 1024 + (size_t)p.body + p.ubytes + 16 * kTcMaxStages + 16;
+  p.smem = 1024 + (size_t)p.body + p.ubytes + p.uring + 16 * kTcMaxStages + 16;
   return p;
+}
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(static_cast<uint32_t>(
+                   __cvta_generic_to_shared(dst))),
+               "l"(src), "r"(valid ? 4 : 0)
+               : "memory");
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -132,9 +144,9 @@ __device__ __forceinline__ void mma_issue(uint32_t tmem_d, uint64_t a, uint64_t 
 // that does not depend on another is issued first, the copies before the
 // tensor-memory allocation.
 template <int H, int MODE>
-__global__ void __launch_bounds__(kTcThreads)
+__global__ void __launch_bounds__(kTcThreads, 1)
 k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int N, int S,
-         uint32_t body, uint32_t ubytes, const int* __restrict__ flags, const float* __restrict__ U32,
+         uint32_t body, uint32_t ubytes, uint32_t uring, const int* __restrict__ flags, const float* __restrict__ U32,
          const double* __restrict__ scal, const double* __restrict__ nu, double* __restrict__ out,
          int* __restrict__ err) {
   constexpr int F = kTcK * H;
@@ -148,8 +160,8 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
   const uint32_t stage_bytes = tc_stage_bytes(F, N);
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  float* Us = reinterpret_cast<float*>(base + body);                   // U tile [N][F]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + body + ubytes);  // full[S], empty[S], U
+  float* Us = reinterpret_cast<float*>(base + body);                           // U tile [N][F] or ring [2][16][F]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + body + ubytes + uring);  // full[S], empty[S], U
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kTcMaxStages + 1);
   __shared__ int fail;
   auto stage_ptr = [&](int st) { return base + (size_t)st * stage_bytes; };
@@ -218,18 +230,23 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
     live[q] = (fl & kFlagActive) != 0;
     fac[q] = hnu * sw * su;
   }
-  // without a staged U tile: this thread's U[b][k] (k = tid + 128 h) for the first 16 columns
-  float u[H][16];
-  auto load_u = [&](int cb, float (&dst)[H][16]) {
+  // without a staged U tile: this thread's U[b][k] (k = tid + 128 h) of 16
+  // columns at a time, copied asynchronously into its own slots of a ring
+  // (each thread reads only what it copied, so no barrier is needed)
+  const int nb = N / 16;
+  auto u_block = [&](int cb) {
+    float* slot = Us + (size_t)(cb % kTcURing) * 16 * F;
 #pragma unroll
     for (int h = 0; h < H; ++h)
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const int r = row0 + cb * 16 + c;
-        dst[h][c] = r < nrows ? __ldg(U32 + (size_t)r * F + tid + kTcK * h) : 0.f;
+        cp_async4(slot + c * F + tid + kTcK * h, U32 + (size_t)(r < nrows ? r : 0) * F + tid + kTcK * h, r < nrows);
       }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  if (!ubytes) load_u(0, u);
+  if (!ubytes)
+    for (int cb = 0; cb < kTcURing && cb < nb; ++cb) u_block(cb);
 
   uint32_t ncols = 32;
   while (ncols < (uint32_t)(H * N)) ncols <<= 1;
@@ -319,15 +336,24 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
     // the (now idle) stage memory
     float* P = reinterpret_cast<float*>(base);
     const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int cb = 0; cb < N / 16; ++cb) {
-      float un[H][16];
+    for (int cb = 0; cb < nb; ++cb) {
+      float u[H][16];
       if (ubytes) {
 #pragma unroll
         for (int h = 0; h < H; ++h)
 #pragma unroll
           for (int c = 0; c < 16; ++c) u[h][c] = Us[(size_t)(cb * 16 + c) * F + tid + kTcK * h];
-      } else if (cb + 1 < N / 16) {
-        load_u(cb + 1, un);
+      } else {
+        if (cb + 1 < nb)
+          asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
+        const float* slot = Us + (size_t)(cb % kTcURing) * 16 * F;
+#pragma unroll
+        for (int h = 0; h < H; ++h)
+#pragma unroll
+          for (int c = 0; c < 16; ++c) u[h][c] = slot[c * F + tid + kTcK * h];
+        if (cb + kTcURing < nb) u_block(cb + kTcURing);
       }
       float p[16];
 #pragma unroll
@@ -346,12 +372,6 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
       }
 #pragma unroll
       for (int c = 0; c < 16; ++c) P[(size_t)(cb * 16 + c) * kPStride + tid] = p[c];
-      if (!ubytes && cb + 1 < N / 16) {
-#pragma unroll
-        for (int h = 0; h < H; ++h)
-#pragma unroll
-          for (int c = 0; c < 16; ++c) u[h][c] = un[h][c];
-      }
     }
     __syncthreads();
     // sum over k for blastwaves tid and tid + 128 (four partial sums)
@@ -371,6 +391,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
       out[(size_t)(row0 + col) * F + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
     }
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after the CTA exits
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -386,17 +407,17 @@ cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, 
   constexpr int F = kTcK * H;
   const int N = std::min(kTcCols, (nrows + 15) / 16 * 16);
   const TcPlan plan = tc_plan(F, N, Gp * (MODE == kTcTf32 ? 2 : 1));
-  if (plan.smem > 2048 + kTcBodyMax + 16 * kTcMaxStages + 16) return cudaErrorInvalidConfiguration;
+  if (plan.smem > kTcDynMax) return cudaErrorInvalidConfiguration;
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_ssc_tc<H, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(2048 + kTcBodyMax + 16 * kTcMaxStages + 16));
+                                         (int)kTcDynMax);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   dim3 grid(F, (nrows + kTcCols - 1) / kTcCols);
   k_ssc_tc<H, MODE><<<grid, kTcThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
-                                                           flags, U32, scal, nu, out, err);
+                                                           plan.uring, flags, U32, scal, nu, out, err);
   return cudaGetLastError();
 }
 

@@ -817,12 +817,16 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 }
 
 // ---------------------------------------------------------------------------
-// Synchrotron and SSA sums of one blastwave for kRadFreqs frequencies: one warp
-// per frequency splits the gamma sum over its lanes; the synchrotron kernel
-// values are generated in FP32 on the fly and never stored. The kernel has no
-// FP64 instruction (each costs a warp 64 cycles of its SM sub-partition's
-// FP64 unit on this part): the FP64 prefactors are applied by finalize_bw.
-__device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk) {
+// Synchrotron and SSA sums of one blastwave: each warp of the CTA takes R
+// frequencies (k = base + r kRadFreqs + warp), its lanes split the gamma sum;
+// the blastwave's setup is paid once for the R frequencies, and the gamma-bin
+// tables and weights of the later frequencies come from L1. The synchrotron
+// kernel values are generated in FP32 on the fly and never stored. The kernel
+// has no FP64 instruction (each costs a warp 64 cycles of its SM
+// sub-partition's FP64 unit on this part): the FP64 prefactors are applied by
+// finalize_bw.
+__device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b, int kblk,
+                              int R) {
   const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
   if (!(S.flags[b] & kFlagActive)) return;
@@ -831,53 +835,54 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);
   const float incrit = rp.x, inlar = rp.y;
   const int kq = tid / kRadLanes, jl = tid % kRadLanes;
-  const int k = kblk * kRadFreqs + kq;
-  const int kk = k < F ? k : F - 1;
-  const float nu = g.nu32[kk];
-  const float a_k = nu * incrit;          // x = a_k / e_j^2
-  const float y_k = g.nu13[kk] * rp.z;    // x^(1/3) = y_k e_j^(-2/3)
-  const float xl = nu * inlar;
   const int jcyc = dermer ? 0 : g.n_cyc;
   const float* w = S.w32 + (size_t)b * G;
   const float* v = S.v32 + (size_t)b * G;
-  float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
-  for (int j = jl; j < G - 1; j += kRadLanes) {
-    const float R = j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
-                              : cyclotron_R32(__ldg(g.psq32 + j), xl);
-    acc = fmaf(R, __ldg(w + j), acc);
-    if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
-      const float x = R * __ldg(v + j);
-      const float t = as + x;
-      ac += fabsf(as) >= fabsf(x) ? (as - t) + x : (x - t) + as;
-      as = t;
+  for (int r = 0; r < R; ++r) {
+    const int k = kblk * (kRadFreqs * R) + r * kRadFreqs + kq;
+    if (k >= F) break;  // warp-uniform
+    const float nu = g.nu32[k];
+    const float a_k = nu * incrit;          // x = a_k / e_j^2
+    const float y_k = g.nu13[k] * rp.z;     // x^(1/3) = y_k e_j^(-2/3)
+    const float xl = nu * inlar;
+    float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
+    for (int j = jl; j < G - 1; j += kRadLanes) {
+      const float R_ = j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
+                                 : cyclotron_R32(__ldg(g.psq32 + j), xl);
+      acc = fmaf(R_, __ldg(w + j), acc);
+      if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
+        const float x = R_ * __ldg(v + j);
+        const float t = as + x;
+        ac += fabsf(as) >= fabsf(x) ? (as - t) + x : (x - t) + as;
+        as = t;
+      }
     }
-  }
-  // combine the kRadLanes partial sums of each frequency
+    // combine the kRadLanes partial sums of each frequency
 #pragma unroll
-  for (int o = 1; o < kRadLanes; o <<= 1) {
-    acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    const float os = __shfl_xor_sync(0xffffffffu, as, o);
-    const float oc = __shfl_xor_sync(0xffffffffu, ac, o);
-    float s, e;
-    two_sum(as, os, s, e);
-    as = s;
-    ac = ac + oc + e;
-  }
-  if (jl == 0 && k < F) {
-    S.syn32[(size_t)b * F + k] = acc;
-    S.ssa32[(size_t)b * F + k] = ssa ? make_float2(as, ac) : make_float2(0.f, 0.f);
+    for (int o = 1; o < kRadLanes; o <<= 1) {
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      const float os = __shfl_xor_sync(0xffffffffu, as, o);
+      const float oc = __shfl_xor_sync(0xffffffffu, ac, o);
+      float s_, e_;
+      two_sum(as, os, s_, e_);
+      as = s_;
+      ac = ac + oc + e_;
+    }
+    if (jl == 0) {
+      S.syn32[(size_t)b * F + k] = acc;
+      S.ssa32[(size_t)b * F + k] = ssa ? make_float2(as, ac) : make_float2(0.f, 0.f);
+    }
   }
 }
 
 template <int KPT>
 __global__ void __launch_bounds__(kRadThreads)
-k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int step) {
+k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int R) {
   static_assert(kRadThreads == kSscThreads, "radiation and SSC tiles share the launch shape");
-  (void)step;
   const int blk = blockIdx.x;
-  const int rc = (g.F + kRadFreqs - 1) / kRadFreqs;
+  const int rc = (g.F + kRadFreqs * R - 1) / (kRadFreqs * R);
   if (blk < rad_blocks) {
-    radiate_block(g, S, prm, blk / rc, blk % rc);
+    radiate_block(g, S, prm, blk / rc, blk % rc, R);
   } else {
     ssc_block<KPT>(g, S, nbw, blk - rad_blocks);
   }
@@ -1139,7 +1144,12 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
 
 cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
                            int step, cudaStream_t st) {
-  const int rc = (g.F + kRadFreqs - 1) / kRadFreqs;
+  (void)step;
+  // frequencies per warp: 1 while the batch is small (latency), more for large
+  // batches so that each warp's per-blastwave setup serves several frequencies
+  const int64_t pairs = (int64_t)nbw * g.F;
+  const int R = pairs <= 40000 ? 1 : pairs <= 160000 ? 2 : pairs <= 640000 ? 4 : 8;
+  const int rc = (g.F + kRadFreqs * R - 1) / (kRadFreqs * R);
   const int rad_blocks = nbw * rc;
   const int ssc_blocks = ssc ? ssc_block_count(g, nbw) : 0;
   const int total = rad_blocks + ssc_blocks;
@@ -1147,13 +1157,13 @@ cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock
   const int kpt = (g.F + kSscThreads - 1) / kSscThreads;
   const size_t smem = ssc ? (size_t)ssc_smem_bytes(g) : 0;
   if (kpt <= 1)
-    k_rad_ssc<1><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+    k_rad_ssc<1><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
   else if (kpt <= 2)
-    k_rad_ssc<2><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+    k_rad_ssc<2><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
   else if (kpt <= 4)
-    k_rad_ssc<4><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+    k_rad_ssc<4><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
   else
-    k_rad_ssc<8><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, step);
+    k_rad_ssc<8><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
   return cudaGetLastError();
 }
 
