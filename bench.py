@@ -39,9 +39,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction"],
+    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction", "uneven-sweep"],
                     help="gaussian-jet: the step benchmark (default); contraction: the emissivity-"
-                         "contraction microbenchmark (65536 states, 256 gamma x 256 nu)")
+                         "contraction microbenchmark (65536 states, 256 gamma x 256 nu); uneven-sweep: a "
+                         "seeded sample of the 4096-set parameter sweep with uneven step counts")
+    ap.add_argument("--sets", type=int, default=64, help="parameter sets of the uneven-sweep workload")
     ap.add_argument("--states", type=int, default=65536)
     ap.add_argument("--fp32-states", type=int, default=4096,
                     help="states of the FP32 CUDA-core variant of the contraction benchmark")
@@ -520,10 +522,75 @@ def contraction_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------- uneven-sweep arm ---
+def sweep_arm(args):
+    """A seeded sample of the batched parameter sweep (top-hat and Gaussian jets
+    of 1-41 layers x FS+RS, uneven 200-2000 step histories) as one batch: one
+    captured graph over the longest history, blastwaves drop out as their
+    histories end."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pyblastafterglowmag_gb300 import _lib, abi, build, histories as H
+    build.build()
+    recs, off, prm, grid = H.sweep_batch(_lib, args.sets, seed=3, workers=os.cpu_count() or 1)
+    nvalid = int((recs["mode"] != 0).sum())
+    nrec, nbw, F = len(recs), len(prm), grid.nfreq
+    dev = torch.device("cuda", local)
+    ctx = _lib.Context(grid, device=local, ssc=True)
+    d_recs = torch.from_numpy(recs.view(np.uint8).copy()).to(dev)
+    d_prm = torch.from_numpy(prm.view(np.uint8).copy()).to(dev)
+    outs = ("j_all", "a_all")
+    d_out = {k: torch.empty((nrec, F), dtype=torch.float64, device=dev) for k in outs}
+    d_ptrs = {k: v.data_ptr() for k, v in d_out.items()}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    status = {"code": 0}
+
+    def one_pass():
+        try:
+            ctx.run_device(d_prm.data_ptr(), nbw, off, d_recs.data_ptr(), d_ptrs)
+        except _lib.PbagError as e:  # the reference would stop this run; the batch completes
+            status.update(code=e.code, blastwave=e.bw, step=e.step)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        one_pass()
+    ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            one_pass()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t = sum(ms) / len(ms)
+    if rank != 0:
+        return
+    lens = np.diff(off)
+    line = {"metric": "blastwave-steps/s (sync+SSC) on 1 GB300, uneven sweep", "value": nvalid / (t * 1e-3),
+            "unit": "blastwave-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
+            "data": "synthetic",
+            "config": {"workload": f"uneven-sweep-{args.sets}-sets-201x128", "sets": args.sets, "blastwaves": nbw,
+                       "records": int(nrec), "valid_blastwave_steps_per_pass": nvalid,
+                       "steps_per_blastwave": [int(lens.min()), int(lens.max())],
+                       "launch": "one captured graph over the longest history",
+                       "l2": "flushed with a 256 MiB device write before every timed pass",
+                       "outputs": list(outs)},
+            "clocks": clk.summary(), "status": status, "gpu_launches": ctx.last_launch_count()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "contraction":
         contraction_arm(args)
+    elif args.workload == "uneven-sweep":
+        sweep_arm(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

@@ -253,6 +253,64 @@ def shock_params(sh):
     return p[0]
 
 
+def layer_dynamics_many(E_iso, Gamma0, n_ism, tb, omega, nsamp=4000):
+    """layer_dynamics for every layer of a jet at once (the RK4 steps of all
+    layers advance together, elementwise the same arithmetic)."""
+    E_iso, Gamma0, omega = (np.asarray(a, dtype=np.float64) for a in (E_iso, Gamma0, omega))
+    L = len(E_iso)
+    rho = n_ism * M_P
+    M0 = E_iso / ((Gamma0 - 1.0) * C_LIGHT ** 2)
+    beta0 = np.sqrt(1 - 1 / Gamma0 ** 2)
+    R0 = beta0 * C_LIGHT * tb[0] * 0.1
+    m0 = 4 / 3 * np.pi * R0 ** 3 * rho
+    m1 = np.maximum(1e6 * M0 * Gamma0, m0 * 1e40)
+
+    def rhs(x, y):
+        m = np.exp(x)
+        gm1 = np.maximum(np.exp(y[0]), 1e-300)
+        G = 1.0 + gm1
+        dudm = -(G + 1.0) / (M0 + 2.0 * G * m)
+        R = (3 * m / (4 * np.pi * rho)) ** (1 / 3)
+        dRdx = R / 3.0
+        beta = np.sqrt(gm1 * (2.0 + gm1)) / G
+        return np.stack([dudm * m, dRdx / (beta * C_LIGHT), dRdx / (beta * G * C_LIGHT),
+                         dRdx * (1 - beta) / (beta * C_LIGHT)])
+
+    y = np.stack([np.log(Gamma0 - 1.0), R0 / (beta0 * C_LIGHT), R0 / (beta0 * Gamma0 * C_LIGHT),
+                  R0 * (1 - beta0) / (beta0 * C_LIGHT)])
+    x0, x1 = np.log(m0), np.log(m1)
+    h = (x1 - x0) / nsamp
+    x = x0.copy()
+    ys = np.empty((nsamp + 1, 4, L))
+    xs = np.empty((nsamp + 1, L))
+    ys[0], xs[0] = y, x
+    for i in range(nsamp):
+        k1 = rhs(x, y)
+        k2 = rhs(x + h / 2, y + h / 2 * k1)
+        k3 = rhs(x + h / 2, y + h / 2 * k2)
+        k4 = rhs(x + h, y + h * k3)
+        y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        x = x + h
+        ys[i + 1], xs[i + 1] = y, x
+    out = []
+    lq = np.log(tb)
+    for l in range(L):
+        lt = np.log(ys[:, 1, l])
+        xl = np.interp(lq, lt, xs[:, l])
+        u = np.interp(lq, lt, ys[:, 0, l])
+        tcom = np.exp(np.interp(lq, lt, np.log(ys[:, 2, l])))
+        tobs = np.exp(np.interp(lq, lt, np.log(ys[:, 3, l])))
+        m_iso = np.exp(xl)
+        gm1 = np.maximum(np.exp(u), 1e-300)
+        G = 1.0 + gm1
+        beta = np.sqrt(gm1 * (2.0 + gm1)) / G
+        R = (3 * m_iso / (4 * np.pi * rho)) ** (1 / 3)
+        frac = omega[l] / (4 * np.pi)
+        out.append(dict(Gamma=G, beta=beta, R=R, m=m_iso * frac, m_iso=m_iso, tcomov=tcom, t_obs=tobs,
+                        M0=M0[l] * frac, M0_iso=M0[l], Gamma0=Gamma0[l], beta0=beta0[l], rho=rho))
+    return out
+
+
 def make_batch(lib, cfg, nsteps=None):
     """Records for every blastwave of one jet: (recs, offsets, params, grid).
 
@@ -264,10 +322,11 @@ def make_batch(lib, cfg, nsteps=None):
     grid = cfg.grid()
     gam, _ = lib.grids(grid)
     lo, hi, E, G0 = layer_table(cfg)
+    omega = 2 * np.pi * (np.cos(lo) - np.cos(hi)) * 2  # both hemispheres
+    dyn = layer_dynamics_many(E, G0, cfg.n_ism, tb, omega)
     recs, params = [], []
     for il in range(cfg.nlayers):
-        omega = 2 * np.pi * (np.cos(lo[il]) - np.cos(hi[il])) * 2  # both hemispheres
-        d = layer_dynamics(E[il], G0[il], cfg.n_ism, tb, omega)
+        d = dyn[il]
         recs.append(shock_records(lib, fs_state(d), d, cfg.fs, gam, tb))
         params.append(shock_params(cfg.fs))
         if cfg.rs is not None:
@@ -278,16 +337,21 @@ def make_batch(lib, cfg, nsteps=None):
     return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid
 
 
+def _sweep_set(cfg):
+    from . import _lib
+    return make_batch(_lib, cfg)
+
+
 def sweep_batch(lib, nsets, seed=3, ngam=201, nfreq=128, min_steps=200, max_steps=2000, ssc=True,
-                max_layers=41):
+                max_layers=41, workers=1):
     """Seeded parameter sweep: nsets jets, each a top-hat or Gaussian with
     1..max_layers layers, log10 E_iso ~ U[50,54], log10 Gamma0 ~ U[1,3],
     log10 n ~ U[-4,0], log10 eps_e ~ U[-3,-0.5], log10 eps_b ~ U[-5,-1],
     p ~ U[2.05,2.8]; every blastwave keeps its first U{min_steps..max_steps}
-    steps (uneven histories)."""
+    steps (uneven histories). workers > 1 builds the jets in a process pool
+    (spawned, so it is safe next to a CUDA context)."""
     rng = np.random.default_rng(seed)
-    all_recs, params, lens = [], [], []
-    grid = None
+    cfgs, counts = [], []
     for _ in range(nsets):
         struct = "tophat" if rng.random() < 0.5 else "gaussian"
         nl = int(rng.integers(1, max_layers + 1))
@@ -298,10 +362,19 @@ def sweep_batch(lib, nsets, seed=3, ngam=201, nfreq=128, min_steps=200, max_step
                         Gamma0=10 ** rng.uniform(1, 3), theta_c=tc, theta_w=min(4 * tc, 0.6),
                         n_ism=10 ** rng.uniform(-4, 0), nlayers=nl, fs=Shock(**sh), rs=Shock(**sh),
                         ngam=ngam, gam1=1.0, gam2=1e9, nfreq=nfreq, ntb=max_steps)
-        recs, off, prm, grid = make_batch(lib, cfg)
+        cfgs.append(cfg)
+        counts.append([int(rng.integers(min_steps, max_steps + 1)) for _ in range(2 * nl)])
+    if workers > 1 and nsets > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(workers, nsets)) as pool:
+            batches = pool.map(_sweep_set, cfgs)
+    else:
+        batches = [make_batch(lib, c) for c in cfgs]
+    all_recs, params, lens = [], [], []
+    grid = None
+    for (recs, off, prm, grid), cnt in zip(batches, counts):
         for b in range(len(off) - 1):
-            n = int(rng.integers(min_steps, max_steps + 1))
-            r = recs[off[b]:off[b] + n]
+            r = recs[off[b]:off[b] + cnt[b]]
             all_recs.append(r)
             lens.append(len(r))
             params.append(prm[b])

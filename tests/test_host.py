@@ -96,3 +96,22 @@ def test_history_generator_is_seeded(lib):
     b = cases.uneven(lib, nsets=2, seed=3)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_vectorised_dynamics_match_per_layer():
+    cfg = H.config_gaussian_ssc()
+    cfg.nlayers = 5
+    tb = np.logspace(np.log10(cfg.tb1), np.log10(cfg.tb2), 200)
+    lo, hi, E, G0 = H.layer_table(cfg)
+    om = 2 * np.pi * (np.cos(lo) - np.cos(hi)) * 2
+    many = H.layer_dynamics_many(E, G0, cfg.n_ism, tb, om, nsamp=800)
+    for i in range(cfg.nlayers):
+        one = H.layer_dynamics(E[i], G0[i], cfg.n_ism, tb, om[i], nsamp=800)
+        for k in ("Gamma", "R", "m", "tcomov", "t_obs"):
+            np.testing.assert_allclose(many[i][k], one[k], rtol=1e-10, atol=0)
+
+
+def test_pooled_sweep_equals_serial(lib):
+    a = H.sweep_batch(lib, 3, seed=11, min_steps=20, max_steps=60, max_layers=3)
+    b = H.sweep_batch(lib, 3, seed=11, min_steps=20, max_steps=60, max_layers=3, workers=2)
+    assert (a[0].tobytes() == b[0].tobytes()) and (a[1] == b[1]).all()
