@@ -261,7 +261,8 @@ enum pbag_ssc_path {
   PBAG_SSC_AUTO = 0,
   PBAG_SSC_CUDA_FP32 = 1,
   PBAG_SSC_TC_SPLIT_BF16 = 2,
-  PBAG_SSC_TC_BF16 = 3
+  PBAG_SSC_TC_BF16 = 3,
+  PBAG_SSC_SURROGATE = 4    /* learned band shapes + exact fallback (pbag_surrogate_configure) */
 };
 int pbag_set_ssc_path(pbag_ctx* ctx, int path);
 
@@ -301,6 +302,56 @@ enum pbag_precision {
 };
 int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph, int syn_method,
                   int precision, double* d_jsyn, double* d_jssc, pbag_status* st);
+
+/* ---- SSC surrogate -------------------------------------------------------
+ * A multilayer perceptron with its own FP32 training and inference kernels:
+ * layers dims[0] -> ... -> dims[nlayers], SiLU between layers, linear output.
+ * Parameters: one FP32 array, per layer W_l [dims[l+1]][dims[l]] (row-major)
+ * then b_l [dims[l+1]]. Device pointers for the data; synchronous. */
+typedef struct pbag_mlp pbag_mlp;
+int pbag_mlp_create(int device, const int* dims, int nlayers, pbag_mlp** out);
+void pbag_mlp_destroy(pbag_mlp* net);
+int64_t pbag_mlp_param_count(const pbag_mlp* net);
+int pbag_mlp_set_params(pbag_mlp* net, const float* host_params);
+/* host_params and/or host_grad (gradients of the last train step) may be NULL */
+int pbag_mlp_get_params(const pbag_mlp* net, float* host_params, float* host_grad);
+int pbag_mlp_forward(pbag_mlp* net, int n, const float* d_x, float* d_y);
+/* One step on n rows: forward, loss = sum(mask (y - t)^2) / (n dims[L]) (mask
+ * may be NULL), gradients, and (update != 0) an Adam update with rate lr.
+ * *loss (host, may be NULL) receives the loss. */
+int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t, const float* d_mask, float lr,
+                        int update, float* loss);
+
+/* The SSC surrogate of a context: exact band integrals of the SSC spectrum
+ * (PBAG_SUR_BANDS bands of nfreq/PBAG_SUR_BANDS frequencies; per band the
+ * power P, and the first and second moments Q, R of x = ln nu - (band centre)
+ * weighted by power: 3 x PBAG_SUR_BANDS projections on the tensor cores). In
+ * each band a baseline shape exp(beta x) matches P and Q exactly; an MLP with
+ * PBAG_SUR_IN inputs and nfreq outputs predicts the log10 correction to it; the
+ * spectrum is scaled to the exact band powers. Error estimate per state: the
+ * power-weighted mismatch of the predicted and exact Q (over P times the band
+ * half width) and R (over P times its square). States whose estimate exceeds
+ * tol are recomputed exactly.
+ * pbag_surrogate_configure: net (may be NULL until trained; not owned; dims
+ *   PBAG_SUR_IN -> ... -> nfreq), feature means and standard deviations (host,
+ *   PBAG_SUR_IN each, NULL: 0 and 1), tol. Needs ssc_tables and nfreq 128/256.
+ *   With a network set, pbag_set_ssc_path(ctx, PBAG_SSC_SURROGATE) makes the
+ *   step use it.
+ * pbag_surrogate_features: unstandardised features [n][PBAG_SUR_IN], the exact
+ *   projections [n][PBAG_SUR_PROJ] (P of every band, then Q, then R) and the
+ *   baseline log10 share of each frequency in its band's power [n][nfreq] of n
+ *   states (f [n][G], B [n], nph [n][F]); any output may be NULL.
+ * pbag_surrogate_contract: j_ssc [n][F] of n states through the surrogate,
+ *   the error estimates (d_err [n], may be NULL) and the number of exact
+ *   recomputations. Device pointers; synchronous. */
+#define PBAG_SUR_BANDS 16
+#define PBAG_SUR_PROJ 48
+#define PBAG_SUR_IN 128
+int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, const float* stdv, float tol);
+int pbag_surrogate_features(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,
+                            float* d_x, double* d_proj, float* d_base, pbag_status* st);
+int pbag_surrogate_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,
+                            double* d_jssc, float* d_err, int* n_fallback, pbag_status* st);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ STATUS_NAMES = {
 PBAG_SKIP, PBAG_INIT, PBAG_EVOLVE = 0, 1, 2
 PBAG_SYN_CSYN, PBAG_SYN_DER09, PBAG_SYN_GSL, PBAG_SYN_BESSEL = 0, 1, 2, 3
 PBAG_ELE_NUMERIC, PBAG_ELE_MIX = 1, 2
-PBAG_SSC_AUTO, PBAG_SSC_CUDA_FP32, PBAG_SSC_TC_SPLIT_BF16, PBAG_SSC_TC_BF16 = 0, 1, 2, 3
+PBAG_SSC_AUTO, PBAG_SSC_CUDA_FP32, PBAG_SSC_TC_SPLIT_BF16, PBAG_SSC_TC_BF16, PBAG_SSC_SURROGATE = 0, 1, 2, 3, 4
 PBAG_PREC_FP32, PBAG_PREC_BF16, PBAG_PREC_SPLIT_BF16, PBAG_PREC_TF32 = 0, 1, 2, 3
 PRECISION_NAMES = {PBAG_PREC_FP32: "fp32", PBAG_PREC_BF16: "bf16", PBAG_PREC_SPLIT_BF16: "split-bf16",
                    PBAG_PREC_TF32: "tf32"}

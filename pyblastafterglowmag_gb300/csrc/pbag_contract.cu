@@ -218,6 +218,28 @@ int cuda_status(cudaError_t e) { return e == cudaErrorMemoryAllocation ? PBAG_ER
 
 }  // namespace
 
+namespace pbag {
+// The contraction workspace of the context, reserved for n states, and the
+// split-BF16 operands (W tiles, U32, scales) of the states f / nph: the first
+// part of pbag_contract, shared with the surrogate.
+int contract_prepare(pbag_ctx* ctx, const CtxView& v, int n, const double* d_f, const double* d_nph, DevState* S,
+                     const void** Wt) {
+  auto* ws = static_cast<ContractWs*>(ctx_get_extension(ctx, kExtContract));
+  if (!ws) {
+    ws = new ContractWs();
+    ws->device = v.device;
+    ctx_set_extension(ctx, kExtContract, ws);
+  }
+  cudaError_t e = ws->reserve(n, kTcSplit, v);
+  if (e != cudaSuccess) return cuda_status(e);
+  *S = ws->S;
+  *Wt = ws->Wt;
+  k_contract_prep<<<n, kPrepThreads, 0, v.stream>>>(v.dg, n, d_f, nullptr, d_nph, PBAG_SYN_CSYN, kTcSplit, 0, 1,
+                                                     ws->S, ws->Wt, ws->prm);
+  return cudaGetLastError() == cudaSuccess ? PBAG_OK : PBAG_ERR_CUDA;
+}
+}  // namespace pbag
+
 extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,
                              int syn_method, int precision, double* d_jsyn, double* d_jssc, pbag_status* st) {
   if (st) {
@@ -271,7 +293,7 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   if (d_jsyn || fp32_ssc) ok(launch_rad_ssc(v.dg, S, ws->prm, n, fp32_ssc, 0, s));
   if (d_jssc && tc)
     ok(launch_ssc_tc_mode(mode, v.F, v.Gp, ws->Wt, mode == kTcTf32 ? (const void*)ws->bt32 : (const void*)v.dg.Bt, n,
-                          S.flags, S.U32, S.scal, v.dg.nu, d_jssc, S.err, s));
+                          S.flags, S.U32, S.scal, v.dg.hnu, v.F, v.F, d_jssc, S.err, s));
   if (d_jsyn) {
     const int64_t tot = (int64_t)n * v.F;
     k_contract_syn_out<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, v.F, S, d_jsyn);

@@ -55,10 +55,11 @@ struct GraphKey {
   const void* ss;
   bool ssc;
   int ssc_path;
+  int64_t sur_gen;
   const void* out[kOutputs];
   bool operator==(const GraphKey& o) const {
     if (nbw != o.nbw || max_len != o.max_len || nrec != o.nrec || recs != o.recs || prm != o.prm ||
-        state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path)
+        state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path || sur_gen != o.sur_gen)
       return false;
     for (int k = 0; k < kOutputs; ++k)
       if (out[k] != o.out[k]) return false;
@@ -83,8 +84,10 @@ struct pbag_ctx {
   // the caller pinned a path
   bool ssc_on_tensor_cores() const {
     return ssc && dg.Bt && (ssc_path == PBAG_SSC_AUTO || ssc_path == PBAG_SSC_TC_SPLIT_BF16 ||
-                            ssc_path == PBAG_SSC_TC_BF16);
+                            ssc_path == PBAG_SSC_TC_BF16 || ssc_path == PBAG_SSC_SURROGATE);
   }
+  // kernels of one step's SSC contraction on the side stream
+  int ssc_side_launches() const { return ssc_path == PBAG_SSC_SURROGATE ? surrogate_launches(this) : 1; }
 
   // radiation sums + SSC contraction of one step; the tensor-core contraction
   // runs on a second stream next to the synchrotron sums (both read only what
@@ -96,7 +99,15 @@ struct pbag_ctx {
     cudaError_t e;
     if ((e = cudaEventRecord(ev_fork, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
-    if ((e = launch_ssc_tc(dg, S, dg.Bt, nbw, ssc_path != PBAG_SSC_TC_BF16, side)) != cudaSuccess) return e;
+    if (ssc_path == PBAG_SSC_SURROGATE) {
+      CtxView v;
+      ctx_view(this, &v);
+      if ((e = surrogate_run(this, v, nbw, S.Abf, S.flags, S.U32, S.scal, S.f, G, S.n, F, S.scal + kScalB, kScal,
+                             S.jssc, S.err, side)) != cudaSuccess)
+        return e;
+    } else if ((e = launch_ssc_tc(dg, S, dg.Bt, nbw, ssc_path != PBAG_SSC_TC_BF16, side)) != cudaSuccess) {
+      return e;
+    }
     if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
     if ((e = launch_rad_ssc(dg, S, d_prm, nbw, false, s, stream)) != cudaSuccess) return e;
     return cudaStreamWaitEvent(stream, ev_join, 0);
@@ -289,6 +300,8 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   int64_t max_len = 0;
   for (int b = 0; b < nbw; ++b) max_len = std::max<int64_t>(max_len, off_h[b + 1] - off_h[b]);
   c->launches = 0;
+  if (c->ssc_path == PBAG_SSC_SURROGATE && nbw > 0 && (e = surrogate_reserve(c, nbw)) != cudaSuccess)
+    return cuda_code(e);
   if (nbw > 0) {
     if ((e = launch_prepare(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int64_t)nrec, c->d_first, c->d_ss,
                             c->stream)) != cudaSuccess)
@@ -310,7 +323,7 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   // Without timing, the step loop (3 launches per step index) is captured once
   // into a CUDA graph per batch shape and buffer set, and replayed.
   if (!c->timing && max_len > 0) {
-    GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, {}};
+    GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, surrogate_generation(c), {}};
     std::memcpy(key.out, &d_out, sizeof(d_out));
     if (!c->graph_exec || !(key == c->graph_key)) {
       if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -338,7 +351,7 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
       c->graph_key = key;
     }
     if (cudaGraphLaunch(c->graph_exec, c->stream) != cudaSuccess) return PBAG_ERR_CUDA;
-    c->launches += (c->ssc_on_tensor_cores() ? 3 : 2) * max_len + 1;
+    c->launches += (c->ssc_on_tensor_cores() ? 2 + c->ssc_side_launches() : 2) * max_len + 1;
     max_len = 0;  // the loop below has nothing left to launch
   }
   for (int64_t s = 0; s < max_len; ++s) {
@@ -494,6 +507,11 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.nu, nu));
   ok(c->grid_upload(&d.dnu_nu, dnu));
   ok(c->grid_upload(&d.inv_hnu, inv_hnu));
+  {
+    std::vector<double> hnu(F);
+    for (int k = 0; k < F; ++k) hnu[k] = cgs::h_pl * nu[k];
+    ok(c->grid_upload(&d.hnu, hnu));
+  }
   ok(c->grid_upload(&d.ssa_nu, ssa_nu));
   // the evolve kernel's tables in one block (GridTab layout)
   d.Ge = (G + 1) / 2 * 2;
@@ -620,8 +638,9 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
 int64_t pbag_last_launch_count(const pbag_ctx* c) { return c ? c->launches : -1; }
 
 int pbag_set_ssc_path(pbag_ctx* c, int path) {
-  if (!c || path < PBAG_SSC_AUTO || path > PBAG_SSC_TC_BF16) return PBAG_ERR_ARG;
+  if (!c || path < PBAG_SSC_AUTO || path > PBAG_SSC_SURROGATE) return PBAG_ERR_ARG;
   if ((path == PBAG_SSC_TC_SPLIT_BF16 || path == PBAG_SSC_TC_BF16) && !c->dg.Bt) return PBAG_ERR_UNSUPPORTED;
+  if (path == PBAG_SSC_SURROGATE && !surrogate_ready(c)) return PBAG_ERR_ARG;  // pbag_surrogate_configure first
   c->ssc_path = path;
   return PBAG_OK;
 }

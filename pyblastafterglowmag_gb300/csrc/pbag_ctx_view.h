@@ -25,9 +25,23 @@ bool ctx_view(const pbag_ctx* c, CtxView* v);
 struct CtxExtension {
   virtual ~CtxExtension() = default;
 };
-enum : int { kExtContract = 0, kExtSlots = 2 };
+enum : int { kExtContract = 0, kExtSurrogate = 1, kExtSlots = 2 };
 CtxExtension* ctx_get_extension(pbag_ctx* c, int slot);
 void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* ext);
+
+// pbag_surrogate.cu: the surrogate SSC contraction of nrows rows (see there)
+cudaError_t surrogate_run(pbag_ctx* ctx, const CtxView& v, int nrows, const void* Wt, const int* flags,
+                          const float* U32, const double* scal, const double* f, int fs, const double* nph, int ns,
+                          const double* Bv, int bs, double* out, int* errs, cudaStream_t st);
+bool surrogate_ready(pbag_ctx* ctx);
+cudaError_t surrogate_reserve(pbag_ctx* ctx, int n);
+int64_t surrogate_generation(pbag_ctx* ctx);
+int surrogate_launches(const pbag_ctx* ctx);
+
+// pbag_contract.cu: reserve the contraction workspace for n states and build
+// their split-BF16 operands (W tiles, U32, scales) into S / Wt
+int contract_prepare(pbag_ctx* ctx, const CtxView& v, int n, const double* d_f, const double* d_nph, DevState* S,
+                     const void** Wt);
 
 }  // namespace pbag
 

@@ -47,6 +47,7 @@ struct DevGrid {
   const float* nu32;     // [F]   nu in FP32
   const double* dnu_nu;  // [F]   (nu[k+1]-nu[k])/nu[k]
   const double* inv_hnu; // [F]   1/(h nu) (microphysics.h:520)
+  const double* hnu;     // [F]   h nu (output scale of the SSC contraction)
   const double* ssa_nu;  // [F]   -1/(8 pi m_e nu^2) (numeric_model.h:211)
   int Gs;                // G rounded up to a multiple of 4 (row stride of KintT)
   int kint_stage;        // bytes of KintT the evolve kernel stages in shared memory (0: read from L2)
@@ -131,7 +132,8 @@ enum : int {
   kScalSw = 8,     // scale of w32
   kScalSv = 9,     // scale of v32
   kScalPref = 10,  // synchrotron prefactor of this step
-  // 11, 12 unused
+  kScalB = 11,       // magnetic field of this step
+  // 12 unused
   kScalFac = 13,     // photon escape factor (dr/c)/vol (microphysics.h:517-518)
   kScalAccNe = 14,   // accel_frac / N_e
   kScalAnpNe = 15,   // accel_frac n' / N_e

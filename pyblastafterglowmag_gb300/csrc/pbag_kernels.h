@@ -35,9 +35,10 @@ cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* B
 // tiles) or kTcTf32 (FP32 tiles in the 4-byte layout), Wt the weight tiles,
 // Kt the kernel slabs
 enum : int { kTcBf16 = 0, kTcSplit = 1, kTcTf32 = 2 };
+// nout slabs (grid x), output o of row r at out[r ostride + o] scaled by oscale[o]
 cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
-                               const int* flags, const float* U32, const double* scal, const double* nu, double* out,
-                               int* err, cudaStream_t st);
+                               const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
+                               int ostride, double* out, int* err, cudaStream_t st);
 // K slabs as TF32 operands (FP32 values rounded to TF32, 4-byte layout, lo parts zero)
 void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32);
 

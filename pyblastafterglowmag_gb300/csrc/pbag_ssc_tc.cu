@@ -147,7 +147,7 @@ template <int H, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int N, int S,
          uint32_t body, uint32_t ubytes, uint32_t uring, const int* __restrict__ flags, const float* __restrict__ U32,
-         const double* __restrict__ scal, const double* __restrict__ nu, double* __restrict__ out,
+         const double* __restrict__ scal, const double* __restrict__ oscale, int ostride, double* __restrict__ out,
          int* __restrict__ err) {
   constexpr int F = kTcK * H;
   constexpr bool kSplit = MODE == kTcSplit;
@@ -219,7 +219,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
   // the blastwaves this thread finishes (columns tid and tid + 128) and their FP64 factors
   bool live[2];
   double fac[2];
-  const double hnu = cgs::h_pl * nu[i];
+  const double hnu = oscale[i];  // h nu_i for the SSC spectrum
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
     const int col = tid + q * kTcThreads, r = row0 + col;
@@ -388,7 +388,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
         a2 += row[k + 2];
         a3 += row[k + 3];
       }
-      out[(size_t)(row0 + col) * F + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
+      out[(size_t)(row0 + col) * ostride + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
     }
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after the CTA exits
@@ -402,8 +402,8 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
 
 template <int H, int MODE>
 cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
-                      const float* U32, const double* scal, const double* nu, double* out, int* err,
-                      cudaStream_t st) {
+                      const float* U32, const double* scal, const double* oscale, int nout, int ostride, double* out,
+                      int* err, cudaStream_t st) {
   constexpr int F = kTcK * H;
   const int N = std::min(kTcCols, (nrows + 15) / 16 * 16);
   const TcPlan plan = tc_plan(F, N, Gp * (MODE == kTcTf32 ? 2 : 1));
@@ -415,9 +415,9 @@ cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, 
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 grid(F, (nrows + kTcCols - 1) / kTcCols);
+  dim3 grid(nout, (nrows + kTcCols - 1) / kTcCols);
   k_ssc_tc<H, MODE><<<grid, kTcThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
-                                                           plan.uring, flags, U32, scal, nu, out, err);
+                                                           plan.uring, flags, U32, scal, oscale, ostride, out, err);
   return cudaGetLastError();
 }
 
@@ -475,14 +475,14 @@ void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std
 }
 
 cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
-                               const int* flags, const float* U32, const double* scal, const double* nu, double* out,
-                               int* err, cudaStream_t st) {
+                               const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
+                               int ostride, double* out, int* err, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
   const auto* w = static_cast<const unsigned char*>(Wt);
   const auto* k = static_cast<const unsigned char*>(Kt);
 #define PBAG_TC_CASE(HH, MM) \
-  return launch_tc<HH, MM>(w, k, Gp, nrows, flags, U32, scal, nu, out, err, st)
+  return launch_tc<HH, MM>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, st)
   if (F == 128) {
     if (mode == kTcSplit) PBAG_TC_CASE(1, kTcSplit);
     if (mode == kTcBf16) PBAG_TC_CASE(1, kTcBf16);
@@ -500,8 +500,8 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
 cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
                           cudaStream_t st) {
   if (!S.Abf || !Bt) return cudaErrorInvalidValue;
-  return launch_ssc_tc_mode(split ? kTcSplit : kTcBf16, g.F, g.Gp, S.Abf, Bt, nbw, S.flags, S.U32, S.scal, g.nu,
-                            S.jssc, S.err, st);
+  return launch_ssc_tc_mode(split ? kTcSplit : kTcBf16, g.F, g.Gp, S.Abf, Bt, nbw, S.flags, S.U32, S.scal, g.hnu,
+                            g.F, g.F, S.jssc, S.err, st);
 }
 
 }  // namespace pbag

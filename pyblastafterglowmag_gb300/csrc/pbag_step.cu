@@ -806,6 +806,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     scal[kScalSw] = unscale_from_exp(wexp);
     scal[kScalSv] = unscale_from_exp(vexp);
     scal[kScalPref] = sc.pref;
+    scal[kScalB] = B;
     float* rp = S.rad32 + (size_t)b * 4;
     rp[0] = sc.inv_ncrit;
     rp[1] = sc.inv_nlar;
