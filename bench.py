@@ -39,11 +39,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction", "uneven-sweep"],
+    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction", "uneven-sweep", "surrogate"],
                     help="gaussian-jet: the step benchmark (default); contraction: the emissivity-"
                          "contraction microbenchmark (65536 states, 256 gamma x 256 nu); uneven-sweep: a "
-                         "seeded sample of the 4096-set parameter sweep with uneven step counts")
+                         "seeded sample of the 4096-set parameter sweep with uneven step counts; surrogate: train "
+                         "the SSC surrogate on states of the sweep, time it against the exact contraction and "
+                         "deploy it on the Gaussian jet")
     ap.add_argument("--sets", type=int, default=64, help="parameter sets of the uneven-sweep workload")
+    ap.add_argument("--train-states", type=int, default=1000000, help="training states of the surrogate workload")
+    ap.add_argument("--epochs", type=int, default=8, help="training epochs of the surrogate workload")
+    ap.add_argument("--tol", type=float, default=0.01, help="error-estimate tolerance of the surrogate")
     ap.add_argument("--states", type=int, default=65536)
     ap.add_argument("--fp32-states", type=int, default=4096,
                     help="states of the FP32 CUDA-core variant of the contraction benchmark")
@@ -585,8 +590,130 @@ def sweep_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------- surrogate arm ---
+def surrogate_arm(args):
+    """SSC surrogate: trained on states of a seeded sweep (the plain GPU step),
+    evaluated on held-out states against the exact contraction (split BF16),
+    timed against it, and deployed on the Gaussian jet with the error estimate
+    and exact fallback."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from pyblastafterglowmag_gb300 import _lib, abi, build, histories as H, surrogate as SG
+    build.build()
+    dev = torch.device("cuda", local)
+    cfg, recs, off, prm, g = workload()
+    _, freq = _lib.grids(g)
+    ctx = _lib.Context(g, device=local, ssc=True)
+    SG.configure(ctx)
+    t0 = time.perf_counter()
+    f, B, nph = SG.sweep_states(ctx, g, nsets=max(args.sets, 8), seed=5, workers=os.cpu_count() or 1, device=local,
+                                max_states=args.train_states)
+    t_gen = time.perf_counter() - t0
+    n = f.shape[0]
+    X = torch.zeros((n, SG.NIN), dtype=torch.float32, device=dev)
+    proj = torch.zeros((n, SG.NPROJ), dtype=torch.float64, device=dev)
+    base = torch.zeros((n, g.nfreq), dtype=torch.float32, device=dev)
+    SG.features(ctx, n, f.data_ptr(), B.data_ptr(), nph.data_ptr(), X.data_ptr(), proj.data_ptr(), base.data_ptr())
+    jex = SG.exact_ssc(ctx, f, B, nph)
+    T, M = SG.make_targets(jex, proj, freq, base)
+    ntr = int(0.9 * n)
+    tr = SG.Trainer(g.nfreq, local, seed=0)
+    Xs = tr.standardise(X.clone())
+    t0 = time.perf_counter()
+    loss = tr.fit(Xs[:ntr], T[:ntr], M[:ntr], epochs=args.epochs, batch=4096, lr=2e-3)
+    torch.cuda.synchronize(dev)
+    t_train = time.perf_counter() - t0
+    va = slice(ntr, n)
+    fv, Bv, nv, jv = f[va].contiguous(), B[va].contiguous(), nph[va].contiguous(), jex[va].contiguous()
+    nv_states = fv.shape[0]
+    # accuracy without fallback, the error estimate, and with the tolerance
+    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
+    j = torch.zeros_like(jv)
+    est = torch.zeros(nv_states, dtype=torch.float32, device=dev)
+    SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), j.data_ptr(), est.data_ptr())
+    err = SG.rel_l2(j, jv)
+    err_base = SG.rel_l2(SG.band_baseline(proj[va], freq, base[va]), jv)
+    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=args.tol)
+    jt = torch.zeros_like(jv)
+    nfb = SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jt.data_ptr())
+    err_t = SG.rel_l2(jt, jv)
+    q = lambda e, p: float(e.quantile(p)) if e.numel() <= 16_000_000 else float(e.float().quantile(p))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ms = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    jj = torch.zeros_like(jv)
+    ms_exact = timed(lambda: ctx.contract_device(nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(),
+                                                 abi.PBAG_SYN_CSYN, abi.PBAG_PREC_SPLIT_BF16, 0, jj.data_ptr()))
+    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
+    ms_sur = timed(lambda: SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jj.data_ptr()))
+    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=args.tol)
+    ms_sur_fb = timed(lambda: SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jj.data_ptr()))
+    # deployment on the Gaussian jet: surrogate step vs plain step
+    outs = ("j_all", "a_all", "f_all", "i_all")
+    plain = ctx.run(recs, off, prm, outputs=outs)
+    ctx.set_ssc_path(abi.PBAG_SSC_SURROGATE)
+    sur = ctx.run(recs, off, prm, outputs=outs)
+    t_sur = min(timeit_run(ctx, recs, off, prm) for _ in range(3))
+    ctx.set_ssc_path(abi.PBAG_SSC_AUTO)
+    t_plain = min(timeit_run(ctx, recs, off, prm) for _ in range(3))
+    num = np.sqrt(((sur["j_all"] - plain["j_all"]) ** 2).sum(axis=1))
+    den = np.sqrt((plain["j_all"] ** 2).sum(axis=1))
+    rows = den > 0
+    dep = num[rows] / den[rows]
+    nvalid = int((recs["mode"] != 0).sum())
+    if rank != 0:
+        return
+    line = {"metric": "SSC surrogate speed-up over the exact contraction (states/s ratio)",
+            "value": ms_exact / ms_sur_fb, "unit": "x", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_sur_fb, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 MLP / bf16x3 projections", "data": "synthetic",
+            "config": {"workload": "ssc-surrogate-201x128", "train_states": ntr, "val_states": nv_states,
+                       "epochs": args.epochs, "net": [SG.NIN, *SG.HIDDEN, g.nfreq], "tol": args.tol,
+                       "train_source": "seeded parameter sweep (seed 5), plain GPU step"},
+            "timing": {"generate_s": t_gen, "train_s": t_train, "final_loss": loss,
+                       "exact_ms": ms_exact, "surrogate_ms_no_fallback": ms_sur, "surrogate_ms_with_fallback": ms_sur_fb,
+                       "states_per_s_exact": nv_states / (ms_exact * 1e-3),
+                       "states_per_s_surrogate": nv_states / (ms_sur_fb * 1e-3),
+                       "speedup_no_fallback": ms_exact / ms_sur},
+            "accuracy": {"rel_l2_median": q(err, 0.5), "rel_l2_p90": q(err, 0.9), "rel_l2_p99": q(err, 0.99),
+                         "baseline_rel_l2_median": q(err_base, 0.5),
+                         "with_fallback_rel_l2_median": q(err_t, 0.5), "with_fallback_rel_l2_p99": q(err_t, 0.99),
+                         "with_fallback_rel_l2_max": float(err_t.max()),
+                         "fallback_fraction": nfb / nv_states,
+                         "accepted_true_error_p99": q(err[est <= args.tol], 0.99) if bool((est <= args.tol).any())
+                         else None},
+            "deployment_gaussian_jet": {"j_all_rel_l2_vs_plain_median": float(np.median(dep)),
+                                        "j_all_rel_l2_vs_plain_p99": float(np.percentile(dep, 99)),
+                                        "blastwave_steps_per_s_surrogate": nvalid / t_sur,
+                                        "blastwave_steps_per_s_plain": nvalid / t_plain}}
+    print(json.dumps(line), flush=True)
+
+
+def timeit_run(ctx, recs, off, prm):
+    t0 = time.perf_counter()
+    ctx.run(recs, off, prm, outputs=("j_all", "a_all", "f_all", "i_all"))
+    return time.perf_counter() - t0
+
+
 def main():
     args = parse()
+    if args.workload == "surrogate":
+        surrogate_arm(args)
+        return
     if args.workload == "contraction":
         contraction_arm(args)
     elif args.workload == "uneven-sweep":
