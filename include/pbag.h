@@ -316,6 +316,11 @@ int pbag_mlp_set_params(pbag_mlp* net, const float* host_params);
 /* host_params and/or host_grad (gradients of the last train step) may be NULL */
 int pbag_mlp_get_params(const pbag_mlp* net, float* host_params, float* host_grad);
 int pbag_mlp_forward(pbag_mlp* net, int n, const float* d_x, float* d_y);
+/* Inference on the tensor cores: weights and activations rounded to BF16, FP32
+ * accumulation, all layers in one kernel (every in-dimension a multiple of 32,
+ * every out-dimension a multiple of 32 up to 256, at most 8 layers; otherwise
+ * PBAG_ERR_UNSUPPORTED). The weights are laid out again after they change. */
+int pbag_mlp_infer(pbag_mlp* net, int n, const float* d_x, float* d_y);
 /* One step on n rows: forward, loss = sum(mask (y - t)^2) / (n dims[L]) (mask
  * may be NULL), gradients, and (update != 0) an Adam update with rate lr.
  * *loss (host, may be NULL) receives the loss. */

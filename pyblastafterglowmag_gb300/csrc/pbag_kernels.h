@@ -50,6 +50,21 @@ void build_ssc_tables(const double* gam, int G, const double* freq, int F, int G
 // the largest dynamic shared memory of k_evolve for any grid
 size_t evolve_smem_max_bytes();
 
+// BF16 MLP inference on the tensor cores (pbag_mlp_tc.cu): layer l maps
+// dims[l] -> dims[l+1] with weights W[l] in the B-operand layout written by
+// mlp_tc_pack and FP32 biases b[l]; SiLU between layers.
+constexpr int kMtMaxOut = 256;
+constexpr int kMtMaxLayers = 8;
+struct MlpTcArgs {
+  int L;
+  int dims[kMtMaxLayers + 1];
+  const uint16_t* W[kMtMaxLayers];
+  const float* b[kMtMaxLayers];
+};
+bool mlp_tc_supported(const int* dims, int L);
+cudaError_t mlp_tc_pack(int N, int K, const float* W, uint16_t* out, cudaStream_t st);
+cudaError_t launch_mlp_tc(const MlpTcArgs& a, int n, const float* X, float* Y, int* err, cudaStream_t st);
+
 }  // namespace pbag
 
 #endif

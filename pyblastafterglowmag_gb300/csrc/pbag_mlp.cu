@@ -13,6 +13,7 @@
 
 #include "pbag.h"
 #include "pbag_ctx_view.h"
+#include "pbag_kernels.h"
 
 namespace {
 
@@ -171,6 +172,11 @@ struct pbag_mlp {
   float* m = nullptr;  // Adam moments
   float* v = nullptr;
   int64_t t = 0;       // Adam step
+  int64_t pgen = 0;    // bumped whenever the parameters change
+  // BF16 copy of the weights in the tensor-core operand layout (inference)
+  uint16_t* wtc = nullptr;
+  int64_t tcgen = -1;  // pgen the copy was made from
+  int* tcerr = nullptr;
   // activations of the last forward pass: Z_l (pre-activation) and H_l per layer
   int cap = 0;
   std::vector<float*> Z, Hs, dH;
@@ -183,6 +189,8 @@ struct pbag_mlp {
     cudaFree(m);
     cudaFree(v);
     cudaFree(loss);
+    cudaFree(wtc);
+    cudaFree(tcerr);
     for (float* x : Z) cudaFree(x);
     for (float* x : Hs) cudaFree(x);
     for (float* x : dH) cudaFree(x);
@@ -264,6 +272,34 @@ struct pbag_mlp {
 };
 
 namespace pbag {
+// BF16 tensor-core inference: lays the weights out again when they changed
+cudaError_t mlp_infer(pbag_mlp* net, int n, const float* X, float* Y, cudaStream_t st) {
+  const int L = net->L();
+  if (!mlp_tc_supported(net->dims.data(), L)) return cudaErrorNotSupported;
+  cudaError_t e = cudaSuccess;
+  size_t tot = 0;
+  for (int l = 0; l < L; ++l) tot += (size_t)net->dims[l + 1] * net->dims[l];
+  if (!net->wtc) {
+    if ((e = cudaMalloc(&net->wtc, tot * sizeof(uint16_t))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&net->tcerr, sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMemset(net->tcerr, 0, sizeof(int))) != cudaSuccess) return e;
+  }
+  MlpTcArgs a{};
+  a.L = L;
+  size_t off = 0;
+  for (int l = 0; l <= L; ++l) a.dims[l] = net->dims[l];
+  for (int l = 0; l < L; ++l) {
+    if (net->tcgen != net->pgen)
+      if ((e = mlp_tc_pack(net->dims[l + 1], net->dims[l], net->p + net->woff[l], net->wtc + off, st)) != cudaSuccess)
+        return e;
+    a.W[l] = net->wtc + off;
+    a.b[l] = net->p + net->boff[l];
+    off += (size_t)net->dims[l + 1] * net->dims[l];
+  }
+  net->tcgen = net->pgen;
+  return launch_mlp_tc(a, n, X, Y, net->tcerr, st);
+}
+int* mlp_infer_error(pbag_mlp* net) { return net->tcerr; }
 // used by the surrogate step path (pbag_surrogate.cu)
 cudaError_t mlp_forward(pbag_mlp* net, int n, const float* X, float* Y, cudaStream_t st) {
   cudaStream_t keep = net->stream;
@@ -327,6 +363,7 @@ int pbag_mlp_set_params(pbag_mlp* net, const float* host) {
   cudaMemset(net->m, 0, net->nparams * sizeof(float));
   cudaMemset(net->v, 0, net->nparams * sizeof(float));
   net->t = 0;
+  net->pgen += 1;
   return PBAG_OK;
 }
 
@@ -352,6 +389,23 @@ int pbag_mlp_forward(pbag_mlp* net, int n, const float* d_x, float* d_y) {
   return e == cudaSuccess ? PBAG_OK : status_of(e);
 }
 
+int pbag_mlp_infer(pbag_mlp* net, int n, const float* d_x, float* d_y) {
+  if (!net || n < 0 || (n > 0 && (!d_x || !d_y))) return PBAG_ERR_ARG;
+  if (!pbag::mlp_tc_supported(net->dims.data(), net->L())) return PBAG_ERR_UNSUPPORTED;
+  if (n == 0) return PBAG_OK;
+  if (cudaSetDevice(net->device) != cudaSuccess) return PBAG_ERR_CUDA;
+  cudaError_t e = pbag::mlp_infer(net, n, d_x, d_y, net->stream);
+  int code = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&code, net->tcerr, sizeof(int), cudaMemcpyDeviceToHost, net->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(net->stream);
+  if (e != cudaSuccess) return status_of(e);
+  if (code != 0) {
+    cudaMemset(net->tcerr, 0, sizeof(int));
+    return code;
+  }
+  return PBAG_OK;
+}
+
 int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t, const float* d_mask, float lr,
                         int update, float* loss) {
   if (!net || n <= 0 || !d_x || !d_t) return PBAG_ERR_ARG;
@@ -362,6 +416,7 @@ int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t
   if (e == cudaSuccess) e = net->backward(n, d_x, Y, d_t, d_mask, (float)n * net->dims.back());
   if (e == cudaSuccess && update) {
     net->t += 1;
+    net->pgen += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f / (1.f - std::pow(b1, (float)net->t));
     const float c2 = 1.f / (1.f - std::pow(b2, (float)net->t));

@@ -33,16 +33,22 @@
 #include <vector>
 
 #include "pbag_kernels.h"
+#include "pbag_tc.cuh"
 
 namespace pbag {
 
 namespace {
 
+using tc::idesc_mma;
+using tc::mbar_wait;
+using tc::mma_issue;
+using tc::smem_desc;
+using tc::smem_u32;
+
 constexpr int kTcThreads = 128;
 constexpr int kTcK = 128;          // accumulator rows (output columns k) per half of the frequency grid
 constexpr int kTcMaxStages = 8;    // ring of chunk stages (all chunks of a small problem at once)
 constexpr int kK8 = kTcChunk16;   // 16-byte K columns of a full chunk
-constexpr int kWaitLimit = 1 << 21;
 constexpr int kPStride = kTcK + 1;  // row stride (floats) of the epilogue's product table
 constexpr size_t kTcDynMax = 231424;       // dynamic shared memory of a CTA (227 KiB less the static part)
 constexpr size_t kTcFixed = 1024 + 256;   // alignment slack, barriers and the tensor-memory slot
@@ -82,58 +88,6 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src, bool valid
                    __cvta_generic_to_shared(dst))),
                "l"(src), "r"(valid ? 4 : 0)
                : "memory");
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// tcgen05 shared-memory matrix descriptor: K-major, no swizzle. lbo = byte
-// stride between core matrices along K, sbo = along M/N.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version of this architecture
-  return d;               // base offset 0, relative LBO, no swizzle
-}
-
-// Instruction descriptor, D = F32, both operands K-major: kind::f16 with A = B =
-// BF16 (type 1), or kind::tf32 with A = B = TF32 (type 2).
-__host__ __device__ constexpr uint32_t idesc_mma(int M, int N, bool tf32) {
-  return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int it = 0; it < kWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (it > 32) __nanosleep(64);
-  }
-  return false;
-}
-
-template <bool kTf32>
-__device__ __forceinline__ void mma_issue(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  if (kTf32)
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-  else
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
 }
 
 // One CTA: output frequency i = blockIdx.x, blastwaves kTcCols*blockIdx.y + [0, N).

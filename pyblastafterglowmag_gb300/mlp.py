@@ -1,5 +1,6 @@
 """Python handle of the C-ABI multilayer perceptron (pbag_mlp_*): FP32
-training and inference kernels of the library, data as device addresses."""
+training kernels, FP32 and BF16 tensor-core inference of the library, data as
+device addresses."""
 import ctypes as C
 
 import numpy as np
@@ -18,6 +19,7 @@ def _l():
         lib.pbag_mlp_set_params.argtypes = [C.c_void_p, P(C.c_float)]
         lib.pbag_mlp_get_params.argtypes = [C.c_void_p, P(C.c_float), P(C.c_float)]
         lib.pbag_mlp_forward.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        lib.pbag_mlp_infer.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         lib.pbag_mlp_train_step.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                             C.c_int, P(C.c_float)]
         lib._mlp_bound = True
@@ -74,6 +76,10 @@ class MLP:
 
     def forward(self, n, d_x, d_y):
         _lib._check(_l().pbag_mlp_forward(self._h, int(n), C.c_void_p(d_x), C.c_void_p(d_y)), "pbag_mlp_forward")
+
+    def infer(self, n, d_x, d_y):
+        """BF16 inference on the tensor cores (pbag_mlp_infer)."""
+        _lib._check(_l().pbag_mlp_infer(self._h, int(n), C.c_void_p(d_x), C.c_void_p(d_y)), "pbag_mlp_infer")
 
     def train_step(self, n, d_x, d_t, d_mask=0, lr=1e-3, update=True):
         loss = C.c_float()
