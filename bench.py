@@ -617,27 +617,33 @@ def surrogate_arm(args):
     SG.features(ctx, n, f.data_ptr(), B.data_ptr(), nph.data_ptr(), X.data_ptr(), proj.data_ptr(), base.data_ptr())
     jex = SG.exact_ssc(ctx, f, B, nph)
     T, M = SG.make_targets(jex, proj, freq, base)
-    ntr = int(0.9 * n)
+    ntr, ncal = int(0.85 * n), int(0.05 * n)
     tr = SG.Trainer(g.nfreq, local, seed=0)
     Xs = tr.standardise(X.clone())
     t0 = time.perf_counter()
     loss = tr.fit(Xs[:ntr], T[:ntr], M[:ntr], epochs=args.epochs, batch=4096, lr=2e-3)
     torch.cuda.synchronize(dev)
     t_train = time.perf_counter() - t0
-    va = slice(ntr, n)
+    cal = slice(ntr, ntr + ncal)
+    scale = SG.calibrate(ctx, tr, f[cal].contiguous(), B[cal].contiguous(), nph[cal].contiguous(),
+                         jex[cal].contiguous())
+    va = slice(ntr + ncal, n)
     fv, Bv, nv, jv = f[va].contiguous(), B[va].contiguous(), nph[va].contiguous(), jex[va].contiguous()
     nv_states = fv.shape[0]
     # accuracy without fallback, the error estimate, and with the tolerance
-    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
+    cfg_sur = lambda tol: SG.configure(ctx, tr.net, tr.mean, tr.std, tol=tol, est_scale=scale)
+    cfg_sur(1e30)
     j = torch.zeros_like(jv)
     est = torch.zeros(nv_states, dtype=torch.float32, device=dev)
     SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), j.data_ptr(), est.data_ptr())
     err = SG.rel_l2(j, jv)
+    err_rows = SG.rel_l2_rows(j, jv)
     err_base = SG.rel_l2(SG.band_baseline(proj[va], freq, base[va]), jv)
-    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=args.tol)
+    cfg_sur(args.tol)
     jt = torch.zeros_like(jv)
     nfb = SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jt.data_ptr())
     err_t = SG.rel_l2(jt, jv)
+    accepted = (est <= args.tol) & torch.isfinite(err_rows)
     q = lambda e, p: float(e.quantile(p)) if e.numel() <= 16_000_000 else float(e.float().quantile(p))
 
     def timed(fn):
@@ -658,9 +664,11 @@ def surrogate_arm(args):
     jj = torch.zeros_like(jv)
     ms_exact = timed(lambda: ctx.contract_device(nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(),
                                                  abi.PBAG_SYN_CSYN, abi.PBAG_PREC_SPLIT_BF16, 0, jj.data_ptr()))
-    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
+    ms_exact_bf16 = timed(lambda: ctx.contract_device(nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(),
+                                                      abi.PBAG_SYN_CSYN, abi.PBAG_PREC_BF16, 0, jj.data_ptr()))
+    cfg_sur(1e30)
     ms_sur = timed(lambda: SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jj.data_ptr()))
-    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=args.tol)
+    cfg_sur(args.tol)
     ms_sur_fb = timed(lambda: SG.contract(ctx, nv_states, fv.data_ptr(), Bv.data_ptr(), nv.data_ptr(), jj.data_ptr()))
     # deployment on the Gaussian jet: surrogate step vs plain step
     outs = ("j_all", "a_all", "f_all", "i_all")
@@ -680,22 +688,28 @@ def surrogate_arm(args):
     line = {"metric": "SSC surrogate speed-up over the exact contraction (states/s ratio)",
             "value": ms_exact / ms_sur_fb, "unit": "x", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_sur_fb, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 MLP / bf16x3 projections", "data": "synthetic",
+            "dtype": "bf16 MLP and projections / bf16x3 fallback", "data": "synthetic",
             "config": {"workload": "ssc-surrogate-201x128", "train_states": ntr, "val_states": nv_states,
                        "epochs": args.epochs, "net": [SG.NIN, *SG.HIDDEN, g.nfreq], "tol": args.tol,
-                       "train_source": "seeded parameter sweep (seed 5), plain GPU step"},
+                       "train_source": "seeded parameter sweep (seed 5), plain GPU step",
+                       "calibration_states": ncal, "est_scale": scale},
             "timing": {"generate_s": t_gen, "train_s": t_train, "final_loss": loss,
-                       "exact_ms": ms_exact, "surrogate_ms_no_fallback": ms_sur, "surrogate_ms_with_fallback": ms_sur_fb,
+                       "exact_ms": ms_exact, "exact_bf16_ms": ms_exact_bf16,
+                       "surrogate_ms_no_fallback": ms_sur, "surrogate_ms_with_fallback": ms_sur_fb,
                        "states_per_s_exact": nv_states / (ms_exact * 1e-3),
                        "states_per_s_surrogate": nv_states / (ms_sur_fb * 1e-3),
-                       "speedup_no_fallback": ms_exact / ms_sur},
+                       "speedup_no_fallback": ms_exact / ms_sur,
+                       "speedup_vs_exact_bf16": ms_exact_bf16 / ms_sur_fb},
             "accuracy": {"rel_l2_median": q(err, 0.5), "rel_l2_p90": q(err, 0.9), "rel_l2_p99": q(err, 0.99),
                          "baseline_rel_l2_median": q(err_base, 0.5),
                          "with_fallback_rel_l2_median": q(err_t, 0.5), "with_fallback_rel_l2_p99": q(err_t, 0.99),
                          "with_fallback_rel_l2_max": float(err_t.max()),
                          "fallback_fraction": nfb / nv_states,
-                         "accepted_true_error_p99": q(err[est <= args.tol], 0.99) if bool((est <= args.tol).any())
-                         else None},
+                         "accepted_true_error_p99": q(err_rows[accepted], 0.99) if bool(accepted.any()) else None,
+                         "accepted_true_error_max": float(err_rows[accepted].max()) if bool(accepted.any())
+                         else None,
+                         "accepted_above_tol_fraction": float((err_rows[accepted] > args.tol).float().mean())
+                         if bool(accepted.any()) else None},
             "deployment_gaussian_jet": {"j_all_rel_l2_vs_plain_median": float(np.median(dep)),
                                         "j_all_rel_l2_vs_plain_p99": float(np.percentile(dep, 99)),
                                         "blastwave_steps_per_s_surrogate": nvalid / t_sur,

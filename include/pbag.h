@@ -327,32 +327,39 @@ int pbag_mlp_infer(pbag_mlp* net, int n, const float* d_x, float* d_y);
 int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t, const float* d_mask, float lr,
                         int update, float* loss);
 
-/* The SSC surrogate of a context: exact band integrals of the SSC spectrum
- * (PBAG_SUR_BANDS bands of nfreq/PBAG_SUR_BANDS frequencies; per band the
- * power P, and the first and second moments Q, R of x = ln nu - (band centre)
- * weighted by power: 3 x PBAG_SUR_BANDS projections on the tensor cores). In
- * each band a baseline shape exp(beta x) matches P and Q exactly; an MLP with
- * PBAG_SUR_IN inputs and nfreq outputs predicts the log10 correction to it; the
- * spectrum is scaled to the exact band powers. Error estimate per state: the
- * power-weighted mismatch of the predicted and exact Q (over P times the band
- * half width) and R (over P times its square). States whose estimate exceeds
- * tol are recomputed exactly.
+/* The SSC surrogate of a context. Exact projections of the SSC spectrum on
+ * the tensor cores (BF16): over PBAG_SUR_BANDS bands of nfreq/PBAG_SUR_BANDS
+ * frequencies the band power P and the power-weighted first and second moments
+ * Q, R of x = ln nu - (band centre), and the spectrum itself at
+ * PBAG_SUR_CHECKS check frequencies (two per band). In each band a baseline
+ * shape exp(beta x + gamma x^2) matches P, Q and R; an MLP with PBAG_SUR_IN
+ * inputs and nfreq outputs (BF16 on the tensor cores) predicts the log10
+ * correction to it; the spectrum is scaled to the exact band powers. Error
+ * estimate per state: est_scale times the relative L2 distance between the
+ * predicted and the exact spectrum at the check frequencies. States whose
+ * estimate exceeds tol are recomputed exactly (split BF16).
  * pbag_surrogate_configure: net (may be NULL until trained; not owned; dims
- *   PBAG_SUR_IN -> ... -> nfreq), feature means and standard deviations (host,
- *   PBAG_SUR_IN each, NULL: 0 and 1), tol. Needs ssc_tables and nfreq 128/256.
- *   With a network set, pbag_set_ssc_path(ctx, PBAG_SSC_SURROGATE) makes the
- *   step use it.
+ *   PBAG_SUR_IN -> ... -> nfreq; call again after the network changes: the
+ *   BF16 weights are laid out then), feature means and standard deviations
+ *   (host, PBAG_SUR_IN each, NULL: 0 and 1), est_scale (> 0), tol. Needs
+ *   ssc_tables and nfreq 128/256. With a network set,
+ *   pbag_set_ssc_path(ctx, PBAG_SSC_SURROGATE) makes the step use it.
  * pbag_surrogate_features: unstandardised features [n][PBAG_SUR_IN], the exact
- *   projections [n][PBAG_SUR_PROJ] (P of every band, then Q, then R) and the
+ *   projections [n][PBAG_SUR_PROJ] (P of every band, then Q, then R, then the
+ *   check frequencies, whose indices pbag_surrogate_checks gives) and the
  *   baseline log10 share of each frequency in its band's power [n][nfreq] of n
  *   states (f [n][G], B [n], nph [n][F]); any output may be NULL.
  * pbag_surrogate_contract: j_ssc [n][F] of n states through the surrogate,
- *   the error estimates (d_err [n], may be NULL) and the number of exact
- *   recomputations. Device pointers; synchronous. */
+ *   the scaled error estimate of each state (d_err, may be NULL) and the number
+ *   of states recomputed exactly. */
 #define PBAG_SUR_BANDS 16
-#define PBAG_SUR_PROJ 48
+#define PBAG_SUR_CHECKS 32
+#define PBAG_SUR_PROJ (3 * PBAG_SUR_BANDS + PBAG_SUR_CHECKS)
 #define PBAG_SUR_IN 128
-int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, const float* stdv, float tol);
+int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, const float* stdv, float est_scale,
+                             float tol);
+/* the frequency index of each check projection (host array of PBAG_SUR_CHECKS) */
+int pbag_surrogate_checks(pbag_ctx* ctx, int* idx);
 int pbag_surrogate_features(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,
                             float* d_x, double* d_proj, float* d_base, pbag_status* st);
 int pbag_surrogate_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,

@@ -32,7 +32,8 @@ void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* ext);
 // pbag_surrogate.cu: the surrogate SSC contraction of nrows rows (see there)
 cudaError_t surrogate_run(pbag_ctx* ctx, const CtxView& v, int nrows, const void* Wt, const int* flags,
                           const float* U32, const double* scal, const double* f, int fs, const double* nph, int ns,
-                          const double* Bv, int bs, double* out, int* errs, cudaStream_t st);
+                          const double* Bv, int bs, double* out, int* errs, cudaStream_t st,
+                          bool host_count = false);
 bool surrogate_ready(pbag_ctx* ctx);
 cudaError_t surrogate_reserve(pbag_ctx* ctx, int n);
 int64_t surrogate_generation(pbag_ctx* ctx);

@@ -35,10 +35,16 @@ cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* B
 // tiles) or kTcTf32 (FP32 tiles in the 4-byte layout), Wt the weight tiles,
 // Kt the kernel slabs
 enum : int { kTcBf16 = 0, kTcSplit = 1, kTcTf32 = 2 };
-// nout slabs (grid x), output o of row r at out[r ostride + o] scaled by oscale[o]
+// nout slabs (grid x), output o of row r at out[r ostride + o] scaled by oscale[o].
+// rows.nlive (device): tiles from that row on exit at once; rows.rowmap
+// (device): row r writes its output and error to row rowmap[r].
+struct TcRows {
+  const int* nlive = nullptr;
+  const int* rowmap = nullptr;
+};
 cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
                                const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
-                               int ostride, double* out, int* err, cudaStream_t st);
+                               int ostride, double* out, int* err, cudaStream_t st, TcRows rows = TcRows{});
 // K slabs as TF32 operands (FP32 values rounded to TF32, 4-byte layout, lo parts zero)
 void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32);
 

@@ -249,13 +249,13 @@ cudaError_t mlp_tc_pack(int N, int K, const float* W, uint16_t* out, cudaStream_
 }
 
 cudaError_t launch_mlp_tc(const MlpTcArgs& a, int n, const float* X, float* Y, int* err, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  static bool attr = false;
+  static bool attr = false;  // set on the first call, which may launch nothing (before any graph capture)
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMtSmem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  if (n <= 0) return cudaSuccess;
   k_mlp_tc<<<(n + kMtRows - 1) / kMtRows, kMtThreads, kMtSmem, st>>>(a, n, X, Y, err);
   return cudaGetLastError();
 }

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int N, int S,
          uint32_t body, uint32_t ubytes, uint32_t uring, const int* __restrict__ flags, const float* __restrict__ U32,
          const double* __restrict__ scal, const double* __restrict__ oscale, int ostride, double* __restrict__ out,
-         int* __restrict__ err) {
+         int* __restrict__ err, const int* __restrict__ nlive, const int* __restrict__ rowmap) {
   constexpr int F = kTcK * H;
   constexpr bool kSplit = MODE == kTcSplit;
   constexpr bool kTf32 = MODE == kTcTf32;
@@ -111,6 +111,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
   const int row0 = blockIdx.y * kTcCols;
+  if (nlive && row0 >= *nlive) return;  // a tile beyond the rows counted on the device
   const uint32_t stage_bytes = tc_stage_bytes(F, N);
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -279,7 +280,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
       fail = 1;
       for (int col = 0; col < N; ++col) {
         const int r = row0 + col;
-        if (r < nrows && (flags[r] & kFlagActive)) atomicCAS(&err[4 * r], 0, PBAG_ERR_TIMEOUT);
+        if (r < nrows && (flags[r] & kFlagActive)) atomicCAS(&err[4 * (rowmap ? rowmap[r] : r)], 0, PBAG_ERR_TIMEOUT);
       }
     }
   }
@@ -342,7 +343,8 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
         a2 += row[k + 2];
         a3 += row[k + 3];
       }
-      out[(size_t)(row0 + col) * ostride + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
+      const int orow = rowmap ? rowmap[row0 + col] : row0 + col;
+      out[(size_t)orow * ostride + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
     }
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");  // no copy may land after the CTA exits
@@ -357,7 +359,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
 template <int H, int MODE>
 cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
                       const float* U32, const double* scal, const double* oscale, int nout, int ostride, double* out,
-                      int* err, cudaStream_t st) {
+                      int* err, TcRows rows, cudaStream_t st) {
   constexpr int F = kTcK * H;
   const int N = std::min(kTcCols, (nrows + 15) / 16 * 16);
   const TcPlan plan = tc_plan(F, N, Gp * (MODE == kTcTf32 ? 2 : 1));
@@ -371,7 +373,8 @@ cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, 
   }
   dim3 grid(nout, (nrows + kTcCols - 1) / kTcCols);
   k_ssc_tc<H, MODE><<<grid, kTcThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
-                                                           plan.uring, flags, U32, scal, oscale, ostride, out, err);
+                                                           plan.uring, flags, U32, scal, oscale, ostride, out, err,
+                                                           rows.nlive, rows.rowmap);
   return cudaGetLastError();
 }
 
@@ -430,13 +433,13 @@ void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std
 
 cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
                                const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
-                               int ostride, double* out, int* err, cudaStream_t st) {
+                               int ostride, double* out, int* err, cudaStream_t st, TcRows rows) {
   if (nrows <= 0) return cudaSuccess;
   if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
   const auto* w = static_cast<const unsigned char*>(Wt);
   const auto* k = static_cast<const unsigned char*>(Kt);
 #define PBAG_TC_CASE(HH, MM) \
-  return launch_tc<HH, MM>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, st)
+  return launch_tc<HH, MM>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, st)
   if (F == 128) {
     if (mode == kTcSplit) PBAG_TC_CASE(1, kTcSplit);
     if (mode == kTcBf16) PBAG_TC_CASE(1, kTcBf16);

@@ -1,17 +1,22 @@
 // pbag_surrogate.cu - learned SSC emissivity with an exact error check.
 //
 // The SSC spectrum of a state (computeSSCSpectrum, numeric_model.h:247-285)
-// is j_i = h nu_i sum_jk K[i][j][k] W_j U_k. Over a band of frequencies, its
-// power P_b = sum_{i in b} j_i dnu_i and the power-weighted moments Q_b, R_b
-// of x_i = ln nu_i - c_b (first and second) are the same bilinear form with
-// the kernel slabs summed over the band: 3 x 16 exact projections, 48 instead
-// of F slabs on the tensor cores (the same contraction kernel). In each band a
-// baseline shape s_i ~ exp(beta x_i) matches P_b and Q_b exactly; an MLP
-// (pbag_mlp, hidden layers of 256) predicts the log10 correction to it from
+// is j_i = h nu_i sum_jk K[i][j][k] W_j U_k. Any linear functional of it is
+// the same bilinear form with the kernel slabs combined: over each of the
+// kNb bands the power P_b = sum_{i in b} j_i dnu_i and the power-weighted
+// first and second moments Q_b, R_b of x_i = ln nu_i - c_b, and j_i itself at
+// kNchk check frequencies (two per band) - kNproj slabs instead of F, run in
+// plain BF16 by the contraction kernel of the step (about 1e-3 relative).
+//
+// In each band the baseline shape s_i ~ exp(beta x_i + gamma x_i^2) matches
+// P, Q and R (Newton on beta, gamma; one thread per band and state). The MLP
+// (BF16 on the tensor cores) predicts the log10 correction to the baseline from
 // the state (B, moments and shape of N(gamma), shape of the seed photon field,
-// shape of the band powers, band tilts); the spectrum is scaled to the exact
-// band powers. The mismatch of the predicted and exact Q and R is the
-// per-state error estimate; states above the tolerance are recomputed exactly.
+// band powers and the baseline's slope and curvature); the spectrum is scaled
+// to the exact band powers. The error estimate of a state is est_scale times
+// the relative L2 distance of the predicted and the exact spectrum at the check
+// frequencies; states above the tolerance are gathered into a dense batch and
+// recomputed exactly (split BF16), their rows written back through a row map.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -24,19 +29,28 @@
 
 namespace pbag {
 
-cudaError_t mlp_forward(pbag_mlp* net, int n, const float* X, float* Y, cudaStream_t st);
+cudaError_t mlp_infer(pbag_mlp* net, int n, const float* X, float* Y, cudaStream_t st);
+int* mlp_infer_error(pbag_mlp* net);
 int mlp_in_dim(const pbag_mlp* net);
 int mlp_out_dim(const pbag_mlp* net);
-int mlp_layers(const pbag_mlp* net);
-cudaError_t mlp_reserve(pbag_mlp* net, int n);
 
 namespace {
 
 constexpr int kNb = PBAG_SUR_BANDS;
+constexpr int kNchk = PBAG_SUR_CHECKS;
+constexpr int kNmom = 3 * kNb;
 constexpr int kNproj = PBAG_SUR_PROJ;
 constexpr int kNin = PBAG_SUR_IN;
-constexpr int kFeatThreads = 128;
-constexpr float kFloor = -30.f;  // log10 floor of the shape features
+constexpr int kMaxF = 256;
+constexpr int kMaxPer = kMaxF / kNb;
+constexpr int kSurWarps = 4;          // states per CTA of the feature and reconstruction kernels (a warp each)
+constexpr float kFloor = -30.f;       // log10 floor of the shape features
+constexpr float kCorrMin = -8.f, kCorrMax = 4.f;  // range of the log10 correction applied
+// feature layout
+enum : int { kFtB = 0, kFtMom = 1, kFtSeed = 6, kFtBandP = 70, kFtBeta = 86, kFtGamma = 102, kFtEle = 118 };
+constexpr int kSeedPts = 64, kElePts = 10;
+static_assert(kFtEle + kElePts == kNin, "feature layout");
+static_assert(kNchk == 32, "one check per lane");
 
 uint16_t bf16_round(float x) {  // round to nearest even (finite inputs)
   uint32_t u;
@@ -51,56 +65,102 @@ float bf16_float(uint16_t h) {
   return x;
 }
 
+// frequency of check c: two per band, half a band apart, the offset turning
+// with the band so that every position inside a band is checked somewhere
+int check_freq(int c, int per) {
+  const int b = c / 2;
+  return b * per + (b + (c % 2) * (per / 2)) % per;
+}
+
 struct Surrogate : CtxExtension {
   int device = 0;
   int F = 0, G = 0, Gp = 0, per = 0;  // per: frequencies per band
   uint16_t* Kp = nullptr;             // projection slabs, split-BF16 operand layout (rows F)
   double* oscale = nullptr;           // [kNproj] output scales
-  double* lnrel = nullptr;            // [F] ln nu_i - (centre of ln nu of its band)
+  float* xrel = nullptr;              // [F] ln nu_i - (centre of ln nu of its band)
   double* invdnu = nullptr;           // [F] 1 / (nu_{i+1} - nu_i)
-  double* hw = nullptr;               // [kNb] half width of each band in ln nu
+  float* hw = nullptr;                // [kNb] half width of each band in ln nu
+  int* chk = nullptr;                 // [kNchk] check frequencies
   float* mean = nullptr;              // [kNin] feature standardisation
   float* stdv = nullptr;
   pbag_mlp* net = nullptr;            // not owned
-  float tol = 0.01f;
+  float tol = 0.01f, est_scale = 1.f;
   int64_t generation = 0;             // bumped by every pbag_surrogate_configure
   int cap = 0;
   float* X = nullptr;                 // [cap][kNin]
   double* proj = nullptr;             // [cap][kNproj]
+  float* fit = nullptr;               // [cap][2 kNb] baseline slope and curvature
+  float* base = nullptr;              // [cap][F] baseline log10 shares
   float* Y = nullptr;                 // [cap][F]
   float* err = nullptr;               // [cap]
-  int* fb = nullptr;                  // [cap] fallback flags (kFlagActive)
-  int* nfb = nullptr;                 // fallback count
+  int* list = nullptr;                // [cap] rows to recompute
+  int* nfb = nullptr;                 // their count
+  // the gathered rows of the exact recomputation (tiles of kTcCols rows)
+  uint16_t* Wc = nullptr;
+  float* Uc = nullptr;
+  double* scalc = nullptr;
+  int* flagc = nullptr;
   ~Surrogate() override {
     cudaSetDevice(device);
-    for (void* p : {(void*)Kp, (void*)oscale, (void*)lnrel, (void*)invdnu, (void*)hw, (void*)mean, (void*)stdv, (void*)X,
-                    (void*)proj, (void*)Y, (void*)err, (void*)fb, (void*)nfb})
+    for (void* p : {(void*)Kp, (void*)oscale, (void*)xrel, (void*)invdnu, (void*)hw, (void*)chk, (void*)mean,
+                    (void*)stdv, (void*)nfb})
       cudaFree(p);
+    free_rows();
+  }
+  void free_rows() {
+    for (void* p : {(void*)X, (void*)proj, (void*)fit, (void*)base, (void*)Y, (void*)err, (void*)list, (void*)Wc,
+                    (void*)Uc, (void*)scalc, (void*)flagc})
+      cudaFree(p);
+    X = nullptr;
+    proj = nullptr;
+    fit = nullptr;
+    base = nullptr;
+    Y = nullptr;
+    err = nullptr;
+    list = nullptr;
+    Wc = nullptr;
+    Uc = nullptr;
+    scalc = nullptr;
+    flagc = nullptr;
+    cap = 0;
   }
   cudaError_t reserve(int n) {
     if (n <= cap) return cudaSuccess;
-    for (void* p : {(void*)X, (void*)proj, (void*)Y, (void*)err, (void*)fb}) cudaFree(p);
-    X = nullptr;
-    proj = nullptr;
-    Y = nullptr;
-    err = nullptr;
-    fb = nullptr;
-    cap = 0;
+    free_rows();
     const size_t c = (size_t)std::max(n, 64);
-    cudaError_t e;
-    if ((e = cudaMalloc(&X, c * kNin * sizeof(float))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&proj, c * kNproj * sizeof(double))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&Y, c * F * sizeof(float))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&err, c * sizeof(float))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&fb, c * sizeof(int))) != cudaSuccess) return e;
+    const size_t tiles = (c + kTcCols - 1) / kTcCols, rows = tiles * kTcCols;
+    cudaError_t e = cudaSuccess;
+    auto get = [&](auto** p, size_t bytes) {
+      if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    get(&X, c * kNin * sizeof(float));
+    get(&proj, c * kNproj * sizeof(double));
+    get(&fit, c * 2 * kNb * sizeof(float));
+    get(&base, c * F * sizeof(float));
+    get(&Y, c * F * sizeof(float));
+    get(&err, c * sizeof(float));
+    get(&list, c * sizeof(int));
+    get(&Wc, tiles * tc_tile_bytes(kTcCols, Gp, 2));
+    get(&Uc, rows * F * sizeof(float));
+    get(&scalc, rows * kScal * sizeof(double));
+    get(&flagc, rows * sizeof(int));
+    // rows of the last tile beyond the gathered ones are read (never used): keep them finite
+    if (e == cudaSuccess) e = cudaMemset(Wc, 0, tiles * tc_tile_bytes(kTcCols, Gp, 2));
+    if (e == cudaSuccess) e = cudaMemset(Uc, 0, rows * F * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(scalc, 0, rows * kScal * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(flagc, 0, rows * sizeof(int));
+    if (e != cudaSuccess) {
+      free_rows();
+      return e;
+    }
     cap = (int)c;
     return cudaSuccess;
   }
 };
 
 // Projection slabs from the FP32 kernel tensor K32[i][j][k] (rows k of a
-// slab, K-dim j), FP64 accumulation over the band, power-of-two scaled, split
-// BF16; band centres and half widths in ln nu.
+// slab, K-dim j): band moments (FP64 accumulation over the band) and check
+// frequencies, each power-of-two scaled and split into BF16 hi + lo.
 int build_projections(const CtxView& v, Surrogate* s) {
   const int F = v.F, Gp = v.Gp;
   std::vector<float> K32((size_t)F * Gp * F);
@@ -110,48 +170,61 @@ int build_projections(const CtxView& v, Surrogate* s) {
     return PBAG_ERR_CUDA;
   s->per = F / kNb;
   std::vector<uint16_t> Kp((size_t)kNproj * tc_tile_elems(F, Gp), 0);
-  std::vector<double> osc(kNproj), lnrel(F), invdnu(F), hw(kNb);
+  std::vector<double> osc(kNproj), invdnu(F), lnrel(F);
+  std::vector<float> xrel(F), hw(kNb);
+  std::vector<int> chk(kNchk);
   for (int i = 0; i < F; ++i) invdnu[i] = 1. / (nu[i + 1] - nu[i]);
-  std::vector<double> slab((size_t)F * Gp);
   for (int b = 0; b < kNb; ++b) {
     const int i0 = b * s->per, i1 = i0 + s->per;
     double c = 0.;
     for (int i = i0; i < i1; ++i) c += std::log(nu[i]);
     c /= s->per;
-    for (int i = i0; i < i1; ++i) lnrel[i] = std::log(nu[i]) - c;
-    hw[b] = 0.5 * (std::log(nu[i1 - 1]) - std::log(nu[i0])) + 1e-300;
-    for (int q = 0; q < 3; ++q) {
-      std::fill(slab.begin(), slab.end(), 0.);
-      double mx = 0.;
-      for (int k = 0; k < F; ++k)
-        for (int j = 0; j < Gp; ++j) {
-          double acc = 0.;
-          for (int i = i0; i < i1; ++i) {
-            const double x = std::log(nu[i]) - c;
-            const double wgt = nu[i] * (nu[i + 1] - nu[i]) * (q == 0 ? 1. : q == 1 ? x : x * x);
-            acc += wgt * (double)K32[((size_t)i * Gp + j) * F + k];
-          }
-          slab[(size_t)k * Gp + j] = acc;
-          mx = std::max(mx, std::fabs(acc));
-        }
-      // scaled so that the largest entry is ~2^96: the small kernel entries
-      // that carry the spectrum's high-frequency tail stay far from the FP32 /
-      // BF16 subnormal range, and the FP32 accumulations (<= 2^9 terms of
-      // operands <= 1 each) stay far below overflow
-      int ex = 0;
-      if (mx > 0.) std::frexp(mx, &ex);
-      const double sc = std::ldexp(1., 96 - ex);
-      const int o = q * kNb + b;
-      osc[o] = cgs::h_pl / sc;
-      uint16_t* T = Kp.data() + (size_t)o * tc_tile_elems(F, Gp);
-      for (int k = 0; k < F; ++k)
-        for (int j = 0; j < Gp; ++j) {
-          const float x = (float)(slab[(size_t)k * Gp + j] * sc);
-          const uint16_t h = bf16_round(x);
-          T[tc_operand_offset(k, j, F, Gp, false)] = h;
-          T[tc_operand_offset(k, j, F, Gp, true)] = bf16_round(x - bf16_float(h));
-        }
+    for (int i = i0; i < i1; ++i) {
+      lnrel[i] = std::log(nu[i]) - c;
+      xrel[i] = (float)lnrel[i];
     }
+    hw[b] = (float)(0.5 * (std::log(nu[i1 - 1]) - std::log(nu[i0])));
+  }
+  for (int c = 0; c < kNchk; ++c) chk[c] = check_freq(c, s->per);
+  std::vector<double> slab((size_t)F * Gp), wgt(F);
+  for (int o = 0; o < kNproj; ++o) {
+    // weights of the frequencies in this projection
+    std::fill(wgt.begin(), wgt.end(), 0.);
+    if (o < kNmom) {
+      const int q = o / kNb, b = o % kNb;
+      for (int i = b * s->per; i < (b + 1) * s->per; ++i) {
+        const double x = lnrel[i];
+        wgt[i] = nu[i] * (nu[i + 1] - nu[i]) * (q == 0 ? 1. : q == 1 ? x : x * x);
+      }
+    } else {
+      const int i = chk[o - kNmom];
+      wgt[i] = nu[i];
+    }
+    double mx = 0.;
+    for (int k = 0; k < F; ++k)
+      for (int j = 0; j < Gp; ++j) {
+        double acc = 0.;
+        for (int i = 0; i < F; ++i)
+          if (wgt[i] != 0.) acc += wgt[i] * (double)K32[((size_t)i * Gp + j) * F + k];
+        slab[(size_t)k * Gp + j] = acc;
+        mx = std::max(mx, std::fabs(acc));
+      }
+    // scaled so that the largest entry is ~2^96: the small kernel entries that
+    // carry the spectrum's high-frequency tail stay far from the FP32 / BF16
+    // subnormal range, and the FP32 accumulations (<= 2^9 terms of operands
+    // <= 1 each) stay far below overflow
+    int ex = 0;
+    if (mx > 0.) std::frexp(mx, &ex);
+    const double sc = std::ldexp(1., 96 - ex);
+    osc[o] = cgs::h_pl / sc;
+    uint16_t* T = Kp.data() + (size_t)o * tc_tile_elems(F, Gp);
+    for (int k = 0; k < F; ++k)
+      for (int j = 0; j < Gp; ++j) {
+        const float x = (float)(slab[(size_t)k * Gp + j] * sc);
+        const uint16_t h = bf16_round(x);
+        T[tc_operand_offset(k, j, F, Gp, false)] = h;
+        T[tc_operand_offset(k, j, F, Gp, true)] = bf16_round(x - bf16_float(h));
+      }
   }
   cudaError_t e = cudaSuccess;
   auto up = [&](auto** dst, const auto& h) {
@@ -160,165 +233,164 @@ int build_projections(const CtxView& v, Surrogate* s) {
   };
   up(&s->Kp, Kp);
   up(&s->oscale, osc);
-  up(&s->lnrel, lnrel);
+  up(&s->xrel, xrel);
   up(&s->invdnu, invdnu);
   up(&s->hw, hw);
+  up(&s->chk, chk);
   return e == cudaSuccess ? PBAG_OK : PBAG_ERR_CUDA;
 }
 
-// Baseline shape of one band: log10 shares s_i ~ exp(beta x_i) (normalised
-// over the band's `per` frequencies) whose mean of x equals mu (Newton on
-// beta; mu clamped just inside the band).
-__device__ void tilt_log10_shares(const double* __restrict__ x, int per, double mu, float* out) {
-  float xl[64];
-  float lo = 1e30f, hi = -1e30f;
-  for (int i = 0; i < per; ++i) {
-    xl[i] = (float)x[i];
-    lo = fminf(lo, xl[i]);
-    hi = fmaxf(hi, xl[i]);
-  }
-  const float span = hi - lo;
-  float m = fminf(fmaxf((float)mu, lo + 0.01f * span), hi - 0.01f * span);
-  float beta = 0.f;
-  for (int it = 0; it < 40; ++it) {
-    float z = 0.f, s1 = 0.f, s2 = 0.f;
-    const float ref = beta >= 0.f ? hi : lo;
-    for (int i = 0; i < per; ++i) {
-      const float w = __expf(beta * (xl[i] - ref));
-      z += w;
-      s1 += w * xl[i];
-      s2 += w * xl[i] * xl[i];
-    }
-    const float mean = s1 / z, var = fmaxf(s2 / z - mean * mean, 1e-12f);
-    beta -= (mean - m) / var;
-    beta = fminf(fmaxf(beta, -400.f / span), 400.f / span);
-  }
-  const float ref = beta >= 0.f ? hi : lo;
-  float z = 0.f;
-  for (int i = 0; i < per; ++i) z += __expf(beta * (xl[i] - ref));
-  const float lz = logf(z);
-  for (int i = 0; i < per; ++i) out[i] = (beta * (xl[i] - ref) - lz) * 0.43429448f;
-}
-
-__device__ float block_max_f(float v, float* red) {
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float r = red[0];
-  for (int i = 1; i < kFeatThreads / 32; ++i) r = fmaxf(r, red[i]);
-  return r;
-}
-__device__ float block_sum_f(float v, float* red) {
+__device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float r = 0.f;
-  for (int i = 0; i < kFeatThreads / 32; ++i) r += red[i];
-  return r;
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
 }
 
-// Feature vector of each state (one CTA per state). f, nph: rows of N(gamma)
+// Baseline of each (state, band): shares s_i ~ exp(beta x_i + gamma x_i^2)
+// over the band whose mean and second moment of x equal Q/P and R/P (clamped
+// into the feasible set). The moment map of (beta, gamma) is the gradient of a
+// convex log-partition function, so Newton on it (steps clipped) converges
+// from zero. Writes beta hw, gamma hw^2 and the log10 shares.
+__global__ void k_sur_fit(int n, int F, int per, const double* __restrict__ proj, const float* __restrict__ xrel,
+                          const float* __restrict__ hwv, float* __restrict__ fit, float* __restrict__ base) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * kNb) return;
+  const int s = t / kNb, b = t % kNb;
+  const double P = proj[(size_t)s * kNproj + b], Q = proj[(size_t)s * kNproj + kNb + b],
+               R = proj[(size_t)s * kNproj + 2 * kNb + b];
+  float x[kMaxPer];
+  for (int i = 0; i < per; ++i) x[i] = xrel[b * per + i];
+  const float hw = hwv[b], lo = x[0], hi = x[per - 1];
+  float beta = 0.f, gam = 0.f;
+  if (P > 0.) {
+    const float mu1 = fminf(fmaxf((float)(Q / P), 0.98f * lo), 0.98f * hi);
+    const float vmax = (hi - mu1) * (mu1 - lo);
+    const float var = fminf(fmaxf((float)(R / P) - mu1 * mu1, 1e-6f * hw * hw), 0.98f * vmax);
+    const float mu2 = mu1 * mu1 + var;
+    for (int it = 0; it < 48; ++it) {
+      float emax = -1e30f;
+      for (int i = 0; i < per; ++i) emax = fmaxf(emax, x[i] * (beta + gam * x[i]));
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
+      for (int i = 0; i < per; ++i) {
+        const float w = __expf(x[i] * (beta + gam * x[i]) - emax), xx = x[i] * x[i];
+        s0 += w;
+        s1 += w * x[i];
+        s2 += w * xx;
+        s3 += w * xx * x[i];
+        s4 += w * xx * xx;
+      }
+      const float is0 = 1.f / s0, m1 = s1 * is0, m2 = s2 * is0, m3 = s3 * is0, m4 = s4 * is0;
+      const float r1 = mu1 - m1, r2 = mu2 - m2;
+      if (fabsf(r1) < 1e-6f * hw && fabsf(r2) < 1e-6f * hw * hw) break;
+      const float J11 = m2 - m1 * m1, J12 = m3 - m1 * m2, J22 = m4 - m2 * m2;
+      const float det = J11 * J22 - J12 * J12;
+      if (!(det > 1e-30f)) break;
+      const float db = (J22 * r1 - J12 * r2) / det, dg = (J11 * r2 - J12 * r1) / det;
+      beta += fminf(fmaxf(db, -20.f / hw), 20.f / hw);
+      gam += fminf(fmaxf(dg, -50.f / (hw * hw)), 50.f / (hw * hw));
+    }
+  }
+  float emax = -1e30f;
+  for (int i = 0; i < per; ++i) emax = fmaxf(emax, x[i] * (beta + gam * x[i]));
+  float s0 = 0.f;
+  for (int i = 0; i < per; ++i) s0 += __expf(x[i] * (beta + gam * x[i]) - emax);
+  const float lz = emax + logf(s0);
+  float* out = base + (size_t)s * F + b * per;
+  for (int i = 0; i < per; ++i) out[i] = (x[i] * (beta + gam * x[i]) - lz) * 0.43429448f;
+  fit[(size_t)s * 2 * kNb + b] = fminf(fmaxf(beta * hw, -40.f), 40.f);
+  fit[(size_t)s * 2 * kNb + kNb + b] = fminf(fmaxf(gam * hw * hw, -80.f), 80.f);
+}
+
+// Feature vector of each state (one warp per state). f, nph: rows of N(gamma)
 // and of the seed photon density (strides fs, ns); B: field (stride bs); proj:
-// the exact band projections. Standardised when mean/stdv are given.
-__global__ void __launch_bounds__(kFeatThreads)
+// the exact projections; fit: the baseline parameters. Standardised when
+// mean/stdv are given.
+__global__ void __launch_bounds__(32 * kSurWarps)
 k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const double* __restrict__ nph, int ns,
-               const double* __restrict__ Bv, int bs, const double* __restrict__ proj, const double* __restrict__ hw,
-               const double* __restrict__ lnrel, int per, const float* __restrict__ mean,
-               const float* __restrict__ stdv, float* __restrict__ X, float* __restrict__ base) {
-  const int s = blockIdx.x, tid = threadIdx.x;
+               const double* __restrict__ Bv, int bs, const double* __restrict__ proj, const float* __restrict__ fit,
+               const float* __restrict__ mean, const float* __restrict__ stdv, float* __restrict__ X) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kSurWarps + warp;
+  if (s >= n) return;
+  __shared__ float feat_all[kSurWarps][kNin];
+  float* feat = feat_all[warp];
   const int G = g.G, F = g.F;
-  __shared__ float red[kFeatThreads / 32];
-  __shared__ float feat[kNin];
   const GridTab T{g.etab, g.Ge, g.Fe};
   const double* fr = f + (size_t)s * fs;
   const double* nr = nph + (size_t)s * ns;
-  for (int d = tid; d < kNin; d += kFeatThreads) feat[d] = 0.f;
   // electron weights w_j = f_j dgamma_j, scaled by a power of two into FP32
   int ex = 0;
-  for (int j = tid; j < G - 1; j += kFeatThreads) ex = max(ex, exp_field(fr[j] * T.gt(kTabDe)[j]));
+  for (int j = lane; j < G - 1; j += 32) ex = max(ex, exp_field(fr[j] * T.gt(kTabDe)[j]));
   ex = __reduce_max_sync(0xffffffffu, ex);
-  __shared__ int redi[kFeatThreads / 32];
-  if ((tid & 31) == 0) redi[tid >> 5] = ex;
-  __syncthreads();
-  ex = max(max(redi[0], redi[1]), max(redi[2], redi[3]));
   const double sw = scale_from_exp(ex);
   float m0 = 0.f, m1 = 0.f;
-  for (int j = tid; j < G - 1; j += kFeatThreads) {
+  for (int j = lane; j < G - 1; j += 32) {
     const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
-    const float lg = logf((float)(1. / T.gt(kTabInvE)[j]));
     m0 += w;
-    m1 += w * lg;
+    m1 += w * -logf((float)T.gt(kTabInvE)[j]);
   }
-  m0 = block_sum_f(m0, red);
-  m1 = block_sum_f(m1, red);
+  m0 = warp_sum(m0);
+  m1 = warp_sum(m1);
   const float mu = m0 > 0.f ? m1 / m0 : 0.f;
   float c2 = 0.f, c3 = 0.f, c4 = 0.f, wmax = 0.f;
-  for (int j = tid; j < G - 1; j += kFeatThreads) {
+  for (int j = lane; j < G - 1; j += 32) {
     const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
-    const float d = logf((float)(1. / T.gt(kTabInvE)[j])) - mu;
+    const float d = -logf((float)T.gt(kTabInvE)[j]) - mu;
     c2 += w * d * d;
     c3 += w * d * d * d;
     c4 += w * d * d * d * d;
     wmax = fmaxf(wmax, w);
   }
-  c2 = block_sum_f(c2, red);
-  c3 = block_sum_f(c3, red);
-  c4 = block_sum_f(c4, red);
-  wmax = block_max_f(wmax, red);
-  if (tid == 0) {
+  c2 = warp_sum(c2);
+  c3 = warp_sum(c3);
+  c4 = warp_sum(c4);
+  wmax = warp_max(wmax);
+  if (lane == 0) {
     const float var = m0 > 0.f ? c2 / m0 : 0.f;
     const float sd = sqrtf(fmaxf(var, 1e-30f));
-    feat[0] = log10f(fmaxf((float)Bv[(size_t)s * bs], 1e-30f));
-    feat[1] = m0 > 0.f ? log10f(m0) - (float)log10(sw) : kFloor;  // log10 of the unscaled N_e
-    feat[2] = mu;
-    feat[3] = log10f(sd);
-    feat[4] = m0 > 0.f ? c3 / m0 / (sd * sd * sd) : 0.f;
-    feat[5] = m0 > 0.f ? c4 / m0 / (var * var + 1e-30f) : 0.f;
+    feat[kFtB] = log10f(fmaxf((float)Bv[(size_t)s * bs], 1e-30f));
+    feat[kFtMom] = m0 > 0.f ? log10f(m0) - (float)log10(sw) : kFloor;  // log10 of the unscaled N_e
+    feat[kFtMom + 1] = mu;
+    feat[kFtMom + 2] = log10f(sd);
+    feat[kFtMom + 3] = m0 > 0.f ? c3 / m0 / (sd * sd * sd) : 0.f;
+    feat[kFtMom + 4] = m0 > 0.f ? c4 / m0 / (var * var + 1e-30f) : 0.f;
   }
-  // electron shape on 24 bins
-  for (int q = tid; q < 24; q += kFeatThreads) {
-    const int j = (int)lrintf(q * (float)(G - 2) / 23.f);
+  if (lane < kElePts) {
+    const int j = (int)lrintf(lane * (float)(G - 2) / (float)(kElePts - 1));
     const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
-    feat[102 + q] = wmax > 0.f ? fmaxf(log10f(fmaxf(w / wmax, 1e-30f)), kFloor) : kFloor;
+    feat[kFtEle + lane] = wmax > 0.f ? fmaxf(log10f(fmaxf(w / wmax, 1e-30f)), kFloor) : kFloor;
   }
-  // seed photon shape on 64 frequencies: u_k = n_k dnu_k / nu_k
+  // seed photon shape on kSeedPts frequencies: u_k = n_k dnu_k / nu_k
   int ue = 0;
-  for (int k = tid; k < F; k += kFeatThreads) ue = max(ue, exp_field(nr[k] * T.ft(kTabDnuNu)[k]));
+  for (int k = lane; k < F; k += 32) ue = max(ue, exp_field(nr[k] * T.ft(kTabDnuNu)[k]));
   ue = __reduce_max_sync(0xffffffffu, ue);
-  __syncthreads();
-  if ((tid & 31) == 0) redi[tid >> 5] = ue;
-  __syncthreads();
-  ue = max(max(redi[0], redi[1]), max(redi[2], redi[3]));
   const double su = scale_from_exp(ue);
   float umax = 0.f;
-  for (int k = tid; k < F; k += kFeatThreads) umax = fmaxf(umax, (float)(nr[k] * T.ft(kTabDnuNu)[k] * su));
-  umax = block_max_f(umax, red);
-  for (int q = tid; q < 64; q += kFeatThreads) {
-    const int k = q * F / 64;
+  for (int k = lane; k < F; k += 32) umax = fmaxf(umax, (float)(nr[k] * T.ft(kTabDnuNu)[k] * su));
+  umax = warp_max(umax);
+  for (int q = lane; q < kSeedPts; q += 32) {
+    const int k = q * F / kSeedPts;
     const float u = (float)(nr[k] * T.ft(kTabDnuNu)[k] * su);
-    feat[6 + q] = umax > 0.f ? fmaxf(log10f(fmaxf(u / umax, 1e-30f)), kFloor) : kFloor;
+    feat[kFtSeed + q] = umax > 0.f ? fmaxf(log10f(fmaxf(u / umax, 1e-30f)), kFloor) : kFloor;
   }
-  // band power shape
-  if (tid < 32) {
-    const double P = tid < kNb ? proj[(size_t)s * kNproj + tid] : 0.;
-    double pm = P;
-    for (int o = 16; o > 0; o >>= 1) pm = fmax(pm, __shfl_xor_sync(0xffffffffu, pm, o));
-    if (tid < kNb) {
-      feat[70 + tid] = pm > 0. ? fmaxf(log10f((float)fmax(P / pm, 1e-30)), kFloor) : kFloor;
-      // tilt of the band: mean of x over its half width
-      const double Q = proj[(size_t)s * kNproj + kNb + tid];
-      feat[86 + tid] = P > 0. ? fminf(fmaxf((float)(Q / P / hw[tid]), -1.f), 1.f) : 0.f;
-    }
+  // band powers and the baseline's slope and curvature
+  const double P = lane < kNb ? proj[(size_t)s * kNproj + lane] : 0.;
+  double pm = P;
+  for (int o = 16; o > 0; o >>= 1) pm = fmax(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+  if (lane < kNb) {
+    feat[kFtBandP + lane] = pm > 0. ? fmaxf(log10f((float)fmax(P / pm, 1e-30)), kFloor) : kFloor;
+    feat[kFtBeta + lane] = fit[(size_t)s * 2 * kNb + lane];
+    feat[kFtGamma + lane] = fit[(size_t)s * 2 * kNb + kNb + lane];
   }
-  // baseline log10 shares of every frequency in its band (for the training targets)
-  if (base && tid < kNb) {
-    const double P = proj[(size_t)s * kNproj + tid], Q = proj[(size_t)s * kNproj + kNb + tid];
-    tilt_log10_shares(lnrel + tid * per, per, P > 0. ? Q / P : 0., base + (size_t)s * F + tid * per);
-  }
-  __syncthreads();
-  for (int d = tid; d < kNin; d += kFeatThreads) {
+  __syncwarp();
+  for (int d = lane; d < kNin; d += 32) {
     float x = feat[d];
     if (!(x == x) || isinf(x)) x = kFloor;
     if (mean) x = (x - mean[d]) / stdv[d];
@@ -327,67 +399,104 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
 }
 
 // Spectrum from the baseline band shapes plus the predicted log10 correction,
-// scaled to the exact band powers; error estimate from the band moments Q and
-// R; fallback flags.
-__global__ void __launch_bounds__(kFeatThreads)
-k_sur_reconstruct(int F, int n, const int* __restrict__ flags, const float* __restrict__ Y,
-                  const double* __restrict__ proj, const double* __restrict__ lnrel, const double* __restrict__ invdnu,
-                  const double* __restrict__ hw, float tol, int per, double* __restrict__ out, float* __restrict__ err,
-                  int* __restrict__ fb, int* __restrict__ nfb) {
-  const int s = blockIdx.x, tid = threadIdx.x;
-  __shared__ float fr[1024];
-  __shared__ double bscale[kNb], be[kNb];
+// scaled to the exact band powers (one warp per state); error estimate from
+// the check frequencies; rows to recompute appended to list.
+__global__ void __launch_bounds__(32 * kSurWarps)
+k_sur_reconstruct(int F, int per, int n, const int* __restrict__ flags, const float* __restrict__ Y,
+                  const float* __restrict__ base, const double* __restrict__ proj, const double* __restrict__ invdnu,
+                  const int* __restrict__ chk, float est_scale, float tol, double* __restrict__ out,
+                  float* __restrict__ err, int* __restrict__ list, int* __restrict__ nfb) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kSurWarps + warp;
+  if (s >= n) return;
+  __shared__ double jr_all[kSurWarps][kMaxF];
+  double* jr = jr_all[warp];
   const bool live = !flags || (flags[s] & kFlagActive);
-  const double* P = proj + (size_t)s * kNproj;
-  if (tid < kNb) {
-    const double Pb = P[tid], Qb = P[kNb + tid];
-    tilt_log10_shares(lnrel + tid * per, per, Pb > 0. ? Qb / Pb : 0., fr + tid * per);
+  const double* Pp = proj + (size_t)s * kNproj;
+  // frequency i = lane + 32 m; its band's lanes are the aligned group of `per`
+  // consecutive lanes (per = 8 or 16), summed by butterflies inside the group
+  for (int m = 0; m < F / 32; ++m) {
+    const int i = lane + 32 * m;
+    // corrections are bounded: the network is not trained on shares below the
+    // training floor, and an outlier must not take over its band's power
+    const float y = fminf(fmaxf(Y[(size_t)s * F + i], kCorrMin), kCorrMax);
+    const float sh = exp10f(fmaxf(base[(size_t)s * F + i] + y, -30.f));
+    float sum = sh;
+    for (int o = 1; o < per; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    const double Pb = Pp[i / per];
+    jr[i] = (Pb > 0. && sum > 0.f) ? Pb * (double)(sh / sum) * invdnu[i] : 0.;
   }
-  __syncthreads();
-  for (int i = tid; i < F; i += kFeatThreads)
-    fr[i] = exp10f(fminf(fmaxf(fr[i] + Y[(size_t)s * F + i], -30.f), 10.f));
-  __syncthreads();
-  if (tid < kNb) {
-    const int b = tid, i0 = b * per;
-    float sum = 0.f;
-    double m1 = 0., m2 = 0.;
-    for (int i = i0; i < i0 + per; ++i) {
-      sum += fr[i];
-      m1 += (double)fr[i] * lnrel[i];
-      m2 += (double)fr[i] * lnrel[i] * lnrel[i];
-    }
-    const double Pb = P[b], Qb = P[kNb + b], Rb = P[2 * kNb + b];
-    const bool ok = Pb > 0. && sum > 0.f;
-    const double isum = ok ? 1. / (double)sum : 0.;
-    bscale[b] = ok ? Pb * isum : 0.;
-    be[b] = ok ? fabs(Pb * m1 * isum - Qb) / (Pb * hw[b]) + fabs(Pb * m2 * isum - Rb) / (Pb * hw[b] * hw[b]) : 0.;
-  }
-  __syncthreads();
+  __syncwarp();
   if (live)
-    for (int i = tid; i < F; i += kFeatThreads) out[(size_t)s * F + i] = bscale[i / per] * (double)fr[i] * invdnu[i];
-  if (tid == 0) {
-    double ptot = 0., e = 0.;
-    for (int b = 0; b < kNb; ++b) ptot += fmax(P[b], 0.);
-    for (int b = 0; b < kNb; ++b) e += ptot > 0. ? fmax(P[b], 0.) / ptot * be[b] : 0.;
+    for (int i = lane; i < F; i += 32) out[(size_t)s * F + i] = jr[i];
+  const double ex = Pp[kNmom + lane];  // one check per lane
+  const double d = jr[chk[lane]] - ex;
+  const double num = warp_sum_d(d * d), den = warp_sum_d(ex * ex);
+  if (lane == 0) {
+    const double e = den > 0. ? est_scale * sqrt(num / den) : (num > 0. ? 1e30 : 0.);
     const bool finite = e == e && !isinf(e);
     err[s] = finite ? (float)e : 1e30f;
-    const bool back = live && (!finite || e > tol);
-    fb[s] = back ? kFlagActive : 0;
-    if (back) atomicAdd(nfb, 1);
+    if (live && (!finite || e > tol)) list[atomicAdd(nfb, 1)] = s;
+  }
+}
+
+// The rows to recompute, gathered into dense operands (one warp per gathered
+// row c; rows from the count on are marked inactive).
+__global__ void __launch_bounds__(32 * kSurWarps)
+k_sur_gather(int rows, int F, int Gp, const int* __restrict__ nfb, const int* __restrict__ list,
+             const uint16_t* __restrict__ Wt, const float* __restrict__ U32, const double* __restrict__ scal,
+             uint16_t* __restrict__ Wc, float* __restrict__ Uc, double* __restrict__ scalc, int* __restrict__ flagc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kSurWarps + warp;
+  if (c >= rows) return;
+  if (c >= *nfb) {
+    if (lane == 0) flagc[c] = 0;
+    return;
+  }
+  const int r = list[c];
+  if (lane == 0) flagc[c] = kFlagActive;
+  if (lane < kScal) scalc[(size_t)c * kScal + lane] = scal[(size_t)r * kScal + lane];
+  for (int k = lane; k < F; k += 32) Uc[(size_t)c * F + k] = U32[(size_t)r * F + k];
+  const uint16_t* src = Wt + (size_t)(r / kTcCols) * tc_tile_elems(kTcCols, Gp);
+  uint16_t* dst = Wc + (size_t)(c / kTcCols) * tc_tile_elems(kTcCols, Gp);
+  for (int j = lane; j < Gp; j += 32) {
+    dst[tc_operand_offset(c % kTcCols, j, kTcCols, Gp, false)] =
+        src[tc_operand_offset(r % kTcCols, j, kTcCols, Gp, false)];
+    dst[tc_operand_offset(c % kTcCols, j, kTcCols, Gp, true)] =
+        src[tc_operand_offset(r % kTcCols, j, kTcCols, Gp, true)];
   }
 }
 
 int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA; }
 
+unsigned warps_grid(int n) { return (unsigned)((n + kSurWarps - 1) / kSurWarps); }
+
+// exact projections and baseline fits of nrows rows (proj, fit, base)
+cudaError_t project_and_fit(Surrogate* sg, const CtxView& v, int nrows, const void* Wt, const int* flags,
+                            const float* U32, const double* scal, double* proj, float* base, int* errs,
+                            cudaStream_t st) {
+  cudaError_t e = launch_ssc_tc_mode(kTcBf16, v.F, v.Gp, Wt, sg->Kp, nrows, flags, U32, scal, sg->oscale, kNproj,
+                                     kNproj, proj, errs, st);
+  if (e != cudaSuccess) return e;
+  const int threads = 128;
+  k_sur_fit<<<(unsigned)((nrows * kNb + threads - 1) / threads), threads, 0, st>>>(nrows, v.F, sg->per, proj,
+                                                                                  sg->xrel, sg->hw, sg->fit, base);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 // The surrogate tail shared by the batch entry point and the step: exact
-// projections, features, MLP, reconstruction with error estimate, exact
-// fallback. Operands: W tiles Wt, U32, scal (SW, SU) of nrows rows; f / nph /
-// B rows for the features; rows with flags & kFlagActive are written to out.
+// projections, baseline fits, features, MLP, reconstruction with error
+// estimate, exact recomputation of the rows above the tolerance. Operands: W
+// tiles Wt, U32, scal (SW, SU) of nrows rows; f / nph / B rows for the
+// features; rows with flags & kFlagActive are written to out. host_count:
+// the number of rows to recompute is read back (one synchronisation) and the
+// exact launch sized to it; otherwise its tiles beyond the count exit at once
+// (graph capture).
 cudaError_t surrogate_run(pbag_ctx* ctx, const CtxView& v, int nrows, const void* Wt, const int* flags,
                           const float* U32, const double* scal, const double* f, int fs, const double* nph, int ns,
-                          const double* Bv, int bs, double* out, int* errs, cudaStream_t st) {
+                          const double* Bv, int bs, double* out, int* errs, cudaStream_t st, bool host_count) {
   auto* sg = static_cast<Surrogate*>(ctx_get_extension(ctx, kExtSurrogate));
   if (!sg || !sg->net) return cudaErrorInvalidValue;
   cudaError_t e = sg->reserve(nrows);
@@ -395,19 +504,35 @@ cudaError_t surrogate_run(pbag_ctx* ctx, const CtxView& v, int nrows, const void
   auto ok = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
   };
-  ok(launch_ssc_tc_mode(kTcSplit, v.F, v.Gp, Wt, sg->Kp, nrows, flags, U32, scal, sg->oscale, kNproj, kNproj,
-                        sg->proj, errs, st));
-  k_sur_features<<<nrows, kFeatThreads, 0, st>>>(v.dg, nrows, f, fs, nph, ns, Bv, bs, sg->proj, sg->hw, sg->lnrel,
-                                                  sg->per, sg->mean, sg->stdv, sg->X, nullptr);
+  ok(project_and_fit(sg, v, nrows, Wt, flags, U32, scal, sg->proj, sg->base, errs, st));
+  if (e == cudaSuccess)
+    k_sur_features<<<warps_grid(nrows), 32 * kSurWarps, 0, st>>>(v.dg, nrows, f, fs, nph, ns, Bv, bs, sg->proj,
+                                                                  sg->fit, sg->mean, sg->stdv, sg->X);
   ok(cudaGetLastError());
-  ok(mlp_forward(sg->net, nrows, sg->X, sg->Y, st));
+  ok(mlp_infer(sg->net, nrows, sg->X, sg->Y, st));
   ok(cudaMemsetAsync(sg->nfb, 0, sizeof(int), st));
-  k_sur_reconstruct<<<nrows, kFeatThreads, 0, st>>>(v.F, nrows, flags, sg->Y, sg->proj, sg->lnrel, sg->invdnu,
-                                                     sg->hw, sg->tol, sg->per, out, sg->err, sg->fb, sg->nfb);
+  if (e == cudaSuccess)
+    k_sur_reconstruct<<<warps_grid(nrows), 32 * kSurWarps, 0, st>>>(v.F, sg->per, nrows, flags, sg->Y, sg->base,
+                                                                     sg->proj, sg->invdnu, sg->chk, sg->est_scale,
+                                                                     sg->tol, out, sg->err, sg->list, sg->nfb);
   ok(cudaGetLastError());
-  // the states whose error estimate is above the tolerance, exactly
-  ok(launch_ssc_tc_mode(kTcSplit, v.F, v.Gp, Wt, v.dg.Bt, nrows, sg->fb, U32, scal, v.dg.hnu, v.F, v.F, out, errs,
-                        st));
+  if (e != cudaSuccess) return e;
+  int rows = nrows;
+  TcRows map;
+  map.rowmap = sg->list;
+  if (host_count) {
+    ok(cudaMemcpyAsync(&rows, sg->nfb, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ok(cudaStreamSynchronize(st));
+    if (e != cudaSuccess || rows == 0) return e;
+  } else {
+    map.nlive = sg->nfb;
+  }
+  k_sur_gather<<<warps_grid(rows), 32 * kSurWarps, 0, st>>>(rows, v.F, v.Gp, sg->nfb, sg->list,
+                                                            static_cast<const uint16_t*>(Wt), U32, scal, sg->Wc,
+                                                            sg->Uc, sg->scalc, sg->flagc);
+  ok(cudaGetLastError());
+  ok(launch_ssc_tc_mode(kTcSplit, v.F, v.Gp, sg->Wc, v.dg.Bt, rows, sg->flagc, sg->Uc, sg->scalc, v.dg.hnu, v.F, v.F,
+                        out, errs, st, map));
   return e;
 }
 
@@ -420,8 +545,7 @@ bool surrogate_ready(pbag_ctx* ctx) {
 cudaError_t surrogate_reserve(pbag_ctx* ctx, int n) {
   auto* sg = static_cast<Surrogate*>(ctx_get_extension(ctx, kExtSurrogate));
   if (!sg || !sg->net) return cudaErrorInvalidValue;
-  cudaError_t e = sg->reserve(n);
-  return e == cudaSuccess ? mlp_reserve(sg->net, n) : e;
+  return sg->reserve(n);
 }
 
 int64_t surrogate_generation(pbag_ctx* ctx) {
@@ -431,8 +555,8 @@ int64_t surrogate_generation(pbag_ctx* ctx) {
 
 int surrogate_launches(const pbag_ctx* ctx) {
   auto* sg = static_cast<Surrogate*>(ctx_get_extension(const_cast<pbag_ctx*>(ctx), kExtSurrogate));
-  // projections, features, the MLP layers, reconstruction, exact fallback
-  return sg && sg->net ? 4 + mlp_layers(sg->net) : 0;
+  // projections, fits, features, MLP, reconstruction, gather, exact recomputation
+  return sg && sg->net ? 7 : 0;
 }
 
 }  // namespace pbag
@@ -441,12 +565,13 @@ using namespace pbag;
 
 extern "C" {
 
-int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, const float* stdv, float tol) {
+int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, const float* stdv, float est_scale,
+                             float tol) {
   CtxView v;
   if (!ctx_view(ctx, &v)) return PBAG_ERR_ARG;
-  if (!v.ssc || !v.dg.Bt || v.F % kNb != 0 || v.F > 1024) return PBAG_ERR_UNSUPPORTED;
+  if (!v.ssc || !v.dg.Bt || (v.F != 128 && v.F != 256)) return PBAG_ERR_UNSUPPORTED;
   if (net && (mlp_in_dim(net) != kNin || mlp_out_dim(net) != v.F)) return PBAG_ERR_ARG;
-  if (!(tol >= 0.f)) return PBAG_ERR_ARG;
+  if (!(tol >= 0.f) || !(est_scale > 0.f)) return PBAG_ERR_ARG;
   if (cudaSetDevice(v.device) != cudaSuccess) return PBAG_ERR_CUDA;
   auto* sg = static_cast<Surrogate*>(ctx_get_extension(ctx, kExtSurrogate));
   if (!sg) {
@@ -470,11 +595,25 @@ int pbag_surrogate_configure(pbag_ctx* ctx, pbag_mlp* net, const float* mean, co
   }
   sg->net = net;
   sg->tol = tol;
+  sg->est_scale = est_scale;
   sg->generation += 1;
   if (mean && cudaMemcpy(sg->mean, mean, kNin * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
     return PBAG_ERR_CUDA;
   if (stdv && cudaMemcpy(sg->stdv, stdv, kNin * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
     return PBAG_ERR_CUDA;
+  if (net) {
+    // lay the BF16 weights out now (a graph captured later replays inference only)
+    if (mlp_infer(net, 0, nullptr, nullptr, v.stream) != cudaSuccess) return PBAG_ERR_UNSUPPORTED;
+    if (cudaStreamSynchronize(v.stream) != cudaSuccess) return PBAG_ERR_CUDA;
+  }
+  return PBAG_OK;
+}
+
+int pbag_surrogate_checks(pbag_ctx* ctx, int* idx) {
+  CtxView v;
+  if (!ctx_view(ctx, &v) || !idx) return PBAG_ERR_ARG;
+  if (v.F % kNb != 0) return PBAG_ERR_UNSUPPORTED;
+  for (int c = 0; c < kNchk; ++c) idx[c] = check_freq(c, v.F / kNb);
   return PBAG_OK;
 }
 
@@ -501,12 +640,11 @@ int pbag_surrogate_features(pbag_ctx* ctx, int n, const double* d_f, const doubl
   if (rc != PBAG_OK) return rc;
   cudaError_t e = sg->reserve(n);
   double* proj = d_proj ? d_proj : sg->proj;
-  if (e == cudaSuccess)
-    e = launch_ssc_tc_mode(kTcSplit, v.F, v.Gp, Wt, sg->Kp, n, S.flags, S.U32, S.scal, sg->oscale, kNproj, kNproj,
-                           proj, S.err, v.stream);
-  if (e == cudaSuccess && (d_x || d_base)) {
-    k_sur_features<<<n, kFeatThreads, 0, v.stream>>>(v.dg, n, d_f, v.G, d_nph, v.F, d_B, 1, proj, sg->hw, sg->lnrel,
-                                                      sg->per, nullptr, nullptr, d_x ? d_x : sg->X, d_base);
+  float* base = d_base ? d_base : sg->base;
+  if (e == cudaSuccess) e = project_and_fit(sg, v, n, Wt, S.flags, S.U32, S.scal, proj, base, S.err, v.stream);
+  if (e == cudaSuccess && d_x) {
+    k_sur_features<<<warps_grid(n), 32 * kSurWarps, 0, v.stream>>>(v.dg, n, d_f, v.G, d_nph, v.F, d_B, 1, proj,
+                                                                    sg->fit, nullptr, nullptr, d_x);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
@@ -536,14 +674,22 @@ int pbag_surrogate_contract(pbag_ctx* ctx, int n, const double* d_f, const doubl
   const void* Wt = nullptr;
   int rc = contract_prepare(ctx, v, n, d_f, d_nph, &S, &Wt);
   if (rc != PBAG_OK) return rc;
-  cudaError_t e = surrogate_run(ctx, v, n, Wt, S.flags, S.U32, S.scal, d_f, v.G, d_nph, v.F, d_B, 1, d_jssc, S.err,
-                                v.stream);
   auto* sg = static_cast<Surrogate*>(ctx_get_extension(ctx, kExtSurrogate));
-  int nfb = 0;
-  if (e == cudaSuccess && d_err) e = cudaMemcpyAsync(d_err, sg->err, n * sizeof(float), cudaMemcpyDeviceToDevice, v.stream);
+  cudaError_t e = surrogate_run(ctx, v, n, Wt, S.flags, S.U32, S.scal, d_f, v.G, d_nph, v.F, d_B, 1, d_jssc, S.err,
+                                v.stream, true);
+  int nfb = 0, code = 0;
+  if (e == cudaSuccess && d_err)
+    e = cudaMemcpyAsync(d_err, sg->err, n * sizeof(float), cudaMemcpyDeviceToDevice, v.stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&nfb, sg->nfb, sizeof(int), cudaMemcpyDeviceToHost, v.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&code, mlp_infer_error(sg->net), sizeof(int), cudaMemcpyDeviceToHost, v.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
   if (e != cudaSuccess) return status_of(e);
+  if (code != 0) {
+    cudaMemset(mlp_infer_error(sg->net), 0, sizeof(int));
+    if (st) st->code = code;
+    return code;
+  }
   if (n_fallback) *n_fallback = nfb;
   if (st) st->code = PBAG_OK;
   return PBAG_OK;

@@ -4,10 +4,15 @@ library's own MLP kernels, pbag_mlp_*).
 Data: comoving states (N(gamma) after a step, B, the photon field of the
 previous radiating step) of seeded blastwaves from the batched parameter sweep,
 evolved by the plain GPU step. Targets: log10 of each frequency's share of its
-band's power in the exact SSC spectrum (pbag_contract, split BF16), masked
-where the band carries no power. Features and the exact band projections come
-from pbag_surrogate_features. The network: PBAG_SUR_IN -> 4 x 256 (SiLU) ->
-nfreq, trained with Adam on masked squared error.
+band's power in the exact SSC spectrum (pbag_contract, split BF16) minus the
+baseline share (the log-parabola matched to the band's exact power, first and
+second moments), weighted by emissivity (zero where the band carries no
+power). Features, the exact projections and the baseline come from
+pbag_surrogate_features. The network: PBAG_SUR_IN -> 4 x 256 (SiLU) -> nfreq,
+trained in FP32 with Adam on weighted squared error by the library's kernels,
+run in BF16 on the tensor cores. The
+error estimate's scale is calibrated on held-out states against the exact
+spectra (calibrate).
 """
 import ctypes as C
 import math
@@ -18,16 +23,20 @@ from . import _lib, abi
 from . import histories as H
 from .mlp import MLP
 
-NIN, NB, NPROJ = 128, 16, 48
+NIN, NB, NCHK = 128, 16, 32
+NPROJ = 3 * NB + NCHK
 HIDDEN = (256, 256, 256, 256)
 TARGET_FLOOR = -12.0
+WEIGHT_FLOOR = 1e-3
 
 
 def _bind():
     lib = _lib.load()
     if not getattr(lib, "_sur_bound", False):
         P = C.POINTER
-        lib.pbag_surrogate_configure.argtypes = [C.c_void_p, C.c_void_p, P(C.c_float), P(C.c_float), C.c_float]
+        lib.pbag_surrogate_configure.argtypes = [C.c_void_p, C.c_void_p, P(C.c_float), P(C.c_float), C.c_float,
+                                                 C.c_float]
+        lib.pbag_surrogate_checks.argtypes = [C.c_void_p, P(C.c_int)]
         lib.pbag_surrogate_features.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p, C.c_void_p, C.c_void_p, P(abi.Status)]
         lib.pbag_surrogate_contract.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -36,14 +45,21 @@ def _bind():
     return lib
 
 
-def configure(ctx, net=None, mean=None, std=None, tol=0.01):
+def configure(ctx, net=None, mean=None, std=None, tol=0.01, est_scale=1.0):
     lib = _bind()
-    fp = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32).ctypes.data_as(
-        C.POINTER(C.c_float))
     m = None if mean is None else np.ascontiguousarray(mean, dtype=np.float32)
     s = None if std is None else np.ascontiguousarray(std, dtype=np.float32)
+    fp = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
     _lib._check(lib.pbag_surrogate_configure(ctx.handle, net.handle if net is not None else None,
-                                             fp(m), fp(s), float(tol)), "pbag_surrogate_configure")
+                                             fp(m), fp(s), float(est_scale), float(tol)),
+                "pbag_surrogate_configure")
+
+
+def checks(ctx):
+    """Frequency index of each check projection (columns 3 NB .. NPROJ of the projections)."""
+    idx = (C.c_int * NCHK)()
+    _lib._check(_bind().pbag_surrogate_checks(ctx.handle, idx), "pbag_surrogate_checks")
+    return np.array(idx[:], dtype=np.int64)
 
 
 def features(ctx, n, d_f, d_B, d_nph, d_x, d_proj, d_base=0):
@@ -114,8 +130,9 @@ def exact_ssc(ctx, f, B, nph):
 
 def make_targets(jssc, proj, freq, base):
     """The network's targets: log10 of each frequency's share of its band's
-    exact power (floored) minus the baseline share (the tilt matched to the
-    band's exact moments); mask where the band carries power."""
+    exact power minus the baseline share (the log-parabola matched to the
+    band's exact moments), and the loss weights (zero where the band carries
+    no power or the share is below the floor)."""
     import torch
     n, F = jssc.shape
     per = F // NB
@@ -125,8 +142,15 @@ def make_targets(jssc, proj, freq, base):
     share = jssc * dnu / torch.where(P > 0, P, torch.ones_like(P))
     t = torch.log10(torch.clamp(share, min=10.0 ** TARGET_FLOOR)).clamp(min=TARGET_FLOOR, max=1.0)
     t = (t - base.to(t.dtype)).clamp(min=-12.0, max=12.0)
-    mask = (P > 0).to(torch.float32)
-    return t.to(torch.float32).contiguous(), mask.contiguous()
+    # frequencies below the floor carry no power that matters; left unmasked
+    # they would dominate the loss with large, meaningless corrections
+    mask = ((P > 0) & (share > 10.0 ** TARGET_FLOOR)).to(torch.float32)
+    # weights: the relative L2 error of a spectrum is dominated by its
+    # brightest frequencies, so each frequency counts with its emissivity
+    # (normalised to a mean of one per state), plus a small floor
+    a = jssc.abs()
+    w = (a / torch.clamp(a.sum(dim=1, keepdim=True), min=1e-300) * F).to(torch.float32)
+    return t.to(torch.float32).contiguous(), ((w + WEIGHT_FLOOR) * mask).contiguous()
 
 
 def band_baseline(proj, freq, base):
@@ -139,6 +163,35 @@ def band_baseline(proj, freq, base):
     dnu = (nu[1:F + 1] - nu[:F])[None, :]
     share = torch.pow(10.0, base.to(torch.float64))
     return proj[:, :NB].clamp(min=0).repeat_interleave(per, dim=1) * share / dnu
+
+
+def rel_l2_rows(x, y):
+    """Relative L2 error of every row (NaN where the reference row is zero)."""
+    import torch
+    num = torch.sqrt(((x - y) ** 2).sum(dim=1))
+    den = torch.sqrt((y ** 2).sum(dim=1))
+    return torch.where(den > 0, num / torch.where(den > 0, den, torch.ones_like(den)),
+                       torch.full_like(den, float("nan")))
+
+
+def calibrate(ctx, trainer, f, B, nph, jex, quantile=0.95):
+    """Scale of the error estimate: the given quantile, over held-out states,
+    of the true relative L2 error divided by the unscaled estimate (the
+    distance at the check frequencies). Leaves the surrogate configured with
+    that scale and no fallback."""
+    import torch
+    configure(ctx, trainer.net, trainer.mean, trainer.std, tol=1e30, est_scale=1.0)
+    n = f.shape[0]
+    j = torch.zeros_like(jex)
+    est = torch.zeros(n, dtype=torch.float32, device=f.device)
+    contract(ctx, n, f.data_ptr(), B.data_ptr(), nph.data_ptr(), j.data_ptr(), est.data_ptr())
+    err = rel_l2_rows(j, jex)
+    ok = torch.isfinite(err)
+    ratio = err[ok] / torch.clamp(est[ok].double(), min=1e-12)
+    scale = float(torch.quantile(ratio.float(), quantile)) if ratio.numel() else 1.0
+    scale = max(scale, 1e-3)
+    configure(ctx, trainer.net, trainer.mean, trainer.std, tol=1e30, est_scale=scale)
+    return scale
 
 
 def rel_l2(x, y):

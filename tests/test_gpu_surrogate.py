@@ -1,8 +1,9 @@
-"""The SSC surrogate: exact band projections against the FP64 oracle, a
-trained network against the method without it (in each band the baseline shape
-matched to the band's exact power and first moment), the error estimate and
-exact fallback, and the surrogate inside the step (tolerance 0: every state
-recomputed exactly, so the step's histories must match the oracle)."""
+"""The SSC surrogate: exact projections (band moments and check frequencies)
+against the FP64 oracle, the log-parabola baseline, a trained network against
+the method without it (the baseline alone), the calibrated error estimate and
+the gathered exact recomputation, and the surrogate inside the step
+(tolerance 0: every state recomputed exactly, so the step's histories must
+match the oracle)."""
 import os
 
 import numpy as np
@@ -43,23 +44,36 @@ def test_band_projections_match_oracle(lib, oracle, cuda_device):
     x = lnu - np.repeat(c, per)
     Q = (jssc * dnu * x).reshape(40, SG.NB, per).sum(axis=2)
     R = (jssc * dnu * x * x).reshape(40, SG.NB, per).sum(axis=2)
+    # plain BF16 operands, FP32 accumulation: ~1e-3 relative
+    big = P > 1e-6 * P.max(axis=1, keepdims=True)
     rel_p = np.abs(proj[:, :SG.NB] - P) / np.maximum(P, 1e-300)
-    assert rel_p[P > 1e-6 * P.max(axis=1, keepdims=True)].max() <= 1e-4
+    assert rel_p[big].max() <= 1e-2 and np.median(rel_p[big]) <= 3e-3
     # log moments: against the band power times the band half width
     hw = 0.5 * (lnu.reshape(SG.NB, per)[:, -1] - lnu.reshape(SG.NB, per)[:, 0])
-    big = P > 1e-6 * P.max(axis=1, keepdims=True)
     rel_q = np.abs(proj[:, SG.NB:2 * SG.NB] - Q) / np.maximum(P * hw, 1e-300)
-    assert rel_q[big].max() <= 1e-4
-    rel_r = np.abs(proj[:, 2 * SG.NB:] - R) / np.maximum(P * hw * hw, 1e-300)
-    assert rel_r[big].max() <= 1e-4
+    assert rel_q[big].max() <= 1e-2
+    rel_r = np.abs(proj[:, 2 * SG.NB:3 * SG.NB] - R) / np.maximum(P * hw * hw, 1e-300)
+    assert rel_r[big].max() <= 1e-2
+    # check frequencies: the spectrum itself
+    idx = SG.checks(ctx)
+    assert len(idx) == SG.NCHK and len(set(idx.tolist())) == SG.NCHK
+    assert all(b * per <= i < (b + 1) * per for b, i in zip(np.repeat(np.arange(SG.NB), 2), idx))
+    jc = jssc[:, idx]
+    rel_c = np.linalg.norm(proj[:, 3 * SG.NB:] - jc, axis=1) / np.linalg.norm(jc, axis=1)
+    assert rel_c.max() <= 1e-2
     assert np.isfinite(d_x.cpu().numpy()).all()
-    # the baseline shares of a band sum to one and match its exact first moment
+    # the baseline shares of a band sum to one and match its exact first and
+    # second moments (where those lie inside the band's feasible set)
     base = d_b.cpu().numpy().astype(np.float64).reshape(40, SG.NB, per)
     sh = 10.0 ** base
     np.testing.assert_allclose(sh.sum(axis=2), 1.0, rtol=1e-4)
-    mu = (sh * x.reshape(SG.NB, per)[None]).sum(axis=2)
-    inside = big & (np.abs(Q / np.maximum(P, 1e-300)) < 0.95 * hw[None, :])
-    assert np.abs(mu - Q / np.maximum(P, 1e-300))[inside].max() <= 1e-3 * hw.max()
+    xb = x.reshape(SG.NB, per)[None]
+    mu1, mu2 = (sh * xb).sum(axis=2), (sh * xb * xb).sum(axis=2)
+    m1 = Q / np.maximum(P, 1e-300)
+    var = R / np.maximum(P, 1e-300) - m1 ** 2
+    inside = big & (np.abs(m1) < 0.9 * hw[None, :]) & (var > 1e-3 * hw[None, :] ** 2)
+    assert np.abs(mu1 - m1)[inside].max() <= 2e-2 * hw.max()
+    assert np.abs(mu2 - R / np.maximum(P, 1e-300))[inside].max() <= 2e-2 * hw.max() ** 2
 
 
 @pytest.fixture(scope="module")
@@ -81,14 +95,17 @@ def trained(lib, cuda_device):
     SG.features(ctx, n, f.data_ptr(), B.data_ptr(), nph.data_ptr(), X.data_ptr(), proj.data_ptr(), base.data_ptr())
     jex = SG.exact_ssc(ctx, f, B, nph)
     T, M = SG.make_targets(jex, proj, freq, base)
-    ntr = int(0.85 * n)
+    ntr, ncal = int(0.75 * n), int(0.1 * n)
     tr = SG.Trainer(g.nfreq, cuda_device, seed=0)
     Xs = tr.standardise(X.clone())
-    tr.fit(Xs[:ntr], T[:ntr], M[:ntr], epochs=20, batch=1024, lr=2e-3)
-    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
-    va = slice(ntr, n)
-    return dict(ctx=ctx, trainer=tr, f=f[va].contiguous(), B=B[va].contiguous(), nph=nph[va].contiguous(),
-                jex=jex[va].contiguous(), proj=proj[va].contiguous(), base=base[va].contiguous(), freq=freq, grid=g)
+    tr.fit(Xs[:ntr], T[:ntr], M[:ntr], epochs=40, batch=1024, lr=2e-3)
+    cal = slice(ntr, ntr + ncal)
+    scale = SG.calibrate(ctx, tr, f[cal].contiguous(), B[cal].contiguous(), nph[cal].contiguous(),
+                         jex[cal].contiguous())
+    va = slice(ntr + ncal, n)
+    return dict(ctx=ctx, trainer=tr, scale=scale, f=f[va].contiguous(), B=B[va].contiguous(),
+                nph=nph[va].contiguous(), jex=jex[va].contiguous(), proj=proj[va].contiguous(),
+                base=base[va].contiguous(), freq=freq, grid=g)
 
 
 def test_network_gains_over_band_baseline(trained):
@@ -103,8 +120,8 @@ def test_network_gains_over_band_baseline(trained):
     med_net, med_base = float(err_net.median()), float(err_base.median())
     print(f"surrogate rel-L2 median {med_net:.4f} p90 {float(err_net.quantile(0.9)):.4f}; "
           f"baseline median {med_base:.4f}")
-    assert med_net < 0.5 * med_base, (med_net, med_base)
-    assert med_net < 0.06
+    assert med_net < 0.6 * med_base, (med_net, med_base)
+    assert med_net < 0.012
 
 
 def test_error_estimate_and_fallback(trained):
@@ -113,24 +130,39 @@ def test_error_estimate_and_fallback(trained):
     d = trained
     n = d["f"].shape[0]
     tol = 0.01
-    SG.configure(d["ctx"], d["trainer"].net, d["trainer"].mean, d["trainer"].std, tol=tol)
+    net, mean, std = d["trainer"].net, d["trainer"].mean, d["trainer"].std
+    SG.configure(d["ctx"], net, mean, std, tol=1e30, est_scale=d["scale"])
+    j0 = torch.zeros_like(d["jex"])
+    est = torch.zeros(n, dtype=torch.float32, device=j0.device)
+    assert SG.contract(d["ctx"], n, d["f"].data_ptr(), d["B"].data_ptr(), d["nph"].data_ptr(), j0.data_ptr(),
+                       est.data_ptr()) == 0
+    err0 = SG.rel_l2_rows(j0, d["jex"])
+    SG.configure(d["ctx"], net, mean, std, tol=tol, est_scale=d["scale"])
     j = torch.zeros_like(d["jex"])
-    est = torch.zeros(n, dtype=torch.float32, device=j.device)
+    est2 = torch.zeros(n, dtype=torch.float32, device=j.device)
     nfb = SG.contract(d["ctx"], n, d["f"].data_ptr(), d["B"].data_ptr(), d["nph"].data_ptr(), j.data_ptr(),
-                      est.data_ptr())
+                      est2.data_ptr())
     back = est > tol
+    assert torch.equal(est, est2)
     assert nfb == int(back.sum())
-    err = SG.rel_l2(j, d["jex"])
-    # recomputed states are exact
-    assert float(err[back].max() if back.any() else 0.0) <= 1e-6
-    SG.configure(d["ctx"], d["trainer"].net, d["trainer"].mean, d["trainer"].std, tol=1e30)
+    err = SG.rel_l2_rows(j, d["jex"])
+    ok = torch.isfinite(err)
+    # recomputed states are exact (the same split-BF16 contraction), the others untouched
+    assert float(err[back & ok].max() if bool((back & ok).any()) else 0.0) <= 1e-6
+    assert torch.equal(j[~back], j0[~back])
+    # the calibrated estimate lets few states above twice the tolerance through
+    acc = ~back & ok
+    print(f"fallback {nfb / n:.3f}; accepted error p99 {float(err0[acc].quantile(0.99)):.4f}")
+    assert float((err0[acc] > 2 * tol).float().mean()) <= 0.02
+    SG.configure(d["ctx"], net, mean, std, tol=1e30, est_scale=d["scale"])
 
 
 def test_step_with_surrogate_at_zero_tolerance_matches_oracle(lib, oracle, cuda_device, trained):
     from pyblastafterglowmag_gb300 import surrogate as SG
     recs, off, prm, grid = cases.gaussian(lib, nlayers=2, nsteps=80)
     ctx = lib.Context(grid, cuda_device, ssc=True)
-    SG.configure(ctx, trained["trainer"].net, trained["trainer"].mean, trained["trainer"].std, tol=0.0)
+    SG.configure(ctx, trained["trainer"].net, trained["trainer"].mean, trained["trainer"].std, tol=0.0,
+                 est_scale=trained["scale"])
     ctx.set_ssc_path(abi.PBAG_SSC_SURROGATE)
     out = ctx.run(recs, off, prm, outputs=cases.TOTALS)
     rc, where, ref = oracle.run(grid, recs, off, prm, outputs=cases.TOTALS)
