@@ -26,17 +26,15 @@ namespace {
 
 using namespace cgs;
 
-constexpr int kPrepThreads = 128;
-
-__device__ int block_max_exp(int v, int* red) {
-  v = __reduce_max_sync(0xffffffffu, v);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  int r = 0;
-  for (int i = 0; i < kPrepThreads / 32; ++i) r = max(r, red[i]);
-  return r;
-}
+constexpr int kPrepWarps = 8;  // states per CTA of the preparation kernel (a warp each)
+// synchrotron constants per unit field (kernels.h:194-202, 427, 471): the
+// prefactors sqrt(3) q^3 / (m_e c^2) (CSYN) and sqrt(3) q^3 / (m_e c c)
+// (Dermer09), and in FP32 4 pi m_e c / (3 q) and 2 pi m_e c / (3 q)
+constexpr double kSqrt3 = 1.7320508075688772;
+constexpr double kPrefCsyn = kSqrt3 * q_e * q_e * q_e / mec2;
+constexpr double kPrefDer = kSqrt3 * q_e * q_e * q_e / (m_e * c_light * c_light);
+constexpr float kIncrit32 = (float)((4. * M_PI * m_e * c_light) / (3. * q_e));
+constexpr float kNuL32 = (float)((2. * pi_ * m_e * c_light) / (3. * q_e));
 
 __device__ __forceinline__ float tf32_rna(float x) {
   uint32_t r;
@@ -44,80 +42,131 @@ __device__ __forceinline__ float tf32_rna(float x) {
   return __uint_as_float(r);
 }
 
-// One CTA per state: the scaled FP32 weights of the synchrotron sum and of the
-// SSC contraction (and its tensor-core operand tile), the seed-photon weights,
-// the per-state scalars. The same formulas as the evolve kernel's epilogue and
-// the step completion (microphysics.h:498-558, numeric_model.h:271-277).
-__global__ void __launch_bounds__(kPrepThreads)
+// One warp per state: the scaled FP32 weights of the synchrotron sum and of
+// the SSC contraction (and its tensor-core operand tile), the seed-photon
+// weights, the per-state scalars. The same formulas as the evolve kernel's
+// epilogue and the step completion (microphysics.h:498-558,
+// numeric_model.h:271-277). The products of the FP64 state values with the
+// grid factors are formed as FP32 mantissa times power of two (f64_mant):
+// every weight keeps FP32 accuracy, each row is scaled by a power of two to a
+// largest value in [1, 2), and the scale goes to the per-state scalars.
+__global__ void __launch_bounds__(32 * kPrepWarps)
 k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __restrict__ Bf,
                 const double* __restrict__ nph, int syn_method, int mode, int want_syn, int want_ssc, DevState S,
                 unsigned char* __restrict__ Wt, pbag_shock_params* __restrict__ prm) {
-  const int s = blockIdx.x, tid = threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kPrepWarps + (threadIdx.x >> 5);
+  if (s >= n) return;
   const int G = g.G, F = g.F;
-  __shared__ int red[kPrepThreads / 32];
-  const GridTab T{g.etab, g.Ge, g.Fe};
   const double* fs = f + (size_t)s * G;
-  const double* t_de = T.gt(kTabDe);
-  const double* t_ie2 = T.gt(kTabInvE2);
-  int wexp = 0, Wexp = 0;
-  for (int j = tid; j < G - 1; j += kPrepThreads) {
-    const double w = fs[j] * t_de[j];
-    wexp = max(wexp, exp_field(w));
-    Wexp = max(Wexp, exp_field(w * t_ie2[j]));
+  const float* m_de = g.tmant + (size_t)kM32De * g.Tm;
+  const int* e_de = g.texp + (size_t)kM32De * g.Tm;
+  const float* m_w = g.tmant + (size_t)kM32DeIe2 * g.Tm;
+  const int* e_w = g.texp + (size_t)kM32DeIe2 * g.Tm;
+  // largest exponents of f_j dgamma_j and f_j dgamma_j / gamma_j^2
+  int wexp = kExpZero, Wexp = kExpZero;
+  for (int j = lane; j < G - 1; j += 32) {
+    int ef;
+    const float mf = f64_mant(fs[j], ef);
+    int e1 = ef + e_de[j], e2 = ef + e_w[j];
+    mant_mul(mf, m_de[j], e1);
+    mant_mul(mf, m_w[j], e2);
+    if (mf != 0.f) {
+      wexp = max(wexp, e1);
+      Wexp = max(Wexp, e2);
+    }
   }
-  wexp = block_max_exp(wexp, red);
-  Wexp = block_max_exp(Wexp, red);
+  wexp = __reduce_max_sync(0xffffffffu, wexp);
+  Wexp = __reduce_max_sync(0xffffffffu, Wexp);
+  if (wexp == kExpZero) wexp = 0;
+  if (Wexp == kExpZero) Wexp = 0;
   double* scal = S.scal + (size_t)s * kScal;
   if (want_syn) {
-    const double sw = scale_from_exp(wexp);
     float* w32 = S.w32 + (size_t)s * G;
-    for (int j = tid; j < G; j += kPrepThreads) w32[j] = j < G - 1 ? (float)(fs[j] * t_de[j] * sw) : 0.f;
+    for (int j = lane; j < G; j += 32) {
+      float w = 0.f;
+      if (j < G - 1) {
+        int e;
+        const float mf = f64_mant(fs[j], e);
+        e += e_de[j];
+        w = f32_ldexp(mant_mul(mf, m_de[j], e), e - wexp);
+      }
+      w32[j] = w;
+    }
   }
   if (want_ssc) {
-    const double sW = scale_from_exp(Wexp);
     float* W = S.W32 + (size_t)s * g.Gp;
+    auto wval = [&](int j) {
+      if (j >= G - 1) return 0.f;
+      int e;
+      const float mf = f64_mant(fs[j], e);
+      e += e_w[j];
+      return f32_ldexp(mant_mul(mf, m_w[j], e), e - Wexp);
+    };
+    for (int j = lane; j < g.Gp; j += 32) W[j] = wval(j);
     const int m = s % kTcCols;
     unsigned char* tile = Wt ? Wt + (size_t)(s / kTcCols) * tc_tile_bytes(kTcCols, g.Gp, mode == kTcTf32 ? 4 : 2)
                              : nullptr;
-    for (int j = tid; j < g.Gp; j += kPrepThreads) {
-      const float w = j < G - 1 ? (float)(fs[j] * t_de[j] * t_ie2[j] * sW) : 0.f;
-      W[j] = w;
-      if (tile && mode == kTcTf32) {
-        *reinterpret_cast<float*>(tile + tc_operand_byte_offset(m, j, kTcCols, g.Gp, 4, false)) = tf32_rna(w);
-      } else if (tile) {
-        const __nv_bfloat16 hi = __float2bfloat16_rn(w);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(w - __bfloat162float(hi));
-        *reinterpret_cast<uint16_t*>(tile + tc_operand_byte_offset(m, j, kTcCols, g.Gp, 2, false)) =
-            __bfloat16_as_ushort(hi);
-        *reinterpret_cast<uint16_t*>(tile + tc_operand_byte_offset(m, j, kTcCols, g.Gp, 2, true)) =
-            __bfloat16_as_ushort(lo);
+    if (tile && mode == kTcTf32) {
+      for (int j = lane; j < g.Gp; j += 32)
+        *reinterpret_cast<float*>(tile + tc_operand_byte_offset(m, j, kTcCols, g.Gp, 4, false)) = tf32_rna(wval(j));
+    } else if (tile) {
+      // eight consecutive K columns of a row are one 16-byte row of a core
+      // matrix: hi and lo parts written as 16-byte words
+      for (int q = lane; q < g.Gp / 8; q += 32) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float w0 = wval(8 * q + 2 * e), w1 = wval(8 * q + 2 * e + 1);
+          const __nv_bfloat16 h0 = __float2bfloat16_rn(w0), h1 = __float2bfloat16_rn(w1);
+          const __nv_bfloat16 l0 = __float2bfloat16_rn(w0 - __bfloat162float(h0));
+          const __nv_bfloat16 l1 = __float2bfloat16_rn(w1 - __bfloat162float(h1));
+          hi[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+          lo[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+        }
+        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, g.Gp, 2, false)) =
+            make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, g.Gp, 2, true)) =
+            make_uint4(lo[0], lo[1], lo[2], lo[3]);
       }
     }
     // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k (microphysics.h:516-523 feeds them to numeric_model.h:271)
     const double* ns = nph + (size_t)s * F;
-    const double* dnu = T.ft(kTabDnuNu);
-    int uexp = 0;
-    for (int k = tid; k < F; k += kPrepThreads) uexp = max(uexp, exp_field(ns[k] * dnu[k]));
-    uexp = block_max_exp(uexp, red);
-    const double su = scale_from_exp(uexp);
+    const float* m_u = g.tmant + (size_t)kM32DnuNu * g.Tm;
+    const int* e_u = g.texp + (size_t)kM32DnuNu * g.Tm;
+    int uexp = kExpZero;
+    for (int k = lane; k < F; k += 32) {
+      int e;
+      const float mn = f64_mant(ns[k], e);
+      e += e_u[k];
+      mant_mul(mn, m_u[k], e);
+      if (mn != 0.f) uexp = max(uexp, e);
+    }
+    uexp = __reduce_max_sync(0xffffffffu, uexp);
+    if (uexp == kExpZero) uexp = 0;
     float* U = S.U32 + (size_t)s * F;
-    for (int k = tid; k < F; k += kPrepThreads) U[k] = (float)(ns[k] * dnu[k] * su);
-    if (tid == 0) {
-      scal[kScalSW] = 3. / 4. * sigma_T * c_light * unscale_from_exp(Wexp);
-      scal[kScalSU] = unscale_from_exp(uexp);
+    for (int k = lane; k < F; k += 32) {
+      int e;
+      const float mn = f64_mant(ns[k], e);
+      e += e_u[k];
+      U[k] = f32_ldexp(mant_mul(mn, m_u[k], e), e - uexp);
+    }
+    if (lane == 0) {
+      scal[kScalSW] = 3. / 4. * sigma_T * c_light * f64_pow2(Wexp);
+      scal[kScalSU] = f64_pow2(uexp);
     }
   }
-  if (tid == 0) {
+  if (lane == 0) {
     // synchrotron kernel constants (kernels.h:194-202, 427, 471)
     const double B = want_syn ? Bf[s] : 1.;
     const bool dermer = syn_method == PBAG_SYN_DER09;
-    const double sqrt3 = 1.7320508075688772;
-    scal[kScalPref] = dermer ? sqrt3 * pow(q_e, 3.) * B / (m_e * c_light * c_light) : sqrt3 * pow(q_e, 3.) * B / mec2;
-    scal[kScalSw] = unscale_from_exp(wexp);
-    const float incrit = (float)((4. * M_PI * m_e * c_light) / (3. * q_e * B));
+    scal[kScalPref] = (dermer ? kPrefDer : kPrefCsyn) * B;
+    scal[kScalSw] = f64_pow2(wexp);
+    const float Bf32 = (float)B;
+    const float incrit = kIncrit32 / Bf32;
     float* rp = S.rad32 + (size_t)s * 4;
     rp[0] = incrit;
-    rp[1] = (float)((2. * pi_ * m_e * c_light) / (3. * q_e * B));
+    rp[1] = kNuL32 / Bf32;
     rp[2] = cbrtf(incrit);
     rp[3] = 0.f;
     S.flags[s] = kFlagActive;
@@ -141,23 +190,19 @@ __global__ void k_contract_syn_out(int n, int F, DevState S, double* __restrict_
   if (bad_value(js) && atomicCAS(&S.err[4 * s], 0, PBAG_ERR_NONFINITE) == 0) S.err[4 * s + 2] = __LINE__;
 }
 
-__global__ void k_contract_first_failure(const int* __restrict__ err, int n, int* __restrict__ out) {
-  __shared__ int best[256];
-  int b = INT_MAX;
-  for (int s = threadIdx.x; s < n; s += blockDim.x)
-    if (err[4 * s] != 0) b = min(b, s);
-  best[threadIdx.x] = b;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) best[threadIdx.x] = min(best[threadIdx.x], best[threadIdx.x + o]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const int s = best[0];
-    out[0] = s == INT_MAX ? PBAG_OK : err[4 * s];
-    out[1] = s == INT_MAX ? -1 : s;
-    out[2] = s == INT_MAX ? 0 : err[4 * s + 2];
-  }
+// The first failing state (smallest index with an error code): every state
+// checked in parallel, the minimum index kept in out[3] (set to a value >= n
+// before), then code, index and site into out[0..2].
+__global__ void k_contract_fail_scan(const int* __restrict__ err, int n, int* __restrict__ out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    if (err[4 * s] != 0) atomicMin(&out[3], s);
+}
+__global__ void k_contract_fail_pick(const int* __restrict__ err, int n, int* __restrict__ out) {
+  const int s = out[3];
+  const bool any = s >= 0 && s < n;  // an index outside [0, n): no state failed
+  out[0] = any ? err[4 * s] : PBAG_OK;
+  out[1] = any ? s : -1;
+  out[2] = any ? err[4 * s + 2] : 0;
 }
 
 // Per-context workspace of pbag_contract, grown on demand.
@@ -234,8 +279,8 @@ int contract_prepare(pbag_ctx* ctx, const CtxView& v, int n, const double* d_f, 
   if (e != cudaSuccess) return cuda_status(e);
   *S = ws->S;
   *Wt = ws->Wt;
-  k_contract_prep<<<n, kPrepThreads, 0, v.stream>>>(v.dg, n, d_f, nullptr, d_nph, PBAG_SYN_CSYN, kTcSplit, 0, 1,
-                                                     ws->S, ws->Wt, ws->prm);
+  k_contract_prep<<<(n + kPrepWarps - 1) / kPrepWarps, 32 * kPrepWarps, 0, v.stream>>>(
+      v.dg, n, d_f, nullptr, d_nph, PBAG_SYN_CSYN, kTcSplit, 0, 1, ws->S, ws->Wt, ws->prm);
   return cudaGetLastError() == cudaSuccess ? PBAG_OK : PBAG_ERR_CUDA;
 }
 }  // namespace pbag
@@ -285,8 +330,9 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   auto ok = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
   };
-  k_contract_prep<<<n, kPrepThreads, 0, s>>>(v.dg, n, d_f, d_B, d_nph, syn_method, mode, d_jsyn ? 1 : 0,
-                                              d_jssc ? 1 : 0, S, tc && d_jssc ? ws->Wt : nullptr, ws->prm);
+  k_contract_prep<<<(n + kPrepWarps - 1) / kPrepWarps, 32 * kPrepWarps, 0, s>>>(
+      v.dg, n, d_f, d_B, d_nph, syn_method, mode, d_jsyn ? 1 : 0, d_jssc ? 1 : 0, S, tc && d_jssc ? ws->Wt : nullptr,
+      ws->prm);
   ok(cudaGetLastError());
   // synchrotron sums (and the CUDA-core SSC contraction in FP32)
   const bool fp32_ssc = d_jssc && !tc;
@@ -299,7 +345,9 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
     k_contract_syn_out<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, v.F, S, d_jsyn);
     ok(cudaGetLastError());
   }
-  k_contract_first_failure<<<1, 256, 0, s>>>(S.err, n, ws->fail);
+  ok(cudaMemsetAsync(ws->fail + 3, 0x7f, sizeof(int), s));  // 0x7f7f7f7f: above any state index
+  k_contract_fail_scan<<<(unsigned)std::min((n + 255) / 256, 1184), 256, 0, s>>>(S.err, n, ws->fail);
+  k_contract_fail_pick<<<1, 1, 0, s>>>(S.err, n, ws->fail);
   ok(cudaGetLastError());
   int fail[3] = {0, -1, 0};
   ok(cudaMemcpyAsync(fail, ws->fail, sizeof(fail), cudaMemcpyDeviceToHost, s));

@@ -513,6 +513,32 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     ok(c->grid_upload(&d.hnu, hnu));
   }
   ok(c->grid_upload(&d.ssa_nu, ssa_nu));
+  {
+    // mantissa / exponent tables (f64_mant) of dgamma, dgamma/gamma^2, dnu/nu
+    d.Tm = std::max(G, F);
+    std::vector<float> tm((size_t)kM32 * d.Tm, 0.f);
+    std::vector<int> te((size_t)kM32 * d.Tm, kExpZero);
+    auto put = [&](int t, int i, double x) {
+      if (x == 0.) return;
+      int ex = 0;
+      const double fr = std::frexp(x, &ex);  // x = fr 2^ex, |fr| in [0.5, 1)
+      float m = (float)(2. * fr);
+      int e2 = ex - 1;
+      if (std::fabs(m) >= 2.f) {
+        m *= 0.5f;
+        ++e2;
+      }
+      tm[(size_t)t * d.Tm + i] = m;
+      te[(size_t)t * d.Tm + i] = e2;
+    };
+    for (int j = 0; j < G - 1; ++j) {
+      put(kM32De, j, de[j]);
+      put(kM32DeIe2, j, de[j] * inv_e2[j]);
+    }
+    for (int k = 0; k < F; ++k) put(kM32DnuNu, k, dnu[k]);
+    ok(c->grid_upload(&d.tmant, tm));
+    ok(c->grid_upload(&d.texp, te));
+  }
   // the evolve kernel's tables in one block (GridTab layout)
   d.Ge = (G + 1) / 2 * 2;
   d.Fe = (F + 1) / 2 * 2;

@@ -58,7 +58,14 @@ struct DevGrid {
   const double* etab;    // the FP64 tables of the evolve kernel in one block (GridTab), staged by one bulk copy
   int Ge, Fe;            // G and F rounded up to even (sub-table strides of etab)
   int etab_doubles;      // size of etab: kTabG * Ge + kTabF * Fe
+  // grid factors as FP32 mantissa in [1, 2) times a power of two (f64_mant),
+  // for products with FP64 state values computed without FP64 arithmetic:
+  // tables kM32De (dgamma), kM32DeIe2 (dgamma / gamma^2), kM32DnuNu (dnu / nu)
+  int Tm;                // table stride: max(G, F)
+  const float* tmant;    // [3][Tm]
+  const int* texp;       // [3][Tm]
 };
+enum : int { kM32De = 0, kM32DeIe2, kM32DnuNu, kM32 };
 
 // Layout of DevGrid::etab: G tables at t * Ge, then F tables at kTabG * Ge + u * Fe.
 enum : int {
@@ -211,6 +218,80 @@ __device__ __forceinline__ int exp_field(double v) { return (__double2hiint(v) >
 __device__ __forceinline__ double scale_from_exp(int E) {
   return (E <= 26 || E >= 2019) ? 1. : __hiloint2double((2045 - E) << 20, 0);
 }
+// ---- FP64 values through FP32 and integer arithmetic -----------------------
+// FP64 arithmetic is slow on this GPU; products of FP64 state values with grid
+// factors that only need FP32 accuracy (tensor-core operands, FP32 sums) are
+// formed as mantissa x power of two.
+constexpr int kExpZero = -100000;  // exponent of a zero (or FP64-subnormal) value
+// x = m 2^e with |m| in [1, 2) rounded to FP32 (nearest even); zero and FP64
+// subnormals give m = 0, e = kExpZero; inf / NaN give m = inf / NaN, e = 0
+__device__ __forceinline__ float f64_mant(double x, int& e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  if (ex == 0) {
+    e = kExpZero;
+    return 0.f;
+  }
+  if (ex == 0x7ff) {
+    e = 0;
+    return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+  }
+  unsigned long long r = m >> 29;
+  const unsigned long long rem = m & 0x1fffffffull;
+  if (rem > 0x10000000ull || (rem == 0x10000000ull && (r & 1ull))) ++r;
+  e = ex - 1023;
+  if (r == (1ull << 23)) {
+    r = 0;
+    ++e;
+  }
+  return __uint_as_float(sign | (127u << 23) | (unsigned)r);
+}
+// the product of two mantissas (|m| in [1, 2) each) renormalised to [1, 2),
+// its exponent added to e
+__device__ __forceinline__ float mant_mul(float a, float b, int& e) {
+  float p = a * b;
+  if (fabsf(p) >= 2.f) {
+    p *= 0.5f;
+    ++e;
+  }
+  return p;
+}
+// m 2^e as FP32 for |m| < 4 (or 0, inf, NaN: unchanged); below the FP32 normal
+// range: zero
+__device__ __forceinline__ float f32_ldexp(float m, int e) {
+  const unsigned u = __float_as_uint(m);
+  const int ex = (int)((u >> 23) & 0xff);
+  if (ex == 0 || ex == 0xff) return m;
+  const int ne = ex + e;
+  if (ne <= 0) return __uint_as_float(u & 0x80000000u);
+  if (ne >= 255) return __uint_as_float((u & 0x80000000u) | 0x7f800000u);
+  return __uint_as_float((u & 0x807fffffu) | ((unsigned)ne << 23));
+}
+// m 2^e as FP64 built from the bits (m an FP32 value, finite or not), without
+// FP64 arithmetic; zero below the FP64 normal range
+__device__ __forceinline__ double f64_from_mant(float m, int e) {
+  const unsigned u = __float_as_uint(m);
+  const int ex = (int)((u >> 23) & 0xff);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (ex == 0) return __longlong_as_double((long long)sign);
+  if (ex == 0xff)
+    return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+  const int ne = ex - 127 + e + 1023;
+  if (ne <= 0) return __longlong_as_double((long long)sign);
+  if (ne >= 2047) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)ne << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// 2^e in FP64, e clamped to the normal range
+__device__ __forceinline__ double f64_pow2(int e) {
+  e = e < -1022 ? -1022 : e > 1023 ? 1023 : e;
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
 // the exact inverse of scale_from_exp(E)
 __device__ __forceinline__ double unscale_from_exp(int E) {
   return (E <= 26 || E >= 2019) ? 1. : __hiloint2double((E + 1) << 20, 0);

@@ -45,6 +45,12 @@ struct TcRows {
 cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
                                const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
                                int ostride, double* out, int* err, cudaStream_t st, TcRows rows = TcRows{});
+// the same contraction with blastwaves on the accumulator rows (pbag_ssc_rows.cu;
+// F = 128, BF16 or split BF16), chosen by launch_ssc_tc_mode for large batches
+bool ssc_rows_supported(int F, int Gp, int mode);
+cudaError_t launch_ssc_rows(int mode, int Gp, const void* Wt, const void* Kt, int nrows, const int* flags,
+                            const float* U32, const double* scal, const double* oscale, int nout, int ostride,
+                            double* out, int* err, TcRows rows, cudaStream_t st);
 // K slabs as TF32 operands (FP32 values rounded to TF32, 4-byte layout, lo parts zero)
 void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32);
 

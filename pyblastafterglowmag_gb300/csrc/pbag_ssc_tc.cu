@@ -54,6 +54,7 @@ constexpr size_t kTcDynMax = 231424;       // dynamic shared memory of a CTA (22
 constexpr size_t kTcFixed = 1024 + 256;   // alignment slack, barriers and the tensor-memory slot
 constexpr size_t kTcUSmemMax = 64 * 1024; // largest U tile staged whole in shared memory
 constexpr int kTcURing = 2;               // otherwise: ring of U column blocks (16 blastwaves each)
+constexpr int kRowsMin = 2048;            // batches from this size on run with blastwaves on the rows
 
 // Dynamic shared memory of one launch: [body: ring of stages of [A hi | A lo (F
 // rows each) | B hi | B lo (N rows each)], reused by the product table][U: the
@@ -436,6 +437,8 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
                                int ostride, double* out, int* err, cudaStream_t st, TcRows rows) {
   if (nrows <= 0) return cudaSuccess;
   if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
+  if (nrows >= kRowsMin && ssc_rows_supported(F, Gp, mode))
+    return launch_ssc_rows(mode, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, st);
   const auto* w = static_cast<const unsigned char*>(Wt);
   const auto* k = static_cast<const unsigned char*>(Kt);
 #define PBAG_TC_CASE(HH, MM) \

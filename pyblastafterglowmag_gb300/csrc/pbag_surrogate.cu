@@ -244,10 +244,6 @@ __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ double warp_sum_d(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 __device__ __forceinline__ float warp_max(float v) {
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
@@ -311,7 +307,8 @@ __global__ void k_sur_fit(int n, int F, int per, const double* __restrict__ proj
 // Feature vector of each state (one warp per state). f, nph: rows of N(gamma)
 // and of the seed photon density (strides fs, ns); B: field (stride bs); proj:
 // the exact projections; fit: the baseline parameters. Standardised when
-// mean/stdv are given.
+// mean/stdv are given. The FP64 inputs enter through mantissa and exponent
+// (f64_mant): no FP64 arithmetic per element.
 __global__ void __launch_bounds__(32 * kSurWarps)
 k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const double* __restrict__ nph, int ns,
                const double* __restrict__ Bv, int bs, const double* __restrict__ proj, const float* __restrict__ fit,
@@ -322,27 +319,42 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
   __shared__ float feat_all[kSurWarps][kNin];
   float* feat = feat_all[warp];
   const int G = g.G, F = g.F;
-  const GridTab T{g.etab, g.Ge, g.Fe};
   const double* fr = f + (size_t)s * fs;
   const double* nr = nph + (size_t)s * ns;
+  constexpr float kLog10_2 = 0.30102999566f;
   // electron weights w_j = f_j dgamma_j, scaled by a power of two into FP32
-  int ex = 0;
-  for (int j = lane; j < G - 1; j += 32) ex = max(ex, exp_field(fr[j] * T.gt(kTabDe)[j]));
-  ex = __reduce_max_sync(0xffffffffu, ex);
-  const double sw = scale_from_exp(ex);
+  const float* m_de = g.tmant + (size_t)kM32De * g.Tm;
+  const int* e_de = g.texp + (size_t)kM32De * g.Tm;
+  auto wmant = [&](int j, int& e) {
+    const float mf = f64_mant(fr[j], e);
+    e += e_de[j];
+    return mant_mul(mf, m_de[j], e);
+  };
+  int wexp = kExpZero;
+  for (int j = lane; j < G - 1; j += 32) {
+    int e;
+    if (wmant(j, e) != 0.f) wexp = max(wexp, e);
+  }
+  wexp = __reduce_max_sync(0xffffffffu, wexp);
+  if (wexp == kExpZero) wexp = 0;
+  auto wval = [&](int j) {
+    int e;
+    const float m = wmant(j, e);
+    return f32_ldexp(m, e - wexp);
+  };
   float m0 = 0.f, m1 = 0.f;
   for (int j = lane; j < G - 1; j += 32) {
-    const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
+    const float w = wval(j);
     m0 += w;
-    m1 += w * -logf((float)T.gt(kTabInvE)[j]);
+    m1 += w * -0.5f * logf(g.ginv2[j]);
   }
   m0 = warp_sum(m0);
   m1 = warp_sum(m1);
   const float mu = m0 > 0.f ? m1 / m0 : 0.f;
   float c2 = 0.f, c3 = 0.f, c4 = 0.f, wmax = 0.f;
   for (int j = lane; j < G - 1; j += 32) {
-    const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
-    const float d = -logf((float)T.gt(kTabInvE)[j]) - mu;
+    const float w = wval(j);
+    const float d = -0.5f * logf(g.ginv2[j]) - mu;
     c2 += w * d * d;
     c3 += w * d * d * d;
     c4 += w * d * d * d * d;
@@ -355,8 +367,10 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
   if (lane == 0) {
     const float var = m0 > 0.f ? c2 / m0 : 0.f;
     const float sd = sqrtf(fmaxf(var, 1e-30f));
-    feat[kFtB] = log10f(fmaxf((float)Bv[(size_t)s * bs], 1e-30f));
-    feat[kFtMom] = m0 > 0.f ? log10f(m0) - (float)log10(sw) : kFloor;  // log10 of the unscaled N_e
+    int eb;
+    const float mb = f64_mant(Bv[(size_t)s * bs], eb);
+    feat[kFtB] = mb > 0.f ? log10f(mb) + eb * kLog10_2 : kFloor;
+    feat[kFtMom] = m0 > 0.f ? log10f(m0) + wexp * kLog10_2 : kFloor;  // log10 of the unscaled N_e
     feat[kFtMom + 1] = mu;
     feat[kFtMom + 2] = log10f(sd);
     feat[kFtMom + 3] = m0 > 0.f ? c3 / m0 / (sd * sd * sd) : 0.f;
@@ -364,28 +378,46 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
   }
   if (lane < kElePts) {
     const int j = (int)lrintf(lane * (float)(G - 2) / (float)(kElePts - 1));
-    const float w = (float)(fr[j] * T.gt(kTabDe)[j] * sw);
+    const float w = wval(j);
     feat[kFtEle + lane] = wmax > 0.f ? fmaxf(log10f(fmaxf(w / wmax, 1e-30f)), kFloor) : kFloor;
   }
   // seed photon shape on kSeedPts frequencies: u_k = n_k dnu_k / nu_k
-  int ue = 0;
-  for (int k = lane; k < F; k += 32) ue = max(ue, exp_field(nr[k] * T.ft(kTabDnuNu)[k]));
-  ue = __reduce_max_sync(0xffffffffu, ue);
-  const double su = scale_from_exp(ue);
+  const float* m_u = g.tmant + (size_t)kM32DnuNu * g.Tm;
+  const int* e_u = g.texp + (size_t)kM32DnuNu * g.Tm;
+  auto umant = [&](int k, int& e) {
+    const float mn = f64_mant(nr[k], e);
+    e += e_u[k];
+    return mant_mul(mn, m_u[k], e);
+  };
+  int uexp = kExpZero;
+  for (int k = lane; k < F; k += 32) {
+    int e;
+    if (umant(k, e) != 0.f) uexp = max(uexp, e);
+  }
+  uexp = __reduce_max_sync(0xffffffffu, uexp);
+  if (uexp == kExpZero) uexp = 0;
+  auto uval = [&](int k) {
+    int e;
+    const float m = umant(k, e);
+    return f32_ldexp(m, e - uexp);
+  };
   float umax = 0.f;
-  for (int k = lane; k < F; k += 32) umax = fmaxf(umax, (float)(nr[k] * T.ft(kTabDnuNu)[k] * su));
+  for (int k = lane; k < F; k += 32) umax = fmaxf(umax, uval(k));
   umax = warp_max(umax);
   for (int q = lane; q < kSeedPts; q += 32) {
-    const int k = q * F / kSeedPts;
-    const float u = (float)(nr[k] * T.ft(kTabDnuNu)[k] * su);
+    const float u = uval(q * F / kSeedPts);
     feat[kFtSeed + q] = umax > 0.f ? fmaxf(log10f(fmaxf(u / umax, 1e-30f)), kFloor) : kFloor;
   }
-  // band powers and the baseline's slope and curvature
-  const double P = lane < kNb ? proj[(size_t)s * kNproj + lane] : 0.;
-  double pm = P;
-  for (int o = 16; o > 0; o >>= 1) pm = fmax(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+  // band powers (log10 relative to the largest) and the baseline's slope and curvature
+  float lp = -1e30f;
   if (lane < kNb) {
-    feat[kFtBandP + lane] = pm > 0. ? fmaxf(log10f((float)fmax(P / pm, 1e-30)), kFloor) : kFloor;
+    int e;
+    const float m = f64_mant(proj[(size_t)s * kNproj + lane], e);
+    if (m > 0.f) lp = log10f(m) + e * kLog10_2;
+  }
+  const float lpmax = warp_max(lp);
+  if (lane < kNb) {
+    feat[kFtBandP + lane] = lpmax > -1e29f && lp > -1e29f ? fmaxf(lp - lpmax, kFloor) : kFloor;
     feat[kFtBeta + lane] = fit[(size_t)s * 2 * kNb + lane];
     feat[kFtGamma + lane] = fit[(size_t)s * 2 * kNb + kNb + lane];
   }
@@ -400,7 +432,8 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
 
 // Spectrum from the baseline band shapes plus the predicted log10 correction,
 // scaled to the exact band powers (one warp per state); error estimate from
-// the check frequencies; rows to recompute appended to list.
+// the check frequencies; rows to recompute appended to list. FP64 values are
+// formed from FP32 mantissas and integer exponents.
 __global__ void __launch_bounds__(32 * kSurWarps)
 k_sur_reconstruct(int F, int per, int n, const int* __restrict__ flags, const float* __restrict__ Y,
                   const float* __restrict__ base, const double* __restrict__ proj, const double* __restrict__ invdnu,
@@ -423,19 +456,27 @@ k_sur_reconstruct(int F, int per, int n, const int* __restrict__ flags, const fl
     const float sh = exp10f(fmaxf(base[(size_t)s * F + i] + y, -30.f));
     float sum = sh;
     for (int o = 1; o < per; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    const double Pb = Pp[i / per];
-    jr[i] = (Pb > 0. && sum > 0.f) ? Pb * (double)(sh / sum) * invdnu[i] : 0.;
+    int ep, ei;
+    const float mp = f64_mant(Pp[i / per], ep);
+    const float mi = f64_mant(invdnu[i], ei);
+    jr[i] = (mp > 0.f && sum > 0.f) ? f64_from_mant(mp * mi * (sh / sum), ep + ei) : 0.;
   }
   __syncwarp();
   if (live)
     for (int i = lane; i < F; i += 32) out[(size_t)s * F + i] = jr[i];
-  const double ex = Pp[kNmom + lane];  // one check per lane
-  const double d = jr[chk[lane]] - ex;
-  const double num = warp_sum_d(d * d), den = warp_sum_d(ex * ex);
+  // relative L2 distance at the check frequencies (one per lane), in FP32
+  // after a common power-of-two scaling
+  int ee, ej;
+  const float me = f64_mant(Pp[kNmom + lane], ee);
+  const float mj = f64_mant(jr[chk[lane]], ej);
+  int E = max(me != 0.f ? ee : kExpZero, mj != 0.f ? ej : kExpZero);
+  E = __reduce_max_sync(0xffffffffu, E);
+  const float a = f32_ldexp(me, ee - E), bq = f32_ldexp(mj, ej - E);
+  const float num = warp_sum((bq - a) * (bq - a)), den = warp_sum(a * a);
   if (lane == 0) {
-    const double e = den > 0. ? est_scale * sqrt(num / den) : (num > 0. ? 1e30 : 0.);
+    const float e = den > 0.f ? est_scale * sqrtf(num / den) : (num > 0.f ? 1e30f : 0.f);
     const bool finite = e == e && !isinf(e);
-    err[s] = finite ? (float)e : 1e30f;
+    err[s] = finite ? e : 1e30f;
     if (live && (!finite || e > tol)) list[atomicAdd(nfb, 1)] = s;
   }
 }

@@ -87,3 +87,31 @@ def test_contract_edge_cases(lib, oracle, cuda_device):
         ctx2.contract_device(2, d_f2.data_ptr(), 0, d_n2.data_ptr(), abi.PBAG_SYN_CSYN, abi.PBAG_PREC_TF32,
                              0, d_jc2.data_ptr())
     assert ei.value.code == abi.PBAG_ERR_UNSUPPORTED
+
+
+def test_large_batch_runs_with_blastwaves_on_rows(lib, oracle, cuda_device):
+    """From 2048 states on (nfreq 128) the SSC contraction runs with blastwaves
+    on the accumulator rows, the W rows resident and the slabs streamed: same
+    bar as the slab-per-CTA kernel, whose result it matches closely."""
+    import torch
+    n = 2300
+    g, f, B, nph, _, jssc_o = _case(oracle, 201, 128, n, seed=12)
+    ctx = lib.Context(g, cuda_device, ssc=True)
+    dev = torch.device("cuda", cuda_device)
+    d_f = torch.from_numpy(f).to(dev)
+    d_B = torch.from_numpy(B).to(dev)
+    d_n = torch.from_numpy(nph).to(dev)
+    for prec, tol in ((abi.PBAG_PREC_SPLIT_BF16, 1e-4), (abi.PBAG_PREC_BF16, 2e-2)):
+        d_jc = torch.zeros((n, 128), dtype=torch.float64, device=dev)
+        ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN, prec, 0,
+                            d_jc.data_ptr())
+        jc = d_jc.cpu().numpy()
+        rel, z = rel_l2_rows(jc, jssc_o)
+        assert z == 0 and rel.max() <= tol, (abi.PRECISION_NAMES[prec], rel.max())
+        # the first 2000 states alone take the slab-per-CTA kernel
+        m = 2000
+        d_small = torch.zeros((m, 128), dtype=torch.float64, device=dev)
+        ctx.contract_device(m, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN, prec, 0,
+                            d_small.data_ptr())
+        rel2, _ = rel_l2_rows(jc[:m], d_small.cpu().numpy())
+        assert rel2.max() <= 1e-5, (abi.PRECISION_NAMES[prec], rel2.max())
