@@ -327,6 +327,17 @@ int pbag_mlp_infer(pbag_mlp* net, int n, const float* d_x, float* d_y);
 int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t, const float* d_mask, float lr,
                         int update, float* loss);
 
+/* Contraction autotuner: the first tensor-core SSC contraction of a shape
+ * (precision, grid, outputs, batch size to a factor of two) launched outside
+ * a graph capture times the candidate kernels and shapes (slab per CTA, or
+ * blastwaves on rows with 1-3 slab chunks per copy and 2-8 CTAs per SM) on
+ * its own data and keeps the fastest for that shape, process-wide. On by
+ * default (environment PBAG_AUTOTUNE=0: off); pbag_autotune(0/1) switches it.
+ * pbag_autotune_report writes one line per tuned shape into buf (len bytes,
+ * NUL-terminated) and returns the full report's length. */
+int pbag_autotune(int enable);
+int pbag_autotune_report(char* buf, int len);
+
 /* The SSC surrogate of a context. Exact projections of the SSC spectrum on
  * the tensor cores (BF16): over PBAG_SUR_BANDS bands of nfreq/PBAG_SUR_BANDS
  * frequencies the band power P and the power-weighted first and second moments

@@ -84,6 +84,23 @@ def grids(grid):
     return gam, freq
 
 
+def autotune(enable=True):
+    """Switch the contraction autotuner (pbag_autotune) on or off."""
+    lib = load()
+    lib.pbag_autotune.argtypes = [C.c_int]
+    _check(lib.pbag_autotune(int(bool(enable))), "pbag_autotune")
+
+
+def autotune_report():
+    """The tuned contraction shapes, one line each (pbag_autotune_report)."""
+    lib = load()
+    lib.pbag_autotune_report.argtypes = [C.c_char_p, C.c_int]
+    n = lib.pbag_autotune_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib.pbag_autotune_report(buf, n + 1)
+    return buf.value.decode()
+
+
 def shock_limits(opts, gam, states, state=None):
     """pbag_shock_limits over a sequence of shock states of one blastwave.
 

@@ -24,6 +24,11 @@ using namespace pbag;
 
 namespace {
 
+__global__ void k_fill_flags(int* __restrict__ flags, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flags[i] = v;
+}
+
 template <typename T>
 cudaError_t dev_alloc(T** p, size_t n) {
   *p = nullptr;
@@ -329,6 +334,27 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
       if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
       c->graph_exec = nullptr;
       cudaGraph_t graph = nullptr;
+      // the contraction autotuner measures outside the capture: one SSC
+      // launch on this batch's buffers with every row active (the flags are
+      // saved and restored; the step writes the contraction's outputs before
+      // it reads them)
+      if (nbw > 0 && c->ssc_on_tensor_cores() && c->ssc_path != PBAG_SSC_SURROGATE) {
+        int* saved = nullptr;
+        if (cudaMalloc(&saved, (size_t)nbw * sizeof(int)) == cudaSuccess) {
+          cudaError_t te = cudaMemcpyAsync(saved, c->S.flags, (size_t)nbw * sizeof(int), cudaMemcpyDeviceToDevice,
+                                           c->stream);
+          if (te == cudaSuccess) {
+            k_fill_flags<<<(nbw + 255) / 256, 256, 0, c->stream>>>(c->S.flags, nbw, kFlagActive);
+            te = cudaGetLastError();
+          }
+          if (te == cudaSuccess)
+            te = launch_ssc_tc(c->dg, c->S, c->dg.Bt, nbw, c->ssc_path != PBAG_SSC_TC_BF16, c->stream);
+          cudaMemcpyAsync(c->S.flags, saved, (size_t)nbw * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+          const cudaError_t se = cudaStreamSynchronize(c->stream);
+          cudaFree(saved);
+          if (te != cudaSuccess || se != cudaSuccess) return PBAG_ERR_CUDA;
+        }
+      }
       if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBAG_ERR_CUDA;
       cudaError_t ce = cudaSuccess;
       for (int64_t s = 0; s < max_len && ce == cudaSuccess; ++s) {

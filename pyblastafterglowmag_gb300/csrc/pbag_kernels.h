@@ -47,10 +47,20 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
                                int ostride, double* out, int* err, cudaStream_t st, TcRows rows = TcRows{});
 // the same contraction with blastwaves on the accumulator rows (pbag_ssc_rows.cu;
 // F = 128, BF16 or split BF16), chosen by launch_ssc_tc_mode for large batches
+// cps: slab chunks per ring stage, ctas: CTAs the output groups aim at (0: defaults)
+struct RowsCfg {
+  int cps = 0;
+  int ctas = 0;
+};
 bool ssc_rows_supported(int F, int Gp, int mode);
 cudaError_t launch_ssc_rows(int mode, int Gp, const void* Wt, const void* Kt, int nrows, const int* flags,
                             const float* U32, const double* scal, const double* oscale, int nout, int ostride,
-                            double* out, int* err, TcRows rows, cudaStream_t st);
+                            double* out, int* err, TcRows rows, RowsCfg cfg, cudaStream_t st);
+// The contraction autotuner (pbag_ssc_tc.cu): per (mode, F, Gp, outputs,
+// batch-size octave) the kernel and its shape measured fastest on the first
+// launch outside a graph capture; on by default (ssc_tune_enable).
+void ssc_tune_enable(bool on);
+int ssc_tune_report(char* buf, int len);
 // K slabs as TF32 operands (FP32 values rounded to TF32, 4-byte layout, lo parts zero)
 void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std::vector<float>& Bt32);
 

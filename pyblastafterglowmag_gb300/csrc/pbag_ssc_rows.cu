@@ -26,7 +26,6 @@
 
 #include <algorithm>
 #include <cstdint>
-#include <cstdlib>
 
 #include "pbag.h"
 #include "pbag_kernels.h"
@@ -285,14 +284,11 @@ k_ssc_rows(const unsigned char* __restrict__ Wt, const unsigned char* __restrict
 template <int MODE>
 cudaError_t launch_rows(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
                         const float* U32, const double* scal, const double* oscale, int nout, int ostride, double* out,
-                        int* err, TcRows rows, cudaStream_t st) {
-  static const int cps_env = [] {
-    const char* e = std::getenv("PBAG_ROWS_CPS");
-    return e ? std::atoi(e) : 0;
-  }();
-  // three chunks per stage measured fastest (bulk copies cost a roughly fixed
-  // latency each, so fewer and larger ones win over a deeper ring)
-  RwPlan plan = rw_plan(Gp, MODE == kTcSplit, cps_env > 0 ? cps_env : 3);
+                        int* err, TcRows rows, RowsCfg cfg, cudaStream_t st) {
+  // three chunks per stage is the default (bulk copies cost a roughly fixed
+  // latency each, so fewer and larger ones win over a deeper ring); the
+  // autotuner of launch_ssc_tc_mode measures the alternatives
+  RwPlan plan = rw_plan(Gp, MODE == kTcSplit, cfg.cps > 0 ? cfg.cps : 3);
   if (plan.S < 2) plan = rw_plan(Gp, MODE == kTcSplit, 1);
   if (plan.S < 2) return cudaErrorInvalidConfiguration;
   static bool attr = false;
@@ -305,7 +301,8 @@ cudaError_t launch_rows(const unsigned char* Wt, const unsigned char* Kt, int Gp
   // groups of outputs: enough CTAs to fill the GPU several times over, at
   // least 8 outputs per CTA
   const int tiles = (nrows + kRwRows - 1) / kRwRows;
-  int groups = std::max(1, std::min((4 * 152 + tiles - 1) / tiles, nout / 8));
+  const int target = cfg.ctas > 0 ? cfg.ctas : 4 * 152;
+  int groups = std::max(1, std::min((target + tiles - 1) / tiles, nout / 8));
   const int gsz = (nout + groups - 1) / groups;
   groups = (nout + gsz - 1) / gsz;
   dim3 grid(tiles, groups);
@@ -323,14 +320,14 @@ bool ssc_rows_supported(int F, int Gp, int mode) {
 
 cudaError_t launch_ssc_rows(int mode, int Gp, const void* Wt, const void* Kt, int nrows, const int* flags,
                             const float* U32, const double* scal, const double* oscale, int nout, int ostride,
-                            double* out, int* err, TcRows rows, cudaStream_t st) {
+                            double* out, int* err, TcRows rows, RowsCfg cfg, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   const auto* w = static_cast<const unsigned char*>(Wt);
   const auto* k = static_cast<const unsigned char*>(Kt);
   if (mode == kTcSplit)
-    return launch_rows<kTcSplit>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, st);
+    return launch_rows<kTcSplit>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, cfg, st);
   if (mode == kTcBf16)
-    return launch_rows<kTcBf16>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, st);
+    return launch_rows<kTcBf16>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, cfg, st);
   return cudaErrorInvalidValue;
 }
 

@@ -29,9 +29,16 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 #include <vector>
 
+#include "pbag.h"
 #include "pbag_kernels.h"
 #include "pbag_tc.cuh"
 
@@ -432,13 +439,38 @@ void build_ssc_tc_operand_tf32(const std::vector<float>& K32, int F, int Gp, std
   }
 }
 
-cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
-                               const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
-                               int ostride, double* out, int* err, cudaStream_t st, TcRows rows) {
-  if (nrows <= 0) return cudaSuccess;
-  if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
-  if (nrows >= kRowsMin && ssc_rows_supported(F, Gp, mode))
-    return launch_ssc_rows(mode, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows, st);
+namespace {
+
+// ---- autotuner --------------------------------------------------------------
+// A choice of kernel for one contraction shape: the slab-per-CTA kernel, or
+// the blastwave-row kernel with its chunks per stage and CTA target.
+struct TcChoice {
+  int kind = 0;  // 0: slab per CTA, 1: blastwaves on rows
+  RowsCfg cfg;
+  float ms = -1.f;  // measured time (-1: default, not measured)
+};
+struct TcKey {
+  int mode, F, Gp, nout, octave;
+  bool operator<(const TcKey& o) const {
+    return std::tie(mode, F, Gp, nout, octave) < std::tie(o.mode, o.F, o.Gp, o.nout, o.octave);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TcKey, TcChoice> g_tune;
+bool g_tune_on = [] {
+  const char* e = std::getenv("PBAG_AUTOTUNE");
+  return !(e && e[0] == '0');
+}();
+
+int octave(int n) {
+  int o = 0;
+  while ((1 << (o + 1)) <= n) ++o;
+  return o;
+}
+
+cudaError_t launch_slab(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows, const int* flags,
+                        const float* U32, const double* scal, const double* oscale, int nout, int ostride, double* out,
+                        int* err, TcRows rows, cudaStream_t st) {
   const auto* w = static_cast<const unsigned char*>(Wt);
   const auto* k = static_cast<const unsigned char*>(Kt);
 #define PBAG_TC_CASE(HH, MM) \
@@ -457,6 +489,100 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
   return cudaErrorInvalidValue;
 }
 
+}  // namespace
+
+void ssc_tune_enable(bool on) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_on = on;
+}
+
+int ssc_tune_report(char* buf, int len) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string r;
+  for (const auto& kv : g_tune) {
+    char line[200];
+    std::snprintf(line, sizeof line, "mode=%d F=%d Gp=%d nout=%d rows~2^%d -> %s cps=%d ctas=%d %.3f ms\n",
+                  kv.first.mode, kv.first.F, kv.first.Gp, kv.first.nout, kv.first.octave,
+                  kv.second.kind ? "rows" : "slab", kv.second.cfg.cps, kv.second.cfg.ctas, kv.second.ms);
+    r += line;
+  }
+  if (buf && len > 0) {
+    std::strncpy(buf, r.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)r.size();
+}
+
+cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const void* Kt, int nrows,
+                               const int* flags, const float* U32, const double* scal, const double* oscale, int nout,
+                               int ostride, double* out, int* err, cudaStream_t st, TcRows rows) {
+  if (nrows <= 0) return cudaSuccess;
+  if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
+  const bool rows_ok = ssc_rows_supported(F, Gp, mode);
+  auto run = [&](const TcChoice& c) {
+    return c.kind ? launch_ssc_rows(mode, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
+                                    c.cfg, st)
+                  : launch_slab(mode, F, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
+                                st);
+  };
+  const TcKey key{mode, F, Gp, nout, octave(nrows)};
+  TcChoice choice;
+  bool known = false, tune = false;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      choice = it->second;
+      known = true;
+    }
+    tune = g_tune_on;
+  }
+  if (!known) {
+    choice.kind = nrows >= kRowsMin && rows_ok ? 1 : 0;  // the default without measurements
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    // candidates are timed only on rows whose output the caller discards or
+    // overwrites anyway (each launch writes the same values), never inside a
+    // graph capture, and never with a device-side row count (its rows are not
+    // known here)
+    if (tune && !rows.nlive && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+      std::vector<TcChoice> cand;
+      cand.push_back(TcChoice{});
+      if (rows_ok)
+        for (int cps : {1, 2, 3})
+          for (int ctas : {2 * 152, 4 * 152, 8 * 152}) {
+            TcChoice c;
+            c.kind = 1;
+            c.cfg.cps = cps;
+            c.cfg.ctas = ctas;
+            cand.push_back(c);
+          }
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+        float best = 1e30f;
+        for (TcChoice& c : cand) {
+          if (run(c) != cudaSuccess) continue;  // warm-up (a shape the kernel refuses is skipped)
+          cudaEventRecord(e0, st);
+          run(c);
+          cudaEventRecord(e1, st);
+          float ms = 0.f;
+          if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) continue;
+          c.ms = ms;
+          if (ms < best) {
+            best = ms;
+            choice = c;
+          }
+        }
+      }
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      cudaGetLastError();
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = choice;
+    }
+  }
+  return run(choice);
+}
+
 cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* Bt, int nbw, bool split,
                           cudaStream_t st) {
   if (!S.Abf || !Bt) return cudaErrorInvalidValue;
@@ -465,3 +591,14 @@ cudaError_t launch_ssc_tc(const DevGrid& g, const DevState& S, const uint16_t* B
 }
 
 }  // namespace pbag
+
+extern "C" {
+
+int pbag_autotune(int enable) {
+  pbag::ssc_tune_enable(enable != 0);
+  return PBAG_OK;
+}
+
+int pbag_autotune_report(char* buf, int len) { return pbag::ssc_tune_report(buf, len); }
+
+}  // extern "C"

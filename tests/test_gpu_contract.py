@@ -90,9 +90,10 @@ def test_contract_edge_cases(lib, oracle, cuda_device):
 
 
 def test_large_batch_runs_with_blastwaves_on_rows(lib, oracle, cuda_device):
-    """From 2048 states on (nfreq 128) the SSC contraction runs with blastwaves
-    on the accumulator rows, the W rows resident and the slabs streamed: same
-    bar as the slab-per-CTA kernel, whose result it matches closely."""
+    """Large batches (nfreq 128) run the SSC contraction with blastwaves on the
+    accumulator rows, the W rows resident and the slabs streamed (or the
+    slab-per-CTA kernel, whichever the autotuner measured faster): the plain
+    path's bar, and the same values as a smaller batch of the same states."""
     import torch
     n = 2300
     g, f, B, nph, _, jssc_o = _case(oracle, 201, 128, n, seed=12)
@@ -108,10 +109,31 @@ def test_large_batch_runs_with_blastwaves_on_rows(lib, oracle, cuda_device):
         jc = d_jc.cpu().numpy()
         rel, z = rel_l2_rows(jc, jssc_o)
         assert z == 0 and rel.max() <= tol, (abi.PRECISION_NAMES[prec], rel.max())
-        # the first 2000 states alone take the slab-per-CTA kernel
+        # the first 2000 states alone: another shape, tuned on its own
         m = 2000
         d_small = torch.zeros((m, 128), dtype=torch.float64, device=dev)
         ctx.contract_device(m, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN, prec, 0,
                             d_small.data_ptr())
         rel2, _ = rel_l2_rows(jc[:m], d_small.cpu().numpy())
         assert rel2.max() <= 1e-5, (abi.PRECISION_NAMES[prec], rel2.max())
+
+
+def test_autotuner_measures_and_keeps_a_choice(lib, oracle, cuda_device):
+    """The first contraction of a shape times the candidate kernels on its own
+    data and keeps the fastest; the result stays at the plain path's bar."""
+    import torch
+    n = 3000
+    g, f, B, nph, _, jssc_o = _case(oracle, 201, 128, n, seed=13)
+    ctx = lib.Context(g, cuda_device, ssc=True)
+    dev = torch.device("cuda", cuda_device)
+    d_f, d_B, d_n = (torch.from_numpy(a).to(dev) for a in (f, B, nph))
+    d_jc = torch.zeros((n, 128), dtype=torch.float64, device=dev)
+    lib.autotune(True)
+    ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN,
+                        abi.PBAG_PREC_SPLIT_BF16, 0, d_jc.data_ptr())
+    report = lib.autotune_report()
+    line = [ln for ln in report.splitlines() if "F=128" in ln and "nout=128" in ln and "2^11" in ln]
+    assert line and " ms" in line[0], report
+    assert float(line[0].split()[-2]) > 0.0, report  # a measured time, not the untuned default
+    rel, z = rel_l2_rows(d_jc.cpu().numpy(), jssc_o)
+    assert z == 0 and rel.max() <= 1e-4
