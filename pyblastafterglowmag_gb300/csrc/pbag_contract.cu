@@ -159,8 +159,8 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
   if (lane == 0) {
     // synchrotron kernel constants (kernels.h:194-202, 427, 471)
     const double B = want_syn ? Bf[s] : 1.;
-    const bool dermer = syn_method == PBAG_SYN_DER09;
-    scal[kScalPref] = (dermer ? kPrefDer : kPrefCsyn) * B;
+    const bool mcc = syn_method == PBAG_SYN_DER09 || syn_method == PBAG_SYN_BESSEL;
+    scal[kScalPref] = (mcc ? kPrefDer : kPrefCsyn) * B;
     scal[kScalSw] = f64_pow2(wexp);
     const float Bf32 = (float)B;
     const float incrit = kIncrit32 / Bf32;
@@ -295,7 +295,7 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   CtxView v;
   if (!ctx_view(ctx, &v) || n < 0) return PBAG_ERR_ARG;
   if (n > 0 && (!d_f || (d_jsyn && !d_B) || (d_jssc && !d_nph))) return PBAG_ERR_ARG;
-  if (syn_method != PBAG_SYN_CSYN && syn_method != PBAG_SYN_DER09) return PBAG_ERR_UNSUPPORTED;
+  if (syn_method < PBAG_SYN_CSYN || syn_method > PBAG_SYN_BESSEL) return PBAG_ERR_ARG;
   if (precision < PBAG_PREC_FP32 || precision > PBAG_PREC_TF32) return PBAG_ERR_ARG;
   const bool tc = precision != PBAG_PREC_FP32;
   if (d_jssc && !v.ssc) return PBAG_ERR_ARG;  // the context was created without SSC tables

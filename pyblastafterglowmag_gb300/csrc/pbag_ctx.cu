@@ -274,7 +274,7 @@ int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, c
     for (int b = 0; b < nbw; ++b) {
       const pbag_shock_params& p = prm_host[b];
       if (p.pp_on) return PBAG_ERR_UNSUPPORTED;
-      if (p.syn_method != PBAG_SYN_CSYN && p.syn_method != PBAG_SYN_DER09) return PBAG_ERR_UNSUPPORTED;
+      if (p.syn_method < PBAG_SYN_CSYN || p.syn_method > PBAG_SYN_BESSEL) return PBAG_ERR_ARG;
       if (p.ele_method != PBAG_ELE_NUMERIC && p.ele_method != PBAG_ELE_MIX) return PBAG_ERR_ARG;
       if (p.max_substeps < 1 || !(p.p > 0.) || !std::isfinite(p.p)) return PBAG_ERR_ARG;
       if (p.ssc_on && !c->ssc) return PBAG_ERR_ARG;
@@ -528,6 +528,20 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.ginv2, ginv2));
   ok(c->grid_upload(&d.psq32, psq));
   ok(c->grid_upload(&d.ginv23, ginv23));
+  {
+    // tabulated synchrotron functions of the GSL and Bessel methods
+    std::vector<float> lg(G);
+    for (int i = 0; i < G; ++i) lg[i] = (float)(-2. * std::log(e[i]));
+    ok(c->grid_upload(&d.lnginv2, lg));
+    std::vector<float> st = syn_table(PBAG_SYN_GSL), sb = syn_table(PBAG_SYN_BESSEL);
+    st.insert(st.end(), sb.begin(), sb.end());
+    ok(c->grid_upload(&d.syntab, st));
+    const double u0 = std::log(kSynTabXmin), h = (std::log(kSynTabXmax) - u0) / (kSynTabN - 1);
+    d.syn_u0 = (float)u0;
+    d.syn_ih = (float)(1. / h);
+    // GSL: x = (h nu / m_e c^2) / (1.5 B gamma^2 / 4.14e13) against nu / nu_crit = nu 4 pi m_e c / (3 q B gamma^2)
+    d.gsl_xs = (float)(cgs::h_by_mec2 * 4.14e13 / 1.5 / (4. * M_PI * cgs::m_e * cgs::c_light / (3. * cgs::q_e)));
+  }
   ok(c->grid_upload(&d.nu13, nu13));
   ok(c->grid_upload(&d.nu32, nu32));
   ok(c->grid_upload(&d.nu, nu));

@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "pbag.h"
+#include "pbag_internal.h"
 #include "pbag_const.h"
 
 namespace pbag {
@@ -41,6 +42,10 @@ struct DevGrid {
   const double* inv_dgb; // [G]   1/delta_grid_bar (numeric_model.h:556)
   const float* ginv2;    // [G]   1/e[j]^2 (FP32, synchrotron argument)
   const float* psq32;    // [G]   e[j]^2 - 1 in FP32 (cyclotron branch)
+  const float* lnginv2;  // [G]   ln(1/e[j]^2): argument of the tabulated synchrotron functions
+  const float* syntab;   // [2][kSynTabN] g(u) of the GSL and Bessel methods (pbag_syntab.cpp)
+  float syn_u0, syn_ih;  // first u of syntab and the inverse spacing
+  float gsl_xs;          // the GSL method's argument over nu / nu_crit (kernels.h:282-285)
   const float* ginv23;   // [G]   e[j]^(-2/3): cube root of the 1/e^2 factor of the synchrotron argument
   const double* nu;      // [F+1] frequency grid, nu[F] = next logspace point
   const float* nu13;     // [F]   cube root of nu
@@ -312,6 +317,19 @@ __device__ __forceinline__ float aharonian_R32(float x, float y) {
   float num = fmaf(0.347f, y4, fmaf(2.21f, y2, 1.f));
   float den = fmaf(0.217f, y4, fmaf(1.353f, y2, 1.f));
   return 1.808f * y * rsqrtf(fmaf(3.4f, y2, 1.f)) * __fdividef(num, den) * expf(-x);
+}
+
+// Tabulated synchrotron function (GSL or Bessel method): R(x) = g(ln x)
+// x^(1/3), g interpolated linearly in u = ln x; lx = ln x, x13 = x^(1/3).
+__device__ __forceinline__ float tabulated_R32(const float* __restrict__ tab, float u0, float ih, float lx,
+                                               float x13) {
+  if (!(lx == lx)) return lx;  // NaN propagates
+  const float p = (lx - u0) * ih;
+  if (p >= (float)(kSynTabN - 1)) return 0.f;
+  if (p <= 0.f) return __ldg(tab) * x13;
+  const int i = (int)p;
+  const float f = p - (float)i, a = __ldg(tab + i), b = __ldg(tab + i + 1);
+  return fmaf(f, b - a, a) * x13;
 }
 
 // Cyclotron branch of cycSynch (kernels.h:428-435) for gamma <= 2.

@@ -47,10 +47,13 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
                                int ostride, double* out, int* err, cudaStream_t st, TcRows rows = TcRows{});
 // the same contraction with blastwaves on the accumulator rows (pbag_ssc_rows.cu;
 // F = 128, BF16 or split BF16), chosen by launch_ssc_tc_mode for large batches
-// cps: slab chunks per ring stage, ctas: CTAs the output groups aim at (0: defaults)
+// cps: slab chunks per ring stage, ctas: CTAs the output groups aim at (0:
+// defaults), lsu: slab stages by 16-byte asynchronous copies of a whole warp
+// instead of one bulk copy
 struct RowsCfg {
   int cps = 0;
   int ctas = 0;
+  int lsu = 0;
 };
 bool ssc_rows_supported(int F, int Gp, int mode);
 cudaError_t launch_ssc_rows(int mode, int Gp, const void* Wt, const void* Kt, int nrows, const int* flags,

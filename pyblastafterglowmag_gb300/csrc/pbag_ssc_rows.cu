@@ -55,6 +55,7 @@ __host__ __device__ constexpr uint32_t rw_stage(bool split, int cps) {
 }
 constexpr size_t kRwDynMax = 231424;
 constexpr int kRwMaxStages = 14;
+constexpr int kRwLsuDepth = 3;  // stages of 16-byte copies in flight per copy warp
 
 struct RwPlan {
   int S, cps;
@@ -75,7 +76,7 @@ inline RwPlan rw_plan(int Gp, bool split, int cps) {
 template <int MODE>
 __global__ void __launch_bounds__(kRwThreads, 1)
 k_ssc_rows(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int gsz,
-           int nout, int S, int cps, const int* __restrict__ flags, const float* __restrict__ U32,
+           int nout, int S, int cps, int lsu, const int* __restrict__ flags, const float* __restrict__ U32,
            const double* __restrict__ scal, const double* __restrict__ oscale, int ostride, double* __restrict__ out,
            int* __restrict__ err, const int* __restrict__ nlive, const int* __restrict__ rowmap) {
   constexpr bool kSplit = MODE == kTcSplit;
@@ -146,25 +147,67 @@ k_ssc_rows(const unsigned char* __restrict__ Wt, const unsigned char* __restrict
         if (kSplit)
           tc::bulk_g2s(smem_u32(As + (size_t)c * kAChunk + part), src + (size_t)kTcCols * kc * 16, part, abar);
       }
-      int g = 0;
-      for (; g < total && !fail; ++g) {
+    }
+    // the slab stages: source, bytes
+    auto stage_src = [&](int g, uint32_t& bytes) {
+      const int ol = g / nst, c0 = (g % nst) * cps, c1 = min(c0 + cps, nchunks);
+      bytes = 0;
+      for (int c = c0; c < c1; ++c) bytes += (hi_only ? 1u : 2u) * kRwF * min(kRwK8, nk8 - c * kRwK8) * 16;
+      return Kt + (size_t)out_of(ol) * tc_tile_bytes(kRwF, Gp, 2) + (size_t)kRwChunkBytes * c0;
+    };
+    if (!lsu) {
+      // one bulk copy per stage, issued by one thread
+      if (lane == 0) {
+        int g = 0;
+        for (; g < total && !fail; ++g) {
+          const int s = g % S;
+          if (g >= S && !tc::mbar_wait_spin(empty(s), (uint32_t)(g / S - 1) & 1)) {
+            fail = 1;
+            break;
+          }
+          uint32_t bytes;
+          const unsigned char* src = stage_src(g, bytes);
+          tc::mbar_expect_tx(full(s), bytes);
+          tc::bulk_g2s(smem_u32(ring + (size_t)s * kStage), src, bytes, full(s));
+        }
+        // copies still in flight complete before the CTA exits (bounded waits)
+        for (int q = max(0, g - S); q < g; ++q) tc::mbar_wait(full(q % S), (uint32_t)(q / S) & 1);
+      }
+    } else {
+      // 16-byte asynchronous copies by the whole warp, kRwLsuDepth stages in
+      // flight; a stage is signalled (proxy fence, then one arrival) once its
+      // copies have landed
+      int g = 0, q = 0;
+      auto signal = [&](int qq) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(full(qq % S));
+      };
+      for (; g < total; ++g) {
         const int s = g % S;
-        if (g >= S && !tc::mbar_wait_spin(empty(s), (uint32_t)(g / S - 1) & 1)) {
-          fail = 1;
+        int stop = 0;
+        if (lane == 0) stop = fail || (g >= S && !tc::mbar_wait_spin(empty(s), (uint32_t)(g / S - 1) & 1));
+        stop = __shfl_sync(0xffffffffu, stop, 0);
+        if (stop) {
+          if (lane == 0) fail = 1;
           break;
         }
-        const int ol = g / nst, c0 = (g % nst) * cps, c1 = min(c0 + cps, nchunks);
-        uint32_t bytes = 0;
-        for (int c = c0; c < c1; ++c) bytes += (hi_only ? 1u : 2u) * kRwF * min(kRwK8, nk8 - c * kRwK8) * 16;
-        tc::mbar_expect_tx(full(s), bytes);
-        tc::bulk_g2s(smem_u32(ring + (size_t)s * kStage),
-                     Kt + (size_t)out_of(ol) * tc_tile_bytes(kRwF, Gp, 2) + (size_t)kRwChunkBytes * c0, bytes,
-                     full(s));
+        uint32_t bytes;
+        const unsigned char* src = stage_src(g, bytes);
+        const uint32_t dst = smem_u32(ring + (size_t)s * kStage);
+        for (uint32_t off = (uint32_t)lane * 16; off < bytes; off += 32 * 16)
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + off), "l"(src + off) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (g - q + 1 > kRwLsuDepth) {
+          asm volatile("cp.async.wait_group %0;" ::"n"(kRwLsuDepth) : "memory");
+          signal(q++);
+        }
       }
-      // copies still in flight complete before the CTA exits (bounded waits)
-      for (int q = max(0, g - S); q < g; ++q) tc::mbar_wait(full(q % S), (uint32_t)(q / S) & 1);
-      tc::mbar_wait(abar, 0);
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      if (g == total)
+        while (q < g) signal(q++);
     }
+    if (lane == 0) tc::mbar_wait(abar, 0);
   } else if (warp == kRwEpiWarps) {
     // MMAs
     if (lane == 0) {
@@ -290,6 +333,8 @@ cudaError_t launch_rows(const unsigned char* Wt, const unsigned char* Kt, int Gp
   // autotuner of launch_ssc_tc_mode measures the alternatives
   RwPlan plan = rw_plan(Gp, MODE == kTcSplit, cfg.cps > 0 ? cfg.cps : 3);
   if (plan.S < 2) plan = rw_plan(Gp, MODE == kTcSplit, 1);
+  // the warp-copy path keeps kRwLsuDepth stages in flight and needs one more to refill
+  if (cfg.lsu && plan.S < kRwLsuDepth + 1) return cudaErrorInvalidConfiguration;
   if (plan.S < 2) return cudaErrorInvalidConfiguration;
   static bool attr = false;
   if (!attr) {
@@ -306,7 +351,8 @@ cudaError_t launch_rows(const unsigned char* Wt, const unsigned char* Kt, int Gp
   const int gsz = (nout + groups - 1) / groups;
   groups = (nout + gsz - 1) / gsz;
   dim3 grid(tiles, groups);
-  k_ssc_rows<MODE><<<grid, kRwThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, gsz, nout, plan.S, plan.cps, flags, U32, scal,
+  k_ssc_rows<MODE><<<grid, kRwThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, gsz, nout, plan.S, plan.cps, cfg.lsu, flags,
+                                                        U32, scal,
                                                         oscale, ostride, out, err, rows.nlive, rows.rowmap);
   return cudaGetLastError();
 }

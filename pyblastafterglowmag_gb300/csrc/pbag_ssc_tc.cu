@@ -501,9 +501,10 @@ int ssc_tune_report(char* buf, int len) {
   std::string r;
   for (const auto& kv : g_tune) {
     char line[200];
-    std::snprintf(line, sizeof line, "mode=%d F=%d Gp=%d nout=%d rows~2^%d -> %s cps=%d ctas=%d %.3f ms\n",
+    std::snprintf(line, sizeof line, "mode=%d F=%d Gp=%d nout=%d rows~2^%d -> %s cps=%d ctas=%d lsu=%d %.3f ms\n",
                   kv.first.mode, kv.first.F, kv.first.Gp, kv.first.nout, kv.first.octave,
-                  kv.second.kind ? "rows" : "slab", kv.second.cfg.cps, kv.second.cfg.ctas, kv.second.ms);
+                  kv.second.kind ? "rows" : "slab", kv.second.cfg.cps, kv.second.cfg.ctas, kv.second.cfg.lsu,
+                  kv.second.ms);
     r += line;
   }
   if (buf && len > 0) {
@@ -548,14 +549,16 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
       std::vector<TcChoice> cand;
       cand.push_back(TcChoice{});
       if (rows_ok)
-        for (int cps : {1, 2, 3})
-          for (int ctas : {2 * 152, 4 * 152, 8 * 152}) {
-            TcChoice c;
-            c.kind = 1;
-            c.cfg.cps = cps;
-            c.cfg.ctas = ctas;
-            cand.push_back(c);
-          }
+        for (int lsu : {0, 1})
+          for (int cps : {1, 2, 3})
+            for (int ctas : {2 * 152, 4 * 152, 8 * 152}) {
+              TcChoice c;
+              c.kind = 1;
+              c.cfg.cps = cps;
+              c.cfg.ctas = ctas;
+              c.cfg.lsu = lsu;
+              cand.push_back(c);
+            }
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
         float best = 1e30f;

@@ -186,8 +186,9 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
                 (s.ib1 > s.ib0 && bad_value(pl_branch_b(T, s, pp, s.ib0, Kb)));
   // synchrotron kernel constants (kernels.h:194-202, 427, 471)
   const double B = q.B;
-  const bool dermer = P.syn_method == PBAG_SYN_DER09;
-  s.pref = dermer ? sqrt3 * pow(q_e, 3.) * B / (m_e * c_light * c_light) : sqrt3 * pow(q_e, 3.) * B / mec2;
+  // Dermer09 and Bessel divide by m_e c c, CSYN and GSL by mec2 (kernels.h:342, 410, 427, 471)
+  const bool mcc = P.syn_method == PBAG_SYN_DER09 || P.syn_method == PBAG_SYN_BESSEL;
+  s.pref = mcc ? sqrt3 * pow(q_e, 3.) * B / (m_e * c_light * c_light) : sqrt3 * pow(q_e, 3.) * B / mec2;
   s.inv_ncrit = (float)((4. * M_PI * m_e * c_light) / (3. * q_e * B));
   s.inv_nlar = (float)((2. * pi_ * m_e * c_light) / (3. * q_e * B));
   s.dr = q.dr;
@@ -832,11 +833,15 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   const int G = g.G, F = g.F;
   if (!(S.flags[b] & kFlagActive)) return;
   const bool ssa = prm[b].ssa_on != 0;
-  const bool dermer = prm[b].syn_method == PBAG_SYN_DER09;
+  const int method = prm[b].syn_method;
+  // GSL and Bessel: the tabulated functions, no cyclotron branch
+  const bool tab = method == PBAG_SYN_GSL || method == PBAG_SYN_BESSEL;
+  const float* stab = g.syntab + (method == PBAG_SYN_BESSEL ? kSynTabN : 0);
+  const float xs = method == PBAG_SYN_GSL ? g.gsl_xs : 1.f;
   const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);
   const float incrit = rp.x, inlar = rp.y;
   const int kq = tid / kRadLanes, jl = tid % kRadLanes;
-  const int jcyc = dermer ? 0 : g.n_cyc;
+  const int jcyc = method == PBAG_SYN_CSYN ? g.n_cyc : 0;
   const float* w = S.w32 + (size_t)b * G;
   const float* v = S.v32 + (size_t)b * G;
   for (int r = 0; r < R; ++r) {
@@ -846,10 +851,13 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
     const float a_k = nu * incrit;          // x = a_k / e_j^2
     const float y_k = g.nu13[k] * rp.z;     // x^(1/3) = y_k e_j^(-2/3)
     const float xl = nu * inlar;
+    const float la = tab ? __logf(a_k * xs) : 0.f, y13 = tab ? cbrtf(a_k * xs) : 0.f;
     float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
     for (int j = jl; j < G - 1; j += kRadLanes) {
-      const float R_ = j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
-                                 : cyclotron_R32(__ldg(g.psq32 + j), xl);
+      const float R_ =
+          tab ? tabulated_R32(stab, g.syn_u0, g.syn_ih, la + __ldg(g.lnginv2 + j), y13 * __ldg(g.ginv23 + j))
+          : j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
+                      : cyclotron_R32(__ldg(g.psq32 + j), xl);
       acc = fmaf(R_, __ldg(w + j), acc);
       if (ssa) {  // Neumaier-compensated sum of the signed SSA terms
         const float x = R_ * __ldg(v + j);

@@ -137,3 +137,20 @@ def test_autotuner_measures_and_keeps_a_choice(lib, oracle, cuda_device):
     assert float(line[0].split()[-2]) > 0.0, report  # a measured time, not the untuned default
     rel, z = rel_l2_rows(d_jc.cpu().numpy(), jssc_o)
     assert z == 0 and rel.max() <= 1e-4
+
+
+@pytest.mark.parametrize("method", [abi.PBAG_SYN_DER09, abi.PBAG_SYN_GSL, abi.PBAG_SYN_BESSEL])
+def test_contract_synchrotron_methods(lib, oracle, cuda_device, method):
+    import torch
+    n = 50
+    g = CT.grid_desc(ngam=201, nfreq=128)
+    gam, freq = oracle.grids(g)
+    f, B = CT.states(gam, n, seed=14)
+    jsyn_o, _ = oracle.contract(g, f, B=B, ssc=False, syn_method=method, threads=os.cpu_count() or 1)
+    ctx = lib.Context(g, cuda_device, ssc=False)
+    dev = torch.device("cuda", cuda_device)
+    d_f, d_B = torch.from_numpy(f).to(dev), torch.from_numpy(B).to(dev)
+    d_js = torch.zeros((n, 128), dtype=torch.float64, device=dev)
+    ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), 0, method, abi.PBAG_PREC_FP32, d_js.data_ptr(), 0)
+    rel, z = rel_l2_rows(d_js.cpu().numpy(), jsyn_o)
+    assert z == 0 and rel.max() <= 1e-4, (method, rel.max())

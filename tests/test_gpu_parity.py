@@ -48,6 +48,14 @@ def test_tophat_dermer_mix(lib, oracle, cuda_device):
                                        ele_method=abi.PBAG_ELE_MIX))
 
 
+@pytest.mark.parametrize("method", [abi.PBAG_SYN_GSL, abi.PBAG_SYN_BESSEL])
+def test_tophat_gsl_bessel(lib, oracle, cuda_device, method):
+    """The GSL and Bessel synchrotron methods (tabulated in FP64 on the host,
+    interpolated on the device) with SSA, against the oracle's direct FP64
+    evaluation."""
+    _compare(lib, oracle, cases.tophat(lib, nsteps=120, ssa=True, syn_method=method))
+
+
 def test_gaussian_ssc(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
 
