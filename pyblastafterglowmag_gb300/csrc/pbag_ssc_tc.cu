@@ -364,6 +364,189 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
   }
 }
 
+// Small batches (N <= kSmallN blastwaves, F = 128, BF16 operands): the whole
+// kernel slab of output i arrives in ONE bulk copy and the N weight rows and
+// U rows by 16-byte asynchronous copies of all threads, so a CTA waits for one
+// copy latency instead of one per chunk and operand part; then all MMAs, and
+// the epilogue of k_ssc_tc. Shared memory: [slab: chunks of (hi | lo) F rows,
+// reused by the product table][W: chunks of (hi | lo) N rows][U: N x F][barrier].
+constexpr int kSmallN = 64;
+__host__ __device__ constexpr size_t small_slab_bytes(int Gp) { return (size_t)2 * kTcK * Gp * 2; }
+__host__ __device__ constexpr size_t small_w_bytes(int N, int Gp) { return (size_t)2 * N * Gp * 2; }
+inline size_t small_smem(int N, int Gp) {
+  return 1024 + small_slab_bytes(Gp) + small_w_bytes(N, Gp) + (size_t)N * kTcK * 4 + 64;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__ Kt, int Gp, int nrows, int N,
+               const int* __restrict__ flags, const float* __restrict__ U32, const double* __restrict__ scal,
+               const double* __restrict__ oscale, int ostride, double* __restrict__ out, int* __restrict__ err,
+               const int* __restrict__ nlive, const int* __restrict__ rowmap) {
+  constexpr int F = kTcK;
+  constexpr bool kSplit = MODE == kTcSplit;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ uint64_t abar;
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int i = blockIdx.x;
+  const int row0 = blockIdx.y * kTcCols;
+  if (nlive && row0 >= *nlive) return;
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  unsigned char* As = base;
+  unsigned char* Bs = base + small_slab_bytes(Gp);
+  float* Us = reinterpret_cast<float*>(Bs + small_w_bytes(N, Gp));
+  const int nk8 = Gp / 8, nchunks = (nk8 + kK8 - 1) / kK8;
+  if (tid == 0) {
+    fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&abar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const uint32_t bytes = (uint32_t)small_slab_bytes(Gp);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&abar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(As)),
+        "l"(Kt + (size_t)i * tc_tile_bytes(F, Gp, 2)), "r"(bytes), "r"(smem_u32(&abar))
+        : "memory");
+  }
+  // W rows [row0, row0 + N) of both parts of every chunk, and the U rows
+  const unsigned char* Wtile = Wt + (size_t)blockIdx.y * tc_tile_bytes(kTcCols, Gp, 2);
+  const int units = N * nk8 * 2;  // 16-byte units of W
+  for (int u = tid; u < units; u += kTcThreads) {
+    const int part = u % 2, q = u / 2, r = q % N, k16 = q / N;  // row, 16-byte K column
+    const int c = k16 / kK8, kk = k16 % kK8, kc = min(kK8, nk8 - c * kK8);
+    const size_t within = (size_t)((r >> 3) * kc + kk) * 128 + (size_t)(r & 7) * 16;
+    const unsigned char* src = Wtile + (size_t)2 * kTcCols * kK8 * 16 * c + (size_t)part * kTcCols * kc * 16 + within;
+    const uint32_t dst = smem_u32(Bs + (size_t)2 * N * kK8 * 16 * c + (size_t)part * N * kc * 16 + within);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  }
+  for (int u = tid; u < N * F / 4; u += kTcThreads) {
+    const int r = u / (F / 4), k4 = u % (F / 4);
+    const int gr = row0 + r < nrows ? row0 + r : row0;  // rows beyond the batch: any finite row
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(Us + (size_t)r * F + 4 * k4)),
+                 "l"(U32 + (size_t)gr * F + 4 * k4)
+                 : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  bool live[2];
+  double fac[2];
+  const double hnu = oscale[i];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int col = tid + q * kTcThreads, r = row0 + col;
+    const bool in = col < N && r < nrows;
+    live[q] = in && (flags[r] & kFlagActive);
+    fac[q] = in ? hnu * scal[(size_t)r * kScal + kScalSW] * scal[(size_t)r * kScal + kScalSU] : 0.;
+  }
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)N) ncols <<= 1;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  const int any = __syncthreads_or((live[0] || live[1]) ? 1 : 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  if (tid == 0) {
+    bool ok = mbar_wait(smem_u32(&abar), 0);
+    if (ok && any) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t idesc = idesc_mma(kTcK, N, false);
+      for (int c = 0; c < nchunks; ++c) {
+        const int kc = min(kK8, nk8 - c * kK8);
+        const uint32_t sbo = (uint32_t)kc * 128;
+        const uint32_t a_hi = smem_u32(As + (size_t)2 * F * kK8 * 16 * c), a_lo = a_hi + (uint32_t)F * kc * 16;
+        const uint32_t b_hi = smem_u32(Bs + (size_t)2 * N * kK8 * 16 * c), b_lo = b_hi + (uint32_t)N * kc * 16;
+        for (int s2 = 0; s2 < kc / 2; ++s2) {
+          const uint32_t ko = (uint32_t)s2 * 256;
+          mma_issue<false>(tmem, smem_desc(a_hi + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc,
+                           (c > 0 || s2 > 0) ? 1u : 0u);
+          if (kSplit) {
+            mma_issue<false>(tmem, smem_desc(a_hi + ko, 128, sbo), smem_desc(b_lo + ko, 128, sbo), idesc, 1u);
+            mma_issue<false>(tmem, smem_desc(a_lo + ko, 128, sbo), smem_desc(b_hi + ko, 128, sbo), idesc, 1u);
+          }
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&mbar))
+                   : "memory");
+      ok = mbar_wait(smem_u32(&mbar), 0);
+    }
+    if (!ok) {
+      fail = 1;
+      for (int col = 0; col < N; ++col) {
+        const int r = row0 + col;
+        if (r < nrows && (flags[r] & kFlagActive)) atomicCAS(&err[4 * (rowmap ? rowmap[r] : r)], 0, PBAG_ERR_TIMEOUT);
+      }
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (any && !fail) {
+    // products D[k][b] U[b][k] of this thread's row k, into a [b][k] table in
+    // the (now idle) slab memory; then the sum over k of each blastwave
+    float* P = reinterpret_cast<float*>(base);
+    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int cb = 0; cb < N / 16; ++cb) {
+      uint32_t v[16];
+      tc::tmem_ld16(tl + (uint32_t)(cb * 16), v);
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        P[(size_t)(cb * 16 + c) * kPStride + tid] = __uint_as_float(v[c]) * Us[(size_t)(cb * 16 + c) * F + tid];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (!live[q]) continue;
+      const int col = tid + q * kTcThreads;
+      const float* row = P + (size_t)col * kPStride;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 8
+      for (int k = 0; k < kTcK; k += 4) {
+        a0 += row[k];
+        a1 += row[k + 1];
+        a2 += row[k + 2];
+        a3 += row[k + 3];
+      }
+      const int orow = rowmap ? rowmap[row0 + col] : row0 + col;
+      out[(size_t)orow * ostride + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+  }
+}
+
+template <int MODE>
+cudaError_t launch_tc_small(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
+                            const float* U32, const double* scal, const double* oscale, int nout, int ostride,
+                            double* out, int* err, TcRows rows, cudaStream_t st) {
+  const int N = (nrows + 15) / 16 * 16;
+  if (N > kSmallN || small_smem(N, Gp) > kTcDynMax) return cudaErrorInvalidConfiguration;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_ssc_tc_small<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kTcDynMax);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_ssc_tc_small<MODE><<<dim3(nout, 1), kTcThreads, small_smem(N, Gp), st>>>(
+      Wt, Kt, Gp, nrows, N, flags, U32, scal, oscale, ostride, out, err, rows.nlive, rows.rowmap);
+  return cudaGetLastError();
+}
+
 template <int H, int MODE>
 cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, int nrows, const int* flags,
                       const float* U32, const double* scal, const double* oscale, int nout, int ostride, double* out,
@@ -445,7 +628,7 @@ namespace {
 // A choice of kernel for one contraction shape: the slab-per-CTA kernel, or
 // the blastwave-row kernel with its chunks per stage and CTA target.
 struct TcChoice {
-  int kind = 0;  // 0: slab per CTA, 1: blastwaves on rows
+  int kind = 0;  // 0: slab per CTA, 1: blastwaves on rows, 2: slab per CTA for small batches
   RowsCfg cfg;
   float ms = -1.f;  // measured time (-1: default, not measured)
 };
@@ -503,7 +686,7 @@ int ssc_tune_report(char* buf, int len) {
     char line[200];
     std::snprintf(line, sizeof line, "mode=%d F=%d Gp=%d nout=%d rows~2^%d -> %s cps=%d ctas=%d lsu=%d %.3f ms\n",
                   kv.first.mode, kv.first.F, kv.first.Gp, kv.first.nout, kv.first.octave,
-                  kv.second.kind ? "rows" : "slab", kv.second.cfg.cps, kv.second.cfg.ctas, kv.second.cfg.lsu,
+                  kv.second.kind == 1 ? "rows" : kv.second.kind == 2 ? "slab-small" : "slab", kv.second.cfg.cps, kv.second.cfg.ctas, kv.second.cfg.lsu,
                   kv.second.ms);
     r += line;
   }
@@ -520,12 +703,28 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
   if (nrows <= 0) return cudaSuccess;
   if (!Wt || !Kt || Gp % 16 != 0) return cudaErrorInvalidValue;
   const bool rows_ok = ssc_rows_supported(F, Gp, mode);
+  const bool small_ok = F == kTcK && nrows <= kSmallN && (mode == kTcSplit || mode == kTcBf16);
   auto run = [&](const TcChoice& c) {
+    const auto* w = static_cast<const unsigned char*>(Wt);
+    const auto* k = static_cast<const unsigned char*>(Kt);
+    if (c.kind == 2)
+      return mode == kTcSplit
+                 ? launch_tc_small<kTcSplit>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
+                                             st)
+                 : launch_tc_small<kTcBf16>(w, k, Gp, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
+                                            st);
     return c.kind ? launch_ssc_rows(mode, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
                                     c.cfg, st)
                   : launch_slab(mode, F, Gp, Wt, Kt, nrows, flags, U32, scal, oscale, nout, ostride, out, err, rows,
                                 st);
   };
+  // an explicit kernel choice (environment PBAG_TC_KERNEL = slab | rows |
+  // slab-small) overrides the tuner where that kernel takes the shape
+  if (const char* force = std::getenv("PBAG_TC_KERNEL")) {
+    TcChoice c;
+    c.kind = !std::strcmp(force, "rows") && rows_ok ? 1 : !std::strcmp(force, "slab-small") && small_ok ? 2 : 0;
+    if (c.kind || !std::strcmp(force, "slab")) return run(c);
+  }
   const TcKey key{mode, F, Gp, nout, octave(nrows)};
   TcChoice choice;
   bool known = false, tune = false;
@@ -548,6 +747,11 @@ cudaError_t launch_ssc_tc_mode(int mode, int F, int Gp, const void* Wt, const vo
     if (tune && !rows.nlive && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
       std::vector<TcChoice> cand;
       cand.push_back(TcChoice{});
+      if (small_ok) {
+        TcChoice c;
+        c.kind = 2;
+        cand.push_back(c);
+      }
       if (rows_ok)
         for (int lsu : {0, 1})
           for (int cps : {1, 2, 3})

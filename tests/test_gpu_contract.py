@@ -154,3 +154,22 @@ def test_contract_synchrotron_methods(lib, oracle, cuda_device, method):
     ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), 0, method, abi.PBAG_PREC_FP32, d_js.data_ptr(), 0)
     rel, z = rel_l2_rows(d_js.cpu().numpy(), jsyn_o)
     assert z == 0 and rel.max() <= 1e-4, (method, rel.max())
+
+
+@pytest.mark.parametrize("kernel", ["slab", "slab-small", "rows"])
+def test_every_contraction_kernel_on_a_small_batch(lib, oracle, cuda_device, monkeypatch, kernel):
+    """Each kernel the autotuner chooses from, forced on the same small batch
+    (40 states, 201 x 128), split and plain BF16, against the oracle."""
+    import torch
+    monkeypatch.setenv("PBAG_TC_KERNEL", kernel)
+    n = 40
+    g, f, B, nph, _, jssc_o = _case(oracle, 201, 128, n, seed=15)
+    ctx = lib.Context(g, cuda_device, ssc=True)
+    dev = torch.device("cuda", cuda_device)
+    d_f, d_B, d_n = (torch.from_numpy(a).to(dev) for a in (f, B, nph))
+    for prec, tol in ((abi.PBAG_PREC_SPLIT_BF16, 1e-4), (abi.PBAG_PREC_BF16, 2e-2)):
+        d_jc = torch.zeros((n, 128), dtype=torch.float64, device=dev)
+        ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), d_n.data_ptr(), abi.PBAG_SYN_CSYN, prec, 0,
+                            d_jc.data_ptr())
+        rel, z = rel_l2_rows(d_jc.cpu().numpy(), jssc_o)
+        assert z == 0 and rel.max() <= tol, (kernel, abi.PRECISION_NAMES[prec], rel.max())

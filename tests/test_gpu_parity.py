@@ -60,6 +60,12 @@ def test_gaussian_ssc(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
 
 
+def test_gaussian_ssc_small_batch_kernel(lib, oracle, cuda_device, monkeypatch):
+    """The step with the small-batch slab kernel forced for its SSC contraction."""
+    monkeypatch.setenv("PBAG_TC_KERNEL", "slab-small")
+    _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=60))
+
+
 def test_gaussian_late_window(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian_window(lib, start=380, nsteps=60))
 
