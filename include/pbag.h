@@ -44,7 +44,8 @@ enum pbag_status_code {
   PBAG_ERR_DLNVDT = -6,     /* dlnV/dt negative or not finite (microphysics.h:406) */
   PBAG_ERR_UNSUPPORTED = -7,/* option the GPU path does not implement          */
   PBAG_ERR_TIMEOUT = -8,    /* a bounded device-side wait ran out              */
-  PBAG_ERR_NOMEM = -9       /* device allocation failed                        */
+  PBAG_ERR_NOMEM = -9,      /* device allocation failed                        */
+  PBAG_ERR_RANGE = -10      /* frequency outside the grid (microphysics.h:1190-1201) */
 };
 
 /* ---- options (same meaning as the reference's parfile options) ----------- */
@@ -172,7 +173,8 @@ typedef struct pbag_limits {
 
 int pbag_abi_version(void);
 /* sizeof of the ABI structs, in the order grid_desc, shock_params, step_rec,
- * outputs, status, limits_opts, shock_state, limits (0..7); for binding checks. */
+ * outputs, status, limits_opts, shock_state, limits, flux_opts, flux_query
+ * (0..9); for binding checks. */
 size_t pbag_sizeof(int which);
 const char* pbag_status_string(int code);
 
@@ -326,6 +328,41 @@ int pbag_mlp_infer(pbag_mlp* net, int n, const float* d_x, float* d_y);
  * *loss (host, may be NULL) receives the loss. */
 int pbag_mlp_train_step(pbag_mlp* net, int n, const float* d_x, const float* d_t, const float* d_mask, float lr,
                         int update, float* loss);
+
+/* ---- EATS flux density from the histories (fluxDens) ---------------------
+ * The observer-frame flux density contribution of EATS cells from a batch's
+ * total_rad.j_all / a_all histories: ElectronAndRadiation::fluxDens
+ * (microphysics.h:1185-1217) - frequency index (findIndex), bilinear
+ * interpolation of j and a in (frequency, radius) between the history rows ia
+ * and ib of the cell's blastwave - followed by computeFluxDensity
+ * (microphysics.h:799-867): Doppler factor, lab-frame emissivity and
+ * absorption, shell thickness (Johannesson 2006, eq. 33), optical depth along
+ * the line of sight, intensity (computeIntensity, microphysics.h:11-58) and
+ * luminosity. One query per cell; queries are independent. FP64. */
+enum pbag_shock_vel { PBAG_VEL_SAME_AS_BW = 0, PBAG_VEL_SHOCK = 1 };             /* "method_vel"  */
+enum pbag_method_ne { PBAG_NE_USE_NPRIME = 0, PBAG_NE_USE_NE = 1 };             /* "method_ne"   */
+enum pbag_method_tau { PBAG_TAU_APPROX = 0, PBAG_TAU_THICK = 1, PBAG_TAU_SMOOTH = 2,
+                       PBAG_TAU_SHARP = 3 };                                     /* "method_tau"  */
+typedef struct pbag_flux_opts {
+  int32_t shock_vel, method_ne, method_tau, pad;
+} pbag_flux_opts;
+/* the arguments of fluxDens, in its order (rsh and dr as fluxDens names them;
+ * computeFluxDensity recomputes dr from ne, r, theta, ncells, Gamma, n_prime) */
+typedef struct pbag_flux_query {
+  int32_t bw;               /* blastwave of the batch                            */
+  int32_t ia, ib;           /* history rows (time indices) bracketing r          */
+  int32_t pad;
+  double theta, ncells, freq, Gamma, GammaSh, acc_fac, mu, r, rsh, dr, n_prime, ne;
+} pbag_flux_query;
+/* d_j_all, d_a_all: the batch's histories [nrec][nfreq] (offsets[] as for
+ * pbag_run_batch, host array of nbw+1); d_r_all: radius of every record
+ * [nrec]; d_q: nq queries; d_flux: nq results. Device pointers; synchronous.
+ * A query whose frequency is outside (freq[0], freq[F-1]) gives
+ * PBAG_ERR_RANGE, a negative or non-finite intensity or luminosity
+ * PBAG_ERR_NONFINITE, both with bw = its blastwave and step = its index. */
+int pbag_flux_dens(pbag_ctx* ctx, const pbag_flux_opts* opts, int nbw, const int64_t* offsets,
+                   const double* d_j_all, const double* d_a_all, const double* d_r_all, int nq,
+                   const pbag_flux_query* d_q, double* d_flux, pbag_status* st);
 
 /* Contraction autotuner: the first tensor-core SSC contraction of a shape
  * (precision, grid, outputs, batch size to a factor of two) launched outside

@@ -695,4 +695,97 @@ int orc_contract(const pbag_grid_desc* g, int n, const double* f, const double* 
   return PBAG_OK;
 }
 
+// ElectronAndRadiation::fluxDens (microphysics.h:1185-1217) with
+// computeFluxDensity (:799-867) and computeIntensity (:11-58), FP64, one query
+// at a time; the frequency grid and the histories of the query's blastwave.
+int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_t* offsets, const double* j_all,
+                  const double* a_all, const double* r_all, int nq, const pbag_flux_query* qs, double* flux,
+                  int* fail_index) {
+  const int F = g->nfreq;
+  std::vector<double> gam(g->ngam), nu(F + 1);
+  orc_build_grids(g, gam.data(), nu.data());
+  *fail_index = -1;
+  for (int t = 0; t < nq; ++t) {
+    const pbag_flux_query& q = qs[t];
+    flux[t] = 0.;
+    if (q.freq >= nu[F - 1] || q.freq <= nu[0]) {  // microphysics.h:1190-1201
+      *fail_index = t;
+      return PBAG_ERR_RANGE;
+    }
+    // findIndex (interpolators.h:13-35)
+    size_t ia_nu;
+    if (q.freq <= nu[0])
+      ia_nu = 0;
+    else if (q.freq >= nu[F - 1])
+      ia_nu = F - 2;
+    else {
+      unsigned a = 0, b = (unsigned)F - 1;
+      while (b - a > 1u) {
+        unsigned i = (b + a) >> 1;
+        if (nu[i] > q.freq)
+          b = i;
+        else
+          a = i;
+      }
+      ia_nu = a;
+    }
+    const size_t ib_nu = ia_nu + 1;
+    const int64_t r0 = offsets[q.bw];
+    // Interp2d::InterpolateBilinear / BilinearInterpolation (interpolators.h:708-801)
+    auto interp = [&](const double* Z) {
+      double q11 = Z[(r0 + q.ia) * F + ia_nu], q12 = Z[(r0 + q.ib) * F + ia_nu];
+      double q21 = Z[(r0 + q.ia) * F + ib_nu], q22 = Z[(r0 + q.ib) * F + ib_nu];
+      double x1 = nu[ia_nu], x2 = nu[ib_nu], y1 = r_all[r0 + q.ia], y2 = r_all[r0 + q.ib];
+      double x2x1 = x2 - x1, y2y1 = y2 - y1, x2x = x2 - q.freq, y2y = y2 - q.r, yy1 = q.r - y1, xx1 = q.freq - x1;
+      return 1.0 / (x2x1 * y2y1) * (q11 * x2x * y2y + q21 * xx1 * y2y + q12 * x2x * yy1 + q22 * xx1 * yy1);
+    };
+    const double em_prime = interp(j_all), abs_prime = interp(a_all);
+    auto beta_of = [](double gm) { return std::sqrt((gm - 1.) * (gm + 1.)) / gm; };  // blastwave_components.h:36
+    double beta = beta_of(q.Gamma);
+    double a = 1.0 - beta * q.mu;
+    double delta_D = q.Gamma * a;
+    double em_lab = em_prime / (delta_D * delta_D);
+    double abs_lab = abs_prime * delta_D;
+    double beta_shock = o->shock_vel == PBAG_VEL_SHOCK ? beta_of(q.GammaSh) : beta_of(q.Gamma);
+    double m2 = q.ne * m_p;
+    double dr = m2 / (2. * pi_ * m_p * q.r * q.r * (1. - std::cos(q.theta) / q.ncells) * q.Gamma * q.n_prime);
+    double dtau;
+    if (q.mu == beta_shock)
+      dtau = 1.0e100;
+    else
+      dtau = abs_lab * dr * (1. - q.mu * beta_shock) / (q.mu - beta_shock);
+    double intensity = em_lab;
+    if (dtau != 0) {
+      double thick = dtau > 0 ? em_lab / dtau : 0.;
+      double u = 1. / 2. + std::exp(-dtau) / dtau - (1 - std::exp(-dtau)) / (dtau * dtau);
+      double approx = dtau > 1.e-3 ? em_lab * (3. * u / dtau) : em_lab;
+      double abs_fac = dtau > 0.0 ? -std::expm1(-dtau) / dtau : std::expm1(dtau) / dtau;
+      double smooth = em_lab * abs_fac;
+      double sharp = em_lab;
+      if (dtau > 1.0)
+        sharp = em_lab / dtau;
+      else if (dtau < -1.0)
+        sharp = 0.0;
+      intensity = o->method_tau == PBAG_TAU_THICK    ? thick
+                  : o->method_tau == PBAG_TAU_SMOOTH ? smooth
+                  : o->method_tau == PBAG_TAU_SHARP  ? sharp
+                                                     : approx;
+    }
+    if (intensity < 0 || !std::isfinite(intensity)) {
+      *fail_index = t;
+      return PBAG_ERR_NONFINITE;
+    }
+    double ashock = 1.0 - q.mu * beta_shock;
+    double lum = o->method_ne == PBAG_NE_USE_NPRIME
+                     ? intensity * q.r * q.r * (dr / ashock)
+                     : intensity * q.ne / (2. * pi_ * (1. - std::cos(q.theta) / q.ncells)) / q.Gamma / ashock;
+    if (lum < 0 || !std::isfinite(lum)) {
+      *fail_index = t;
+      return PBAG_ERR_NONFINITE;
+    }
+    flux[t] = lum;
+  }
+  return PBAG_OK;
+}
+
 }  // extern "C"

@@ -36,6 +36,13 @@ int orc_ssc_kernel(const double* gam, int G, const double* freq, int F, double* 
 int orc_contract(const pbag_grid_desc* g, int n, const double* f, const double* B, const double* nph, int syn_method,
                  double* jsyn, double* jssc, int threads);
 
+/* fluxDens / computeFluxDensity (microphysics.h:799-867, 1185-1217) for nq
+ * queries over the histories of a batch; on a failure the failing query's
+ * index in *fail_index and the status code. */
+int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_t* offsets, const double* j_all,
+                  const double* a_all, const double* r_all, int nq, const pbag_flux_query* qs, double* flux,
+                  int* fail_index);
+
 /* Flags for orc_run. */
 enum {
   ORC_HOIST_HEATING = 1,  /* compute the (substep-invariant) cooling terms once per

@@ -63,6 +63,8 @@ class Oracle:
                                 P(abi.Outputs), C.c_int, C.c_int, C.c_int, P(abi.Status)]
         lib.orc_contract.argtypes = [P(abi.GridDesc), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                      C.c_void_p, C.c_void_p, C.c_int]
+        lib.orc_flux_dens.argtypes = [P(abi.GridDesc), P(abi.FluxOpts), P(C.c_int64), P(C.c_double), P(C.c_double),
+                                      P(C.c_double), C.c_int, C.c_void_p, P(C.c_double), P(C.c_int)]
         self.lib = lib
 
     def grids(self, grid):
@@ -119,6 +121,19 @@ class Oracle:
         return rc, (st.bw, st.step), arrays
 
 
+    def flux_dens(self, grid, opts, offsets, j_all, a_all, r_all, queries):
+        """orc_flux_dens: (status, failing query index, flux[nq])."""
+        q = np.ascontiguousarray(queries, dtype=abi.FLUX_QUERY_DTYPE)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        flux = np.zeros(len(q))
+        fail = C.c_int(-1)
+        rc = self.lib.orc_flux_dens(C.byref(grid), C.byref(opts), off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                    abi.dptr(np.ascontiguousarray(j_all)), abi.dptr(np.ascontiguousarray(a_all)),
+                                    abi.dptr(np.ascontiguousarray(r_all)), len(q), q.ctypes.data,
+                                    abi.dptr(flux), C.byref(fail))
+        return rc, fail.value, flux
+
+
 class Reference:
     def __init__(self, path=REF_SO):
         if not os.path.exists(path) and not build_reference():
@@ -134,6 +149,8 @@ class Reference:
             [C.c_double, C.c_double, C.c_int, P(C.c_double), P(C.c_double)]
         lib.ref_run.argtypes = [P(abi.GridDesc), C.c_void_p, C.c_int, P(C.c_int64), C.c_void_p,
                                 P(abi.Outputs)]
+        lib.ref_flux_dens.argtypes = [P(abi.GridDesc), P(abi.FluxOpts), C.c_int, P(C.c_double), P(C.c_double),
+                                      P(C.c_double), C.c_int, C.c_void_p, P(C.c_double)]
         self.lib = lib
 
     def grids(self, grid):
@@ -189,6 +206,19 @@ class Reference:
         if rc != 0:
             raise RuntimeError(f"orc_contract failed: {rc}")
         return jsyn, jssc
+
+    def flux_dens(self, grid, opts, j_all, a_all, r_arr, queries):
+        """ElectronAndRadiation::fluxDens itself on queries of one blastwave
+        (histories [nr][F], radii [nr]); only queries the reference does not
+        exit on."""
+        q = np.ascontiguousarray(queries, dtype=abi.FLUX_QUERY_DTYPE)
+        flux = np.zeros(len(q))
+        j = np.ascontiguousarray(j_all, dtype=np.float64)
+        a = np.ascontiguousarray(a_all, dtype=np.float64)
+        r = np.ascontiguousarray(r_arr, dtype=np.float64)
+        self.lib.ref_flux_dens(C.byref(grid), C.byref(opts), len(r), abi.dptr(j), abi.dptr(a), abi.dptr(r), len(q),
+                               q.ctypes.data, abi.dptr(flux))
+        return flux
 
     def run(self, grid, recs, offsets, params, outputs=("j_all", "a_all", "f_all", "i_all")):
         recs = np.ascontiguousarray(recs, dtype=abi.STEP_DTYPE)

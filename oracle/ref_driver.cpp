@@ -243,4 +243,40 @@ int ref_run(const pbag_grid_desc* g, const pbag_shock_params* prm, int nbw, cons
   return 0;
 }
 
+// ElectronAndRadiation::fluxDens itself on nq queries of one blastwave: an
+// object set up with the flux options, its total_rad.j_all / a_all replaced by
+// the given histories [nr][F], r_arr the radii of the rows.
+int ref_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, int nr, const double* j_all,
+                  const double* a_all, const double* r_arr, int nq, const pbag_flux_query* qs, double* flux) {
+  static const char* vel_s[] = {"sameAsBW", "shockVel"};
+  static const char* ne_s[] = {"usenprime", "useNe"};
+  static const char* tau_s[] = {"approx", "thick", "smooth", "sharp"};
+  Vector gam, freq;
+  make_freq_grid(g, freq);
+  SynKernel sk;
+  SSCKernel ck;
+  pbag_shock_params s{};
+  s.p = 2.2;
+  s.eps_e = 0.1;
+  s.max_substeps = 1000;
+  s.ele_method = PBAG_ELE_NUMERIC;
+  StrDbMap pars = make_pars(g, &s, 1e-3);
+  StrStrMap opts = make_opts(&s, false, "useU_e", "useTe", "useB", "useU_b", "none");
+  opts["method_vel_fs"] = vel_s[o->shock_vel];
+  opts["method_ne_fs"] = ne_s[o->method_ne];
+  opts["method_tau_fs"] = tau_s[o->method_tau];
+  ElectronAndRadiation er(LOG_SILENT, gam, freq, sk, ck, false);
+  er.setPars(pars, opts, (size_t)nr, 0, 0, 0.1, 1.0, true);
+  const size_t F = (size_t)g->nfreq;
+  er.total_rad.j_all.assign(j_all, j_all + (size_t)nr * F);
+  er.total_rad.a_all.assign(a_all, a_all + (size_t)nr * F);
+  Vector r(r_arr, r_arr + nr);
+  for (int t = 0; t < nq; ++t) {
+    const pbag_flux_query& q = qs[t];
+    flux[t] = er.fluxDens(EjectaID2::STUCT_TYPE::ipiecewise, q.theta, q.ncells, (size_t)q.ia, (size_t)q.ib, q.freq,
+                          q.Gamma, q.GammaSh, q.acc_fac, q.mu, q.r, q.rsh, q.dr, q.n_prime, q.ne, r);
+  }
+  return 0;
+}
+
 }  // extern "C"

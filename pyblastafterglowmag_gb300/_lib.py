@@ -84,6 +84,20 @@ def grids(grid):
     return gam, freq
 
 
+def flux_dens(ctx, opts, offsets, d_j_all, d_a_all, d_r_all, nq, d_q, d_flux):
+    """pbag_flux_dens: EATS flux densities of nq queries (device addresses;
+    offsets a host int64 array of nbw+1)."""
+    lib = load()
+    lib.pbag_flux_dens.argtypes = [C.c_void_p, C.POINTER(abi.FluxOpts), C.c_int, C.POINTER(C.c_int64),
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                   C.POINTER(abi.Status)]
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    st = abi.Status()
+    _check(lib.pbag_flux_dens(ctx.handle, C.byref(opts), len(off) - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                              C.c_void_p(d_j_all), C.c_void_p(d_a_all), C.c_void_p(d_r_all), int(nq),
+                              C.c_void_p(d_q), C.c_void_p(d_flux), C.byref(st)), "pbag_flux_dens", st)
+
+
 def autotune(enable=True):
     """Switch the contraction autotuner (pbag_autotune) on or off."""
     lib = load()

@@ -17,6 +17,7 @@ PBAG_ERR_DLNVDT = -6
 PBAG_ERR_UNSUPPORTED = -7
 PBAG_ERR_TIMEOUT = -8
 PBAG_ERR_NOMEM = -9
+PBAG_ERR_RANGE = -10
 
 STATUS_NAMES = {
     PBAG_OK: "ok",
@@ -28,6 +29,7 @@ STATUS_NAMES = {
     PBAG_ERR_DLNVDT: "invalid dlnV/dt",
     PBAG_ERR_UNSUPPORTED: "unsupported option",
     PBAG_ERR_TIMEOUT: "device wait timed out",
+    PBAG_ERR_RANGE: "frequency outside the grid",
     PBAG_ERR_NOMEM: "device allocation failed",
 }
 
@@ -124,3 +126,19 @@ def make_outputs(arrays):
         a = arrays.get(f)
         setattr(out, f, dptr(a) if a is not None else C.POINTER(C.c_double)())
     return out
+
+
+# ---- EATS flux density (pbag_flux_dens) ---------------------------------------
+PBAG_VEL_SAME_AS_BW, PBAG_VEL_SHOCK = 0, 1
+PBAG_NE_USE_NPRIME, PBAG_NE_USE_NE = 0, 1
+PBAG_TAU_APPROX, PBAG_TAU_THICK, PBAG_TAU_SMOOTH, PBAG_TAU_SHARP = 0, 1, 2, 3
+
+
+class FluxOpts(C.Structure):
+    _fields_ = [("shock_vel", C.c_int32), ("method_ne", C.c_int32), ("method_tau", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+FLUX_QUERY_DTYPE = np.dtype([("bw", np.int32), ("ia", np.int32), ("ib", np.int32), ("pad", np.int32)] +
+                            [(f, np.float64) for f in ("theta", "ncells", "freq", "Gamma", "GammaSh", "acc_fac",
+                                                        "mu", "r", "rsh", "dr", "n_prime", "ne")])

@@ -106,6 +106,8 @@ size_t pbag_sizeof(int which) {
     case 5: return sizeof(pbag_limits_opts);
     case 6: return sizeof(pbag_shock_state);
     case 7: return sizeof(pbag_limits);
+    case 8: return sizeof(pbag_flux_opts);
+    case 9: return sizeof(pbag_flux_query);
     default: return 0;
   }
 }

@@ -1,6 +1,7 @@
 """Host-side parts of libpbag (no GPU needed): the library loads, exports
 every entry point include/pbag.h declares with matching struct layouts, and
 its grid builder and per-step shock-scalar prep match the reference."""
+import ctypes as C
 import os
 import re
 
@@ -36,6 +37,8 @@ def test_struct_layouts(lib):
     so = lib.load()
     assert so.pbag_abi_version() == 1
     assert so.pbag_sizeof(2) == abi.STEP_DTYPE.itemsize == 136
+    assert so.pbag_sizeof(8) == C.sizeof(abi.FluxOpts) == 16
+    assert so.pbag_sizeof(9) == abi.FLUX_QUERY_DTYPE.itemsize == 112
 
 
 def test_grids_match_reference_fixture(lib):
