@@ -91,7 +91,7 @@ typedef struct pbag_shock_params {
   int32_t ssa_on;           /* use_ssa_{fs,rs}                                  */
   int32_t ssc_on;           /* method_ssc_{fs,rs} == "numeric"                  */
   int32_t adi_on;           /* num_ele_use_adi_loss_{fs,rs} (default yes)       */
-  int32_t pp_on;            /* method_pp_{fs,rs}: must be 0 (not implemented)   */
+  int32_t pp_on;            /* method_pp_{fs,rs} "numeric": pair source, absorption and attenuation (needs ssc_on) */
   int32_t reserved;
 } pbag_shock_params;
 

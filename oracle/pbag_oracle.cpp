@@ -163,6 +163,34 @@ double ssc_nava(double nu, double gam, double nu_tilde) {
   return K;
 }
 
+// Pair-production rate kernel (numeric_model.h:295-303)
+inline double pp_R(double nu, double nu_t) {
+  double x = nu * nu_t;
+  double varbl = x * (h_pl / m_e / c_light / c_light) * (h_pl / m_e / c_light / c_light);
+  double res = 0.;
+  if (varbl - 1 > 0) res = 0.652 * c_light * sigma_T * (varbl * varbl - 1) * std::log(varbl) / (varbl * varbl * varbl);
+  return res;
+}
+
+// computePPinjection (numeric_model.h:305-340): pairs injected at the electron
+// energy of photon frequency nu from the photon density n[F]
+double pp_injection(const std::vector<double>& nu_g, int F, double nu, const std::vector<double>& n) {
+  size_t idx = F - 1;
+  for (int i = 0; i < F - 1; i++)
+    if ((nu_g[i] < nu) && (nu_g[i + 1] >= nu)) {
+      idx = i;
+      break;
+    }
+  const double c4 = c_light * c_light * c_light * c_light;
+  double integ = 0;
+  for (int i = 0; i < F - 1; i++) {
+    if (nu_g[i] * nu * h_pl * h_pl / m_e / m_e / c4 < 1.) continue;
+    integ += n[i] * pp_R(nu, nu_g[i]) * (nu_g[i + 1] - nu_g[i]);
+  }
+  double fac = 4. * m_e * (c_light * c_light) / h_pl;
+  return fac * n[idx] * integ;  // Eq. 51 of Miceli & Nava
+}
+
 // microphysics/microphysics.h:11-58, METHOD_TAU::iAPPROX branch
 inline double intensity_approx(double em, double dtau) {
   if (dtau == 0) return em;
@@ -217,14 +245,14 @@ void build_tables(const pbag_grid_desc* g, bool ssc, Tables& t) {
 // Per-blastwave state and scratch (ElectronAndRadiation members).
 struct BW {
   std::vector<double> f, dfde, tmp, gsyn, gadi, gssc, heat, src, a, b, c, d, cp, dp;
-  std::vector<double> ker, sj, sa, cj, n, tj, ta, ti, spe;
+  std::vector<double> ker, sj, sa, cj, n, tj, ta, ti, spe, ppa;
   double dr_comov = 0, vol = 0, N = -1;
   bool init = false, syn_seen = false;
   void alloc(int G, int F) {
     for (auto* v : {&f, &dfde, &tmp, &gsyn, &gadi, &gssc, &heat, &src, &a, &b, &c, &d, &cp, &dp, &spe})
       v->assign(G, 0.);
     ker.assign((size_t)F * G, 0.);
-    for (auto* v : {&sj, &sa, &cj, &n, &tj, &ta, &ti}) v->assign(F, 0.);
+    for (auto* v : {&sj, &sa, &cj, &n, &tj, &ta, &ti, &ppa}) v->assign(F, 0.);
   }
 };
 
@@ -384,6 +412,13 @@ int evolve(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_r
   for (int i = 0; i < G; i++)
     w.src[i] = ((T.e[i] > r.gamma_min) && (T.e[i] <= r.gamma_max)) ? w.N * norm * std::pow(T.e[i], index) : 0.;
   const bool ssc = P.ssc_on && T.has_ssc;
+  // addPPSource (numeric_model.h:727-733): pairs from the photon density of
+  // the previous radiating step join the source (microphysics.h:457-459)
+  if (ssc && P.pp_on)
+    for (int i = 0; i < G; i++) {
+      double nu1 = 2. * T.e[i] * m_e * c_light * c_light / h_pl;
+      w.src[i] += pp_injection(T.nu, T.F, nu1, w.n) * w.vol;
+    }
   if (flags & ORC_HOIST_HEATING) {
     if (!heat_cool(T, w, r.B, dlnVdt, ssc, inner)) return PBAG_ERR_NONFINITE;
     setup_vectors(T, w, delta_t);
@@ -462,6 +497,14 @@ int radiate(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_
       w.cj[i] = acc;
     }
   }
+  // computePPabsorption (numeric_model.h:343-356) from the previous photon density
+  const bool pp = P.pp_on && ssc;
+  if (pp)
+    for (int i = 0; i < F; i++) {
+      double integ = 0;
+      for (int j = 0; j < F - 1; j++) integ += pp_R(T.nu[i], T.nu[j]) * w.n[j] * (T.nu[j + 1] - T.nu[j]);
+      w.ppa[i] = integ / c_light;
+    }
   // new photon density (microphysics.h:516-523)
   const bool num = P.ele_method == PBAG_ELE_NUMERIC;
   double Tesc = w.dr_comov / c_light;
@@ -477,6 +520,13 @@ int radiate(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_
   double n_ele = 0.;
   for (int i = 0; i < G - 1; i++) n_ele += w.f[i] * (T.e[i + 1] - T.e[i]);
   if (n_ele <= 0) return PBAG_ERR_NELE;
+  // pair-production attenuation of the total emissivity (microphysics.h:565-574)
+  if (num && pp)
+    for (int i = 0; i < F; i++) {
+      double tau_pp = w.ppa[i] * w.dr_comov;
+      double atten = (-std::expm1(-tau_pp) / tau_pp);
+      if (tau_pp > 0.) w.tj[i] = w.tj[i] * atten;
+    }
   // normalisation (microphysics.h:577-586)
   const double acc = r.accel_frac, np = r.n_prime;
   for (int i = 0; i < F; i++) {
@@ -506,10 +556,15 @@ int radiate(const Tables& T, const pbag_shock_params& P, BW& w, const pbag_step_
     put(out->syn_i_all, in, F);
   }
   if (ssc && (out->ssc_j_all || out->ssc_i_all)) {
-    std::vector<double> j(F);
-    for (int i = 0; i < F; i++) j[i] = w.cj[i] * acc;
+    std::vector<double> j(F), in(F);
+    for (int i = 0; i < F; i++) {
+      j[i] = w.cj[i] * acc;
+      // ssc.a is the pair-production absorption (0 without it, then I = j)
+      double a = pp ? w.ppa[i] / n_ele * acc * np : 0.;
+      in[i] = intensity_approx(j[i], a * w.dr_comov);
+    }
     put(out->ssc_j_all, j, F);
-    put(out->ssc_i_all, j, F);  // ssc.a == 0 without pair production, so I = j
+    put(out->ssc_i_all, in, F);
   }
   put(out->ele_f_all, w.f, G);
   put(out->gdot_syn_all, w.gsyn, G);

@@ -52,7 +52,7 @@ StrStrMap make_opts(const pbag_shock_params* s, bool dense, const char* lfmin, c
   opts["method_ele_fs"] = s->ele_method == PBAG_ELE_MIX ? "mix" : "numeric";
   opts["method_synchrotron_fs"] = syn_name(s->syn_method);
   opts["method_ssc_fs"] = s->ssc_on ? "numeric" : "none";
-  opts["method_pp_fs"] = "none";
+  opts["method_pp_fs"] = s->pp_on ? "numeric" : "none";
   opts["use_ssa_fs"] = s->ssa_on ? "yes" : "no";
   opts["num_ele_use_adi_loss_fs"] = s->adi_on ? "yes" : "no";
   opts["save_spec"] = dense ? "yes" : "no";

@@ -273,7 +273,7 @@ int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, c
   if (prm_host) {
     for (int b = 0; b < nbw; ++b) {
       const pbag_shock_params& p = prm_host[b];
-      if (p.pp_on) return PBAG_ERR_UNSUPPORTED;
+      if (p.pp_on && !p.ssc_on) return PBAG_ERR_PARAM;  // "PP requires SSC" (microphysics_base.h:394-397)
       if (p.syn_method < PBAG_SYN_CSYN || p.syn_method > PBAG_SYN_BESSEL) return PBAG_ERR_ARG;
       if (p.ele_method != PBAG_ELE_NUMERIC && p.ele_method != PBAG_ELE_MIX) return PBAG_ERR_ARG;
       if (p.max_substeps < 1 || !(p.p > 0.) || !std::isfinite(p.p)) return PBAG_ERR_ARG;
@@ -528,6 +528,36 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   ok(c->grid_upload(&d.ginv2, ginv2));
   ok(c->grid_upload(&d.psq32, psq));
   ok(c->grid_upload(&d.ginv23, ginv23));
+  {
+    // pair-production rate kernel R (numeric_model.h:295-303) on the grids
+    auto ppR = [](double nu, double nu_t) {
+      const double x = nu * nu_t;
+      const double l = cgs::h_pl / cgs::m_e / cgs::c_light / cgs::c_light;
+      const double v = x * l * l;
+      return v - 1 > 0 ? 0.652 * cgs::c_light * cgs::sigma_T * (v * v - 1) * std::log(v) / (v * v * v) : 0.;
+    };
+    const int Gs = (G + 3) / 4 * 4;  // the row stride of KintT (d.Gs)
+    std::vector<float> inj((size_t)F * Gs, 0.f), ab((size_t)F * F, 0.f);
+    std::vector<int> idx(G, F - 1);
+    const double c4 = cgs::c_light * cgs::c_light * cgs::c_light * cgs::c_light;
+    for (int i = 0; i < G; ++i) {
+      const double nu1 = 2. * e[i] * cgs::m_e * cgs::c_light * cgs::c_light / cgs::h_pl;
+      for (int k = 0; k < F - 1; ++k)
+        if ((nu[k] < nu1) && (nu[k + 1] >= nu1)) {
+          idx[i] = k;
+          break;
+        }
+      for (int k = 0; k < F - 1; ++k) {
+        if (nu[k] * nu1 * cgs::h_pl * cgs::h_pl / cgs::m_e / cgs::m_e / c4 < 1.) continue;
+        inj[(size_t)k * Gs + i] = (float)(ppR(nu1, nu[k]) * (nu[k + 1] - nu[k]));
+      }
+    }
+    for (int i = 0; i < F; ++i)
+      for (int k = 0; k < F - 1; ++k) ab[(size_t)k * F + i] = (float)(ppR(nu[i], nu[k]) * (nu[k + 1] - nu[k]) / cgs::c_light);
+    ok(c->grid_upload(&d.ppinjT, inj));
+    ok(c->grid_upload(&d.ppidx, idx));
+    ok(c->grid_upload(&d.ppabsT, ab));
+  }
   {
     // tabulated synchrotron functions of the GSL and Bessel methods
     std::vector<float> lg(G);

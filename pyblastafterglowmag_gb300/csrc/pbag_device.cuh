@@ -46,6 +46,10 @@ struct DevGrid {
   const float* syntab;   // [2][kSynTabN] g(u) of the GSL and Bessel methods (pbag_syntab.cpp)
   float syn_u0, syn_ih;  // first u of syntab and the inverse spacing
   float gsl_xs;          // the GSL method's argument over nu / nu_crit (kernels.h:282-285)
+  // pair production (numeric_model.h:295-356): FP32 tables of the rate kernel
+  const float* ppinjT;   // [F][Gs] R(nu1_i, nu_k) (nu_{k+1} - nu_k), k < F-1 (nu1_i = 2 e_i m_e c^2 / h)
+  const int* ppidx;      // [G]     photon bin of nu1_i (computePPinjection's idx)
+  const float* ppabsT;   // [F][F]  R(nu_i, nu_k) (nu_{k+1} - nu_k) / c at [k][i], k < F-1
   const float* ginv23;   // [G]   e[j]^(-2/3): cube root of the 1/e^2 factor of the synchrotron argument
   const double* nu;      // [F+1] frequency grid, nu[F] = next logspace point
   const float* nu13;     // [F]   cube root of nu

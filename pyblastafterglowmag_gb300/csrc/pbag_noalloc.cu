@@ -128,7 +128,7 @@ int check_params_host(const CtxView& v, const pbag_shock_params* d_prm, int nbw)
       return PBAG_ERR_CUDA;
     for (int k = 0; k < n; ++k) {
       const pbag_shock_params& p = chunk[k];
-      if (p.pp_on) return PBAG_ERR_UNSUPPORTED;
+      if (p.pp_on && !p.ssc_on) return PBAG_ERR_PARAM;  // "PP requires SSC" (microphysics_base.h:394-397)
       if (p.syn_method < PBAG_SYN_CSYN || p.syn_method > PBAG_SYN_BESSEL) return PBAG_ERR_ARG;
       if (p.ele_method != PBAG_ELE_NUMERIC && p.ele_method != PBAG_ELE_MIX) return PBAG_ERR_ARG;
       if (p.max_substeps < 1 || !(p.p > 0.) || !std::isfinite(p.p)) return PBAG_ERR_ARG;

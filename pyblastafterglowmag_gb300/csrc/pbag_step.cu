@@ -264,7 +264,7 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
 template <int FQ>
 __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
                            const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
-                           float* sh_v, double* sh_usv, int* sh_state);
+                           float* sh_v, double* sh_usv, int* sh_state, float* sh_pp);
 
 // ---------------------------------------------------------------------------
 // Chang-Cooper substeps (numeric_model.h:19-43, 682-708) of one blastwave-step.
@@ -453,6 +453,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   __shared__ __align__(8) uint64_t bars[2];  // tables, kernel integral
   __shared__ int sh_state[2];                // flags and error code after the previous step's completion
   __shared__ double sh_usv;                  // inverse scale of sh_v
+  __shared__ float sh_pp[PBAG_MAX_BINS];     // scaled photon density of the pair-production sums
   const GridTab T{sh_tab, g.Ge, g.Fe};
 
   if (tid == 0) {
@@ -533,7 +534,8 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   int flags = flags0, errc = err0;
   bool have_v = false;
   if (step > 0) {
-    const int fin = finalize_bw<FQ>(g, T, S, off, P, b, step - 1, out, flags0, err0, sh_v, &sh_usv, sh_state);
+    const int fin =
+        finalize_bw<FQ>(g, T, S, off, P, b, step - 1, out, flags0, err0, sh_v, &sh_usv, sh_state, sh_pp);
     if (fin) {
       __syncthreads();
       flags = sh_state[0];
@@ -656,6 +658,31 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     }
     if (tid == 0) sh_f[G - 1] = 0.;  // heating_term[G-1] is never set (numeric_model.h:761)
     if (__syncthreads_or(hbad ? 1 : 0)) PBAG_FAIL(PBAG_ERR_NONFINITE, __LINE__);
+    // pair production (addPPSource, numeric_model.h:727-733, with
+    // computePPinjection :305-340): pairs from the photon density of the
+    // previous radiating step join the source of every bin; the sums over the
+    // photon grid in FP32 with the density scaled by a power of two
+    double inj[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) inj[q] = 0.;
+    if (ssc && P.pp_on) {
+      const double* n = S.n + (size_t)b * F;
+      int pexp = 0;
+      for (int k = tid; k < F - 1; k += kStepThreads) pexp = max(pexp, exp_field(n[k]));
+      pexp = block_max_int(pexp, red_i[0]);
+      const double sp = scale_from_exp(pexp), usp = unscale_from_exp(pexp);
+      for (int k = tid; k < F; k += kStepThreads) sh_pp[k] = k < F - 1 ? (float)(n[k] * sp) : 0.f;
+      __syncthreads();
+      const double ppfac = 4. * m_e * (c_light * c_light) / h_pl;
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        const int j = tid * C + q;
+        if (j >= G) continue;
+        float acc = 0.f;
+        for (int k = 0; k < F - 1; ++k) acc = fmaf(sh_pp[k], __ldg(g.ppinjT + (size_t)k * Gs + j), acc);
+        inj[q] = ppfac * n[g.ppidx[j]] * ((double)acc * usp) * sc.vol;
+      }
+    }
     // tridiagonal coefficients (numeric_model.h:539-675 with dispersion = 0,
     // delta_j = 0): a = 0, b_k = 1 + dt H_{k-1}/dgb_k (b_0 = b_{G-1} = 1),
     // c_k = -dt H_k/dgb_k (c_{G-1} = 0)
@@ -670,7 +697,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
         const double Hf = j < G - 1 ? sh_f[j] : 0.;
         const double bb = 1. + (odg * Hb) * delta_t;
         const double cc = (odg * Hf) * -delta_t;
-        const double Q = (j >= sc.iq0 && j < sc.iq1) ? sc.Ns * ppq[q] : 0.;
+        const double Q = ((j >= sc.iq0 && j < sc.iq1) ? sc.Ns * ppq[q] : 0.) + inj[q];
         ib[q] = 1. / bb;
         bt[q] = -(cc * ib[q]);
         qb[q] = (Q * delta_t) * ib[q];
@@ -921,7 +948,7 @@ __device__ __forceinline__ double intensity_approx(double em, double dtau) {
 template <int FQ>
 __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
                             const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
-                            float* sh_v, double* sh_usv, int* sh_state) {
+                            float* sh_v, double* sh_usv, int* sh_state, float* sh_pp) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int F = g.F;
   __shared__ int red_f[3][kStepWarps];
@@ -978,8 +1005,36 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     }
     return 2;
   }
-  // new photon density (microphysics.h:516-523), totals and normalisation (:540-586)
+  // pair-production absorption (computePPabsorption, numeric_model.h:343-356)
+  // from the previous photon density, before it is overwritten
   double* n = S.n + (size_t)b * F;
+  const bool pp = ssc && P.pp_on;
+  double ppa[FQ];
+#pragma unroll
+  for (int q = 0; q < FQ; ++q) ppa[q] = 0.;
+  if (pp) {
+    int pexp = 0;
+    for (int k = tid; k < F - 1; k += kStepThreads) pexp = max(pexp, exp_field(n[k]));
+    pexp = __reduce_max_sync(0xffffffffu, pexp);
+    if (lane == 0) red_f[0][warp] = pexp;
+    __syncthreads();
+    pexp = 0;
+#pragma unroll
+    for (int v = 0; v < kStepWarps; ++v) pexp = max(pexp, red_f[0][v]);
+    const double sp = scale_from_exp(pexp), usp = unscale_from_exp(pexp);
+    for (int k = tid; k < F; k += kStepThreads) sh_pp[k] = k < F - 1 ? (float)(n[k] * sp) : 0.f;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+      const int k = tid + q * kStepThreads;
+      if (k >= F) continue;
+      float acc = 0.f;
+      for (int j = 0; j < F - 1; ++j) acc = fmaf(sh_pp[j], __ldg(g.ppabsT + (size_t)j * F + k), acc);
+      ppa[q] = (double)acc * usp;
+    }
+    __syncthreads();  // every thread has read the previous density
+  }
+  // new photon density (microphysics.h:516-523), totals and normalisation (:540-586)
   const double* inv_hnu = T.ft(kTabInvHnu);
   const double* dnu = T.ft(kTabDnuNu);
   const double* ksc = T.ft(kTabKscale);
@@ -998,7 +1053,11 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     un[q] = u;
     uexp = max(uexp, exp_field(u));
     if (k < F - 1) vexp = max(vexp, exp_field(u * ksc[k]));
-    const double tj0 = js + c;
+    double tj0 = js + c;
+    if (num && pp) {  // pair-production attenuation (microphysics.h:565-574)
+      const double tau_pp = ppa[q] * dr;
+      if (tau_pp > 0.) tj0 = tj0 * (-expm1(-tau_pp) / tau_pp);
+    }
     const double ta = asv[q] * anp_ne;
     const double ti = intensity_approx(tj0 * acc, ta * dr);
     const double tj = tj0 * acc_ne;
@@ -1019,7 +1078,8 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     if (ssc) {
       const double cj = cs[q] * acc;
       if (out.ssc_j_all) out.ssc_j_all[row * F + k] = cj;
-      if (out.ssc_i_all) out.ssc_i_all[row * F + k] = cj;  // ssc.a = 0 without pair production
+      // ssc.a is the pair-production absorption (0 without it: I = j)
+      if (out.ssc_i_all) out.ssc_i_all[row * F + k] = pp ? intensity_approx(cj, ppa[q] * anp_ne * dr) : cj;
     }
   }
   // one reduction: the scales of U and of the cooling weights, the checks
@@ -1099,16 +1159,17 @@ k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_sh
   if (step >= off[b + 1] - off[b]) return;
   const pbag_shock_params P = prm[b];
   const GridTab T{g.etab, g.Ge, g.Fe};
+  __shared__ float sh_pp[PBAG_MAX_BINS];
   const int fq = (g.F + kStepThreads - 1) / kStepThreads;
   int fin;
   if (fq <= 1)
-    fin = finalize_bw<1>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+    fin = finalize_bw<1>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else if (fq <= 2)
-    fin = finalize_bw<2>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+    fin = finalize_bw<2>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else if (fq <= 4)
-    fin = finalize_bw<4>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+    fin = finalize_bw<4>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else
-    fin = finalize_bw<8>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr);
+    fin = finalize_bw<8>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   if (fin == 1) history_rows_g(g, S, (size_t)(off[b] + step), b, out);
 }
 

@@ -60,6 +60,15 @@ def test_gaussian_ssc(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
 
 
+def test_gaussian_ssc_pair_production(lib, oracle, cuda_device):
+    """method_pp numeric: the pair source of every electron bin, the pair
+    absorption and the attenuation of the total emissivity, every history."""
+    recs, off, prm, grid = cases.gaussian(lib, nlayers=3, nsteps=80)
+    prm = prm.copy()
+    prm["pp_on"] = 1
+    _compare(lib, oracle, (recs, off, prm, grid))
+
+
 def test_gaussian_ssc_small_batch_kernel(lib, oracle, cuda_device, monkeypatch):
     """The step with the small-batch slab kernel forced for its SSC contraction."""
     monkeypatch.setenv("PBAG_TC_KERNEL", "slab-small")
@@ -107,10 +116,10 @@ def test_unsupported_options_rejected(lib, cuda_device):
     recs, off, prm, grid = cases.tophat(lib, nsteps=10)
     ctx = Context(grid, device=0, ssc=False)
     p = prm.copy()
-    p["pp_on"] = 1
+    p["pp_on"] = 1  # pair production needs SSC (microphysics_base.h:394-397)
     with pytest.raises(PbagError) as ei:
         ctx.run(recs, off, p)
-    assert ei.value.code == abi.PBAG_ERR_UNSUPPORTED
+    assert ei.value.code == abi.PBAG_ERR_PARAM
     p = prm.copy()
     p["ssc_on"] = 1  # context built without SSC tables
     with pytest.raises(PbagError) as ei:

@@ -79,6 +79,25 @@ def test_live_reference_matches_oracle(lib, oracle, reference):
             np.testing.assert_array_equal(o[k], r[k], err_msg=k)
 
 
+def test_live_reference_matches_oracle_with_pair_production(lib, oracle, reference):
+    """Pair production (method_pp numeric: the pair source of numeric_model.h:
+    727-733, the absorption of :343-356 and the attenuation of
+    microphysics.h:565-574) with SSC and SSA, every history."""
+    recs, off, prm, grid = cases.gaussian(lib, nlayers=2, nsteps=50, ngam=64, nfreq=40)
+    prm = prm.copy()
+    prm["pp_on"] = 1
+    r = reference.run(grid, recs, off, prm, outputs=cases.ALL_OUTPUTS)
+    rc, where, o = oracle.run(grid, recs, off, prm, outputs=cases.ALL_OUTPUTS, outer_threads=4)
+    assert rc == 0, where
+    for k in cases.ALL_OUTPUTS:
+        np.testing.assert_array_equal(o[k], r[k], err_msg=k)
+    # pair production changes the result
+    prm0 = prm.copy()
+    prm0["pp_on"] = 0
+    _, _, base = oracle.run(grid, recs, off, prm0, outputs=("j_all",))
+    assert not np.array_equal(base["j_all"], o["j_all"])
+
+
 def test_oracle_reports_reference_exit_conditions(lib, oracle):
     """Conditions on which the reference calls exit(1) become status codes."""
     recs, off, prm, grid = cases.tophat(lib, nsteps=40)
