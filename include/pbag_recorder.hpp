@@ -27,6 +27,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "pbag.h"
@@ -49,6 +50,46 @@ struct Histories {
   std::vector<double>* syn_j_all = nullptr, *syn_a_all = nullptr, *syn_i_all = nullptr;  // syn.*
   std::vector<double>* ssc_j_all = nullptr, *ssc_i_all = nullptr;                         // ssc.*
 };
+
+// The datasets the reference's spectrum writer stores for one blastwave
+// (Ejecta::computeSaveEjectaSpectrum, ejecta.h:354-455), in its order and with
+// its names (suffix "_fs" or "_rs"), pointing at the vectors a Recorder filled.
+// syn.f_all and ssc.f_all are never set by the reference (their photon
+// densities are commented out, numeric_model.h:182, 283): they are written as
+// zeros of the history's size, held here.
+struct WriterDatasets {
+  std::vector<std::pair<std::string, const std::vector<double>*>> items;
+  std::vector<double> zeros;
+};
+inline WriterDatasets writer_datasets(const Histories& h, bool rs, bool ele_numeric, bool ssa, bool ssc) {
+  WriterDatasets d;
+  const std::string sfx = rs ? "_rs" : "_fs";
+  const size_t n = h.j_all ? h.j_all->size() : 0;
+  d.zeros.assign(n, 0.);
+  auto add = [&](const char* name, const std::vector<double>* v) {
+    if (v) d.items.emplace_back(std::string(name) + sfx, v);
+  };
+  if (ele_numeric) {
+    add("n_ele", h.ele_f_all);
+    add("gam_dot_syn", h.gdot_syn_all);
+    add("gam_dot_adi", h.gdot_adi_all);
+    add("gam_dot_ssc", h.gdot_ssc_all);
+  }
+  add("syn_f", &d.zeros);
+  add("syn_j", h.syn_j_all);
+  add("syn_i", h.syn_i_all);
+  if (ssa) add("syn_a", h.syn_a_all);
+  if (ssc) {
+    add("ssc_f", &d.zeros);
+    add("ssc_j", h.ssc_j_all);
+    add("ssc_i", h.ssc_i_all);
+  }
+  add("total_f", h.f_all);
+  add("total_j", h.j_all);
+  add("total_i", h.i_all);
+  if (ssa) add("total_a", h.a_all);
+  return d;
+}
 
 class Recorder {
  public:

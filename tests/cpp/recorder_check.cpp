@@ -49,6 +49,14 @@ int main(int argc, char** argv) {
     o.write(reinterpret_cast<const char*>(j[b].data()), (std::streamsize)(j[b].size() * sizeof(double)));
     o.write(reinterpret_cast<const char*>(a[b].data()), (std::streamsize)(a[b].size() * sizeof(double)));
   }
+  // the spectrum writer's datasets of the first blastwave (total j, a only here)
+  pbag::Histories h0;
+  h0.j_all = &j[0];
+  h0.a_all = &a[0];
+  const pbag::WriterDatasets ds = pbag::writer_datasets(h0, false, true, true, true);
+  std::printf("datasets");
+  for (const auto& it : ds.items) std::printf(" %s:%zu", it.first.c_str(), it.second->size());
+  std::printf("\n");
   std::printf("rc %d bw %d step %d\n", rc, st.bw, st.step);
   return rc == PBAG_OK ? 0 : 1;
 }

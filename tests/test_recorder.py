@@ -35,6 +35,9 @@ def test_recorder_replay_matches_batch(lib, cuda_device, tmp_path):
     r = subprocess.run([str(exe), files["grid"], files["params"], files["offsets"], files["records"], str(out)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+    # the spectrum writer's names (ejecta.h:354-455) for the vectors a caller gave
+    names = [w.split(":")[0] for w in r.stdout.split("datasets", 1)[1].splitlines()[0].split()]
+    assert names == ["syn_f_fs", "ssc_f_fs", "total_j_fs", "total_a_fs"], r.stdout
     got = np.fromfile(out, dtype=np.float64)
     ctx = lib.Context(grid, cuda_device, ssc=True)
     ref = ctx.run(recs, off, prm, outputs=("j_all", "a_all"))
