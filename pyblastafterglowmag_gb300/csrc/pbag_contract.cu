@@ -27,6 +27,7 @@ namespace {
 using namespace cgs;
 
 constexpr int kPrepWarps = 8;  // states per CTA of the preparation kernel (a warp each)
+constexpr int kSynBatchMin = 512;  // batches from this size on take the tabulated synchrotron sums
 // synchrotron constants per unit field (kernels.h:194-202, 427, 471): the
 // prefactors sqrt(3) q^3 / (m_e c^2) (CSYN) and sqrt(3) q^3 / (m_e c c)
 // (Dermer09), and in FP32 4 pi m_e c / (3 q) and 2 pi m_e c / (3 q)
@@ -176,6 +177,117 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
     p.ssc_on = want_ssc;
     prm[s] = p;
   }
+}
+
+// Synchrotron sums of a large batch (computeSynSpectrum, numeric_model.h:
+// 148-184, kernel values of kernels.h:414-538): one warp per (state, 8
+// frequencies), lanes over gamma; the synchrotron function is interpolated
+// from its FP64-built table (g(u) = R(e^u) e^(-u/3) on a uniform grid in
+// u = ln x, staged in shared memory once per persistent CTA) instead of
+// evaluating the fit per term: x = a_k / gamma^2 gives u = ln a_k + ln(1 /
+// gamma^2) from two tables, and x^(1/3) = a_k^(1/3) gamma^(-2/3). The
+// cyclotron branch of CSYN (gamma <= 2) is evaluated directly.
+constexpr int kSbWarps = 8;  // warps of a CTA
+constexpr int kSbF = 8;      // frequencies of a warp's work item
+constexpr int kSbBlocksPerSm = 3;
+inline size_t syn_batch_smem(int G) { return (size_t)kSynTabN * 4 + (size_t)2 * G * 4; }
+
+__global__ void __launch_bounds__(32 * kSbWarps)
+k_syn_batch(DevGrid g, DevState S, int method, int items) {
+  extern __shared__ float sb_smem[];
+  float* tab = sb_smem;
+  float* lng = tab + kSynTabN;
+  float* g23 = lng + g.G;
+  __shared__ float cst[kSbWarps][3][kSbF];  // per warp item: ln a_k, a_k^(1/3), nu_k / nu_L
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int G = g.G, F = g.F;
+  const float* src = g.syntab + (method == PBAG_SYN_GSL ? 0 : method == PBAG_SYN_BESSEL ? kSynTabN : 2 * kSynTabN);
+  for (int i = tid; i < kSynTabN; i += blockDim.x) tab[i] = src[i];
+  for (int j = tid; j < G; j += blockDim.x) {
+    lng[j] = g.lnginv2[j];
+    g23[j] = g.ginv23[j];
+  }
+  __syncthreads();
+  const float xs = method == PBAG_SYN_GSL ? g.gsl_xs : 1.f;
+  const float lxs = logf(xs), cxs = cbrtf(xs);
+  const int jcyc = method == PBAG_SYN_CSYN ? g.n_cyc : 0;
+  const float u0 = g.syn_u0, ih = g.syn_ih, pmax = (float)(g.syn_n - 1);
+  const int nfb = (F + kSbF - 1) / kSbF;
+  for (int item = blockIdx.x * kSbWarps + warp; item < items; item += gridDim.x * kSbWarps) {
+    const int b = item / nfb, k0 = (item % nfb) * kSbF;
+    const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);  // incrit, inlar, cbrt(incrit)
+    if (lane < kSbF) {
+      const int k = min(k0 + lane, F - 1);
+      cst[warp][0][lane] = g.lnnu[k] + logf(rp.x) + lxs;
+      cst[warp][1][lane] = g.nu13[k] * rp.z * cxs;
+      cst[warp][2][lane] = g.nu32[k] * rp.y;
+    }
+    __syncwarp();
+    float acc[kSbF], la[kSbF], y13[kSbF], xl[kSbF];
+#pragma unroll
+    for (int q = 0; q < kSbF; ++q) {
+      acc[q] = 0.f;
+      la[q] = (cst[warp][0][q] - u0) * ih;  // table position of ln a_k
+      y13[q] = cst[warp][1][q];
+      xl[q] = cst[warp][2][q];
+    }
+    const float* w = S.w32 + (size_t)b * G;
+    for (int j = lane; j < G - 1; j += 32) {
+      const float wj = __ldg(w + j);
+      if (j < jcyc) {
+        const float psq = __ldg(g.psq32 + j);
+#pragma unroll
+        for (int q = 0; q < kSbF; ++q) acc[q] = fmaf(cyclotron_R32(psq, xl[q]), wj, acc[q]);
+      } else {
+        const float lg = lng[j] * ih, gg = g23[j];
+#pragma unroll
+        for (int q = 0; q < kSbF; ++q) {
+          const float p = la[q] + lg;
+          float R = 0.f;
+          if (p < pmax) {
+            if (p <= 0.f) {
+              R = tab[0];
+            } else {
+              const int i = (int)p;
+              const float a = tab[i];
+              R = fmaf(p - (float)i, tab[i + 1] - a, a);
+            }
+            R *= y13[q] * gg;
+          } else if (!(p == p)) {
+            R = p;  // NaN propagates
+          }
+          acc[q] = fmaf(R, wj, acc[q]);
+        }
+      }
+    }
+    float mine = 0.f;
+#pragma unroll
+    for (int q = 0; q < kSbF; ++q) {
+      float v = acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == q) mine = v;
+    }
+    if (lane < kSbF && k0 + lane < F) S.syn32[(size_t)b * F + k0 + lane] = mine;
+    __syncwarp();  // the item's constants are read before the next item writes them
+  }
+}
+
+cudaError_t launch_syn_batch(const DevGrid& g, const DevState& S, int n, int method, cudaStream_t st) {
+  static int sms = 0;
+  static bool attr = false;
+  if (!attr) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaFuncSetAttribute(k_syn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)syn_batch_smem(PBAG_MAX_BINS));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int items = n * ((g.F + kSbF - 1) / kSbF);
+  const int blocks = std::max(1, std::min((items + kSbWarps - 1) / kSbWarps, kSbBlocksPerSm * std::max(sms, 1)));
+  k_syn_batch<<<blocks, 32 * kSbWarps, syn_batch_smem(g.G), st>>>(g, S, method, items);
+  return cudaGetLastError();
 }
 
 // j_syn from the FP32 sums: prefactor and scale (numeric_model.h:148-184);
@@ -336,7 +448,10 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   ok(cudaGetLastError());
   // synchrotron sums (and the CUDA-core SSC contraction in FP32)
   const bool fp32_ssc = d_jssc && !tc;
-  if (d_jsyn || fp32_ssc) ok(launch_rad_ssc(v.dg, S, ws->prm, n, fp32_ssc, 0, s));
+  if (d_jsyn && !fp32_ssc && n >= kSynBatchMin)
+    ok(launch_syn_batch(v.dg, S, n, syn_method, s));  // large batches: the tabulated function
+  else if (d_jsyn || fp32_ssc)
+    ok(launch_rad_ssc(v.dg, S, ws->prm, n, fp32_ssc, 0, s));
   if (d_jssc && tc)
     ok(launch_ssc_tc_mode(mode, v.F, v.Gp, ws->Wt, mode == kTcTf32 ? (const void*)ws->bt32 : (const void*)v.dg.Bt, n,
                           S.flags, S.U32, S.scal, v.dg.hnu, v.F, v.F, d_jssc, S.err, s));

@@ -563,12 +563,20 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     std::vector<float> lg(G);
     for (int i = 0; i < G; ++i) lg[i] = (float)(-2. * std::log(e[i]));
     ok(c->grid_upload(&d.lnginv2, lg));
-    std::vector<float> st = syn_table(PBAG_SYN_GSL), sb = syn_table(PBAG_SYN_BESSEL);
+    double u0 = 0., h = 0.;
+    int tn = 0;
+    syn_table_grid(std::log(e[1] / e[0]), &u0, &h, &tn);
+    std::vector<float> st = syn_table(PBAG_SYN_GSL, u0, h, tn), sb = syn_table(PBAG_SYN_BESSEL, u0, h, tn),
+                       sa = syn_table(PBAG_SYN_CSYN, u0, h, tn);
     st.insert(st.end(), sb.begin(), sb.end());
+    st.insert(st.end(), sa.begin(), sa.end());
+    std::vector<float> lnu(F);
+    for (int k = 0; k < F; ++k) lnu[k] = (float)std::log(nu[k]);
+    ok(c->grid_upload(&d.lnnu, lnu));
     ok(c->grid_upload(&d.syntab, st));
-    const double u0 = std::log(kSynTabXmin), h = (std::log(kSynTabXmax) - u0) / (kSynTabN - 1);
     d.syn_u0 = (float)u0;
     d.syn_ih = (float)(1. / h);
+    d.syn_n = tn;
     // GSL: x = (h nu / m_e c^2) / (1.5 B gamma^2 / 4.14e13) against nu / nu_crit = nu 4 pi m_e c / (3 q B gamma^2)
     d.gsl_xs = (float)(cgs::h_by_mec2 * 4.14e13 / 1.5 / (4. * M_PI * cgs::m_e * cgs::c_light / (3. * cgs::q_e)));
   }

@@ -43,8 +43,10 @@ struct DevGrid {
   const float* ginv2;    // [G]   1/e[j]^2 (FP32, synchrotron argument)
   const float* psq32;    // [G]   e[j]^2 - 1 in FP32 (cyclotron branch)
   const float* lnginv2;  // [G]   ln(1/e[j]^2): argument of the tabulated synchrotron functions
-  const float* syntab;   // [2][kSynTabN] g(u) of the GSL and Bessel methods (pbag_syntab.cpp)
+  const float* syntab;   // [3][kSynTabN] g(u) of the GSL, Bessel and Aharonian functions (pbag_syntab.cpp)
+  const float* lnnu;     // [F]   ln nu
   float syn_u0, syn_ih;  // first u of syntab and the inverse spacing
+  int syn_n;             // points of each table (zero after them)
   float gsl_xs;          // the GSL method's argument over nu / nu_crit (kernels.h:282-285)
   // pair production (numeric_model.h:295-356): FP32 tables of the rate kernel
   const float* ppinjT;   // [F][Gs] R(nu1_i, nu_k) (nu_{k+1} - nu_k), k < F-1 (nu1_i = 2 e_i m_e c^2 / h)
@@ -325,11 +327,11 @@ __device__ __forceinline__ float aharonian_R32(float x, float y) {
 
 // Tabulated synchrotron function (GSL or Bessel method): R(x) = g(ln x)
 // x^(1/3), g interpolated linearly in u = ln x; lx = ln x, x13 = x^(1/3).
-__device__ __forceinline__ float tabulated_R32(const float* __restrict__ tab, float u0, float ih, float lx,
+__device__ __forceinline__ float tabulated_R32(const float* __restrict__ tab, float u0, float ih, int n, float lx,
                                                float x13) {
   if (!(lx == lx)) return lx;  // NaN propagates
   const float p = (lx - u0) * ih;
-  if (p >= (float)(kSynTabN - 1)) return 0.f;
+  if (p >= (float)(n - 1)) return 0.f;
   if (p <= 0.f) return __ldg(tab) * x13;
   const int i = (int)p;
   const float f = p - (float)i, a = __ldg(tab + i), b = __ldg(tab + i + 1);

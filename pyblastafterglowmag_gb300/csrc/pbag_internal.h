@@ -12,13 +12,15 @@ namespace pbag {
 // Electron grid gam[G] and photon grid freq[F+1] (see pbag_build_grids).
 void build_grids(const pbag_grid_desc* g, double* gam, double* freq);
 
-// Tabulated synchrotron function of the GSL or Bessel method (pbag_syntab.cpp):
-// g(u) = R(e^u) e^(-u/3) at kSynTabN points u uniform in [ln kSynTabXmin,
-// ln kSynTabXmax].
+// Tabulated synchrotron functions (pbag_syntab.cpp): g(u) = R(e^u) e^(-u/3)
+// at n <= kSynTabN points u0 + i h covering [ln kSynTabXmin, ln kSynTabXmax]
+// (zero after them); syn_table_grid picks h from the electron grid's step
+// dlng = ln(e[1] / e[0]). method: GSL, Bessel, or CSYN / Dermer09 (the fit).
 constexpr int kSynTabN = 16384;
 constexpr double kSynTabXmin = 1e-12;
 constexpr double kSynTabXmax = 120.;
-std::vector<float> syn_table(int method);
+void syn_table_grid(double dlng, double* u0, double* h, int* n);
+std::vector<float> syn_table(int method, double u0, double h, int n);
 
 }  // namespace pbag
 

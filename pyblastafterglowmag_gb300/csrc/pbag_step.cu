@@ -882,7 +882,7 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
     float acc = 0.f, as = 0.f, ac = 0.f;  // synchrotron sum; SSA sum and its compensation
     for (int j = jl; j < G - 1; j += kRadLanes) {
       const float R_ =
-          tab ? tabulated_R32(stab, g.syn_u0, g.syn_ih, la + __ldg(g.lnginv2 + j), y13 * __ldg(g.ginv23 + j))
+          tab ? tabulated_R32(stab, g.syn_u0, g.syn_ih, g.syn_n, la + __ldg(g.lnginv2 + j), y13 * __ldg(g.ginv23 + j))
           : j >= jcyc ? aharonian_R32(a_k * __ldg(g.ginv2 + j), y_k * __ldg(g.ginv23 + j))
                       : cyclotron_R32(__ldg(g.psq32 + j), xl);
       acc = fmaf(R_, __ldg(w + j), acc);

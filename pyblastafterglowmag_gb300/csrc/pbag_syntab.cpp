@@ -1,11 +1,13 @@
-// pbag_syntab.cpp - tabulated synchrotron functions of the "GSL" and "Bessel"
-// methods of SynKernel (kernels.h:211-342, 396-412) for the GPU radiation sums.
+// pbag_syntab.cpp - tabulated synchrotron functions of SynKernel for the GPU
+// radiation sums: the "GSL" and "Bessel" methods (kernels.h:211-342, 396-412),
+// and the Aharonian fit of "CSYN" / "Dermer09" (kernels.h:420-427, 463-469)
+// for the batch contraction, which interpolates instead of evaluating the fit.
 //
 // Both functions depend on the state only through their argument x: the GSL
 // method's F(x) = x int_x^inf K_5/3 (x = h nu / m_e c^2 / (1.5 B / 4.14e13
 // gamma^2), kernels.h:282-285), the Bessel method's 2 t^2 (K_4/3 K_1/3 -
 // 3/5 t (K_4/3^2 - K_1/3^2)) (t = nu / nu_crit). They are tabulated once per
-// process in FP64 on the host as g(u) = R(e^u) e^(-u/3), u = ln x, on a uniform
+// context in FP64 on the host as g(u) = R(e^u) e^(-u/3), u = ln x, on a uniform
 // grid in u; g is smooth and tends to a constant for x -> 0 (R ~ x^(1/3)), so
 // the device interpolates g linearly and multiplies by x^(1/3), which it forms
 // from its tabulated factors. Below the table g keeps its first value; above it
@@ -16,6 +18,7 @@
 // summed by Clenshaw's recurrence; the Bessel functions come from the C++17
 // special functions of the standard library (as the reference's own
 // std::cyl_bessel_k, kernels.h:403-404).
+#include <algorithm>
 #include <cmath>
 #include <stdexcept>
 #include <vector>
@@ -85,14 +88,35 @@ double synchrotron_bessel(double t) {
   }
 }
 
+// the Aharonian et al. (2010) fit of CSYN and Dermer09 (kernels.h:420-427, 463-469)
+double synchrotron_aharonian(double x) {
+  const double x13 = std::cbrt(x), x23 = x13 * x13, x43 = x23 * x23;
+  return 1.808 * x13 / std::sqrt(1 + 3.4 * x23) * (1. + 2.21 * x23 + 0.347 * x43) /
+         (1. + 1.353 * x23 + 0.217 * x43) * std::exp(-x);
+}
+
 }  // namespace
 
-std::vector<float> syn_table(int method) {
-  std::vector<float> g(kSynTabN);
-  const double h = (std::log(kSynTabXmax) - std::log(kSynTabXmin)) / (kSynTabN - 1);
-  for (int i = 0; i < kSynTabN; ++i) {
-    const double u = std::log(kSynTabXmin) + i * h, x = std::exp(u);
-    const double R = method == PBAG_SYN_GSL ? synchrotron_F(x) : synchrotron_bessel(x);
+void syn_table_grid(double dlng, double* u0, double* h, int* n) {
+  // spacing: the step of ln(1/gamma^2) between neighbouring electron bins is
+  // m spacings, m odd, so that the lanes of a warp (consecutive bins) read
+  // the table at indices m apart: distinct shared-memory banks
+  const double span = std::log(kSynTabXmax) - std::log(kSynTabXmin);
+  const double step2 = 2. * dlng;
+  int m = (int)std::lround(step2 / 2e-3) | 1;
+  while (m > 1 && span / (step2 / m) + 2 > kSynTabN) m -= 2;
+  *h = step2 / m;
+  *u0 = std::log(kSynTabXmin);
+  *n = std::min(kSynTabN, (int)std::ceil(span / *h) + 2);
+}
+
+std::vector<float> syn_table(int method, double u0, double h, int n) {
+  std::vector<float> g(kSynTabN, 0.f);
+  for (int i = 0; i < n; ++i) {
+    const double u = u0 + i * h, x = std::exp(u);
+    const double R = method == PBAG_SYN_GSL      ? synchrotron_F(x)
+                     : method == PBAG_SYN_BESSEL ? synchrotron_bessel(x)
+                                                 : synchrotron_aharonian(x);
     g[i] = (float)(R * std::exp(-u / 3.));
   }
   return g;

@@ -139,10 +139,12 @@ def test_autotuner_measures_and_keeps_a_choice(lib, oracle, cuda_device):
     assert z == 0 and rel.max() <= 1e-4
 
 
-@pytest.mark.parametrize("method", [abi.PBAG_SYN_DER09, abi.PBAG_SYN_GSL, abi.PBAG_SYN_BESSEL])
-def test_contract_synchrotron_methods(lib, oracle, cuda_device, method):
+@pytest.mark.parametrize("n", [50, 700])
+@pytest.mark.parametrize("method", [abi.PBAG_SYN_CSYN, abi.PBAG_SYN_DER09, abi.PBAG_SYN_GSL, abi.PBAG_SYN_BESSEL])
+def test_contract_synchrotron_methods(lib, oracle, cuda_device, method, n):
+    """Every synchrotron method, on a small batch (the kernel values of each
+    term) and on a large one (the tabulated functions, interpolated)."""
     import torch
-    n = 50
     g = CT.grid_desc(ngam=201, nfreq=128)
     gam, freq = oracle.grids(g)
     f, B = CT.states(gam, n, seed=14)
