@@ -190,35 +190,38 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
 constexpr int kSbWarps = 8;  // warps of a CTA
 constexpr int kSbF = 8;      // frequencies of a warp's work item
 constexpr int kSbBlocksPerSm = 3;
-inline size_t syn_batch_smem(int G) { return (size_t)kSynTabN * 4 + (size_t)2 * G * 4; }
+inline size_t syn_batch_smem(int G) { return (size_t)kSynTab2N * 8 + (size_t)2 * G * 4; }
 
 __global__ void __launch_bounds__(32 * kSbWarps)
 k_syn_batch(DevGrid g, DevState S, int method, int items) {
-  extern __shared__ float sb_smem[];
-  float* tab = sb_smem;
-  float* lng = tab + kSynTabN;
+  extern __shared__ float2 sb_smem[];
+  float2* tab = sb_smem;  // value / slope pairs
+  float* lng = reinterpret_cast<float*>(tab + kSynTab2N);
   float* g23 = lng + g.G;
   __shared__ float cst[kSbWarps][3][kSbF];  // per warp item: ln a_k, a_k^(1/3), nu_k / nu_L
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int G = g.G, F = g.F;
-  const float* src = g.syntab + (method == PBAG_SYN_GSL ? 0 : method == PBAG_SYN_BESSEL ? kSynTabN : 2 * kSynTabN);
-  for (int i = tid; i < kSynTabN; i += blockDim.x) tab[i] = src[i];
+  const float2* src =
+      g.syntab2 + (method == PBAG_SYN_GSL ? 0 : method == PBAG_SYN_BESSEL ? kSynTab2N : 2 * kSynTab2N);
+  for (int i = tid; i < kSynTab2N; i += blockDim.x) tab[i] = src[i];
+  const float ih = g.syn2_ih, u0 = g.syn2_u0;
   for (int j = tid; j < G; j += blockDim.x) {
-    lng[j] = g.lnginv2[j];
+    lng[j] = g.lnginv2[j] * ih;  // table positions
     g23[j] = g.ginv23[j];
   }
   __syncthreads();
   const float xs = method == PBAG_SYN_GSL ? g.gsl_xs : 1.f;
   const float lxs = logf(xs), cxs = cbrtf(xs);
   const int jcyc = method == PBAG_SYN_CSYN ? g.n_cyc : 0;
-  const float u0 = g.syn_u0, ih = g.syn_ih, pmax = (float)(g.syn_n - 1);
+  const int last = g.syn2_n - 1;
   const int nfb = (F + kSbF - 1) / kSbF;
+  constexpr float kRound = 12582912.f;  // 1.5 2^23: x + kRound rounds x to an integer in the mantissa
   for (int item = blockIdx.x * kSbWarps + warp; item < items; item += gridDim.x * kSbWarps) {
     const int b = item / nfb, k0 = (item % nfb) * kSbF;
     const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);  // incrit, inlar, cbrt(incrit)
     if (lane < kSbF) {
       const int k = min(k0 + lane, F - 1);
-      cst[warp][0][lane] = g.lnnu[k] + logf(rp.x) + lxs;
+      cst[warp][0][lane] = (g.lnnu[k] + logf(rp.x) + lxs - u0) * ih;  // table position of ln a_k
       cst[warp][1][lane] = g.nu13[k] * rp.z * cxs;
       cst[warp][2][lane] = g.nu32[k] * rp.y;
     }
@@ -227,7 +230,7 @@ k_syn_batch(DevGrid g, DevState S, int method, int items) {
 #pragma unroll
     for (int q = 0; q < kSbF; ++q) {
       acc[q] = 0.f;
-      la[q] = (cst[warp][0][q] - u0) * ih;  // table position of ln a_k
+      la[q] = cst[warp][0][q];
       y13[q] = cst[warp][1][q];
       xl[q] = cst[warp][2][q];
     }
@@ -239,24 +242,17 @@ k_syn_batch(DevGrid g, DevState S, int method, int items) {
 #pragma unroll
         for (int q = 0; q < kSbF; ++q) acc[q] = fmaf(cyclotron_R32(psq, xl[q]), wj, acc[q]);
       } else {
-        const float lg = lng[j] * ih, gg = g23[j];
+        const float lg = lng[j], gw = g23[j] * wj;
 #pragma unroll
         for (int q = 0; q < kSbF; ++q) {
+          // nearest table point i (clamped: below the table the first, flat
+          // point; from the last point on zero) and the offset from it
           const float p = la[q] + lg;
-          float R = 0.f;
-          if (p < pmax) {
-            if (p <= 0.f) {
-              R = tab[0];
-            } else {
-              const int i = (int)p;
-              const float a = tab[i];
-              R = fmaf(p - (float)i, tab[i + 1] - a, a);
-            }
-            R *= y13[q] * gg;
-          } else if (!(p == p)) {
-            R = p;  // NaN propagates
-          }
-          acc[q] = fmaf(R, wj, acc[q]);
+          const float r = p + kRound;
+          const int i = min(max(__float_as_int(r) - __float_as_int(kRound), 0), last);
+          const float f = p - (r - kRound);  // offset from the nearest point (unused where clamped: slope 0)
+          const float2 t = tab[i];
+          acc[q] = fmaf(fmaf(f, t.y, t.x) * y13[q], gw, acc[q]);
         }
       }
     }

@@ -577,6 +577,21 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     d.syn_u0 = (float)u0;
     d.syn_ih = (float)(1. / h);
     d.syn_n = tn;
+    // value / slope pairs for the batch sums (a coarser grid, matched the same way)
+    double u2 = 0., h2 = 0.;
+    int n2 = 0;
+    syn_table_grid(std::log(e[1] / e[0]), &u2, &h2, &n2, kSynTab2N);
+    std::vector<float> t2;
+    for (int m : {PBAG_SYN_GSL, PBAG_SYN_BESSEL, PBAG_SYN_CSYN}) {
+      const std::vector<float> t = syn_table2(m, u2, h2, n2);
+      t2.insert(t2.end(), t.begin(), t.end());
+    }
+    const float* t2p = nullptr;
+    ok(c->grid_upload(&t2p, t2));
+    d.syntab2 = reinterpret_cast<const float2*>(t2p);
+    d.syn2_u0 = (float)u2;
+    d.syn2_ih = (float)(1. / h2);
+    d.syn2_n = n2;
     // GSL: x = (h nu / m_e c^2) / (1.5 B gamma^2 / 4.14e13) against nu / nu_crit = nu 4 pi m_e c / (3 q B gamma^2)
     d.gsl_xs = (float)(cgs::h_by_mec2 * 4.14e13 / 1.5 / (4. * M_PI * cgs::m_e * cgs::c_light / (3. * cgs::q_e)));
   }

@@ -47,6 +47,9 @@ struct DevGrid {
   const float* lnnu;     // [F]   ln nu
   float syn_u0, syn_ih;  // first u of syntab and the inverse spacing
   int syn_n;             // points of each table (zero after them)
+  const float2* syntab2; // [3][kSynTab2N] value / slope pairs of the same functions (batch sums)
+  float syn2_u0, syn2_ih;
+  int syn2_n;
   float gsl_xs;          // the GSL method's argument over nu / nu_crit (kernels.h:282-285)
   // pair production (numeric_model.h:295-356): FP32 tables of the rate kernel
   const float* ppinjT;   // [F][Gs] R(nu1_i, nu_k) (nu_{k+1} - nu_k), k < F-1 (nu1_i = 2 e_i m_e c^2 / h)

@@ -19,8 +19,14 @@ void build_grids(const pbag_grid_desc* g, double* gam, double* freq);
 constexpr int kSynTabN = 16384;
 constexpr double kSynTabXmin = 1e-12;
 constexpr double kSynTabXmax = 120.;
-void syn_table_grid(double dlng, double* u0, double* h, int* n);
+void syn_table_grid(double dlng, double* u0, double* h, int* n, int nmax = kSynTabN);
 std::vector<float> syn_table(int method, double u0, double h, int n);
+// The same function as value / slope pairs (g(u_i), (g(u_{i+1}) - g(u_{i-1})) / 2)
+// for interpolation around the nearest point, kSynTab2N pairs; the slope is 0
+// at the first point (g is flat there) and value and slope are 0 from the
+// last point on.
+constexpr int kSynTab2N = 8192;
+std::vector<float> syn_table2(int method, double u0, double h, int n);
 
 }  // namespace pbag
 

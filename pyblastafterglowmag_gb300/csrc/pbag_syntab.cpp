@@ -97,17 +97,18 @@ double synchrotron_aharonian(double x) {
 
 }  // namespace
 
-void syn_table_grid(double dlng, double* u0, double* h, int* n) {
+void syn_table_grid(double dlng, double* u0, double* h, int* n, int nmax) {
   // spacing: the step of ln(1/gamma^2) between neighbouring electron bins is
   // m spacings, m odd, so that the lanes of a warp (consecutive bins) read
   // the table at indices m apart: distinct shared-memory banks
   const double span = std::log(kSynTabXmax) - std::log(kSynTabXmin);
   const double step2 = 2. * dlng;
-  int m = (int)std::lround(step2 / 2e-3) | 1;
-  while (m > 1 && span / (step2 / m) + 2 > kSynTabN) m -= 2;
+  const double target = 2. * span / nmax;
+  int m = (int)std::lround(step2 / target) | 1;
+  while (m > 1 && span / (step2 / m) + 2 > nmax) m -= 2;
   *h = step2 / m;
   *u0 = std::log(kSynTabXmin);
-  *n = std::min(kSynTabN, (int)std::ceil(span / *h) + 2);
+  *n = std::min(nmax, (int)std::ceil(span / *h) + 2);
 }
 
 std::vector<float> syn_table(int method, double u0, double h, int n) {
@@ -120,6 +121,24 @@ std::vector<float> syn_table(int method, double u0, double h, int n) {
     g[i] = (float)(R * std::exp(-u / 3.));
   }
   return g;
+}
+
+std::vector<float> syn_table2(int method, double u0, double h, int n) {
+  std::vector<double> g((size_t)n + 1, 0.);
+  for (int i = 0; i < n; ++i) {
+    const double u = u0 + i * h, x = std::exp(u);
+    const double R = method == PBAG_SYN_GSL      ? synchrotron_F(x)
+                     : method == PBAG_SYN_BESSEL ? synchrotron_bessel(x)
+                                                 : synchrotron_aharonian(x);
+    g[i] = R * std::exp(-u / 3.);
+  }
+  g[n - 1] = 0.;  // from the last point on: zero
+  std::vector<float> t((size_t)2 * kSynTab2N, 0.f);
+  for (int i = 0; i < n - 1; ++i) {
+    t[2 * i] = (float)g[i];
+    t[2 * i + 1] = i == 0 ? 0.f : (float)(0.5 * (g[i + 1] - g[i - 1]));
+  }
+  return t;
 }
 
 }  // namespace pbag
