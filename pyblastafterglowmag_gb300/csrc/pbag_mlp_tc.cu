@@ -36,9 +36,10 @@ using tc::smem_u32;
 constexpr int kMtRows = 128;
 constexpr int kMtEpiWarps = 8;
 constexpr int kMtThreads = 32 * (kMtEpiWarps + 1);
-constexpr int kMtStages = 8;
-constexpr int kMtKc = 32;                                     // K columns per stage
-constexpr uint32_t kMtStageBytes = kMtMaxOut * kMtKc * 2;     // 16 KiB
+constexpr int kMtStages = 4;
+constexpr int kMtKc = 32;                                     // K columns of a stage: a multiple of this
+constexpr int kMtKcMax = 64;                                  // ... up to this (fewer, larger copies)
+constexpr uint32_t kMtStageBytes = kMtMaxOut * kMtKcMax * 2;  // 32 KiB
 constexpr uint32_t kMtActBytes = kMtRows * kMtMaxOut * 2;     // 64 KiB
 constexpr size_t kMtSmem = 1024 + kMtActBytes + (size_t)kMtStages * kMtStageBytes;
 
@@ -86,17 +87,20 @@ k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y,
   if (warp == kMtEpiWarps) {
     if (lane == 0) {
       // copies and MMAs
+      // K columns per stage of layer l: 64 where the in-dimension allows
+      auto kcl = [&](int l) { return a.dims[l] % kMtKcMax == 0 ? kMtKcMax : kMtKc; };
       int total = 0;
-      for (int l = 0; l < a.L; ++l) total += a.dims[l] / kMtKc;
+      for (int l = 0; l < a.L; ++l) total += a.dims[l] / kcl(l);
       int ll = 0, lc = 0;  // next chunk to copy: layer, chunk
       auto load_next = [&](int st) {
         const int N = a.dims[ll + 1];
-        const uint32_t bytes = (uint32_t)N * kMtKc * 2;
+        const int kc = kcl(ll);
+        const uint32_t bytes = (uint32_t)N * kc * 2;
         const uint32_t bar = smem_u32(&bars[st]);
         tc::mbar_expect_tx(bar, bytes);
         tc::bulk_g2s(smem_u32(ring + (size_t)st * kMtStageBytes),
-                     a.W[ll] + (size_t)lc * N * kMtKc, bytes, bar);
-        if (++lc == a.dims[ll] / kMtKc) {
+                     a.W[ll] + (size_t)lc * N * kc, bytes, bar);
+        if (++lc == a.dims[ll] / kc) {
           lc = 0;
           ++ll;
         }
@@ -111,7 +115,7 @@ k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y,
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int N = a.dims[l + 1], nc = a.dims[l] / kMtKc;
+        const int N = a.dims[l + 1], kc = kcl(l), nc = a.dims[l] / kc;
         const uint32_t idesc = tc::idesc_mma(kMtRows, N, false);
         for (int c = 0; c < nc; ++c) {
           const int st = g % kMtStages;
@@ -121,9 +125,8 @@ k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y,
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sb = smem_u32(ring + (size_t)st * kMtStageBytes);
-#pragma unroll
-          for (int s = 0; s < kMtKc / 16; ++s) {
-            const uint64_t ad = tc::smem_desc(smem_u32(act) + (uint32_t)(4 * c + 2 * s) * kMtRows * 16,
+          for (int s = 0; s < kc / 16; ++s) {
+            const uint64_t ad = tc::smem_desc(smem_u32(act) + (uint32_t)((kc / 8) * c + 2 * s) * kMtRows * 16,
                                               kMtRows * 16, 128);
             const uint64_t bd = tc::smem_desc(sb + (uint32_t)(2 * s) * N * 16, (uint32_t)N * 16, 128);
             tc::mma_issue<false>(tmem, ad, bd, idesc, (c > 0 || s > 0) ? 1u : 0u);
