@@ -59,11 +59,8 @@ def parse():
     return ap.parse_args()
 
 
-def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+from pyblastafterglowmag_gb300.replicas import dist_info  # noqa: E402
+from pyblastafterglowmag_gb300 import replicas  # noqa: E402
 
 
 def workload():
@@ -222,9 +219,7 @@ def gb300_arm(args):
     import torch
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    replicas.init(world)
     from pyblastafterglowmag_gb300 import _lib, abi, build
     build.build()
     cfg, recs, off, prm, grid = workload()
@@ -243,9 +238,7 @@ def gb300_arm(args):
     stream = torch.cuda.current_stream(dev)
 
     def barrier():
-        torch.cuda.synchronize(dev)
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier(world, dev)
 
     def one_pass():
         ctx.run_device(d_prm.data_ptr(), nbw, off, d_recs.data_ptr(), d_ptrs)
@@ -288,12 +281,8 @@ def gb300_arm(args):
     timing = ctx.timing()
     ctx.set_timing(False)
     prof_passes = 1
-    total_ms = float(sum(ev_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * nvalid * args.steps / (total_ms * 1e-3)
+    total_ms = replicas.max_over_ranks(float(sum(ev_ms)), world)
+    value = replicas.job_rate(nvalid * args.steps, total_ms * 1e-3, world)
 
     # end to end through the host-buffer entry point (pinned host memory)
     h_recs = torch.from_numpy(recs.view(np.uint8).copy()).pin_memory()
@@ -325,12 +314,8 @@ def gb300_arm(args):
         t0 = time.perf_counter()
         e2e_pass()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_t)
-    if world > 1:
-        t = torch.tensor([e2e_total], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * nvalid * args.steps / e2e_total
+    e2e_total = replicas.max_over_ranks(sum(e2e_t), world)
+    e2e_value = replicas.job_rate(nvalid * args.steps, e2e_total, world)
     h2d = int(recs.nbytes + prm.nbytes + off_c.nbytes)
     d2h = int(nrec * F * 8 * len(outs))
 
@@ -536,9 +521,12 @@ def sweep_arm(args):
     import torch
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
+    replicas.init(world)
     from pyblastafterglowmag_gb300 import _lib, abi, build, histories as H
     build.build()
-    recs, off, prm, grid = H.sweep_batch(_lib, args.sets, seed=3, workers=os.cpu_count() or 1)
+    # rank r runs sets r*sets .. (r+1)*sets-1 of the seeded sweep (weak scaling)
+    recs, off, prm, grid = H.sweep_batch(_lib, args.sets, seed=3, workers=os.cpu_count() or 1,
+                                         first=rank * args.sets)
     nvalid = int((recs["mode"] != 0).sum())
     nrec, nbw, F = len(recs), len(prm), grid.nfreq
     dev = torch.device("cuda", local)
@@ -561,6 +549,7 @@ def sweep_arm(args):
         flush.zero_()
         one_pass()
     ms = []
+    replicas.barrier(world, dev)
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.zero_()
@@ -572,12 +561,14 @@ def sweep_arm(args):
             e1.record()
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
-    t = sum(ms) / len(ms)
+    replicas.barrier(world, dev)
+    t = replicas.max_over_ranks(sum(ms) / len(ms), world)
+    value = replicas.job_rate(nvalid, t * 1e-3, world)
     if rank != 0:
         return
     lens = np.diff(off)
-    line = {"metric": "blastwave-steps/s (sync+SSC) on 1 GB300, uneven sweep", "value": nvalid / (t * 1e-3),
-            "unit": "blastwave-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+    line = {"metric": "blastwave-steps/s (sync+SSC) on 1 GB300, uneven sweep", "value": value,
+            "unit": "blastwave-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32",
             "data": "synthetic",
             "config": {"workload": f"uneven-sweep-{args.sets}-sets-201x128", "sets": args.sets, "blastwaves": nbw,
@@ -591,6 +582,37 @@ def sweep_arm(args):
 
 
 # ------------------------------------------------------- surrogate arm ---
+def surrogate_profile(args, dev, n=100_000):
+    """Kernel passes for ncu captures of the surrogate's kernels: n seeded
+    states on the 201 x 128 grid (seed photons = their own synchrotron
+    spectra), a random-init network with no fallback (the same kernels and
+    shapes as a trained one), args.profile surrogate passes, then as many
+    exact split-BF16 contractions."""
+    import torch
+    from pyblastafterglowmag_gb300 import _lib, abi, contraction as CT, surrogate as SG
+    g = CT.grid_desc(ngam=201, nfreq=128)
+    gam, freq = _lib.grids(g)
+    f, B = CT.states(gam, n, seed=4)
+    ctx = _lib.Context(g, dev.index, ssc=True)
+    d_f = torch.from_numpy(f).to(dev)
+    d_B = torch.from_numpy(B).to(dev)
+    d_js = torch.zeros((n, g.nfreq), dtype=torch.float64, device=dev)
+    ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), 0, abi.PBAG_SYN_CSYN, abi.PBAG_PREC_FP32,
+                        d_js.data_ptr(), 0)
+    nph = torch.from_numpy(CT.seed_photons(d_js.cpu().numpy(), freq)).to(dev)
+    SG.configure(ctx)
+    tr = SG.Trainer(g.nfreq, dev.index, seed=0)
+    SG.configure(ctx, tr.net, tr.mean, tr.std, tol=1e30)
+    j = torch.zeros((n, g.nfreq), dtype=torch.float64, device=dev)
+    for _ in range(args.profile):
+        SG.contract(ctx, n, d_f.data_ptr(), d_B.data_ptr(), nph.data_ptr(), j.data_ptr())
+    for _ in range(args.profile):
+        ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), nph.data_ptr(), abi.PBAG_SYN_CSYN,
+                            abi.PBAG_PREC_SPLIT_BF16, 0, j.data_ptr())
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile_passes": args.profile, "states": n, "workload": "surrogate-kernels-201x128"}))
+
+
 def surrogate_arm(args):
     """SSC surrogate: trained on states of a seeded sweep (the plain GPU step),
     evaluated on held-out states against the exact contraction (split BF16),
@@ -602,6 +624,8 @@ def surrogate_arm(args):
     from pyblastafterglowmag_gb300 import _lib, abi, build, histories as H, surrogate as SG
     build.build()
     dev = torch.device("cuda", local)
+    if args.profile:
+        return surrogate_profile(args, dev)
     cfg, recs, off, prm, g = workload()
     _, freq = _lib.grids(g)
     ctx = _lib.Context(g, device=local, ssc=True)

@@ -51,30 +51,44 @@ __device__ __forceinline__ float tf32_rna(float x) {
 // grid factors are formed as FP32 mantissa times power of two (f64_mant):
 // every weight keeps FP32 accuracy, each row is scaled by a power of two to a
 // largest value in [1, 2), and the scale goes to the per-state scalars.
+// WPL: electron bins per lane (Gp <= 32 WPL); the mantissas and exponents of
+// N(gamma) stay in registers, the SSC row is staged in shared memory for the
+// tile's 16-byte rows of eight consecutive bins.
+template <int WPL>
 __global__ void __launch_bounds__(32 * kPrepWarps)
 k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __restrict__ Bf,
                 const double* __restrict__ nph, int syn_method, int mode, int want_syn, int want_ssc, DevState S,
                 unsigned char* __restrict__ Wt, pbag_shock_params* __restrict__ prm) {
+  __shared__ __align__(16) float srow_all[kPrepWarps][32 * WPL];
   const int lane = threadIdx.x & 31;
   const int s = blockIdx.x * kPrepWarps + (threadIdx.x >> 5);
   if (s >= n) return;
+  float* srow = srow_all[threadIdx.x >> 5];
   const int G = g.G, F = g.F;
   const double* fs = f + (size_t)s * G;
   const float* m_de = g.tmant + (size_t)kM32De * g.Tm;
   const int* e_de = g.texp + (size_t)kM32De * g.Tm;
   const float* m_w = g.tmant + (size_t)kM32DeIe2 * g.Tm;
   const int* e_w = g.texp + (size_t)kM32DeIe2 * g.Tm;
-  // largest exponents of f_j dgamma_j and f_j dgamma_j / gamma_j^2
+  // N(gamma) as mantissa and exponent (bin lane + 32 q), and the largest
+  // exponents of f_j dgamma_j and f_j dgamma_j / gamma_j^2
+  float mf[WPL];
+  int ef[WPL];
   int wexp = kExpZero, Wexp = kExpZero;
-  for (int j = lane; j < G - 1; j += 32) {
-    int ef;
-    const float mf = f64_mant(fs[j], ef);
-    int e1 = ef + e_de[j], e2 = ef + e_w[j];
-    mant_mul(mf, m_de[j], e1);
-    mant_mul(mf, m_w[j], e2);
-    if (mf != 0.f) {
-      wexp = max(wexp, e1);
-      Wexp = max(Wexp, e2);
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const int j = lane + 32 * q;
+    mf[q] = 0.f;
+    ef[q] = kExpZero;
+    if (j < G - 1) {
+      mf[q] = f64_mant(__ldg(fs + j), ef[q]);
+      if (mf[q] != 0.f) {
+        int e1 = ef[q] + __ldg(e_de + j), e2 = ef[q] + __ldg(e_w + j);
+        mant_mul(mf[q], __ldg(m_de + j), e1);
+        mant_mul(mf[q], __ldg(m_w + j), e2);
+        wexp = max(wexp, e1);
+        Wexp = max(Wexp, e2);
+      }
     }
   }
   wexp = __reduce_max_sync(0xffffffffu, wexp);
@@ -84,50 +98,66 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
   double* scal = S.scal + (size_t)s * kScal;
   if (want_syn) {
     float* w32 = S.w32 + (size_t)s * G;
-    for (int j = lane; j < G; j += 32) {
-      float w = 0.f;
-      if (j < G - 1) {
-        int e;
-        const float mf = f64_mant(fs[j], e);
-        e += e_de[j];
-        w = f32_ldexp(mant_mul(mf, m_de[j], e), e - wexp);
+#pragma unroll
+    for (int q = 0; q < WPL; ++q) {
+      const int j = lane + 32 * q;
+      if (j < G) {
+        float w = 0.f;
+        if (j < G - 1) {
+          int e = ef[q] + __ldg(e_de + j);
+          w = f32_ldexp(mant_mul(mf[q], __ldg(m_de + j), e), e - wexp);
+        }
+        w32[j] = w;
       }
-      w32[j] = w;
     }
   }
   if (want_ssc) {
-    float* W = S.W32 + (size_t)s * g.Gp;
-    auto wval = [&](int j) {
-      if (j >= G - 1) return 0.f;
-      int e;
-      const float mf = f64_mant(fs[j], e);
-      e += e_w[j];
-      return f32_ldexp(mant_mul(mf, m_w[j], e), e - Wexp);
-    };
-    for (int j = lane; j < g.Gp; j += 32) W[j] = wval(j);
+    const int Gp = g.Gp;
     const int m = s % kTcCols;
-    unsigned char* tile = Wt ? Wt + (size_t)(s / kTcCols) * tc_tile_bytes(kTcCols, g.Gp, mode == kTcTf32 ? 4 : 2)
+    unsigned char* tile = Wt ? Wt + (size_t)(s / kTcCols) * tc_tile_bytes(kTcCols, Gp, mode == kTcTf32 ? 4 : 2)
                              : nullptr;
+    // the SSC weights of the row: to the FP32 rows (CUDA-core contraction) or
+    // through shared memory to the tensor-core tile
+    float* W = S.W32 + (size_t)s * Gp;
+#pragma unroll
+    for (int q = 0; q < WPL; ++q) {
+      const int j = lane + 32 * q;
+      if (j < Gp) {
+        float w = 0.f;
+        if (j < G - 1) {
+          int e = ef[q] + __ldg(e_w + j);
+          w = f32_ldexp(mant_mul(mf[q], __ldg(m_w + j), e), e - Wexp);
+        }
+        if (tile)
+          srow[j] = w;
+        else
+          W[j] = w;
+      }
+    }
+    __syncwarp();
     if (tile && mode == kTcTf32) {
-      for (int j = lane; j < g.Gp; j += 32)
-        *reinterpret_cast<float*>(tile + tc_operand_byte_offset(m, j, kTcCols, g.Gp, 4, false)) = tf32_rna(wval(j));
+      for (int j = lane; j < Gp; j += 32)
+        *reinterpret_cast<float*>(tile + tc_operand_byte_offset(m, j, kTcCols, Gp, 4, false)) = tf32_rna(srow[j]);
     } else if (tile) {
       // eight consecutive K columns of a row are one 16-byte row of a core
       // matrix: hi and lo parts written as 16-byte words
-      for (int q = lane; q < g.Gp / 8; q += 32) {
+      for (int q = lane; q < Gp / 8; q += 32) {
+        const float4 a = *reinterpret_cast<const float4*>(srow + 8 * q);
+        const float4 b = *reinterpret_cast<const float4*>(srow + 8 * q + 4);
+        const float wv[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
         uint32_t hi[4], lo[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          const float w0 = wval(8 * q + 2 * e), w1 = wval(8 * q + 2 * e + 1);
+          const float w0 = wv[2 * e], w1 = wv[2 * e + 1];
           const __nv_bfloat16 h0 = __float2bfloat16_rn(w0), h1 = __float2bfloat16_rn(w1);
           const __nv_bfloat16 l0 = __float2bfloat16_rn(w0 - __bfloat162float(h0));
           const __nv_bfloat16 l1 = __float2bfloat16_rn(w1 - __bfloat162float(h1));
           hi[e] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
           lo[e] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
         }
-        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, g.Gp, 2, false)) =
+        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, Gp, 2, false)) =
             make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, g.Gp, 2, true)) =
+        *reinterpret_cast<uint4*>(tile + tc_operand_byte_offset(m, 8 * q, kTcCols, Gp, 2, true)) =
             make_uint4(lo[0], lo[1], lo[2], lo[3]);
       }
     }
@@ -177,6 +207,14 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
     p.ssc_on = want_ssc;
     prm[s] = p;
   }
+}
+
+template <typename... A>
+void launch_prep(int Gp, int blocks, cudaStream_t st, A... args) {
+  if (Gp <= 32 * 8)
+    k_contract_prep<8><<<blocks, 32 * kPrepWarps, 0, st>>>(args...);
+  else
+    k_contract_prep<32><<<blocks, 32 * kPrepWarps, 0, st>>>(args...);
 }
 
 // Synchrotron sums of a large batch (computeSynSpectrum, numeric_model.h:
@@ -387,8 +425,8 @@ int contract_prepare(pbag_ctx* ctx, const CtxView& v, int n, const double* d_f, 
   if (e != cudaSuccess) return cuda_status(e);
   *S = ws->S;
   *Wt = ws->Wt;
-  k_contract_prep<<<(n + kPrepWarps - 1) / kPrepWarps, 32 * kPrepWarps, 0, v.stream>>>(
-      v.dg, n, d_f, nullptr, d_nph, PBAG_SYN_CSYN, kTcSplit, 0, 1, ws->S, ws->Wt, ws->prm);
+  launch_prep(v.dg.Gp, (n + kPrepWarps - 1) / kPrepWarps, v.stream, v.dg, n, d_f, (const double*)nullptr, d_nph,
+              (int)PBAG_SYN_CSYN, (int)kTcSplit, 0, 1, ws->S, ws->Wt, ws->prm);
   return cudaGetLastError() == cudaSuccess ? PBAG_OK : PBAG_ERR_CUDA;
 }
 }  // namespace pbag
@@ -438,9 +476,8 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   auto ok = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
   };
-  k_contract_prep<<<(n + kPrepWarps - 1) / kPrepWarps, 32 * kPrepWarps, 0, s>>>(
-      v.dg, n, d_f, d_B, d_nph, syn_method, mode, d_jsyn ? 1 : 0, d_jssc ? 1 : 0, S, tc && d_jssc ? ws->Wt : nullptr,
-      ws->prm);
+  launch_prep(v.dg.Gp, (n + kPrepWarps - 1) / kPrepWarps, s, v.dg, n, d_f, d_B, d_nph, syn_method, mode,
+              d_jsyn ? 1 : 0, d_jssc ? 1 : 0, S, tc && d_jssc ? ws->Wt : (unsigned char*)nullptr, ws->prm);
   ok(cudaGetLastError());
   // synchrotron sums (and the CUDA-core SSC contraction in FP32)
   const bool fp32_ssc = d_jssc && !tc;

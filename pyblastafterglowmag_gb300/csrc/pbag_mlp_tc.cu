@@ -36,12 +36,16 @@ using tc::smem_u32;
 constexpr int kMtRows = 128;
 constexpr int kMtEpiWarps = 8;
 constexpr int kMtThreads = 32 * (kMtEpiWarps + 1);
-constexpr int kMtStages = 4;
+// two CTAs per SM (shared memory 2 x 112 KiB, tensor memory 2 x 256 columns):
+// the MMAs and copies of one overlap the epilogue of the other
+constexpr int kMtCtasPerSm = 2;
+constexpr int kMtStages = 3;
 constexpr int kMtKc = 32;                                     // K columns of a stage: a multiple of this
-constexpr int kMtKcMax = 64;                                  // ... up to this (fewer, larger copies)
-constexpr uint32_t kMtStageBytes = kMtMaxOut * kMtKcMax * 2;  // 32 KiB
+constexpr int kMtKcMax = 32;                                  // ... up to this
+constexpr uint32_t kMtStageBytes = kMtMaxOut * kMtKcMax * 2;  // 16 KiB
 constexpr uint32_t kMtActBytes = kMtRows * kMtMaxOut * 2;     // 64 KiB
-constexpr size_t kMtSmem = 1024 + kMtActBytes + (size_t)kMtStages * kMtStageBytes;
+constexpr size_t kMtSmem = 128 + kMtActBytes + (size_t)kMtStages * kMtStageBytes;
+static_assert(kMtCtasPerSm * (kMtSmem + 1024 + 256) <= 233472, "two CTAs per SM");
 
 // byte offset of element (row r, column k) of a K-major operand with `rows`
 // rows: core matrix (r/8, k/8) at (k/8)*rows*16 + (r/8)*128
@@ -54,14 +58,14 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-__global__ void __launch_bounds__(kMtThreads, 1)
+__global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm)
 k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y, int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ uint64_t bars[2 * kMtStages + 2];  // full[S], empty[S], acc full, activations ready
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int fail;
   unsigned char* base =
-      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
   unsigned char* act = base;
   unsigned char* ring = base + kMtActBytes;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -186,8 +190,15 @@ k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y,
         uint32_t v[16];
         tc::tmem_ld16(tl + (uint32_t)col0, v);
         float y[16];
+        const float4* b4 = reinterpret_cast<const float4*>(bias + col0);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) y[c] = __uint_as_float(v[c]) + __ldg(bias + col0 + c);
+        for (int c = 0; c < 4; ++c) {
+          const float4 bb = __ldg(b4 + c);
+          y[4 * c] = __uint_as_float(v[4 * c]) + bb.x;
+          y[4 * c + 1] = __uint_as_float(v[4 * c + 1]) + bb.y;
+          y[4 * c + 2] = __uint_as_float(v[4 * c + 2]) + bb.z;
+          y[4 * c + 3] = __uint_as_float(v[4 * c + 3]) + bb.w;
+        }
         if (last) {
           if (row0 + r < n) {
             float4* dst = reinterpret_cast<float4*>(Y + (size_t)(row0 + r) * N + col0);
@@ -196,7 +207,7 @@ k_mlp_tc(MlpTcArgs a, int n, const float* __restrict__ X, float* __restrict__ Y,
           }
         } else {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) y[c] = y[c] / (1.f + __expf(-y[c]));  // SiLU
+          for (int c = 0; c < 16; ++c) y[c] = __fdividef(y[c], 1.f + __expf(-y[c]));  // SiLU (0 where exp overflows)
 #pragma unroll
           for (int k8 = 0; k8 < 2; ++k8) {
             const uint4 w = make_uint4(pack_bf16(y[8 * k8], y[8 * k8 + 1]), pack_bf16(y[8 * k8 + 2], y[8 * k8 + 3]),

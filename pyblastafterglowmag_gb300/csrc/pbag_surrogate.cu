@@ -42,7 +42,6 @@ constexpr int kNmom = 3 * kNb;
 constexpr int kNproj = PBAG_SUR_PROJ;
 constexpr int kNin = PBAG_SUR_IN;
 constexpr int kMaxF = 256;
-constexpr int kMaxPer = kMaxF / kNb;
 constexpr int kSurWarps = 4;          // states per CTA of the feature and reconstruction kernels (a warp each)
 constexpr float kFloor = -30.f;       // log10 floor of the shape features
 constexpr float kCorrMin = -8.f, kCorrMax = 4.f;  // range of the log10 correction applied
@@ -254,14 +253,17 @@ __device__ __forceinline__ float warp_max(float v) {
 // into the feasible set). The moment map of (beta, gamma) is the gradient of a
 // convex log-partition function, so Newton on it (steps clipped) converges
 // from zero. Writes beta hw, gamma hw^2 and the log10 shares.
-__global__ void k_sur_fit(int n, int F, int per, const double* __restrict__ proj, const float* __restrict__ xrel,
+template <int PER>
+__global__ void k_sur_fit(int n, int F, const double* __restrict__ proj, const float* __restrict__ xrel,
                           const float* __restrict__ hwv, float* __restrict__ fit, float* __restrict__ base) {
+  constexpr int per = PER;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * kNb) return;
   const int s = t / kNb, b = t % kNb;
   const double P = proj[(size_t)s * kNproj + b], Q = proj[(size_t)s * kNproj + kNb + b],
                R = proj[(size_t)s * kNproj + 2 * kNb + b];
-  float x[kMaxPer];
+  float x[PER];
+#pragma unroll
   for (int i = 0; i < per; ++i) x[i] = xrel[b * per + i];
   const float hw = hwv[b], lo = x[0], hi = x[per - 1];
   float beta = 0.f, gam = 0.f;
@@ -308,7 +310,9 @@ __global__ void k_sur_fit(int n, int F, int per, const double* __restrict__ proj
 // and of the seed photon density (strides fs, ns); B: field (stride bs); proj:
 // the exact projections; fit: the baseline parameters. Standardised when
 // mean/stdv are given. The FP64 inputs enter through mantissa and exponent
-// (f64_mant): no FP64 arithmetic per element.
+// (f64_mant): no FP64 arithmetic per element. WPL: electron bins per lane
+// (G - 1 <= 32 WPL), held in registers across the passes over N(gamma).
+template <int WPL>
 __global__ void __launch_bounds__(32 * kSurWarps)
 k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const double* __restrict__ nph, int ns,
                const double* __restrict__ Bv, int bs, const double* __restrict__ proj, const float* __restrict__ fit,
@@ -325,45 +329,53 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
   // electron weights w_j = f_j dgamma_j, scaled by a power of two into FP32
   const float* m_de = g.tmant + (size_t)kM32De * g.Tm;
   const int* e_de = g.texp + (size_t)kM32De * g.Tm;
-  auto wmant = [&](int j, int& e) {
-    const float mf = f64_mant(fr[j], e);
-    e += e_de[j];
-    return mant_mul(mf, m_de[j], e);
-  };
+  float wm[WPL];
+  int we[WPL];
   int wexp = kExpZero;
-  for (int j = lane; j < G - 1; j += 32) {
-    int e;
-    if (wmant(j, e) != 0.f) wexp = max(wexp, e);
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const int j = lane + 32 * q;
+    wm[q] = 0.f;
+    we[q] = kExpZero;
+    if (j < G - 1) {
+      const float mf = f64_mant(__ldg(fr + j), we[q]);
+      we[q] += __ldg(e_de + j);
+      wm[q] = mant_mul(mf, __ldg(m_de + j), we[q]);
+      if (wm[q] != 0.f) wexp = max(wexp, we[q]);
+    }
   }
   wexp = __reduce_max_sync(0xffffffffu, wexp);
   if (wexp == kExpZero) wexp = 0;
-  auto wval = [&](int j) {
-    int e;
-    const float m = wmant(j, e);
-    return f32_ldexp(m, e - wexp);
-  };
-  float m0 = 0.f, m1 = 0.f;
-  for (int j = lane; j < G - 1; j += 32) {
-    const float w = wval(j);
-    m0 += w;
-    m1 += w * -0.5f * logf(g.ginv2[j]);
+  float w[WPL], lg[WPL];
+  float m0 = 0.f, m1 = 0.f, wmax = 0.f;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const int j = lane + 32 * q;
+    w[q] = 0.f;
+    lg[q] = 0.f;
+    if (j < G - 1) {
+      w[q] = f32_ldexp(wm[q], we[q] - wexp);
+      lg[q] = -0.5f * __ldg(g.lnginv2 + j);  // ln gamma_j
+      m0 += w[q];
+      m1 += w[q] * lg[q];
+      wmax = fmaxf(wmax, w[q]);
+    }
   }
   m0 = warp_sum(m0);
   m1 = warp_sum(m1);
+  wmax = warp_max(wmax);
   const float mu = m0 > 0.f ? m1 / m0 : 0.f;
-  float c2 = 0.f, c3 = 0.f, c4 = 0.f, wmax = 0.f;
-  for (int j = lane; j < G - 1; j += 32) {
-    const float w = wval(j);
-    const float d = -0.5f * logf(g.ginv2[j]) - mu;
-    c2 += w * d * d;
-    c3 += w * d * d * d;
-    c4 += w * d * d * d * d;
-    wmax = fmaxf(wmax, w);
+  float c2 = 0.f, c3 = 0.f, c4 = 0.f;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const float d = lg[q] - mu, wd2 = w[q] * d * d;
+    c2 += wd2;
+    c3 += wd2 * d;
+    c4 += wd2 * d * d;
   }
   c2 = warp_sum(c2);
   c3 = warp_sum(c3);
   c4 = warp_sum(c4);
-  wmax = warp_max(wmax);
   if (lane == 0) {
     const float var = m0 > 0.f ? c2 / m0 : 0.f;
     const float sd = sqrtf(fmaxf(var, 1e-30f));
@@ -376,37 +388,58 @@ k_sur_features(DevGrid g, int n, const double* __restrict__ f, int fs, const dou
     feat[kFtMom + 3] = m0 > 0.f ? c3 / m0 / (sd * sd * sd) : 0.f;
     feat[kFtMom + 4] = m0 > 0.f ? c4 / m0 / (var * var + 1e-30f) : 0.f;
   }
-  if (lane < kElePts) {
-    const int j = (int)lrintf(lane * (float)(G - 2) / (float)(kElePts - 1));
-    const float w = wval(j);
-    feat[kFtEle + lane] = wmax > 0.f ? fmaxf(log10f(fmaxf(w / wmax, 1e-30f)), kFloor) : kFloor;
+  // N(gamma) at kElePts bins spread over the grid, relative to its largest weight
+  // (bin j sits in lane j % 32, register j / 32)
+  {
+    const int j = lane < kElePts ? (int)lrintf(lane * (float)(G - 2) / (float)(kElePts - 1)) : 0;
+    float wj = 0.f;
+#pragma unroll
+    for (int q = 0; q < WPL; ++q) {
+      const float v = __shfl_sync(0xffffffffu, w[q], j & 31);
+      if (q == (j >> 5)) wj = v;
+    }
+    if (lane < kElePts) feat[kFtEle + lane] = wmax > 0.f ? fmaxf(log10f(fmaxf(wj / wmax, 1e-30f)), kFloor) : kFloor;
   }
   // seed photon shape on kSeedPts frequencies: u_k = n_k dnu_k / nu_k
   const float* m_u = g.tmant + (size_t)kM32DnuNu * g.Tm;
   const int* e_u = g.texp + (size_t)kM32DnuNu * g.Tm;
-  auto umant = [&](int k, int& e) {
-    const float mn = f64_mant(nr[k], e);
-    e += e_u[k];
-    return mant_mul(mn, m_u[k], e);
-  };
+  // (frequency k = lane + 32 q in register q; F <= 256)
+  float um[8];
+  int ue[8];
   int uexp = kExpZero;
-  for (int k = lane; k < F; k += 32) {
-    int e;
-    if (umant(k, e) != 0.f) uexp = max(uexp, e);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int k = lane + 32 * q;
+    um[q] = 0.f;
+    ue[q] = kExpZero;
+    if (k < F) {
+      const float mn = f64_mant(__ldg(nr + k), ue[q]);
+      ue[q] += __ldg(e_u + k);
+      um[q] = mant_mul(mn, __ldg(m_u + k), ue[q]);
+      if (um[q] != 0.f) uexp = max(uexp, ue[q]);
+    }
   }
   uexp = __reduce_max_sync(0xffffffffu, uexp);
   if (uexp == kExpZero) uexp = 0;
-  auto uval = [&](int k) {
-    int e;
-    const float m = umant(k, e);
-    return f32_ldexp(m, e - uexp);
-  };
+  float uv[8];
   float umax = 0.f;
-  for (int k = lane; k < F; k += 32) umax = fmaxf(umax, uval(k));
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    uv[q] = lane + 32 * q < F ? f32_ldexp(um[q], ue[q] - uexp) : 0.f;
+    umax = fmaxf(umax, uv[q]);
+  }
   umax = warp_max(umax);
-  for (int q = lane; q < kSeedPts; q += 32) {
-    const float u = uval(q * F / kSeedPts);
-    feat[kFtSeed + q] = umax > 0.f ? fmaxf(log10f(fmaxf(u / umax, 1e-30f)), kFloor) : kFloor;
+  // kSeedPts frequencies k = q F / kSeedPts: register k / 32 of lane k % 32
+  for (int q0 = 0; q0 < kSeedPts; q0 += 32) {
+    const int k = (q0 + lane) * F / kSeedPts;
+    float u = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float v = __shfl_sync(0xffffffffu, uv[q], k & 31);
+      if (q == (k >> 5)) u = v;
+    }
+    if (q0 + lane < kSeedPts)
+      feat[kFtSeed + q0 + lane] = umax > 0.f ? fmaxf(log10f(fmaxf(u / umax, 1e-30f)), kFloor) : kFloor;
   }
   // band powers (log10 relative to the largest) and the baseline's slope and curvature
   float lp = -1e30f;
@@ -512,6 +545,14 @@ int status_of(cudaError_t e) { return e == cudaErrorMemoryAllocation ? PBAG_ERR_
 
 unsigned warps_grid(int n) { return (unsigned)((n + kSurWarps - 1) / kSurWarps); }
 
+template <typename... A>
+void launch_features(int G, unsigned grid, cudaStream_t st, A... args) {
+  if (G - 1 <= 32 * 8)
+    k_sur_features<8><<<grid, 32 * kSurWarps, 0, st>>>(args...);
+  else
+    k_sur_features<32><<<grid, 32 * kSurWarps, 0, st>>>(args...);
+}
+
 // exact projections and baseline fits of nrows rows (proj, fit, base)
 cudaError_t project_and_fit(Surrogate* sg, const CtxView& v, int nrows, const void* Wt, const int* flags,
                             const float* U32, const double* scal, double* proj, float* base, int* errs,
@@ -520,8 +561,11 @@ cudaError_t project_and_fit(Surrogate* sg, const CtxView& v, int nrows, const vo
                                      kNproj, proj, errs, st);
   if (e != cudaSuccess) return e;
   const int threads = 128;
-  k_sur_fit<<<(unsigned)((nrows * kNb + threads - 1) / threads), threads, 0, st>>>(nrows, v.F, sg->per, proj,
-                                                                                  sg->xrel, sg->hw, sg->fit, base);
+  const unsigned grid = (unsigned)((nrows * kNb + threads - 1) / threads);
+  if (sg->per == 8)
+    k_sur_fit<8><<<grid, threads, 0, st>>>(nrows, v.F, proj, sg->xrel, sg->hw, sg->fit, base);
+  else
+    k_sur_fit<16><<<grid, threads, 0, st>>>(nrows, v.F, proj, sg->xrel, sg->hw, sg->fit, base);
   return cudaGetLastError();
 }
 
@@ -547,7 +591,7 @@ cudaError_t surrogate_run(pbag_ctx* ctx, const CtxView& v, int nrows, const void
   };
   ok(project_and_fit(sg, v, nrows, Wt, flags, U32, scal, sg->proj, sg->base, errs, st));
   if (e == cudaSuccess)
-    k_sur_features<<<warps_grid(nrows), 32 * kSurWarps, 0, st>>>(v.dg, nrows, f, fs, nph, ns, Bv, bs, sg->proj,
+    launch_features(v.dg.G, warps_grid(nrows), st, v.dg, nrows, f, fs, nph, ns, Bv, bs, sg->proj,
                                                                   sg->fit, sg->mean, sg->stdv, sg->X);
   ok(cudaGetLastError());
   ok(mlp_infer(sg->net, nrows, sg->X, sg->Y, st));
@@ -684,7 +728,7 @@ int pbag_surrogate_features(pbag_ctx* ctx, int n, const double* d_f, const doubl
   float* base = d_base ? d_base : sg->base;
   if (e == cudaSuccess) e = project_and_fit(sg, v, n, Wt, S.flags, S.U32, S.scal, proj, base, S.err, v.stream);
   if (e == cudaSuccess && d_x) {
-    k_sur_features<<<warps_grid(n), 32 * kSurWarps, 0, v.stream>>>(v.dg, n, d_f, v.G, d_nph, v.F, d_B, 1, proj,
+    launch_features(v.dg.G, warps_grid(n), v.stream, v.dg, n, d_f, v.G, d_nph, v.F, d_B, 1, proj,
                                                                     sg->fit, nullptr, nullptr, d_x);
     e = cudaGetLastError();
   }

@@ -343,16 +343,18 @@ def _sweep_set(cfg):
 
 
 def sweep_batch(lib, nsets, seed=3, ngam=201, nfreq=128, min_steps=200, max_steps=2000, ssc=True,
-                max_layers=41, workers=1):
+                max_layers=41, workers=1, first=0):
     """Seeded parameter sweep: nsets jets, each a top-hat or Gaussian with
     1..max_layers layers, log10 E_iso ~ U[50,54], log10 Gamma0 ~ U[1,3],
     log10 n ~ U[-4,0], log10 eps_e ~ U[-3,-0.5], log10 eps_b ~ U[-5,-1],
     p ~ U[2.05,2.8]; every blastwave keeps its first U{min_steps..max_steps}
-    steps (uneven histories). workers > 1 builds the jets in a process pool
-    (spawned, so it is safe next to a CUDA context)."""
+    steps (uneven histories). first: index of the first set in the seeded
+    sequence (sets first .. first+nsets-1 of the same sweep, so that ranks
+    can take disjoint shards of it). workers > 1 builds the jets in a process
+    pool (spawned, so it is safe next to a CUDA context)."""
     rng = np.random.default_rng(seed)
     cfgs, counts = [], []
-    for _ in range(nsets):
+    for i in range(first + nsets):
         struct = "tophat" if rng.random() < 0.5 else "gaussian"
         nl = int(rng.integers(1, max_layers + 1))
         sh = dict(eps_e=10 ** rng.uniform(-3, -0.5), eps_b=10 ** rng.uniform(-5, -1),
@@ -362,8 +364,10 @@ def sweep_batch(lib, nsets, seed=3, ngam=201, nfreq=128, min_steps=200, max_step
                         Gamma0=10 ** rng.uniform(1, 3), theta_c=tc, theta_w=min(4 * tc, 0.6),
                         n_ism=10 ** rng.uniform(-4, 0), nlayers=nl, fs=Shock(**sh), rs=Shock(**sh),
                         ngam=ngam, gam1=1.0, gam2=1e9, nfreq=nfreq, ntb=max_steps)
-        cfgs.append(cfg)
-        counts.append([int(rng.integers(min_steps, max_steps + 1)) for _ in range(2 * nl)])
+        cnt = [int(rng.integers(min_steps, max_steps + 1)) for _ in range(2 * nl)]
+        if i >= first:
+            cfgs.append(cfg)
+            counts.append(cnt)
     if workers > 1 and nsets > 1:
         import multiprocessing as mp
         with mp.get_context("spawn").Pool(min(workers, nsets)) as pool:
