@@ -371,6 +371,7 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
 // the epilogue of k_ssc_tc. Shared memory: [slab: chunks of (hi | lo) F rows,
 // reused by the product table][W: chunks of (hi | lo) N rows][U: N x F][barrier].
 constexpr int kSmallN = 64;
+static_assert(2 * kSmallN <= kTcThreads, "one W row part per thread in k_ssc_tc_small");
 __host__ __device__ constexpr size_t small_slab_bytes(int Gp) { return (size_t)2 * kTcK * Gp * 2; }
 __host__ __device__ constexpr size_t small_w_bytes(int N, int Gp) { return (size_t)2 * N * Gp * 2; }
 inline size_t small_smem(int N, int Gp) {
@@ -390,6 +391,8 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
   __shared__ uint64_t mbar;
   __shared__ uint32_t tmem_slot;
   __shared__ int fail;
+  __shared__ double sh_fac[kSmallN];  // per column: output factor
+  __shared__ int sh_live[kSmallN];    // per column: a live row
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
   const int row0 = blockIdx.y * kTcCols;
@@ -416,14 +419,18 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
   }
   // W rows [row0, row0 + N) of both parts of every chunk, and the U rows
   const unsigned char* Wtile = Wt + (size_t)blockIdx.y * tc_tile_bytes(kTcCols, Gp, 2);
-  const int units = N * nk8 * 2;  // 16-byte units of W
-  for (int u = tid; u < units; u += kTcThreads) {
-    const int part = u % 2, q = u / 2, r = q % N, k16 = q / N;  // row, 16-byte K column
-    const int c = k16 / kK8, kk = k16 % kK8, kc = min(kK8, nk8 - c * kK8);
-    const size_t within = (size_t)((r >> 3) * kc + kk) * 128 + (size_t)(r & 7) * 16;
-    const unsigned char* src = Wtile + (size_t)2 * kTcCols * kK8 * 16 * c + (size_t)part * kTcCols * kc * 16 + within;
-    const uint32_t dst = smem_u32(Bs + (size_t)2 * N * kK8 * 16 * c + (size_t)part * N * kc * 16 + within);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  // thread (row r, part) of the first 2N threads copies its 16-byte unit of
+  // every K column (2N <= kTcThreads): no division by the runtime N
+  if (tid < 2 * N) {
+    const int part = tid & 1, r = tid >> 1;
+    for (int k16 = 0; k16 < nk8; ++k16) {
+      const int c = k16 / kK8, kk = k16 - c * kK8, kc = min(kK8, nk8 - c * kK8);
+      const size_t within = (size_t)((r >> 3) * kc + kk) * 128 + (size_t)(r & 7) * 16;
+      const unsigned char* src =
+          Wtile + (size_t)2 * kTcCols * kK8 * 16 * c + (size_t)part * kTcCols * kc * 16 + within;
+      const uint32_t dst = smem_u32(Bs + (size_t)2 * N * kK8 * 16 * c + (size_t)part * N * kc * 16 + within);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
   }
   for (int u = tid; u < N * F / 4; u += kTcThreads) {
     const int r = u / (F / 4), k4 = u % (F / 4);
@@ -442,6 +449,10 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
     const bool in = col < N && r < nrows;
     live[q] = in && (flags[r] & kFlagActive);
     fac[q] = in ? hnu * scal[(size_t)r * kScal + kScalSW] * scal[(size_t)r * kScal + kScalSU] : 0.;
+    if (col < N) {  // published by the barriers below
+      sh_fac[col] = fac[q];
+      sh_live[col] = live[q] ? 1 : 0;
+    }
   }
   uint32_t ncols = 32;
   while (ncols < (uint32_t)N) ncols <<= 1;
@@ -504,21 +515,29 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
         P[(size_t)(cb * 16 + c) * kPStride + tid] = __uint_as_float(v[c]) * Us[(size_t)(cb * 16 + c) * F + tid];
     }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      if (!live[q]) continue;
-      const int col = tid + q * kTcThreads;
-      const float* row = P + (size_t)col * kPStride;
+    // sum over k of each column by a pair of neighbouring threads (half of k
+    // each, the second half in a rotated order so the pair reads distinct banks)
+    {
+      const int col = tid >> 1, half = tid & 1;
+      const bool in = col < N && sh_live[col] != 0;
       float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-#pragma unroll 8
-      for (int k = 0; k < kTcK; k += 4) {
-        a0 += row[k];
-        a1 += row[k + 1];
-        a2 += row[k + 2];
-        a3 += row[k + 3];
+      if (in) {
+        const float* row = P + (size_t)col * kPStride + (kTcK / 2) * half;
+#pragma unroll 4
+        for (int kk = 0; kk < kTcK / 2; kk += 4) {
+          const int k = (kk + 16 * half) & (kTcK / 2 - 1);
+          a0 += row[k];
+          a1 += row[k + 1];
+          a2 += row[k + 2];
+          a3 += row[k + 3];
+        }
       }
-      const int orow = rowmap ? rowmap[row0 + col] : row0 + col;
-      out[(size_t)orow * ostride + i] = fac[q] * (double)((a0 + a1) + (a2 + a3));
+      float v = (a0 + a1) + (a2 + a3);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (in && half == 0) {
+        const int orow = rowmap ? rowmap[row0 + col] : row0 + col;
+        out[(size_t)orow * ostride + i] = sh_fac[col] * (double)v;
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

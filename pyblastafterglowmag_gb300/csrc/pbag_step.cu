@@ -630,11 +630,54 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     double* gssc = gadi + G;
     const int Gs = g.Gs;
     bool hbad = false;
-    for (int i = tid; i < G - 1; i += kStepThreads) {
+    // SSC cooling GEMV of this thread's (at most two) bins together, two
+    // partial sums per bin: four independent FMA chains instead of one
+    float accA = 0.f, accB = 0.f;
+    const bool gemv2 = ssc && G - 1 <= 2 * kStepThreads;
+    if (gemv2 && tid < G - 1) {
+      const int i0 = tid, i1 = tid + kStepThreads < G - 1 ? tid + kStepThreads : tid;
+      const float* k0 = kint_smem ? sh_k + i0 : g.KintT + i0;
+      const float* k1 = kint_smem ? sh_k + i1 : g.KintT + i1;
+      float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+      int k = 0;
+      if (kint_smem) {
+#pragma unroll 4
+        for (; k + 1 < F - 1; k += 2) {
+          const float v0 = sh_v[k], v1 = sh_v[k + 1];
+          a0 = fmaf(v0, k0[(size_t)k * Gs], a0);
+          b0 = fmaf(v0, k1[(size_t)k * Gs], b0);
+          a1 = fmaf(v1, k0[(size_t)(k + 1) * Gs], a1);
+          b1 = fmaf(v1, k1[(size_t)(k + 1) * Gs], b1);
+        }
+        if (k < F - 1) {
+          a0 = fmaf(sh_v[k], k0[(size_t)k * Gs], a0);
+          b0 = fmaf(sh_v[k], k1[(size_t)k * Gs], b0);
+        }
+      } else {
+#pragma unroll 8
+        for (; k + 1 < F - 1; k += 2) {
+          const float v0 = sh_v[k], v1 = sh_v[k + 1];
+          a0 = fmaf(v0, __ldg(k0 + (size_t)k * Gs), a0);
+          b0 = fmaf(v0, __ldg(k1 + (size_t)k * Gs), b0);
+          a1 = fmaf(v1, __ldg(k0 + (size_t)(k + 1) * Gs), a1);
+          b1 = fmaf(v1, __ldg(k1 + (size_t)(k + 1) * Gs), b1);
+        }
+        if (k < F - 1) {
+          a0 = fmaf(sh_v[k], __ldg(k0 + (size_t)k * Gs), a0);
+          b0 = fmaf(sh_v[k], __ldg(k1 + (size_t)k * Gs), b0);
+        }
+      }
+      accA = a0 + a1;
+      accB = b0 + b1;
+    }
+    for (int i = tid, m = 0; i < G - 1; i += kStepThreads, ++m) {
       const double vs = c_syn * T.gt(kTabHalf2)[i];
       const double va = sc.dlnVdt * T.gt(kTabHadi)[i];
       double vc = 0.;
-      if (ssc) {
+      if (gemv2) {
+        vc = c_ssc * (double)(m == 0 ? accA : accB) * T.gt(kTabIhalf2)[i];
+        gssc[i] = vc;
+      } else if (ssc) {
         float acc = 0.f;
         if (kint_smem) {
           const float* kc = sh_k + i;
@@ -911,6 +954,111 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   }
 }
 
+// The same sums with the lane's gamma-bin inputs (JQ bins per lane, j = lane +
+// 32 q, G - 1 <= 32 JQ) loaded once into registers and used for all R
+// frequencies of the warp, and the synchrotron function (gamma > 2; every
+// method) read from its value/slope table around the nearest point instead of
+// evaluated: x = a_k / gamma_j^2 gives the table position from two logs, R(x) =
+// g(ln x) x^(1/3) with x^(1/3) = a_k^(1/3) gamma_j^(-2/3) (relative error of
+// the table ~1e-5). The cyclotron branch of CSYN (gamma <= 2) is evaluated.
+// Every independent load is issued before the first use (one latency round).
+template <int JQ, int RM>
+__device__ void radiate_block_regs(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int b,
+                                   int kblk, int R) {
+  const int tid = threadIdx.x;
+  const int G = g.G, F = g.F;
+  const int kq = tid / kRadLanes, jl = tid % kRadLanes;
+  const int flg = S.flags[b];
+  const pbag_shock_params* pb = prm + b;
+  const int ssa_on = pb->ssa_on, method = pb->syn_method;
+  const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);
+  float nuv[RM], nu13v[RM], lnuv[RM];
+#pragma unroll
+  for (int r = 0; r < RM; ++r) {
+    const int k = kblk * (kRadFreqs * R) + r * kRadFreqs + kq;
+    const bool in = r < R && k < F;
+    nuv[r] = in ? __ldg(g.nu32 + k) : 0.f;
+    nu13v[r] = in ? __ldg(g.nu13 + k) : 0.f;
+    lnuv[r] = in ? __ldg(g.lnnu + k) : 0.f;
+  }
+  const float* w = S.w32 + (size_t)b * G;
+  const float* v = S.v32 + (size_t)b * G;
+  const float ih = g.syn2_ih;
+  float wv[JQ], vv[JQ], lgp[JQ], x13[JQ], ps[JQ];
+#pragma unroll
+  for (int q = 0; q < JQ; ++q) {
+    const int j = jl + kRadLanes * q;
+    const bool in = j < G - 1;
+    wv[q] = in ? __ldg(w + j) : 0.f;
+    vv[q] = in ? __ldg(v + j) : 0.f;
+    lgp[q] = in ? __ldg(g.lnginv2 + j) * ih : 0.f;  // table position of ln(1/gamma^2)
+    x13[q] = in ? __ldg(g.ginv23 + j) : 0.f;
+    ps[q] = in ? __ldg(g.psq32 + j) : 0.f;
+  }
+  if (!(flg & kFlagActive)) return;
+  const bool ssa = ssa_on != 0;
+  const float2* tab =
+      g.syntab2 + (method == PBAG_SYN_GSL ? 0 : method == PBAG_SYN_BESSEL ? kSynTab2N : 2 * kSynTab2N);
+  const float xs = method == PBAG_SYN_GSL ? g.gsl_xs : 1.f;
+  const float lxs = logf(xs) + logf(rp.x), cxs = cbrtf(xs);
+  const float inlar = rp.y;
+  const int jcyc = method == PBAG_SYN_CSYN ? g.n_cyc : 0;
+  const int last = g.syn2_n - 1;
+  constexpr float kRound = 12582912.f;  // 1.5 2^23: x + kRound rounds x to an integer in the mantissa
+#pragma unroll
+  for (int r = 0; r < RM; ++r) {
+    const int k = kblk * (kRadFreqs * R) + r * kRadFreqs + kq;
+    if (r >= R || k >= F) break;  // warp-uniform
+    const float la = (lnuv[r] + lxs - g.syn2_u0) * ih;  // table position of ln a_k
+    const float y13 = nu13v[r] * rp.z * cxs;            // a_k^(1/3)
+    const float xl = nuv[r] * inlar;
+    float acc = 0.f, as = 0.f, ac = 0.f;
+#pragma unroll
+    for (int q = 0; q < JQ; ++q) {
+      const int j = jl + kRadLanes * q;
+      if (j < G - 1) {
+        float R_;
+        // the cyclotron bins (jcyc <= 32) are all in register 0: the branch
+        // exists in the first unrolled iteration only
+        if (q > 0 || j >= jcyc) {
+          const float p = la + lgp[q];
+          const float rr = p + kRound;
+          const int i = min(max(__float_as_int(rr) - __float_as_int(kRound), 0), last);
+          const float f = p - (rr - kRound);
+          const float2 t = __ldg(tab + i);
+          R_ = fmaf(f, t.y, t.x) * (y13 * x13[q]);
+        } else {
+          R_ = cyclotron_R32(ps[q], xl);
+        }
+        acc = fmaf(R_, wv[q], acc);
+        if (ssa) {
+          const float x = R_ * vv[q];
+          const float t = as + x;
+          ac += fabsf(as) >= fabsf(x) ? (as - t) + x : (x - t) + as;
+          as = t;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < kRadLanes; o <<= 1) {
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      const float os = __shfl_xor_sync(0xffffffffu, as, o);
+      const float oc = __shfl_xor_sync(0xffffffffu, ac, o);
+      float s_, e_;
+      two_sum(as, os, s_, e_);
+      as = s_;
+      ac = ac + oc + e_;
+    }
+    if (jl == 0) {
+      S.syn32[(size_t)b * F + k] = acc;
+      S.ssa32[(size_t)b * F + k] = ssa ? make_float2(as, ac) : make_float2(0.f, 0.f);
+    }
+  }
+}
+
+constexpr int kRadJq = 8;    // gamma bins per lane held in registers (G - 1 <= 256)
+constexpr int kRadRMax = 2;  // frequencies per warp of the register path
+
 template <int KPT>
 __global__ void __launch_bounds__(kRadThreads)
 k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int R) {
@@ -918,7 +1066,10 @@ k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int 
   const int blk = blockIdx.x;
   const int rc = (g.F + kRadFreqs * R - 1) / (kRadFreqs * R);
   if (blk < rad_blocks) {
-    radiate_block(g, S, prm, blk / rc, blk % rc, R);
+    if (g.G - 1 <= kRadJq * kRadLanes && g.n_cyc <= kRadLanes && R <= kRadRMax)
+      radiate_block_regs<kRadJq, kRadRMax>(g, S, prm, blk / rc, blk % rc, R);
+    else
+      radiate_block(g, S, prm, blk / rc, blk % rc, R);
   } else {
     ssc_block<KPT>(g, S, nbw, blk - rad_blocks);
   }
@@ -1215,10 +1366,13 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
 cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
                            int step, cudaStream_t st) {
   (void)step;
-  // frequencies per warp: 1 while the batch is small (latency), more for large
-  // batches so that each warp's per-blastwave setup serves several frequencies
+  // frequencies per warp: each warp's per-blastwave setup and gamma-bin loads
+  // serve R frequencies; with the register path R = 2 keeps a small batch's
+  // CTAs (42 blastwaves x 128 frequencies: 672) resident in one wave next to
+  // the SSC kernel while each warp's work stays short
   const int64_t pairs = (int64_t)nbw * g.F;
-  const int R = pairs <= 40000 ? 1 : pairs <= 160000 ? 2 : pairs <= 640000 ? 4 : 8;
+  const bool regs = g.G - 1 <= kRadJq * kRadLanes && g.n_cyc <= kRadLanes;
+  const int R = !regs ? (pairs <= 40000 ? 1 : pairs <= 160000 ? 2 : pairs <= 640000 ? 4 : 8) : kRadRMax;
   const int rc = (g.F + kRadFreqs * R - 1) / (kRadFreqs * R);
   const int rad_blocks = nbw * rc;
   const int ssc_blocks = ssc ? ssc_block_count(g, nbw) : 0;
