@@ -341,6 +341,161 @@ __device__ bool cc_scan(double (&fr)[C], const double (&ib)[C], const double (&q
   return bad;
 }
 
+// ---- double-float: an FP32 pair (hi + lo, ~48-bit significand) ------------
+// On this part an FP64 warp instruction occupies its sub-partition's FP64 unit
+// for 64 cycles, so the substep recurrence runs in pairs of FP32 values instead
+// (Dekker's products with FMA, Knuth's two-sum; every operand of the
+// recurrence is non-negative, so no cancellation), scaled per blastwave by a
+// power of two into the FP32 range.
+struct dfl {
+  float hi, lo;
+};
+
+// x 2^s as a pair, from the bits of x (no FP64 arithmetic): hi = the leading
+// 24 bits, lo = the remaining 29 rounded to 24; 0 below the FP32 normal range,
+// inf above it
+__device__ __forceinline__ dfl dfl_from(double x, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned long long m = b & 0xfffffffffffffull;
+  if (ex == 0) return {__uint_as_float(sign), 0.f};
+  if (ex == 0x7ff) return {__uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u)), 0.f};
+  const int e = ex - 1023 + s;  // exponent of the scaled value
+  if (e + 127 >= 255) return {__uint_as_float(sign | 0x7f800000u), 0.f};
+  if (e + 127 <= 0) return {__uint_as_float(sign), 0.f};
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29));
+  const unsigned r = (unsigned)(m & 0x1fffffffull);
+  float lo = r ? f32_ldexp((float)r, e - 52) : 0.f;
+  if (sign) lo = -lo;
+  const float h2 = hi + lo;  // normalise: |lo| <= ulp(hi) / 2
+  return {h2, lo - (h2 - hi)};
+}
+// (hi + lo) 2^-s in FP64: the two parts built from their bits, one FP64 add
+__device__ __forceinline__ double dfl_to(dfl a, int s) { return f64_from_mant(a.hi, -s) + f64_from_mant(a.lo, -s); }
+__device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  const float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+  const float hi = p + e;
+  return {hi, e - (hi - p)};
+}
+// a b + c
+__device__ __forceinline__ dfl dfl_fma(dfl a, dfl b, dfl c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+  const float s = p + c.hi;
+  const float v = s - p;
+  e += ((p - (s - v)) + (c.hi - v)) + c.lo;
+  const float hi = s + e;
+  return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ bool dfl_bad(dfl a) {  // negative, inf or NaN (as bad_value)
+  const unsigned u = __float_as_uint(a.hi);
+  return (u & 0x7f800000u) == 0x7f800000u || (u > 0x80000000u);
+}
+__device__ __forceinline__ dfl dfl_shfl_down(dfl a, int d) {
+  return {__shfl_down_sync(0xffffffffu, a.hi, d), __shfl_down_sync(0xffffffffu, a.lo, d)};
+}
+
+// cc_scan in double-float: the same recurrence, scan tree and order of
+// operations, with the state and source scaled by 2^s (s from the block's
+// largest exponent of f and Q dt / b, so that the values stay far inside the
+// FP32 range for the <= kScanMaxSub substeps of this path). Returns false
+// (and leaves fr untouched) when a coefficient or product leaves the FP32
+// range: the caller then runs the FP64 scan. *bad as cc_scan's result.
+template <int C>
+__device__ bool cc_scan_df(double (&fr)[C], const double (&ib)[C], const double (&qb)[C], const double (&bt)[C],
+                           int n_sub, double (*xs)[kStepWarps], double* pw0, int* red, bool* bad_out) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  bool bad = false;
+  int E = 0;
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    bad |= bad_value(fr[q]);  // the check before the first substep, on the FP64 values
+    E = max(E, max(exp_field(fr[q]), exp_field(qb[q])));
+  }
+  E = block_max_int(E, red);
+  const int s = 1023 - E - 8;  // largest scaled input ~2^-8
+  dfl f[C], ibd[C], qbd[C], btd[C];
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    f[q] = dfl_from(fr[q], s);
+    ibd[q] = dfl_from(ib[q], 0);
+    qbd[q] = dfl_from(qb[q], s);
+    btd[q] = dfl_from(bt[q], 0);
+  }
+  dfl P = {1.f, 0.f};
+#pragma unroll
+  for (int q = 0; q < C; ++q) P = dfl_mul(P, btd[q]);
+  dfl pk[5];
+  dfl Pc = P;
+#pragma unroll
+  for (int lev = 0; lev < 5; ++lev) {
+    const int d = 1 << lev;
+    const dfl Po = dfl_shfl_down(Pc, d);
+    pk[lev] = Pc;
+    if (lane + d < 32) Pc = dfl_mul(Pc, Po);
+  }
+  dfl Pwn = dfl_shfl_down(Pc, 1);
+  if (lane == 31) Pwn = {1.f, 0.f};
+  // every coefficient and product in range (finite; a product may underflow to 0)
+#pragma unroll
+  for (int q = 0; q < C; ++q)
+    ok &= isfinite(ibd[q].hi) && isfinite(qbd[q].hi) && isfinite(btd[q].hi) && isfinite(f[q].hi) && !bad_value(fr[q]);
+#pragma unroll
+  for (int lev = 0; lev < 5; ++lev) ok &= isfinite(pk[lev].hi);
+  ok &= isfinite(Pc.hi) && isfinite(Pwn.hi);
+  dfl* pw = reinterpret_cast<dfl*>(pw0);
+  if (lane == 0) pw[warp] = Pc;
+  if (!__syncthreads_and(ok ? 1 : 0)) return false;
+  dfl pwr[kStepWarps];
+#pragma unroll
+  for (int v = 0; v < kStepWarps; ++v) pwr[v] = pw[v];
+  bool okc = true;
+#pragma unroll
+  for (int v = 0; v < kStepWarps; ++v) okc &= isfinite(pwr[v].hi);
+  // a barrier also before a fallback: the FP64 scan rewrites pw0
+  if (!__syncthreads_and(okc ? 1 : 0)) return false;
+  dfl (*xd)[kStepWarps] = reinterpret_cast<dfl(*)[kStepWarps]>(xs);
+  for (int m = 0; m < n_sub; ++m) {
+    dfl a[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      if (m > 0) bad |= dfl_bad(f[q]);
+      a[q] = dfl_fma(f[q], ibd[q], qbd[q]);
+    }
+    dfl A = a[C - 1];
+#pragma unroll
+    for (int q = C - 2; q >= 0; --q) A = dfl_fma(btd[q], A, a[q]);
+    dfl Sx = A;
+#pragma unroll
+    for (int lev = 0; lev < 5; ++lev) {
+      const int d = 1 << lev;
+      const dfl So = dfl_shfl_down(Sx, d);
+      if (lane + d < 32) Sx = dfl_fma(pk[lev], So, Sx);
+    }
+    dfl Sn = dfl_shfl_down(Sx, 1);
+    if (lane == 31) Sn = {0.f, 0.f};
+    if (lane == 0) xd[m & 1][warp] = Sx;
+    __syncthreads();
+    dfl carry = {0.f, 0.f};
+#pragma unroll
+    for (int v = kStepWarps - 1; v > 0; --v)
+      if (v > warp) carry = dfl_fma(pwr[v], carry, xd[m & 1][v]);
+    dfl fn = dfl_fma(Pwn, carry, Sn);
+#pragma unroll
+    for (int q = C - 1; q >= 0; --q) {
+      f[q] = dfl_fma(btd[q], fn, a[q]);
+      fn = f[q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < C; ++q) fr[q] = dfl_to(f[q], s);
+  *bad_out = bad;
+  return true;
+}
+
 // Systolic pipeline: thread t runs substep m at tick m + (T-1-t), taking the
 // right neighbour's new first bin of the same substep from the tick before.
 // n_sub + T - 1 ticks of C dependent FMAs: it wins for many substeps.
@@ -747,8 +902,11 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
       }
     }
     const int Tn = (G + C - 1) / C;  // threads that own bins
-    const bool sbad = n_sub < kScanMaxSub ? cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0)
-                                          : cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
+    bool sbad = false;
+    if (n_sub >= kScanMaxSub)
+      sbad = cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
+    else if (!cc_scan_df<C>(fr, ib, qb, bt, n_sub, xs, pw0, red_i[0], &sbad))
+      sbad = cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0);
     __syncthreads();  // every heating value has been read: sh_f takes N(gamma)
 #pragma unroll
     for (int q = 0; q < C; ++q) {
