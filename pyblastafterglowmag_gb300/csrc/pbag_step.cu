@@ -43,6 +43,15 @@ __device__ int block_max_int(int v, int* red) {
   return r;
 }
 
+// (float)(x * scale_from_exp(E)) without FP64 arithmetic: the same single
+// rounding of x's significand (f64_mant), the power of two added to the
+// exponent; 0 below the FP32 normal range
+__device__ __forceinline__ float f32_scaled(double x, int E) {
+  int e;
+  const float m = f64_mant(x, e);
+  return f32_ldexp(m, (E <= 26 || E >= 2019) ? e : e + 1022 - E);
+}
+
 // Record the first error of a blastwave (later ones are ignored).
 __device__ void set_error(const DevState& S, int b, int code, int step, int site) {
   if (atomicCAS(&S.err[4 * b], 0, code) == 0) {
@@ -958,18 +967,16 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     wexp = max(wexp, red_i[1][v]);
     Wexp = max(Wexp, red_i[2][v]);
   }
-  const double sw = scale_from_exp(wexp);
   float* w32 = S.w32 + (size_t)b * G;
-  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? (float)(sh_f[i] * t_de[i] * sw) : 0.f;
+  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? f32_scaled(sh_f[i] * t_de[i], wexp) : 0.f;
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   // (FP32 for the CUDA-core contraction, BF16 hi + lo tiles for the tensor cores)
   if (P.ssc_on && g.K32 != nullptr) {
-    const double sW = scale_from_exp(Wexp);
     float* W = S.W32 + (size_t)b * g.Gp;
     uint16_t* A = S.Abf ? S.Abf + (size_t)(b / kTcCols) * tc_tile_elems(kTcCols, g.Gp) : nullptr;
     const int m = b % kTcCols;
     for (int j = tid; j < g.Gp; j += kStepThreads) {
-      const float w = j < G - 1 ? (float)(sh_f[j] * t_de[j] * t_inv_e2[j] * sW) : 0.f;
+      const float w = j < G - 1 ? f32_scaled(sh_f[j] * t_de[j] * t_inv_e2[j], Wexp) : 0.f;
       W[j] = w;
       if (A) {
         const __nv_bfloat16 hi = __float2bfloat16_rn(w);
@@ -1014,9 +1021,8 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     vexp = 0;
 #pragma unroll
     for (int v = 0; v < kStepWarps; ++v) vexp = max(vexp, red_i[0][v]);
-    const double svd = scale_from_exp(vexp);
     float* v32 = S.v32 + (size_t)b * G;
-    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? (float)(sh_vd[i] * svd) : 0.f;
+    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? f32_scaled(sh_vd[i], vexp) : 0.f;
   }
   if (!positive(ne) && !is_nan(ne)) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // n_ele <= 0 (microphysics.h:560-563)
   if (tid == 0) {
@@ -1026,9 +1032,6 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     scal[kScalVol] = sc.vol;
     scal[kScalNele] = ne;
     scal[kScalFac] = sc.fac;
-    const double acc_ne = accel / ne;
-    scal[kScalAccNe] = acc_ne;
-    scal[kScalAnpNe] = accel * n_prime / ne;
     scal[kScalAcc] = accel;
     scal[kScalNp] = n_prime;
     scal[kScalNsub] = (double)sc.n_sub;
@@ -1042,6 +1045,10 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     rp[2] = cbrtf(sc.inv_ncrit);
     rp[3] = 0.f;
     S.flags[b] = flags | kFlagActive;
+  } else if (tid == 32) {  // the two divisions on other sub-partitions' FP64 units, next to thread 0's work
+    S.scal[(size_t)b * kScal + kScalAccNe] = accel / ne;
+  } else if (tid == 64) {
+    S.scal[(size_t)b * kScal + kScalAnpNe] = accel * n_prime / ne;
   }
 #undef PBAG_FAIL
 }
