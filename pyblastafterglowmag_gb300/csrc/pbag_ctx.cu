@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -510,6 +511,10 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   d.F = F;
   d.Gp = c->Gp;
   d.n_cyc = n_cyc;
+  {
+    const char* sf = std::getenv("PBAG_SCAN_FP64");
+    d.scan_fp64 = (sf && sf[0] == '1') ? 1 : 0;
+  }
   d.dlog_gam = (e[1] - e[0]) / e[0];
   cudaError_t err = cudaSuccess;
   auto ok = [&](cudaError_t x) {

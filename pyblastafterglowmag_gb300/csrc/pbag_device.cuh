@@ -29,6 +29,7 @@ constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinali
 struct DevGrid {
   int G, F, Gp;          // Gp: G rounded up to a multiple of 16 (padded SSC operand)
   int n_cyc;             // number of bins with e[j] <= 2 (cyclotron branch of cycSynch)
+  int scan_fp64;         // Chang-Cooper scan in FP64 only (PBAG_SCAN_FP64=1), else double-float first
   double dlog_gam;       // (e[1]-e[0])/e[0] (microphysics.h:413)
   const double* e;       // [G]   gamma grid e[i] = step^i
   const double* inv_e;   // [G]   1/e

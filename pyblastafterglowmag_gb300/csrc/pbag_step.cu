@@ -914,7 +914,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     bool sbad = false;
     if (n_sub >= kScanMaxSub)
       sbad = cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
-    else if (!cc_scan_df<C>(fr, ib, qb, bt, n_sub, xs, pw0, red_i[0], &sbad))
+    else if (g.scan_fp64 || !cc_scan_df<C>(fr, ib, qb, bt, n_sub, xs, pw0, red_i[0], &sbad))
       sbad = cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0);
     __syncthreads();  // every heating value has been read: sh_f takes N(gamma)
 #pragma unroll

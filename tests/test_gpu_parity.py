@@ -75,6 +75,13 @@ def test_gaussian_ssc_small_batch_kernel(lib, oracle, cuda_device, monkeypatch):
     _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=60))
 
 
+def test_gaussian_ssc_fp64_scan(lib, oracle, cuda_device, monkeypatch):
+    """The Chang-Cooper substeps with the FP64 scan forced (the path a step
+    takes when its coefficients leave the FP32 range of the double-float scan)."""
+    monkeypatch.setenv("PBAG_SCAN_FP64", "1")
+    _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
+
+
 def test_gaussian_late_window(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian_window(lib, start=380, nsteps=60))
 
