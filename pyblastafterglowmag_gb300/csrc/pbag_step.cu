@@ -935,17 +935,21 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   const double* t_de = T.gt(kTabDe);
   double ne = 0.;
   int wexp = 0, Wexp = 0;
+  double wk[C], Wk[C];  // f_j dgamma_j and f_j dgamma_j / e_j^2 of this thread's bins (tid + 128 k)
 #pragma unroll
   for (int k = 0; k < C; ++k) {
     const int i = tid + k * kStepThreads;
+    wk[k] = Wk[k] = 0.;
     if (i < G) {
       const double fi = sh_f[i];
       sh_t[i] = fi * t_inv_e2[i];  // f / e / e (numeric_model.h:194-195)
       if (i < G - 1) {
         const double w = fi * t_de[i];
+        wk[k] = w;
+        Wk[k] = w * t_inv_e2[i];
         ne += w;  // N_e (microphysics.h:556-558)
         wexp = max(wexp, exp_field(w));
-        Wexp = max(Wexp, exp_field(w * t_inv_e2[i]));
+        Wexp = max(Wexp, exp_field(Wk[k]));
       }
     }
   }
@@ -968,15 +972,23 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     Wexp = max(Wexp, red_i[2][v]);
   }
   float* w32 = S.w32 + (size_t)b * G;
-  for (int i = tid; i < G; i += kStepThreads) w32[i] = i < G - 1 ? f32_scaled(sh_f[i] * t_de[i], wexp) : 0.f;
+#pragma unroll
+  for (int k = 0; k < C; ++k) {
+    const int i = tid + k * kStepThreads;
+    if (i < G) w32[i] = f32_scaled(wk[k], wexp);  // wk = 0 for the last bin
+  }
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   // (FP32 for the CUDA-core contraction, BF16 hi + lo tiles for the tensor cores)
   if (P.ssc_on && g.K32 != nullptr) {
     float* W = S.W32 + (size_t)b * g.Gp;
     uint16_t* A = S.Abf ? S.Abf + (size_t)(b / kTcCols) * tc_tile_elems(kTcCols, g.Gp) : nullptr;
     const int m = b % kTcCols;
-    for (int j = tid; j < g.Gp; j += kStepThreads) {
-      const float w = j < G - 1 ? f32_scaled(sh_f[j] * t_de[j] * t_inv_e2[j], Wexp) : 0.f;
+    // Gp <= 128 C (G <= 128 C, Gp its multiple of 16): bin j = tid + 128 k
+#pragma unroll
+    for (int k = 0; k < C; ++k) {
+      const int j = tid + k * kStepThreads;
+      if (j >= g.Gp) continue;
+      const float w = f32_scaled(Wk[k], Wexp);  // Wk = 0 from the last bin on
       W[j] = w;
       if (A) {
         const __nv_bfloat16 hi = __float2bfloat16_rn(w);
