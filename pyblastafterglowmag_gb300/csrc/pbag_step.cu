@@ -1292,6 +1292,7 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
   // every load first
   const double dr = scal[kScalDr], acc = scal[kScalAcc];
   const double pref = scal[kScalPref], ssw = scal[kScalSw], ssv = scal[kScalSv];
+  const int ew = exp_field(ssw) - 1023, ev = exp_field(ssv) - 1023;  // both are powers of two
   const double fac = scal[kScalFac], acc_ne = scal[kScalAccNe], anp_ne = scal[kScalAnpNe];
   float s32[FQ];
   float2 a32[FQ];
@@ -1313,11 +1314,14 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     const int k = tid + q * kStepThreads;
     jsv[q] = asv[q] = 0.;
     if (k < F) {
-      const double js = k < F - 1 ? pref * ((double)s32[q] * ssw) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
+      // (double)s * ssw with ssw a power of two, built from the bits (exactly the
+      // same value without the FP64 conversion and product)
+      const double js = k < F - 1 ? pref * f64_from_mant(s32[q], ew) : 0.;  // j_syn[F-1] = 0 (numeric_model.h:157)
       if (bad_value(js)) jbad = true;
       jsv[q] = js;
       if (P.ssa_on) {
-        double a = fabs(pref * (((double)a32[q].x + (double)a32[q].y) * ssv) * T.ft(kTabSsaNu)[k]);  // :206-211
+        const double sa = f64_from_mant(a32[q].x, ev) + f64_from_mant(a32[q].y, ev);  // ((double)x + (double)y) ssv
+        double a = fabs(pref * sa * T.ft(kTabSsaNu)[k]);  // :206-211
         if (not_finite(a)) a = 1e99;
         asv[q] = a;
       }
@@ -1368,11 +1372,11 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
   const double* ksc = T.ft(kTabKscale);
   bool bad = false, seen = false;
   int uexp = 0, vexp = 0;
-  double un[FQ];
+  double un[FQ], uk[FQ];  // u_k = n_k dnu_k and u_k kscale_k
 #pragma unroll
   for (int q = 0; q < FQ; ++q) {
     const int k = tid + q * kStepThreads;
-    un[q] = 0.;
+    un[q] = uk[q] = 0.;
     if (k >= F) continue;
     const double js = jsv[q], c = num ? cs[q] : 0.;
     const double nk = js * fac * inv_hnu[k] + c * fac * inv_hnu[k];
@@ -1380,7 +1384,10 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     const double u = nk * dnu[k];
     un[q] = u;
     uexp = max(uexp, exp_field(u));
-    if (k < F - 1) vexp = max(vexp, exp_field(u * ksc[k]));
+    if (k < F - 1) {
+      uk[q] = u * ksc[k];
+      vexp = max(vexp, exp_field(uk[q]));
+    }
     double tj0 = js + c;
     if (num && pp) {  // pair-production attenuation (microphysics.h:565-574)
       const double tau_pp = ppa[q] * dr;
@@ -1429,17 +1436,16 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     any |= (unsigned)red_f[2][v];
   }
   if (ssc) {
-    // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k of this step's SSC contraction
-    const double su = scale_from_exp(uexp);
+    // seed-photon weights n_k (nu_{k+1}-nu_k)/nu_k of this step's SSC contraction,
+    // and the cooling weights n_k dnu_k/nu_k kscale_k of the next step
+    // (numeric_model.h:395-400), scaled to FP32 through their bits
     float* U = S.U32 + (size_t)b * F;
-    // cooling weights n_k dnu_k/nu_k kscale_k of the next step (numeric_model.h:395-400)
-    const double sv = scale_from_exp(vexp);
 #pragma unroll
     for (int q = 0; q < FQ; ++q) {
       const int k = tid + q * kStepThreads;
       if (k >= F) continue;
-      U[k] = (float)(un[q] * su);
-      if (sh_v) sh_v[k] = k < F - 1 ? (float)(un[q] * ksc[k] * sv) : 0.f;
+      U[k] = f32_scaled(un[q], uexp);
+      if (sh_v) sh_v[k] = k < F - 1 ? f32_scaled(uk[q], vexp) : 0.f;
     }
   }
   if (tid == 0) {
