@@ -82,6 +82,26 @@ def test_gaussian_ssc_fp64_scan(lib, oracle, cuda_device, monkeypatch):
     _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
 
 
+def test_double_float_scan_matches_fp64_scan(lib, cuda_device, monkeypatch):
+    """The double-float substeps against the FP64 ones on the same batch: the
+    electron histories agree to far below the plain-path bar (the pairs carry
+    ~48 significant bits); the emissivities, formed from FP32 weights of those
+    histories, to within an FP32 rounding."""
+    recs, off, prm, grid = cases.gaussian(lib, nlayers=3, nsteps=120)
+    outs = ("ele_f_all", "j_all")
+    ctx = Context(grid, device=0, ssc=True)
+    df = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    monkeypatch.setenv("PBAG_SCAN_FP64", "1")
+    ctx = Context(grid, device=0, ssc=True)
+    f64 = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    for k, tol in (("ele_f_all", 1e-9), ("j_all", 1e-6)):
+        rel, zero_mismatch = rel_l2_rows(df[k], f64[k])
+        assert zero_mismatch == 0, k
+        assert rel.max() <= tol, (k, rel.max())
+
+
 def test_gaussian_late_window(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian_window(lib, start=380, nsteps=60))
 
