@@ -74,7 +74,7 @@ def config_dict(cfg, recs, prm, extra=None):
     d = {"workload": WORKLOAD, "blastwaves": int(len(prm)), "layers": cfg.nlayers,
          "shocks": "forward+reverse", "ngam": cfg.ngam, "nfreq": cfg.nfreq, "ntb": cfg.ntb,
          "valid_blastwave_steps_per_pass": int((recs["mode"] != 0).sum()),
-         "radiation": "synchrotron(CSYN)+SSA+SSC", "solve": "Chang-Cooper FP64",
+         "radiation": "synchrotron(CSYN)+SSA+SSC", "solve": "Chang-Cooper, FP64 state, double-float substeps",
          "ssc_contraction": "FP32 accumulate, per-blastwave power-of-two scaling",
          "l2": "flushed with a 256 MiB device write before every timed pass",
          "inputs": "seeded synthetic blastwave histories (thin-shell dynamics)"}
@@ -142,10 +142,13 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------- cpu baseline ---
-def cpu_sample(recs, off, prm, grid, seconds, threads):
+def cpu_sample(recs, off, prm, grid, seconds, threads, inner=0):
     """Time the oracle port on a bounded sample of the workload: windows of
     consecutive steps spread over every blastwave's history, each window
-    re-initialised at its first step. Returns (bw-steps/s, description)."""
+    re-initialised at its first step. threads: blastwaves in parallel, one per
+    thread; inner > 0: the reference's own arrangement instead, blastwaves one
+    after another with the inner loops on `inner` threads (its num_threads(4)
+    OpenMP loops). Returns (bw-steps/s, description, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     from pyblastafterglowmag_gb300 import abi
@@ -165,10 +168,12 @@ def cpu_sample(recs, off, prm, grid, seconds, threads):
         o[1:] = np.cumsum(lens)
         return np.concatenate(rr), o, np.array(pp, dtype=abi.SHOCK_PARAMS_DTYPE)
 
+    kw = (dict(flags=pyoracle.ORC_INNER_OMP, outer_threads=1, inner_threads=inner) if inner > 0
+          else dict(flags=0, outer_threads=threads))
     # calibrate on a small sample, then size the sample to ~`seconds`
     r, o, p = make(1, 4)
     t0 = time.perf_counter()
-    orc.run(grid, r, o, p, flags=0, outer_threads=threads)
+    orc.run(grid, r, o, p, **kw)
     t1 = time.perf_counter() - t0
     per_step = max(t1 / max(int((r["mode"] != 0).sum()), 1), 1e-6)
     budget_steps = seconds / per_step
@@ -176,12 +181,14 @@ def cpu_sample(recs, off, prm, grid, seconds, threads):
     nwin = int(max(1, min(40, budget_steps / (wlen * nbw))))
     r, o, p = make(nwin, wlen)
     t0 = time.perf_counter()
-    rc, where, _ = orc.run(grid, r, o, p, flags=0, outer_threads=threads)
+    rc, where, _ = orc.run(grid, r, o, p, **kw)
     dt = time.perf_counter() - t0
     n = int((r["mode"] != 0).sum())
+    how = (f"blastwaves one after another, inner loops on {inner} threads as in the reference" if inner > 0
+           else "one blastwave per thread")
     desc = (f"{nbw} blastwaves x {nwin} windows x {wlen} consecutive steps spread over the 1000-step "
             f"histories ({n} valid blastwave-steps), FP64 oracle port in the reference's loop structure "
-            f"(cooling terms recomputed every substep), one blastwave per thread")
+            f"(cooling terms recomputed every substep), {how}")
     return n / dt, desc, dt
 
 
@@ -364,6 +371,8 @@ def gb300_arm(args):
                   "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
     threads = os.cpu_count() or 1
     cpu_v, cpu_desc, _ = cpu_sample(recs, off, prm, grid, args.cpu_sample_seconds, threads)
+    # the reference's own arrangement (blastwaves serial, inner loops on 4 threads)
+    asis_v, asis_desc, _ = cpu_sample(recs, off, prm, grid, min(8.0, args.cpu_sample_seconds), threads, inner=4)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
@@ -373,7 +382,8 @@ def gb300_arm(args):
             "gpu_launches": int(launches),
             "roofline": roofline,
             "roofline_contraction": roofline_c,
-            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_desc},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_desc,
+                             "as_is": {"value": asis_v, "unit": UNIT, "cores": 4, "sample": asis_desc}},
             "wall_s_timed_region": t_wall}
     print(json.dumps(line), flush=True)
 
