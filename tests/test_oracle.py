@@ -64,6 +64,20 @@ def test_hoisted_heating_is_bitwise_identical(oracle):
         np.testing.assert_array_equal(a[k], b[k])
 
 
+def test_inner_threads_are_bitwise_identical(oracle):
+    """The reference's own arrangement (blastwaves serial, inner loops on 4
+    threads; the benchmark's as-is CPU figure) gives the serial results."""
+    import pyoracle
+    d = load("run_gauss.npz")
+    g = grid_of(d["grid"])
+    _, _, a = oracle.run(g, d["recs"], d["offsets"], d["params"], flags=0)
+    rc, _, b = oracle.run(g, d["recs"], d["offsets"], d["params"], flags=pyoracle.ORC_INNER_OMP,
+                          outer_threads=1, inner_threads=4)
+    assert rc == 0
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
 def test_live_reference_matches_oracle(lib, oracle, reference):
     for batch in (cases.tophat(lib, nsteps=120, ssa=True),
                   cases.tophat(lib, nsteps=80, syn_method=abi.PBAG_SYN_DER09, ele_method=abi.PBAG_ELE_MIX),
