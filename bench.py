@@ -63,10 +63,15 @@ from pyblastafterglowmag_gb300.replicas import dist_info  # noqa: E402
 from pyblastafterglowmag_gb300 import replicas  # noqa: E402
 
 
-def workload():
-    from pyblastafterglowmag_gb300 import _lib, histories as H
+def workload(tables=None):
+    """The Gaussian jet's step records. tables: what builds the grids and the
+    shock scalars - the library (default) or, for the CPU arm, the oracle,
+    which produces the same bytes without loading the library."""
+    from pyblastafterglowmag_gb300 import histories as H
+    if tables is None:
+        from pyblastafterglowmag_gb300 import _lib as tables
     cfg = H.config_gaussian_ssc()
-    recs, off, prm, grid = H.make_batch(_lib, cfg)
+    recs, off, prm, grid = H.make_batch(tables, cfg)
     return cfg, recs, off, prm, grid
 
 
@@ -177,8 +182,9 @@ def cpu_sample(recs, off, prm, grid, seconds, threads, inner=0):
     t1 = time.perf_counter() - t0
     per_step = max(t1 / max(int((r["mode"] != 0).sum()), 1), 1e-6)
     budget_steps = seconds / per_step
-    wlen = 8
-    nwin = int(max(1, min(40, budget_steps / (wlen * nbw))))
+    # long windows: the first step of each is the (cheaper) initialisation
+    wlen = 25
+    nwin = int(max(1, min(16, budget_steps / (wlen * nbw))))
     r, o, p = make(nwin, wlen)
     t0 = time.perf_counter()
     rc, where, _ = orc.run(grid, r, o, p, **kw)
@@ -193,15 +199,16 @@ def cpu_sample(recs, off, prm, grid, seconds, threads, inner=0):
 
 
 def reference_arm(args):
+    """The reference's CPU path alone: the oracle port (the reference's loop
+    structure, bit-exact against the compiled reference) builds the records and
+    runs the step; the GPU library is neither built nor loaded."""
     rank, world, local = dist_info()
     if rank != 0:
         return
-    from pyblastafterglowmag_gb300 import build
-    build.build()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build_oracle()
-    cfg, recs, off, prm, grid = workload()
+    cfg, recs, off, prm, grid = workload(pyoracle.Oracle())
     threads = os.cpu_count() or 1
     per_step = max(10.0, min(60.0, 150.0 / max(args.steps + args.warmup, 1)))
     vals, dts, desc = [], [], ""
@@ -369,6 +376,7 @@ def gb300_arm(args):
                   "flops_per_blastwave_step": contraction_flops_per_bw_step(grid),
                   "avg_launch_us": 1e3 * ms_c / nl_c if nl_c else None,
                   "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
+    parity = output_check(recs, off, prm, grid, {k: v.numpy() for k, v in h_out.items()})
     threads = os.cpu_count() or 1
     cpu_v, cpu_desc, _ = cpu_sample(recs, off, prm, grid, args.cpu_sample_seconds, threads)
     # the reference's own arrangement (blastwaves serial, inner loops on 4 threads)
@@ -384,8 +392,38 @@ def gb300_arm(args):
             "roofline_contraction": roofline_c,
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cpu_desc,
                              "as_is": {"value": asis_v, "unit": UNIT, "cores": 4, "sample": asis_desc}},
+            "parity": parity,
             "wall_s_timed_region": t_wall}
     print(json.dumps(line), flush=True)
+
+
+def output_check(recs, off, prm, grid, got, bws=(0, 1, 10, 11, 40, 41), tol=1e-4):
+    """The histories of the last end-to-end pass against the FP64 oracle on a
+    sample of whole blastwaves (each blastwave's history is independent, so a
+    subset runs exactly as in the batch): per-row relative L2 of every timed
+    output, its maximum per history."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from pyblastafterglowmag_gb300 import abi
+    orc = pyoracle.Oracle()
+    rows = np.concatenate([np.arange(off[b], off[b + 1]) for b in bws])
+    lens = [int(off[b + 1] - off[b]) for b in bws]
+    o = np.zeros(len(bws) + 1, dtype=np.int64)
+    o[1:] = np.cumsum(lens)
+    p = np.array([prm[b] for b in bws], dtype=abi.SHOCK_PARAMS_DTYPE)
+    rc, where, ref = orc.run(grid, recs[rows], o, p, outputs=tuple(got), outer_threads=len(bws))
+    worst = {}
+    for k, r in ref.items():
+        g = got[k][rows]
+        num = np.sqrt(((g - r) ** 2).sum(axis=1))
+        den = np.sqrt((r ** 2).sum(axis=1))
+        rel = num[den > 0] / den[den > 0]
+        zero_bad = int(((den == 0) & (num > 0)).sum())
+        worst[k] = float(rel.max()) if rel.size else 0.0
+        if zero_bad:
+            worst[k] = float("inf")
+    return {"blastwaves": list(bws), "rows": int(len(rows)), "oracle_status": int(rc),
+            "max_rel_l2": worst, "tol": tol, "ok": bool(rc == 0 and max(worst.values()) <= tol)}
 
 
 # ------------------------------------------------------ contraction arm ---

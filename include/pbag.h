@@ -225,34 +225,43 @@ int pbag_run_batch(pbag_ctx* ctx, const pbag_shock_params* prm, int nbw, const i
                    const pbag_step_rec* recs, const pbag_outputs* out, pbag_status* st);
 
 /* Same as pbag_run_batch with prm, recs and every output pointer in DEVICE
- * memory of the context's device (off stays a host array). Returns after the
- * batch has finished on the device. */
+ * memory of the context's device (off stays a host array). stream (a
+ * cudaStream_t, may be NULL) is the caller's stream whose work produces the
+ * inputs: the call waits for it before it reads them. The batch runs on the
+ * context's own stream; the call returns after it has finished there. */
 int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
                           const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st,
                           void* stream);
 
 /* Allocation-free variant of pbag_run_batch_device. No counterpart in the
  * reference: it exists for callers that cannot allocate device memory while
- * they run the step - code recording into a CUDA graph, hosts that only hand
- * out memory from their own pool, latency-critical loops that must not pay an
- * allocation - and keeps every intermediate buffer in one fixed __device__
- * array of PBAG_NOALLOC_SCRATCH_BYTES inside the library instead of memory the
- * context allocates. It calls no cudaMalloc/cudaFree; inputs and outputs are
- * the caller's device buffers exactly as for pbag_run_batch_device, on a
- * context created beforehand (pbag_create allocates the grid tables).
+ * they run the step - hosts that hand out device memory only from their own
+ * pool, latency-critical loops that must not pay an allocation or the device
+ * synchronisation one can cause - and keeps every intermediate buffer in one
+ * fixed __device__ array of PBAG_NOALLOC_SCRATCH_BYTES inside the library
+ * instead of memory the context allocates. It calls no cudaMalloc/cudaFree;
+ * inputs and outputs are the caller's device buffers exactly as for
+ * pbag_run_batch_device, on a context created beforehand (pbag_create
+ * allocates the grid tables). It runs the same preparation, evolve and
+ * radiation kernels, except that its SSC contraction is always the FP32
+ * CUDA-core one (whatever pbag_set_ssc_path chose); results agree with
+ * pbag_run_batch_device within the plain-path tolerance. The call is
+ * synchronous: it reads the shock parameters back to validate them and
+ * returns after the batch has finished.
  * Limit: the batch needs about 17 KiB per blastwave of 201 x 128 bins plus
  * 120 B per record (all rounded to 256 B blocks); a larger batch returns
  * PBAG_ERR_ARG with st->site set to the KiB it would need.
  * The first call on a device looks up the array's device address (once per
- * device); make that first call before any stream capture. Every call shares
- * the array and it keeps the last call's contents (the call clears what must
- * start at zero): calls that overlap on the GPU race, so issue them one at a
- * time. Every GPU that loads the library holds the array until exit. */
+ * device). Every call shares the array and it keeps the last call's contents
+ * (the call clears what must start at zero): calls that overlap on the GPU
+ * race, so issue them one at a time. Every GPU that loads the library holds
+ * the array until exit. */
 #define PBAG_NOALLOC_SCRATCH_BYTES (16u << 20)
 int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw, const int64_t* off,
                            const pbag_step_rec* d_recs, const pbag_outputs* d_out, pbag_status* st);
 
-/* Number of kernels the last run launched (diagnostics). */
+/* Number of kernels the last run (pbag_run_batch, pbag_run_batch_device or
+ * pbag_run_batch_noalloc) launched (diagnostics). */
 int64_t pbag_last_launch_count(const pbag_ctx* ctx);
 
 /* How the SSC spectrum (numeric_model.h:247-285) is contracted. AUTO uses

@@ -844,3 +844,134 @@ int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Shock scalars (microphysics_base.h:575-966). The members the reference keeps
+// on its ElectronAndRadiaionBase object live in `Mem`; every call follows the
+// order of computeEleSpectrumLimits: checkParams, computeMagneticField,
+// computeGammaMax, computeGammaMin, computeGammaCool.
+namespace {
+
+struct Mem {
+  const pbag_limits_opts* o;
+  double eprime, Gamma, GammaSh, betaSh, t_e, tcomov, n_prime;
+  double B, gamma_min, gamma_max, gamma_c, accel_frac, Theta, z_cool;
+};
+
+double beta_of(double g) { return std::sqrt((g - 1.) * (g + 1.)) / g; }  // EQS::BetaFromGamma
+
+double gm_func(double x, const Mem& m) {  // gammaMinFunc (microphysics_base.h:792-806)
+  const double p = m.o->p;
+  const double ave = m.o->eps_e * m.eprime / (m.n_prime * m_e * c_light * c_light);
+  if (p == 1) return (m.gamma_max - m.gamma_min) / (std::log(m.gamma_max) - std::log(m.gamma_min)) - ave;
+  if (p == 2) return (std::log(m.gamma_max) - std::log(m.gamma_min)) / (-1. / m.gamma_max + 1. / m.gamma_min) - ave;
+  return (p - 1) / (p - 2) * (std::pow(m.gamma_max, -p + 2) - std::pow(x, -p + 2)) /
+             (std::pow(m.gamma_max, -p + 1) - std::pow(x, -p + 1)) -
+         ave;
+}
+
+double bisect_gm(double a, double b, double xtol, double rtol, int iters, const Mem& m, int& status) {
+  // rootfinders.h:17-58
+  status = 0;
+  const double fa0 = gm_func(a, m), fb0 = gm_func(b, m);
+  if (fa0 * fb0 > 0) { status = -1; return 0.; }
+  if (fa0 == 0) { status = -1; return a; }
+  if (fb0 == 0) { status = -1; return b; }
+  double fa = fa0, d = b - a;
+  for (int k = 0; k < iters; ++k) {
+    d *= 0.5;
+    const double mid = a + d;
+    const double fm = gm_func(mid, m);
+    if (fm * fa >= 0) a = mid;
+    if (fm == 0 || std::fabs(d) < xtol + rtol * std::fabs(mid)) return mid;
+  }
+  status = -1;
+  return a;
+}
+
+}  // namespace
+
+extern "C" int orc_shock_limits(const pbag_limits_opts* o, const double* gam, int ngam, int n,
+                                const pbag_shock_state* in, double* state, pbag_limits* out) {
+  if (!o || !gam || ngam < 2 || n < 0 || !state || (n > 0 && (!in || !out))) return PBAG_ERR_ARG;
+  Mem m{};
+  m.o = o;
+  m.gamma_min = state[0], m.gamma_max = state[1], m.gamma_c = state[2], m.accel_frac = state[3];
+  m.B = state[4], m.Theta = state[5], m.z_cool = state[6];
+  const bool analytic = o->ele_analytic != 0;
+  const double egrid_lo = gam[0], egrid_hi = gam[ngam - 1];
+  for (int s = 0; s < n; ++s) {
+    const pbag_shock_state& x = in[s];
+    m.GammaSh = x.GammaSh, m.eprime = x.e_prime, m.Gamma = x.Gamma, m.betaSh = beta_of(x.GammaSh);
+    m.t_e = x.t_e, m.tcomov = x.tcomov, m.n_prime = x.n_prime;
+    const bool ok = !(m.betaSh < o->beta_min);  // checkParams
+    if (ok) {
+      if (o->eps_e <= 0 || o->eps_b <= 0 || o->eps_t < 0 || o->p <= 0 || m.n_prime <= 0 || m.eprime < 0 ||
+          !std::isfinite(m.eprime))
+        return PBAG_ERR_PARAM;
+      // computeMagneticField
+      const double Bub = std::sqrt(8. * pi_ * (m.eprime * o->eps_b));
+      const double Bsh = std::sqrt(32. * M_PI * o->eps_b * (m.GammaSh - 1.) * (m.GammaSh + 3. / 4) * m.n_prime * m_p *
+                                   (c_light * c_light));
+      const double Bmag = std::sqrt(9.0 * M_PI * o->eps_b * m.n_prime * o->mu * m_p) * (m.betaSh * c_light);
+      m.B = o->method_B == 0 ? Bub : o->method_B == 2 ? Bsh : Bmag;
+      // computeGammaMax
+      if (o->method_gamma_max == 0) m.gamma_max = std::sqrt(6.0 * pi_ * q_e / sigma_T / m.B);
+      if (!analytic && m.gamma_max > 0.99 * egrid_hi) m.gamma_max = 0.99 * egrid_hi;
+      // computeGammaMin
+      const double p = o->p;
+      int status = 0;
+      const double g1 = (p - 2.) / (p - 1.) * (m.eprime * o->eps_e) / (m.n_prime * m_e * c_light * c_light);
+      const double g2 = (p - 2.) / (p - 1.) * (m_p / m_e) * o->eps_e * beta_of(m.GammaSh);
+      const double g3 = (p - 2.) / (p - 1.) * (o->eps_e * m_p / m_e * (m.GammaSh - 1.) + 1.);
+      const double th0 = o->eps_t * (9.0 * o->mu * m_p / (32.0 * o->mu_e * m_e)) * m.betaSh * m.betaSh;
+      m.Theta = (5.0 * th0 - 6.0 + std::sqrt(25.0 * th0 * th0 + 180.0 * th0 + 36.0)) / 30.0;  // Margalit21::Theta_fun
+      m.z_cool = (6.0 * M_PI * m_e * c_light / (sigma_T * m.B * m.B * m.t_e)) / m.Theta;
+      const double g4 = 1. + (6.0 + 15.0 * m.Theta) / (4.0 + 5.0 * m.Theta) * m.Theta;  // Margalit21::gamma_m_fun
+      if (o->method_gamma_min == 0) m.gamma_min = g1;
+      else if (o->method_gamma_min == 2) m.gamma_min = g2;
+      else if (o->method_gamma_min == 3) m.gamma_min = g3;
+      else if (o->method_gamma_min == 4) m.gamma_min = g4;
+      else if (o->method_gamma_min == 1) {
+        m.gamma_min = bisect_gm(1., 1.e8, 0., .001, 100, m, status);
+        if (status < 0 && g1 > 1.5) m.gamma_min = g1;
+      } else {
+        return PBAG_ERR_ARG;
+      }
+      const double gM = m.gamma_max, gm = m.gamma_min;
+      const double ayache = (std::pow(gM, 2 - p) - std::pow(gm - 1., 2. - p)) / (std::pow(gM, 2. - p) - 1.) *
+                            (std::pow(gM, 1. - p) - 1.) / (std::pow(gM, 1. - p) - std::pow(gm - 1., 1. - p));
+      const double sironi = (p - 2.0) / (p - 1.0) * o->eps_e * m.eprime / (m.n_prime * m_e * c_light * c_light);
+      if (m.gamma_min < 2. || status < 0) {
+        if (o->method_nonrel == 0) m.accel_frac = 1;
+        else if (o->method_nonrel == 1) m.accel_frac = m.gamma_min;
+        else if (o->method_nonrel == 2 || o->method_nonrel == 3) {
+          if (p < 2.) return PBAG_ERR_PARAM;
+          m.accel_frac = o->method_nonrel == 2 ? ayache : sironi;
+        } else {
+          return PBAG_ERR_ARG;
+        }
+        if (m.accel_frac > 1.) m.accel_frac = 1;
+        if (m.gamma_min < 1.) m.gamma_min = 1;
+      }
+      if (!std::isfinite(m.gamma_min) || !std::isfinite(m.accel_frac) || m.accel_frac < 0) return PBAG_ERR_NONFINITE;
+      if (!analytic && m.gamma_min < egrid_lo) {
+        m.gamma_min = egrid_lo;
+        if (m.gamma_min > 1e8) return PBAG_ERR_PARAM;
+      }
+      // computeGammaCool
+      if (o->method_gamma_c == 0) m.gamma_c = 6. * pi_ * m_e * c_light / (sigma_T * m.B * m.B) * x.t_e / m.Gamma;
+      else if (o->method_gamma_c == 1) m.gamma_c = (6. * pi_ * m_e * c_light) / (sigma_T * m.B * m.B * m.tcomov);
+      if (m.gamma_c <= 1.) m.gamma_c = 1.001;
+      if (!analytic && m.gamma_c > m.gamma_max) m.gamma_c = m.gamma_max;
+    }
+    pbag_limits& r = out[s];
+    r.B = m.B, r.gamma_min = m.gamma_min, r.gamma_max = m.gamma_max, r.gamma_c = m.gamma_c;
+    r.accel_frac = m.accel_frac, r.Theta = m.Theta, r.z_cool = m.z_cool;
+    r.valid = ok ? 1 : 0;
+    r.reserved = 0;
+  }
+  state[0] = m.gamma_min, state[1] = m.gamma_max, state[2] = m.gamma_c, state[3] = m.accel_frac;
+  state[4] = m.B, state[5] = m.Theta, state[6] = m.z_cool;
+  return PBAG_OK;
+}

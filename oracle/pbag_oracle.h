@@ -43,6 +43,13 @@ int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_
                   const double* a_all, const double* r_all, int nq, const pbag_flux_query* qs, double* flux,
                   int* fail_index);
 
+/* Per-step shock scalars of one blastwave object over n consecutive calls of
+ * updateSockProperties + computeEleSpectrumLimits (microphysics_base.h:575-605,
+ * 642-652, 736-966; Bisect rootfinders.h:17-58), with the same arguments and
+ * the same persistent-state convention as pbag_shock_limits (pbag.h). */
+int orc_shock_limits(const pbag_limits_opts* o, const double* gam, int ngam, int n, const pbag_shock_state* in,
+                     double* state, pbag_limits* out);
+
 /* Flags for orc_run. */
 enum {
   ORC_HOIST_HEATING = 1,  /* compute the (substep-invariant) cooling terms once per

@@ -20,7 +20,9 @@ from pyblastafterglowmag_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpbag_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpbaref.so")
-REF_SRC = "/root/reference/src"
+# the reference project's src/ directory: PBAG_REF_SRC, else a checkout named
+# "reference" next to this repository
+REF_SRC = os.environ.get("PBAG_REF_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")
 
 ORC_HOIST_HEATING = 1
 ORC_INNER_OMP = 2
@@ -65,7 +67,25 @@ class Oracle:
                                      C.c_void_p, C.c_void_p, C.c_int]
         lib.orc_flux_dens.argtypes = [P(abi.GridDesc), P(abi.FluxOpts), P(C.c_int64), P(C.c_double), P(C.c_double),
                                       P(C.c_double), C.c_int, C.c_void_p, P(C.c_double), P(C.c_int)]
+        lib.orc_shock_limits.argtypes = [P(abi.LimitsOpts), P(C.c_double), C.c_int, C.c_int, C.c_void_p,
+                                         P(C.c_double), C.c_void_p]
         self.lib = lib
+
+    def shock_limits(self, opts, gam, states, state=None):
+        """orc_shock_limits over a sequence of shock states of one blastwave
+        (the same arguments and results as the library's shock_limits), so that
+        histories.make_batch(Oracle(), cfg) builds step records without the
+        product library."""
+        states = np.ascontiguousarray(states, dtype=abi.SHOCK_STATE_DTYPE)
+        out = np.zeros(len(states), dtype=abi.LIMITS_DTYPE)
+        if state is None:
+            state = np.array([-1.0, 1e7, -1.0, 1.0, -1.0, -1.0, -1.0])
+        gam = np.ascontiguousarray(gam, dtype=np.float64)
+        rc = self.lib.orc_shock_limits(C.byref(opts), abi.dptr(gam), len(gam), len(states), states.ctypes.data,
+                                       abi.dptr(state), out.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"orc_shock_limits failed: {rc}")
+        return out
 
     def grids(self, grid):
         gam = np.zeros(grid.ngam)

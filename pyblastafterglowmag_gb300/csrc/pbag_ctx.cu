@@ -746,6 +746,8 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
   reset_status(st);
   if (!c || !d_out || (nbw > 0 && (!d_prm || !d_recs))) return PBAG_ERR_ARG;
   if (cudaSetDevice(c->device) != cudaSuccess) return PBAG_ERR_CUDA;
+  // the inputs may come from work still running on the caller's stream
+  if (stream && cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess) return PBAG_ERR_CUDA;
   std::vector<pbag_shock_params> hp((size_t)std::max(nbw, 0));
   if (nbw > 0 && cudaMemcpy(hp.data(), d_prm, hp.size() * sizeof(pbag_shock_params), cudaMemcpyDeviceToHost) !=
                      cudaSuccess)
@@ -755,7 +757,6 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
     if (st) st->code = rc;
     return rc;
   }
-  (void)stream;
   return run_device(c, d_prm, nbw, off, d_recs, *d_out, st);
 }
 
@@ -799,6 +800,10 @@ void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* x) {
   if (!c || slot < 0 || slot >= kExtSlots) return;
   delete c->ext[slot];
   c->ext[slot] = x;
+}
+
+void ctx_set_launches(pbag_ctx* c, int64_t n) {
+  if (c) c->launches = n;
 }
 
 bool ctx_view(const pbag_ctx* c, CtxView* v) {

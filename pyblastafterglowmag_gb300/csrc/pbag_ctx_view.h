@@ -19,6 +19,8 @@ struct CtxView {
 
 // Fills *v from c; false when c is null.
 bool ctx_view(const pbag_ctx* c, CtxView* v);
+// The kernel count pbag_last_launch_count reports for c's last run.
+void ctx_set_launches(pbag_ctx* c, int64_t n);
 
 // A per-context workspace owned by an entry point of another translation
 // unit: created on first use, destroyed with the context.

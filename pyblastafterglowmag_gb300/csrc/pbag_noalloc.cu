@@ -1,14 +1,17 @@
 // pbag_noalloc.cu - a variant of the batch step that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc at the moment they run the step: code
-// that runs while a CUDA graph is being captured into which an allocation
-// cannot be recorded, hosts that hand out device memory only through their own
-// pool, or latency-critical loops where an allocation (and the implicit device
-// synchronisation it may cause) is not acceptable. For them,
-// pbag_run_batch_noalloc does what pbag_run_batch_device does - same kernels,
-// same results - but keeps every intermediate buffer (per-blastwave state,
-// per-record scalars, offsets, error records) in one file-scope __device__
-// array of fixed size instead of memory the context allocates on demand.
+// Some callers cannot call cudaMalloc at the moment they run the step: hosts
+// that hand out device memory only through their own pool, or latency-critical
+// loops where an allocation (and the implicit device synchronisation it may
+// cause) is not acceptable. For them, pbag_run_batch_noalloc evolves a batch as
+// pbag_run_batch_device does - same preparation, evolve and radiation kernels,
+// results within the same tolerance - but keeps every intermediate buffer
+// (per-blastwave state, per-record scalars, offsets, error records) in one
+// file-scope __device__ array of fixed size instead of memory the context
+// allocates on demand. Its SSC contraction is always the FP32 CUDA-core one
+// (the tensor-core operand tiles would need more scratch), whatever
+// pbag_set_ssc_path chose for the context. The call is synchronous: it reads
+// the parameters back to validate them and waits for the batch to finish.
 //
 // That array is part of the loaded module: every GPU that loads the library
 // holds its PBAG_NOALLOC_SCRATCH_BYTES until the process exits. All calls
@@ -150,6 +153,7 @@ extern "C" int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_
   CtxView v;
   if (!ctx_view(ctx, &v) || !d_out || !off || nbw < 0 || (nbw > 0 && (!d_prm || !d_recs))) return PBAG_ERR_ARG;
   if (off[0] != 0) return PBAG_ERR_ARG;
+  if (nbw > 0 && off[nbw] > ((int64_t)1 << 40)) return PBAG_ERR_ARG;  // keeps scratch_need free of overflow
   int64_t max_len = 0;
   for (int b = 0; b < nbw; ++b) {
     if (off[b + 1] < off[b] || off[b + 1] - off[b] > ((int64_t)1 << 30)) return PBAG_ERR_ARG;
@@ -233,6 +237,9 @@ extern "C" int pbag_run_batch_noalloc(pbag_ctx* ctx, const pbag_shock_params* d_
   }
   ok(cudaStreamSynchronize(s));
   if (e != cudaSuccess) return PBAG_ERR_CUDA;
+  // kernels of this call: preparation (3, or 2 without records), evolve and
+  // radiation per step, the completion of the last step, the failure scan
+  ctx_set_launches(ctx, nbw > 0 ? (nrec > 0 ? 3 : 2) + 2 * max_len + (max_len > 0 ? 1 : 0) + 1 : 0);
   if (st) {
     st->code = fail[0];
     st->bw = fail[1];

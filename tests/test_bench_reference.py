@@ -32,3 +32,16 @@ def test_reference_arm_under_torchrun():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("gaussian-jet-21-layers")
+
+
+def test_reference_arm_loads_no_gpu_library():
+    """The CPU arm builds its records and runs the step with the oracle alone:
+    the GPU library is never loaded into its process."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--cpu-sample-seconds', '2']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED', int('libpbag.so' in maps), int('libpbag_oracle.so' in maps))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    tail = [ln for ln in r.stdout.splitlines() if ln.startswith("LOADED")]
+    assert tail == ["LOADED 0 1"], r.stdout[-2000:]

@@ -77,17 +77,19 @@ def test_gaussian_ssc_small_batch_kernel(lib, oracle, cuda_device, monkeypatch):
 
 def test_gaussian_ssc_fp64_scan(lib, oracle, cuda_device, monkeypatch):
     """The Chang-Cooper substeps with the FP64 scan forced (the path a step
-    takes when its coefficients leave the FP32 range of the double-float scan)."""
+    takes when its coefficients leave the FP32 range of the double-float scan),
+    on a window of the jet whose Chang-Cooper steps take 2-95 substeps."""
     monkeypatch.setenv("PBAG_SCAN_FP64", "1")
-    _compare(lib, oracle, cases.gaussian(lib, nlayers=3, nsteps=120))
+    _compare(lib, oracle, cases.jet_window(lib, (0, 1, 2, 3), 280, 140))
 
 
 def test_double_float_scan_matches_fp64_scan(lib, cuda_device, monkeypatch):
     """The double-float substeps against the FP64 ones on the same batch: the
     electron histories agree to far below the plain-path bar (the pairs carry
     ~48 significant bits); the emissivities, formed from FP32 weights of those
-    histories, to within an FP32 rounding."""
-    recs, off, prm, grid = cases.gaussian(lib, nlayers=3, nsteps=120)
+    histories, to within an FP32 rounding. The window's Chang-Cooper steps
+    take 2-95 substeps (242 steps) or 96-125 (36 steps)."""
+    recs, off, prm, grid = cases.jet_window(lib, (0, 1, 2, 3), 280, 140)
     outs = ("ele_f_all", "j_all")
     ctx = Context(grid, device=0, ssc=True)
     df = ctx.run(recs, off, prm, outputs=outs)
@@ -107,7 +109,9 @@ def test_gaussian_late_window(lib, oracle, cuda_device):
 
 
 def test_uneven_batch(lib, oracle, cuda_device):
-    _compare(lib, oracle, cases.uneven(lib), outputs=cases.TOTALS)
+    """Three seeded sweep jets with uneven histories (up to 1000 substeps per
+    step, 59 steps on the systolic path), every history."""
+    _compare(lib, oracle, cases.uneven(lib))
 
 
 def test_error_status_matches_oracle(lib, oracle, cuda_device):

@@ -118,3 +118,31 @@ def test_pooled_sweep_equals_serial(lib):
     a = H.sweep_batch(lib, 3, seed=11, min_steps=20, max_steps=60, max_layers=3)
     b = H.sweep_batch(lib, 3, seed=11, min_steps=20, max_steps=60, max_layers=3, workers=2)
     assert (a[0].tobytes() == b[0].tobytes()) and (a[1] == b[1]).all()
+
+
+def test_oracle_shock_limits_match_reference_fixture(oracle):
+    """The oracle's own restatement of computeEleSpectrumLimits against the
+    values the reference produced, for every option set of the fixture."""
+    d = np.load(os.path.join(GOLD, "shock_limits.npz"))
+    a = d["grid"]
+    gam, _ = oracle.grids(abi.GridDesc(int(a[0]), int(a[1]), *map(float, a[2:])))
+    for (gm, gc, gx, bm, nr, p), ref in zip(d["opts"], d["out"]):
+        o = abi.LimitsOpts()
+        o.p, o.eps_e, o.eps_b, o.eps_t = p, 0.1, 1e-3, 0.5
+        o.beta_min, o.mu, o.mu_e = 1e-5, 0.62, 1.18
+        o.method_B, o.method_gamma_min, o.method_gamma_c = int(bm), int(gm), int(gc)
+        o.method_gamma_max, o.method_nonrel, o.ele_analytic = int(gx), int(nr), 0
+        state = np.array([-1.0, 1e7, 1e5 if int(gc) == 2 else -1.0, 1.0, -1.0, -1.0, -1.0])
+        got = oracle.shock_limits(o, gam, d["states"], state=state)
+        cols = ["B", "gamma_min", "gamma_max", "gamma_c", "accel_frac", "Theta", "z_cool"]
+        g = np.stack([got[c] for c in cols] + [got["valid"].astype(float)], axis=1)
+        np.testing.assert_allclose(g, ref, rtol=1e-13, atol=0, err_msg=str((gm, gc, gx, bm, nr, p)))
+
+
+def test_oracle_built_records_equal_library_built_records(lib, oracle):
+    """The benchmark's CPU arm builds the Gaussian jet's step records with the
+    oracle alone; they are the same bytes the library's host code produces."""
+    a = H.make_batch(lib, H.config_gaussian_ssc())
+    b = H.make_batch(oracle, H.config_gaussian_ssc())
+    assert a[0].tobytes() == b[0].tobytes()
+    assert (a[1] == b[1]).all() and a[2].tobytes() == b[2].tobytes()

@@ -1,8 +1,10 @@
 """pbag_run_batch_noalloc: the step for callers that cannot allocate device
-memory while they run it (graph capture, pool-only hosts, latency-critical
-loops). It keeps all intermediates in a fixed array inside the library, so it
-must give the same histories as pbag_run_batch_device on the same device
-buffers, call after call, and must reject a batch that does not fit.
+memory while they run it (hosts that hand out device memory only from their
+own pool, latency-critical loops). It keeps all intermediates in a fixed array
+inside the library, so it must give the same histories as
+pbag_run_batch_device on the same device buffers (within the plain-path
+tolerance: its SSC contraction is the FP32 CUDA-core one), call after call,
+and must reject a batch that does not fit.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test."""
@@ -67,6 +69,9 @@ def test_noalloc_matches_device_entry_point_twice(lib, cuda_device):
         assert rc == abi.PBAG_OK, (rc, st.bw, st.step, st.site)
         if call == 1:
             assert torch.cuda.mem_get_info()[0] == free_before, "the call allocated device memory"
+        # preparation (3), evolve + radiation per step, the last completion, the failure scan
+        max_len = int((off[1:] - off[:-1]).max())
+        assert ctx.last_launch_count() == 3 + 2 * max_len + 1 + 1
         got = {k: v.cpu().numpy() for k, v in bufs.items()}
         for k in OUTS:
             assert np.isfinite(got[k]).all(), k
