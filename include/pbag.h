@@ -201,6 +201,25 @@ int pbag_shock_limits(const pbag_limits_opts* o, const double* gam, int ngam, in
 
 typedef struct pbag_ctx pbag_ctx;  /* opaque device context */
 
+/* Per-step shock scalars of a whole batch on the GPU, for callers that hold
+ * the histories on the device (the post-processing mode, where every state of
+ * a blastwave is known before its electrons are evolved): pbag_shock_limits
+ * for every blastwave at once, on the electron grid of ctx. Blastwave b owns
+ * the states off[b] .. off[b+1]-1 (host array of nbw+1, as for pbag_run_batch)
+ * and has options d_opts[b]; row b of d_state [nbw][7] carries its members as
+ * the state argument of pbag_shock_limits does (initialise it the same way; on
+ * return it holds the members after the last state); d_out receives one
+ * pbag_limits per state. Device pointers; synchronous. Results equal the host
+ * prep's to rounding (device pow and log differ in the last bits, which can
+ * move the useNumeric bisection by one of its 0.1 % steps where gammaMinFunc
+ * is within rounding of zero at a midpoint). On a failure st names the
+ * blastwave and step of the earliest failing state; later results of that
+ * blastwave are not meaningful.
+ * Replaces: updateSockProperties + computeEleSpectrumLimits
+ * (microphysics_base.h:575-605, 642-652, 808-966) over whole histories. */
+int pbag_shock_limits_device(pbag_ctx* ctx, int nbw, const int64_t* off, const pbag_limits_opts* d_opts,
+                             const pbag_shock_state* d_in, double* d_state, pbag_limits* d_out, pbag_status* st);
+
 /* Create a device context for one grid (one CommonTables entry of the
  * reference, microphysics/common.h:93-117) on CUDA device `device`. When
  * ssc_tables != 0 the SSC kernel K[i][j][k] (kernels.h:49-117) and its

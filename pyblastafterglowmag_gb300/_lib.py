@@ -32,6 +32,9 @@ def _check(rc, what, st=None):
         raise PbagError(rc, what)
 
 
+P_I64 = C.POINTER(C.c_int64)
+
+
 def load():
     """The loaded library (raises if it has not been built)."""
     global _lib
@@ -131,6 +134,22 @@ def shock_limits(opts, gam, states, state=None):
                                  states.ctypes.data, abi.dptr(state), out.ctypes.data),
            "pbag_shock_limits")
     return out
+
+
+def shock_limits_device(ctx, off, d_opts, d_in, d_state, d_out):
+    """pbag_shock_limits_device: the shock scalars of every state of nbw
+    blastwaves on the GPU (device addresses; off a host int64 array of
+    nbw+1). Returns the pbag_status."""
+    lib = load()
+    lib.pbag_shock_limits_device.argtypes = [C.c_void_p, C.c_int, P_I64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.POINTER(abi.Status)]
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    st = abi.Status()
+    rc = lib.pbag_shock_limits_device(ctx.handle, len(off) - 1, off.ctypes.data_as(P_I64), C.c_void_p(d_opts),
+                                      C.c_void_p(d_in), C.c_void_p(d_state), C.c_void_p(d_out), C.byref(st))
+    if rc != 0:
+        raise PbagError(rc, "pbag_shock_limits_device", st.bw, st.step, st.site)
+    return st
 
 
 class Context:

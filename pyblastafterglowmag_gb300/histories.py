@@ -337,6 +337,40 @@ def make_batch(lib, cfg, nsteps=None):
     return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid
 
 
+def driver_arrays(lib, cfg, nsteps=None):
+    """Per blastwave (ordered as make_batch orders them) the quantities the
+    reference's blastwave driver passes to ElectronAndRadiation at every
+    burster time (blastwave_radiation.h:976-1182): a list of (is_rs, dict of
+    arrays) with valid, U_p, Gamma, GammaSh, t_e, t_b, tcomov, n_prime,
+    n_protons, M2, rho2, R, thickness (passed at the first valid step) and the
+    comoving thickness (passed to the evolution). `valid` marks the steps
+    make_batch records (the driver skips the others)."""
+    tb = np.logspace(np.log10(cfg.tb1), np.log10(cfg.tb2), cfg.ntb)
+    if nsteps is not None:
+        tb = tb[:nsteps]
+    gam, _ = lib.grids(cfg.grid())
+    lo, hi, E, G0 = layer_table(cfg)
+    omega = 2 * np.pi * (np.cos(lo) - np.cos(hi)) * 2
+    dyn = layer_dynamics_many(E, G0, cfg.n_ism, tb, omega)
+    out = []
+    for il in range(cfg.nlayers):
+        d = dyn[il]
+        for is_rs, st, sh in ((False, fs_state(d), cfg.fs), (True, rs_state(d) if cfg.rs is not None else None, cfg.rs)):
+            if st is None:
+                continue
+            ss = np.zeros(len(tb), dtype=abi.SHOCK_STATE_DTYPE)
+            ss["e_prime"], ss["Gamma"], ss["GammaSh"] = st["u_p"], st["Gamma"], st["GammaSh"]
+            ss["t_e"], ss["t_b"], ss["tcomov"] = d["t_obs"], tb, d["tcomov"]
+            ss["n_prime"], ss["n_protons"] = st["rho2"] / M_P, st["m2"] / M_P
+            lim = lib.shock_limits(limits_opts(sh), gam, ss)
+            valid = st["valid"] & (lim["valid"] == 1) & (st["u_p"] > 0) & (st["rho2"] > 0)
+            out.append((is_rs, dict(valid=valid.astype(np.float64), U_p=st["u_p"], Gamma=st["Gamma"],
+                                    GammaSh=st["GammaSh"], t_e=d["t_obs"], t_b=tb, tcomov=d["tcomov"],
+                                    n_prime=st["rho2"] / M_P, n_protons=st["m2"] / M_P, M2=st["m2"],
+                                    rho2=st["rho2"], R=d["R"], thickness=st["thick"], dr=st["dr"])))
+    return out
+
+
 def _sweep_set(cfg):
     from . import _lib
     return make_batch(_lib, cfg)
