@@ -593,6 +593,13 @@ def sweep_arm(args):
         except _lib.PbagError as e:  # the reference would stop this run; the batch completes
             status.update(code=e.code, blastwave=e.bw, step=e.step)
 
+    if args.profile:
+        for _ in range(args.profile):
+            one_pass()
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_passes": args.profile, "launches_per_pass": ctx.last_launch_count(),
+                          "blastwaves": nbw}))
+        return
     for _ in range(args.warmup):
         flush.zero_()
         one_pass()
@@ -610,6 +617,13 @@ def sweep_arm(args):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
     replicas.barrier(world, dev)
+    # per-kernel-class device time: one more pass with a CUDA event pair
+    # around every launch (direct launches instead of the captured graph)
+    ctx.set_timing(True)
+    flush.zero_()
+    one_pass()
+    timing = ctx.timing()
+    ctx.set_timing(False)
     t = replicas.max_over_ranks(sum(ms) / len(ms), world)
     value = replicas.job_rate(nvalid, t * 1e-3, world)
     if rank != 0:
@@ -625,7 +639,10 @@ def sweep_arm(args):
                        "launch": "one captured graph over the longest history",
                        "l2": "flushed with a 256 MiB device write before every timed pass",
                        "outputs": list(outs)},
-            "clocks": clk.summary(), "status": status, "gpu_launches": ctx.last_launch_count()}
+            "clocks": clk.summary(), "status": status, "gpu_launches": ctx.last_launch_count(),
+            "kernel_ms_per_pass": {k: v[0] for k, v in timing.items()},
+            "kernel_launches_per_pass": {k: v[1] for k, v in timing.items()},
+            "kernel_timing": "CUDA events around every launch on the library stream, one extra pass with direct launches"}
     print(json.dumps(line), flush=True)
 
 

@@ -268,7 +268,7 @@ int pbag_run_batch_device(pbag_ctx* ctx, const pbag_shock_params* d_prm, int nbw
  * synchronous: it reads the shock parameters back to validate them and
  * returns after the batch has finished.
  * Limit: the batch needs about 17 KiB per blastwave of 201 x 128 bins plus
- * 120 B per record (all rounded to 256 B blocks); a larger batch returns
+ * 128 B per record (all rounded to 256 B blocks); a larger batch returns
  * PBAG_ERR_ARG with st->site set to the KiB it would need.
  * The first call on a device looks up the array's device address (once per
  * device). Every call shares the array and it keeps the last call's contents

@@ -62,10 +62,12 @@ struct GraphKey {
   bool ssc;
   int ssc_path;
   int64_t sur_gen;
+  const void* synbank;
   const void* out[kOutputs];
   bool operator==(const GraphKey& o) const {
     if (nbw != o.nbw || max_len != o.max_len || nrec != o.nrec || recs != o.recs || prm != o.prm ||
-        state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path || sur_gen != o.sur_gen)
+        state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path || sur_gen != o.sur_gen ||
+        synbank != o.synbank)
       return false;
     for (int k = 0; k < kOutputs; ++k)
       if (out[k] != o.out[k]) return false;
@@ -100,8 +102,10 @@ struct pbag_ctx {
   // k_evolve wrote) and joins the main stream before the next step
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  cudaError_t launch_radiation(const pbag_shock_params* d_prm, int nbw, int s) {
-    if (!ssc_on_tensor_cores()) return launch_rad_ssc(dg, S, d_prm, nbw, ssc, s, stream);
+  cudaError_t launch_radiation(const DevGrid& gg, const DevState& SS, const pbag_shock_params* d_prm, int nbw, int s) {
+    const bool syn_tc = SS.Dsyn != nullptr;  // synchrotron / SSA sums on the tensor cores
+    if (!ssc_on_tensor_cores())
+      return syn_tc ? launch_syn_tc(gg, SS, nbw, stream) : launch_rad_ssc(gg, SS, d_prm, nbw, ssc, s, stream);
     cudaError_t e;
     if ((e = cudaEventRecord(ev_fork, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
@@ -115,8 +119,39 @@ struct pbag_ctx {
       return e;
     }
     if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
-    if ((e = launch_rad_ssc(dg, S, d_prm, nbw, false, s, stream)) != cudaSuccess) return e;
+    if ((e = syn_tc ? launch_syn_tc(gg, SS, nbw, stream) : launch_rad_ssc(gg, SS, d_prm, nbw, false, s, stream)) !=
+        cudaSuccess)
+      return e;
     return cudaStreamWaitEvent(stream, ev_join, 0);
+  }
+  // the tensor-core synchrotron sums: bank geometry (set at creation when the
+  // grid allows them), the banks of the four method classes (built on first
+  // use), the switch PBAG_SYN_TC=0 (CUDA-core sums)
+  bool sb_ok = false;
+  SynBankGeom sb{};
+  double sb_lnnu0 = 0., sb_lnxs = 0., sb_dnu = 0.;
+  const uint16_t* sb_bank[4] = {};
+  bool syn_tc_enabled() const {
+    const char* v = std::getenv("PBAG_SYN_TC");
+    return sb_ok && !(v && v[0] == '0');
+  }
+  // bank of the method class of syn_method: CSYN (cyclotron bins apart), Dermer09, GSL, Bessel
+  static int syn_class(int syn_method) {
+    return syn_method == PBAG_SYN_CSYN ? 0 : syn_method == PBAG_SYN_DER09 ? 1 : syn_method == PBAG_SYN_GSL ? 2 : 3;
+  }
+  cudaError_t syn_bank(int cls, const uint16_t** out) {
+    if (!sb_bank[cls]) {
+      std::vector<uint16_t> bank;
+      const int method = cls == 0 ? PBAG_SYN_CSYN : cls == 1 ? PBAG_SYN_DER09 : cls == 2 ? PBAG_SYN_GSL : PBAG_SYN_BESSEL;
+      build_syn_bank(method, cls == 0 ? dg.n_cyc : 0, gam.data(), G, Gp, sb_dnu, sb, bank);
+      const uint16_t* p = nullptr;
+      cudaError_t e = grid_upload(&p, bank);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the host vector goes out of scope
+      if (e != cudaSuccess) return e;
+      sb_bank[cls] = p;
+    }
+    *out = sb_bank[cls];
+    return cudaSuccess;
   }
   // batch buffers, grown on demand
   int cap_bw = 0;
@@ -168,6 +203,8 @@ struct pbag_ctx {
     for (void* p : state_mem) cudaFree(p);
     state_mem.clear();
     S.Abf = nullptr;
+    S.Sbf = nullptr;
+    S.Dsyn = nullptr;
     cap_bw = 0;
     d_off = nullptr;
     d_first = nullptr;
@@ -219,6 +256,11 @@ struct pbag_ctx {
     if ((e = state_alloc(&S.scal, cap * kScal)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.flags, cap)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.err, cap * 4)) != cudaSuccess) return e;
+    if (sb_ok) {
+      const size_t tiles = (cap + dg.sb_tbw - 1) / dg.sb_tbw;
+      if ((e = state_alloc(&S.Sbf, tiles * tc_tile_elems(2 * dg.sb_tbw, Gp))) != cudaSuccess) return e;
+      if ((e = state_alloc(&S.Dsyn, tiles * (size_t)sb.P * 2 * dg.sb_tbw * sb.M)) != cudaSuccess) return e;
+    }
     cap_bw = (int)cap;
     return cudaSuccess;
   }
@@ -257,6 +299,9 @@ struct pbag_ctx {
       return e;
     if ((e = z(S.scal, n * kScal * sizeof(double))) != cudaSuccess) return e;
     if ((e = z(S.flags, n * sizeof(int))) != cudaSuccess) return e;
+    if (S.Sbf && (e = z(S.Sbf, (n + dg.sb_tbw - 1) / dg.sb_tbw * tc_tile_elems(2 * dg.sb_tbw, Gp) *
+                                   sizeof(uint16_t))) != cudaSuccess)
+      return e;
     return z(S.err, n * 4 * sizeof(int));
   }
 };
@@ -285,10 +330,21 @@ int check_batch(const pbag_ctx* c, const pbag_shock_params* prm_host, int nbw, c
 }
 
 // Runs every step of the batch; all pointers are device pointers except off_h.
-int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off_h,
-               const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st) {
+// syn_cls >= 0: the synchrotron / SSA sums on the tensor cores with the bank of
+// that method class.
+int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64_t* off_h,
+                    const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st, int syn_cls) {
   cudaError_t e = c->reserve_bw(nbw);
   if (e != cudaSuccess) return cuda_code(e);
+  // this run's grid tables and state: the bank and its buffers only on the tensor-core path
+  DevGrid gg = c->dg;
+  DevState SS = c->S;
+  if (syn_cls >= 0) {
+    if ((e = c->syn_bank(syn_cls, &gg.synbank)) != cudaSuccess) return cuda_code(e);
+  } else {
+    SS.Sbf = nullptr;
+    SS.Dsyn = nullptr;
+  }
   const size_t nrec = (size_t)off_h[nbw];
   if ((e = c->reserve_rec(nrec, false)) != cudaSuccess) return cuda_code(e);
   if ((e = cudaMemcpyAsync(c->d_off, off_h, sizeof(int64_t) * (nbw + 1), cudaMemcpyHostToDevice, c->stream)) !=
@@ -309,7 +365,7 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   if (c->ssc_path == PBAG_SSC_SURROGATE && nbw > 0 && (e = surrogate_reserve(c, nbw)) != cudaSuccess)
     return cuda_code(e);
   if (nbw > 0) {
-    if ((e = launch_prepare(c->dg, c->S, d_recs, c->d_off, d_prm, nbw, (int64_t)nrec, c->d_first, c->d_ss,
+    if ((e = launch_prepare(gg, SS, d_recs, c->d_off, d_prm, nbw, (int64_t)nrec, c->d_first, c->d_ss,
                             c->stream)) != cudaSuccess)
       return PBAG_ERR_CUDA;
     c->launches += nrec > 0 ? 3 : 2;
@@ -329,7 +385,8 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   // Without timing, the step loop (3 launches per step index) is captured once
   // into a CUDA graph per batch shape and buffer set, and replayed.
   if (!c->timing && max_len > 0) {
-    GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, surrogate_generation(c), {}};
+    GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, surrogate_generation(c),
+                 gg.synbank, {}};
     std::memcpy(key.out, &d_out, sizeof(d_out));
     if (!c->graph_exec || !(key == c->graph_key)) {
       if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
@@ -359,11 +416,11 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
       if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBAG_ERR_CUDA;
       cudaError_t ce = cudaSuccess;
       for (int64_t s = 0; s < max_len && ce == cudaSuccess; ++s) {
-        ce = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream);
-        if (ce == cudaSuccess) ce = c->launch_radiation(d_prm, nbw, (int)s);
+        ce = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream);
+        if (ce == cudaSuccess) ce = c->launch_radiation(gg, SS, d_prm, nbw, (int)s);
       }
       if (ce == cudaSuccess)
-        ce = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)(max_len - 1), d_out, c->stream);
+        ce = launch_finalize(gg, SS, c->d_off, d_prm, nbw, (int)(max_len - 1), d_out, c->stream);
       cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
       if (ce != cudaSuccess || ee != cudaSuccess || !graph) {
         if (graph) cudaGraphDestroy(graph);
@@ -383,17 +440,17 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
   }
   for (int64_t s = 0; s < max_len; ++s) {
     if (!mark(kClassEvolve, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_evolve(c->dg, c->S, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) !=
+    if ((e = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) !=
         cudaSuccess)
       return PBAG_ERR_CUDA;
     if (!mark(kClassEvolve, false)) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
-    if ((e = c->launch_radiation(d_prm, nbw, (int)s)) != cudaSuccess) return PBAG_ERR_CUDA;
+    if ((e = c->launch_radiation(gg, SS, d_prm, nbw, (int)s)) != cudaSuccess) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
     c->launches += c->ssc_on_tensor_cores() ? 3 : 2;
     if (s == max_len - 1) {
       if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
-      if ((e = launch_finalize(c->dg, c->S, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
+      if ((e = launch_finalize(gg, SS, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
         return PBAG_ERR_CUDA;
       if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
       c->launches += 1;
@@ -427,6 +484,30 @@ int run_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const int64
     st->site = site;
   }
   return code;
+}
+
+// The synchrotron / SSA sums run on the tensor cores when the grid and the
+// batch allow it (every blastwave of one synchrotron method class, the SSC
+// contraction on the tensor cores or off); a field outside the bank's range
+// reruns the batch with the CUDA-core sums. hprm: the shock parameters on the host.
+int run_device(pbag_ctx* c, const pbag_shock_params* hprm, const pbag_shock_params* d_prm, int nbw,
+               const int64_t* off_h, const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st) {
+  int cls = -1;
+  if (c->syn_tc_enabled() && nbw > 0) {
+    bool any_ssc = false;
+    cls = pbag_ctx::syn_class(hprm[0].syn_method);
+    for (int b = 0; b < nbw; ++b) {
+      any_ssc = any_ssc || hprm[b].ssc_on;
+      if (pbag_ctx::syn_class(hprm[b].syn_method) != cls) cls = -1;
+    }
+    if (cls >= 0 && any_ssc && !c->ssc_on_tensor_cores()) cls = -1;  // the CUDA-core SSC kernel sums both
+  }
+  pbag_status ls{};
+  int rc = run_device_once(c, d_prm, nbw, off_h, d_recs, d_out, &ls, cls);
+  if (cls >= 0 && rc == PBAG_ERR_UNSUPPORTED && ls.site == kSiteSynBank)
+    rc = run_device_once(c, d_prm, nbw, off_h, d_recs, d_out, &ls, -1);
+  if (st) *st = ls;
+  return rc;
 }
 
 void reset_status(pbag_status* st) {
@@ -599,6 +680,23 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     d.syn2_n = n2;
     // GSL: x = (h nu / m_e c^2) / (1.5 B gamma^2 / 4.14e13) against nu / nu_crit = nu 4 pi m_e c / (3 q B gamma^2)
     d.gsl_xs = (float)(cgs::h_by_mec2 * 4.14e13 / 1.5 / (4. * M_PI * cgs::m_e * cgs::c_light / (3. * cgs::q_e)));
+    // the tensor-core synchrotron sums (pbag_syn_tc.cu): the bank's geometry;
+    // the banks themselves are built on first use, per method class
+    if (syn_tc_supported(G, F)) {
+      const double xs = cgs::h_by_mec2 * 4.14e13 / 1.5 / (4. * M_PI * cgs::m_e * cgs::c_light / (3. * cgs::q_e));
+      c->sb_dnu = std::log(nu[1] / nu[0]);
+      syn_tc_geometry(c->sb_dnu, nu[0], xs, F, &c->sb);
+      d.sb_P = c->sb.P;
+      d.sb_M = c->sb.M;
+      d.sb_mlo = c->sb.mlo;
+      d.sb_nlo = c->sb.n_lo;
+      d.sb_nhi = c->sb.n_hi;
+      d.sb_ih = 1. / c->sb.h;
+      d.sb_lnnu0 = std::log(nu[0]);
+      d.sb_lnxs_gsl = std::log(xs);
+      d.sb_tbw = syn_tc_tile_bw(c->Gp);
+      c->sb_ok = true;
+    }
   }
   ok(c->grid_upload(&d.nu13, nu13));
   ok(c->grid_upload(&d.nu32, nu32));
@@ -727,7 +825,7 @@ int pbag_run_batch(pbag_ctx* c, const pbag_shock_params* prm, int nbw, const int
   if (nbw && cudaMemcpyAsync(c->d_prm, prm, nbw * sizeof(pbag_shock_params), cudaMemcpyHostToDevice, c->stream) !=
                  cudaSuccess)
     return PBAG_ERR_CUDA;
-  rc = run_device(c, c->d_prm, nbw, off, c->d_recs, dout, st);
+  rc = run_device(c, prm, c->d_prm, nbw, off, c->d_recs, dout, st);
   if (rc == PBAG_ERR_CUDA || rc == PBAG_ERR_NOMEM) return rc;
   // copy the histories back even on a physics error (rows before the failure are valid)
   for (int fi = 0; fi < kOutputs; ++fi) {
@@ -757,7 +855,7 @@ int pbag_run_batch_device(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, 
     if (st) st->code = rc;
     return rc;
   }
-  return run_device(c, d_prm, nbw, off, d_recs, *d_out, st);
+  return run_device(c, hp.data(), d_prm, nbw, off, d_recs, *d_out, st);
 }
 
 int64_t pbag_last_launch_count(const pbag_ctx* c) { return c ? c->launches : -1; }

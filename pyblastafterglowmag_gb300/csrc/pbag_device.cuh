@@ -22,6 +22,7 @@ constexpr int kKintStageMax = 112 * 1024;  // largest SSC kernel-integral table 
 constexpr int kScanMaxSub = 96;       // below this many substeps the solve is a parallel scan
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
 constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
+constexpr int kSiteSynBank = 900001;  // status site: a field outside the synchrotron bank's range
 
 // Read-only tables of one grid (one CommonTables entry), device pointers.
 // Products and reciprocals the reference recomputes every step are tabulated
@@ -79,6 +80,15 @@ struct DevGrid {
   int Tm;                // table stride: max(G, F)
   const float* tmant;    // [3][Tm]
   const int* texp;       // [3][Tm]
+  // synchrotron kernel bank of the tensor-core radiation sums (pbag_syn_tc.cu),
+  // for the method class of the running batch; null: CUDA-core sums
+  const uint16_t* synbank;  // [P][M/128] BF16 hi/lo operand slabs of 128 rows x Gp
+  int sb_P, sb_M, sb_mlo;   // sub-shifts, bank rows, index of the first row
+  int sb_tbw;               // blastwaves per weight tile (2 weight rows each)
+  int sb_nlo, sb_nhi;       // shift nodes the bank covers (s / h)
+  double sb_ih;             // 1 / h = P / dnu
+  double sb_lnnu0;          // ln nu_0
+  double sb_lnxs_gsl;       // ln of the GSL method's argument scale (gsl_xs)
 };
 enum : int { kM32De = 0, kM32DeIe2, kM32DnuNu, kM32 };
 
@@ -113,6 +123,7 @@ struct StepScal {
   int ia0, ia1;      // first branch of the analytic distribution: bins [ia0, ia1)
   int ib0, ib1;      // second branch: bins [ib0, ib1)
   int iq0, iq1;      // injection (source) bins [iq0, iq1)
+  double syn_shift;  // (ln nu_crit1(B) - ln nu_0 - ln xs) / h: the bank shift of the synchrotron kernel
 };
 
 enum : int {
@@ -140,6 +151,11 @@ struct DevState {
   double* scal;    // [nbw][kScal] per-step scalars handed between kernels
   int* flags;      // [nbw]      kFlag* bits
   int* err;        // [nbw][4]   first error: code, step index, check site, unused
+  // tensor-core radiation sums (null: CUDA-core sums): the synchrotron and SSA
+  // weights as BF16 hi/lo operand tiles of sb_tbw blastwaves (rows 2b: w,
+  // 2b+1: v), and the bank products D [tile][P][2 sb_tbw][sb_M]
+  uint16_t* Sbf;
+  float* Dsyn;
 };
 
 enum : int {
@@ -155,7 +171,7 @@ enum : int {
   kScalSv = 9,     // scale of v32
   kScalPref = 10,  // synchrotron prefactor of this step
   kScalB = 11,       // magnetic field of this step
-  // 12 unused
+  kScalSynShift = 12,  // bank shift s / h of the synchrotron kernel (tensor-core sums)
   kScalFac = 13,     // photon escape factor (dr/c)/vol (microphysics.h:517-518)
   kScalAccNe = 14,   // accel_frac / N_e
   kScalAnpNe = 15,   // accel_frac n' / N_e

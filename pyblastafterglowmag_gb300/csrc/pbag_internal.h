@@ -27,6 +27,9 @@ std::vector<float> syn_table(int method, double u0, double h, int n);
 // last point on.
 constexpr int kSynTab2N = 8192;
 std::vector<float> syn_table2(int method, double u0, double h, int n);
+// The synchrotron function R(x) of a method in FP64 (GSL: F(x); Bessel: the
+// K_4/3 K_1/3 form; CSYN and Dermer09: the Aharonian fit), x = nu / nu_crit.
+double syn_shape(int method, double x);
 
 }  // namespace pbag
 

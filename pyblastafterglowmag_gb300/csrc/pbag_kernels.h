@@ -26,6 +26,23 @@ cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* 
 // kernel attributes (dynamic shared memory limits); call once per device
 cudaError_t configure_kernels();
 
+// tensor-core synchrotron / SSA sums (pbag_syn_tc.cu): a bank of the
+// synchrotron kernel at kSynBankP sub-shifts of the frequency step, covering
+// fields B in [kSynBankBmin, kSynBankBmax] G
+constexpr int kSynBankP = 8;
+constexpr double kSynBankBmin = 1e-12, kSynBankBmax = 1e12;
+struct SynBankGeom {
+  int P, M, mlo, n_lo, n_hi;
+  double h;
+};
+bool syn_tc_supported(int G, int F);
+int syn_tc_tile_bw(int Gp);
+void syn_tc_geometry(double dnu, double nu0, double xs_gsl, int F, SynBankGeom* g);
+// the bank of one synchrotron method (bins j < jc left out: CSYN's cyclotron bins)
+void build_syn_bank(int method, int jc, const double* gam, int G, int Gp, double dnu, const SynBankGeom& sg,
+                    std::vector<uint16_t>& out);
+cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st);
+
 // tensor-core SSC contraction (pbag_ssc_tc.cu), for F = 128 or 256
 bool ssc_tc_supported(int F);
 void build_ssc_tc_operand(const std::vector<float>& K32, int F, int Gp, std::vector<uint16_t>& Bt);

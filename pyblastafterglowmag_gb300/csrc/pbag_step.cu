@@ -201,10 +201,22 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   s.inv_ncrit = (float)((4. * M_PI * m_e * c_light) / (3. * q_e * B));
   s.inv_nlar = (float)((2. * pi_ * m_e * c_light) / (3. * q_e * B));
   s.dr = q.dr;
+  // the shift of the blastwave's synchrotron kernel against the tensor-core
+  // bank: ln x = k dnu - s - 2 j dlng, s = ln nu_crit1(B) - ln nu_0 - ln xs
+  bool bank_oor = false;
+  if (g.synbank && B > 0) {
+    const double lxs = P.syn_method == PBAG_SYN_GSL ? g.sb_lnxs_gsl : 0.;
+    s.syn_shift = (log((3. * q_e * B) / (4. * M_PI * m_e * c_light)) - g.sb_lnnu0 - lxs) * g.sb_ih;
+    const double n = floor(s.syn_shift);
+    bank_oor = !(n - 1. >= (double)g.sb_nlo && n + 2. <= (double)g.sb_nhi);
+  }
   if (init) {
     s.vol = q.m_p1 / q.rho_p1;
     s.fac = s.dr / c_light / s.vol;
-    if (pl_bad) {
+    if (bank_oor) {  // field outside the bank: the caller reruns the batch on CUDA cores
+      s.err = PBAG_ERR_UNSUPPORTED;
+      s.site = kSiteSynBank;
+    } else if (pl_bad) {
       s.err = PBAG_ERR_NONFINITE;
       s.site = __LINE__;
     } else if (B < 0) {  // evalSynKernel (kernels.h:529-532)
@@ -224,6 +236,12 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
   if (pl_bad) {
     s.err = PBAG_ERR_NONFINITE;
     s.site = __LINE__;
+    out[r] = s;
+    return;
+  }
+  if (bank_oor) {
+    s.err = PBAG_ERR_UNSUPPORTED;
+    s.site = kSiteSynBank;
     out[r] = s;
     return;
   }
@@ -972,10 +990,23 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     Wexp = max(Wexp, red_i[2][v]);
   }
   float* w32 = S.w32 + (size_t)b * G;
+  // weight rows of the tensor-core synchrotron sums: row 2 (b mod tbw) of
+  // tile b / tbw, BF16 hi + lo (pbag_syn_tc.cu)
+  uint16_t* Sb = S.Sbf ? S.Sbf + (size_t)(b / g.sb_tbw) * tc_tile_elems(2 * g.sb_tbw, g.Gp) : nullptr;
+  const int srow = 2 * (b % max(g.sb_tbw, 1));
 #pragma unroll
   for (int k = 0; k < C; ++k) {
     const int i = tid + k * kStepThreads;
-    if (i < G) w32[i] = f32_scaled(wk[k], wexp);  // wk = 0 for the last bin
+    if (i < G) {
+      const float w = f32_scaled(wk[k], wexp);  // wk = 0 for the last bin
+      w32[i] = w;
+      if (Sb) {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+        Sb[tc_operand_offset(srow, i, 2 * g.sb_tbw, g.Gp, false)] = __bfloat16_as_ushort(hi);
+        Sb[tc_operand_offset(srow, i, 2 * g.sb_tbw, g.Gp, true)] =
+            __bfloat16_as_ushort(__float2bfloat16_rn(w - __bfloat162float(hi)));
+      }
+    }
   }
   // SSC electron weights W_j = f_j (e_{j+1}-e_j) 3/4 sigma_T c / e_j^2 (numeric_model.h:271-277)
   // (FP32 for the CUDA-core contraction, BF16 hi + lo tiles for the tensor cores)
@@ -1034,7 +1065,16 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 #pragma unroll
     for (int v = 0; v < kStepWarps; ++v) vexp = max(vexp, red_i[0][v]);
     float* v32 = S.v32 + (size_t)b * G;
-    for (int i = tid; i < G; i += kStepThreads) v32[i] = i < G - 1 ? f32_scaled(sh_vd[i], vexp) : 0.f;
+    for (int i = tid; i < G; i += kStepThreads) {
+      const float v = i < G - 1 ? f32_scaled(sh_vd[i], vexp) : 0.f;
+      v32[i] = v;
+      if (Sb) {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+        Sb[tc_operand_offset(srow + 1, i, 2 * g.sb_tbw, g.Gp, false)] = __bfloat16_as_ushort(hi);
+        Sb[tc_operand_offset(srow + 1, i, 2 * g.sb_tbw, g.Gp, true)] =
+            __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(hi)));
+      }
+    }
   }
   if (!positive(ne) && !is_nan(ne)) PBAG_FAIL(PBAG_ERR_NELE, __LINE__);  // n_ele <= 0 (microphysics.h:560-563)
   if (tid == 0) {
@@ -1051,6 +1091,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     scal[kScalSv] = unscale_from_exp(vexp);
     scal[kScalPref] = sc.pref;
     scal[kScalB] = B;
+    scal[kScalSynShift] = sc.syn_shift;
     float* rp = S.rad32 + (size_t)b * 4;
     rp[0] = sc.inv_ncrit;
     rp[1] = sc.inv_nlar;
@@ -1297,13 +1338,61 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
   float s32[FQ];
   float2 a32[FQ];
   double cs[FQ];
+  if (S.Dsyn) {
+    // tensor-core sums: cubic interpolation over the four bank nodes around the
+    // blastwave's shift (pbag_syn_tc.cu), then CSYN's cyclotron bins on CUDA cores
+    const double shd = scal[kScalSynShift];
+    const double fl = floor(shd);
+    const int n = (int)fl;
+    const float r = (float)(shd - fl);
+    const float L[4] = {-r * (r - 1.f) * (r - 2.f) * (1.f / 6.f), (r + 1.f) * (r - 1.f) * (r - 2.f) * 0.5f,
+                        -(r + 1.f) * r * (r - 2.f) * 0.5f, (r + 1.f) * r * (r - 1.f) * (1.f / 6.f)};
+    const int tbw = g.sb_tbw, M = g.sb_M, Pb = g.sb_P;
+    const float* Dt = S.Dsyn + ((size_t)(b / tbw) * Pb * 2 * tbw + 2 * (b % tbw)) * M;
+    int base[4];
 #pragma unroll
-  for (int q = 0; q < FQ; ++q) {
-    const int k = tid + q * kStepThreads;
-    const bool in = k < F;
-    s32[q] = in ? syn32[k] : 0.f;
-    a32[q] = (in && P.ssa_on) ? ssa32[k] : make_float2(0.f, 0.f);
-    cs[q] = (in && ssc) ? jssc[k] : 0.;
+    for (int a = 0; a < 4; ++a) {
+      const int na = n - 1 + a;
+      const int qa = na >= 0 ? na / Pb : -((-na + Pb - 1) / Pb);
+      base[a] = (na - qa * Pb) * 2 * tbw * M - qa - g.sb_mlo;  // + k: the row of output k
+    }
+    const bool cyc = P.syn_method == PBAG_SYN_CSYN && g.n_cyc > 0;
+    const float inlar = S.rad32[(size_t)b * 4 + 1];
+    const float* wv = S.w32 + (size_t)b * g.G;
+    const float* vv = S.v32 + (size_t)b * g.G;
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+      const int k = tid + q * kStepThreads;
+      float sj = 0.f, sa = 0.f;
+      if (k < F) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float* d = Dt + base[a] + k;
+          sj = fmaf(L[a], d[0], sj);
+          if (P.ssa_on) sa = fmaf(L[a], d[M], sa);
+        }
+        if (cyc) {
+          const float xl = g.nu32[k] * inlar;
+          for (int j = 0; j < g.n_cyc; ++j) {
+            const float R_ = cyclotron_R32(g.psq32[j], xl);
+            sj = fmaf(R_, wv[j], sj);
+            if (P.ssa_on) sa = fmaf(R_, vv[j], sa);
+          }
+        }
+      }
+      s32[q] = sj;
+      a32[q] = make_float2(sa, 0.f);
+      cs[q] = (k < F && ssc) ? jssc[k] : 0.;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < FQ; ++q) {
+      const int k = tid + q * kStepThreads;
+      const bool in = k < F;
+      s32[q] = in ? syn32[k] : 0.f;
+      a32[q] = (in && P.ssa_on) ? ssa32[k] : make_float2(0.f, 0.f);
+      cs[q] = (in && ssc) ? jssc[k] : 0.;
+    }
   }
   // synchrotron emissivity and SSA absorption from the FP32 sums
   // (numeric_model.h:148-238): the prefactor and the power-of-two scales

@@ -97,6 +97,11 @@ double synchrotron_aharonian(double x) {
 
 }  // namespace
 
+double syn_shape(int method, double x) {
+  return method == PBAG_SYN_GSL ? synchrotron_F(x) : method == PBAG_SYN_BESSEL ? synchrotron_bessel(x)
+                                                                               : synchrotron_aharonian(x);
+}
+
 void syn_table_grid(double dlng, double* u0, double* h, int* n, int nmax) {
   // spacing: the step of ln(1/gamma^2) between neighbouring electron bins is
   // m spacings, m odd, so that the lanes of a warp (consecutive bins) read

@@ -156,3 +156,32 @@ def test_unsupported_options_rejected(lib, cuda_device):
     with pytest.raises(PbagError) as ei:
         ctx.run(recs, off, p)
     assert ei.value.code == abi.PBAG_ERR_ARG
+
+
+@pytest.mark.parametrize("method", [abi.PBAG_SYN_CSYN, abi.PBAG_SYN_DER09, abi.PBAG_SYN_GSL, abi.PBAG_SYN_BESSEL])
+def test_tensor_core_synchrotron_sums_match_cuda_core_sums(lib, cuda_device, monkeypatch, method):
+    """The synchrotron and SSA sums as a GEMM against the shifted kernel bank
+    (tensor cores, split BF16) against the CUDA-core sums on the same batch:
+    the synchrotron and SSA histories agree to far below the plain-path bar."""
+    recs, off, prm, grid = cases.tophat(lib, nsteps=120, ssa=True, syn_method=method)
+    outs = ("syn_j_all", "syn_a_all", "j_all", "a_all")
+    ctx = Context(grid, device=0, ssc=False)
+    tc = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    monkeypatch.setenv("PBAG_SYN_TC", "0")
+    ctx = Context(grid, device=0, ssc=False)
+    cc = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    for k in outs:
+        rel, zm = rel_l2_rows(tc[k], cc[k])
+        assert zm == 0 and rel.max() <= 2e-5, (k, rel.max())
+
+
+def test_field_outside_synchrotron_bank_falls_back(lib, oracle, cuda_device):
+    """A magnetic field outside the range the tensor-core bank covers
+    (1e-12..1e12 G) sends the whole batch to the CUDA-core sums; the result
+    still matches the oracle."""
+    recs, off, prm, grid = cases.tophat(lib, nsteps=40, ssa=True)
+    recs = recs.copy()
+    recs["B"][20:] *= 1e-14
+    _compare(lib, oracle, (recs, off, prm, grid), outputs=cases.TOTALS)
