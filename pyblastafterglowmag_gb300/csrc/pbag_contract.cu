@@ -98,6 +98,10 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
   double* scal = S.scal + (size_t)s * kScal;
   if (want_syn) {
     float* w32 = S.w32 + (size_t)s * G;
+    // the tensor-core synchrotron sums (pbag_syn_tc.cu): one BF16 hi / lo
+    // weight row per state, tiles of 2 sb_tbw states
+    const int tb1 = 2 * g.sb_tbw;
+    uint16_t* Sb = S.Sbf ? S.Sbf + (size_t)(s / tb1) * tc_tile_elems(tb1, g.Gp) : nullptr;
 #pragma unroll
     for (int q = 0; q < WPL; ++q) {
       const int j = lane + 32 * q;
@@ -108,6 +112,12 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
           w = f32_ldexp(mant_mul(mf[q], __ldg(m_de + j), e), e - wexp);
         }
         w32[j] = w;
+        if (Sb) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+          Sb[tc_operand_offset(s % tb1, j, tb1, g.Gp, false)] = __bfloat16_as_ushort(hi);
+          Sb[tc_operand_offset(s % tb1, j, tb1, g.Gp, true)] =
+              __bfloat16_as_ushort(__float2bfloat16_rn(w - __bfloat162float(hi)));
+        }
       }
     }
   }
@@ -202,6 +212,16 @@ k_contract_prep(DevGrid g, int n, const double* __restrict__ f, const double* __
     rp[3] = 0.f;
     S.flags[s] = kFlagActive;
     for (int q = 0; q < 4; ++q) S.err[4 * s + q] = 0;
+    if (want_syn && S.Sbf) {  // the state's shift against the synchrotron bank
+      const double lxs = syn_method == PBAG_SYN_GSL ? g.sb_lnxs_gsl : 0.;
+      const double sh = (log((3. * q_e * B) / (4. * M_PI * m_e * c_light)) - g.sb_lnnu0 - lxs) * g.sb_ih;
+      scal[kScalSynShift] = sh;
+      const double nn = floor(sh);
+      if (!(B > 0) || !(nn - 1. >= (double)g.sb_nlo && nn + 2. <= (double)g.sb_nhi)) {
+        S.err[4 * s] = PBAG_ERR_UNSUPPORTED;
+        S.err[4 * s + 2] = kSiteSynBank;
+      }
+    }
     pbag_shock_params p{};
     p.syn_method = syn_method;
     p.ssc_on = want_ssc;
@@ -326,12 +346,37 @@ cudaError_t launch_syn_batch(const DevGrid& g, const DevState& S, int n, int met
 
 // j_syn from the FP32 sums: prefactor and scale (numeric_model.h:148-184);
 // j_syn[F-1] = 0. A negative or non-finite value is the reference's exit.
-__global__ void k_contract_syn_out(int n, int F, DevState S, double* __restrict__ jsyn) {
+// With the tensor-core sums (S.Dsyn): the cubic interpolation over the
+// state's four bank nodes (pbag_syn_tc.cu) plus CSYN's cyclotron bins.
+__global__ void k_contract_syn_out(int n, int F, DevGrid g, DevState S, int syn_method, double* __restrict__ jsyn) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)n * F) return;
   const int s = (int)(idx / F), k = (int)(idx - (int64_t)s * F);
   const double* scal = S.scal + (size_t)s * kScal;
-  const double js = k < F - 1 ? scal[kScalPref] * ((double)S.syn32[idx] * scal[kScalSw]) : 0.;
+  float sum;
+  if (S.Dsyn) {
+    const double shd = scal[kScalSynShift];
+    const double fl = floor(shd);
+    const int nn = (int)fl;
+    float L[4], d[4];
+    bank_weights((float)(shd - fl), L);
+    const int tb1 = 2 * g.sb_tbw, M = g.sb_M, Pb = g.sb_P;
+    const float* Dt = S.Dsyn + ((size_t)(s / tb1) * Pb * tb1 + s % tb1) * M;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int na = nn - 1 + a;
+      const int qa = na >= 0 ? na / Pb : -((-na + Pb - 1) / Pb);
+      d[a] = Dt[(size_t)(na - qa * Pb) * tb1 * M + k - qa - g.sb_mlo];
+    }
+    sum = fmaxf(bank_interp(L, d), 0.f);
+    if (syn_method == PBAG_SYN_CSYN) {
+      const float xl = g.nu32[k] * S.rad32[(size_t)s * 4 + 1];
+      for (int j = 0; j < g.n_cyc; ++j) sum = fmaf(cyclotron_R32(g.psq32[j], xl), S.w32[(size_t)s * g.G + j], sum);
+    }
+  } else {
+    sum = S.syn32[idx];
+  }
+  const double js = k < F - 1 ? scal[kScalPref] * ((double)sum * scal[kScalSw]) : 0.;
   jsyn[idx] = js;
   if (bad_value(js) && atomicCAS(&S.err[4 * s], 0, PBAG_ERR_NONFINITE) == 0) S.err[4 * s + 2] = __LINE__;
 }
@@ -379,6 +424,7 @@ struct ContractWs : CtxExtension {
     if (n <= cap && mode == cap_mode) return cudaSuccess;
     for (void* p : mem) cudaFree(p);
     mem.clear();
+    S = DevState{};
     cap = 0;
     const size_t c = (size_t)std::max(n, 64);
     const size_t rows = (c + kTcCols - 1) / kTcCols * kTcCols;  // whole tensor-core tiles
@@ -399,6 +445,13 @@ struct ContractWs : CtxExtension {
     const size_t wt = rows / kTcCols * tc_tile_bytes(kTcCols, v.Gp, mode == kTcTf32 ? 4 : 2);
     if ((e = take(&Wt, wt)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(Wt, 0, wt, v.stream)) != cudaSuccess) return e;
+    if (v.dg.sb_tbw > 0) {  // the tensor-core synchrotron sums: one weight row per state
+      const int tb1 = 2 * v.dg.sb_tbw;
+      const size_t tiles = (c + tb1 - 1) / tb1;
+      if ((e = take(&S.Sbf, tiles * tc_tile_elems(tb1, v.Gp))) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(S.Sbf, 0, tiles * tc_tile_elems(tb1, v.Gp) * 2, v.stream)) != cudaSuccess) return e;
+      if ((e = take(&S.Dsyn, tiles * (size_t)v.dg.sb_P * tb1 * v.dg.sb_M)) != cudaSuccess) return e;
+    }
     cap = (int)c;
     cap_mode = mode;
     return cudaSuccess;
@@ -431,8 +484,25 @@ int contract_prepare(pbag_ctx* ctx, const CtxView& v, int n, const double* d_f, 
 }
 }  // namespace pbag
 
+namespace {
+int contract_run(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph, int syn_method,
+                 int precision, double* d_jsyn, double* d_jssc, pbag_status* st, bool bank_ok);
+}
+
 extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph,
                              int syn_method, int precision, double* d_jsyn, double* d_jssc, pbag_status* st) {
+  pbag_status ls{};
+  int rc = contract_run(ctx, n, d_f, d_B, d_nph, syn_method, precision, d_jsyn, d_jssc, &ls, true);
+  // a field outside the synchrotron bank's range: the CUDA-core sums instead
+  if (rc == PBAG_ERR_UNSUPPORTED && ls.site == kSiteSynBank)
+    rc = contract_run(ctx, n, d_f, d_B, d_nph, syn_method, precision, d_jsyn, d_jssc, &ls, false);
+  if (st) *st = ls;
+  return rc;
+}
+
+namespace {
+int contract_run(pbag_ctx* ctx, int n, const double* d_f, const double* d_B, const double* d_nph, int syn_method,
+                 int precision, double* d_jsyn, double* d_jssc, pbag_status* st, bool bank_ok) {
   if (st) {
     st->code = PBAG_ERR_ARG;
     st->bw = st->step = -1;
@@ -476,12 +546,22 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   auto ok = [&](cudaError_t x) {
     if (e == cudaSuccess) e = x;
   };
-  launch_prep(v.dg.Gp, (n + kPrepWarps - 1) / kPrepWarps, s, v.dg, n, d_f, d_B, d_nph, syn_method, mode,
+  // synchrotron sums of large batches on the tensor cores when the grid allows
+  const bool fp32_ssc = d_jssc && !tc;
+  DevGrid gg = v.dg;
+  const bool bank = bank_ok && d_jsyn && !fp32_ssc && n >= kSynBatchMin && S.Sbf &&
+                    ctx_syn_bank(ctx, syn_method, &gg);
+  if (!bank) {
+    S.Sbf = nullptr;
+    S.Dsyn = nullptr;
+  }
+  launch_prep(v.dg.Gp, (n + kPrepWarps - 1) / kPrepWarps, s, gg, n, d_f, d_B, d_nph, syn_method, mode,
               d_jsyn ? 1 : 0, d_jssc ? 1 : 0, S, tc && d_jssc ? ws->Wt : (unsigned char*)nullptr, ws->prm);
   ok(cudaGetLastError());
   // synchrotron sums (and the CUDA-core SSC contraction in FP32)
-  const bool fp32_ssc = d_jssc && !tc;
-  if (d_jsyn && !fp32_ssc && n >= kSynBatchMin)
+  if (bank)
+    ok(launch_syn_tc(gg, S, n, s, 1));  // the bank GEMM, interpolated in k_contract_syn_out
+  else if (d_jsyn && !fp32_ssc && n >= kSynBatchMin)
     ok(launch_syn_batch(v.dg, S, n, syn_method, s));  // large batches: the tabulated function
   else if (d_jsyn || fp32_ssc)
     ok(launch_rad_ssc(v.dg, S, ws->prm, n, fp32_ssc, 0, s));
@@ -490,7 +570,7 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
                           S.flags, S.U32, S.scal, v.dg.hnu, v.F, v.F, d_jssc, S.err, s));
   if (d_jsyn) {
     const int64_t tot = (int64_t)n * v.F;
-    k_contract_syn_out<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, v.F, S, d_jsyn);
+    k_contract_syn_out<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, v.F, gg, S, syn_method, d_jsyn);
     ok(cudaGetLastError());
   }
   ok(cudaMemsetAsync(ws->fail + 3, 0x7f, sizeof(int), s));  // 0x7f7f7f7f: above any state index
@@ -509,3 +589,4 @@ extern "C" int pbag_contract(pbag_ctx* ctx, int n, const double* d_f, const doub
   }
   return fail[0];
 }
+}  // namespace

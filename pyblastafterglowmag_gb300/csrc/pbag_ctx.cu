@@ -131,9 +131,19 @@ struct pbag_ctx {
   SynBankGeom sb{};
   double sb_lnnu0 = 0., sb_lnxs = 0., sb_dnu = 0.;
   const uint16_t* sb_bank[4] = {};
-  bool syn_tc_enabled() const {
+  // PBAG_SYN_TC=0: always the CUDA-core sums; =1: the tensor-core sums
+  // whenever the grid allows; unset: the tensor-core sums for batches of at
+  // least kSynTcMinBw blastwaves. A small batch's CUDA-core sums run next to
+  // the SSC contraction and cost the step nothing, while the bank's
+  // interpolation lengthens the step completion on the critical path; a large
+  // batch's CUDA-core sums are issue-bound and the GEMM wins (measured: 42
+  // blastwaves 1.25 M -> 1.10 M blastwave-steps/s, 2 370 blastwaves 3.43 M ->
+  // 3.98 M).
+  static constexpr int kSynTcMinBw = 128;
+  bool syn_tc_enabled(int nbw = 1 << 30) const {
     const char* v = std::getenv("PBAG_SYN_TC");
-    return sb_ok && !(v && v[0] == '0');
+    if (!sb_ok || (v && v[0] == '0')) return false;
+    return (v && v[0] == '1') || nbw >= kSynTcMinBw;
   }
   // bank of the method class of syn_method: CSYN (cyclotron bins apart), Dermer09, GSL, Bessel
   static int syn_class(int syn_method) {
@@ -493,7 +503,7 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
 int run_device(pbag_ctx* c, const pbag_shock_params* hprm, const pbag_shock_params* d_prm, int nbw,
                const int64_t* off_h, const pbag_step_rec* d_recs, const pbag_outputs& d_out, pbag_status* st) {
   int cls = -1;
-  if (c->syn_tc_enabled() && nbw > 0) {
+  if (c->syn_tc_enabled(nbw) && nbw > 0) {
     bool any_ssc = false;
     cls = pbag_ctx::syn_class(hprm[0].syn_method);
     for (int b = 0; b < nbw; ++b) {
@@ -902,6 +912,11 @@ void ctx_set_extension(pbag_ctx* c, int slot, CtxExtension* x) {
 
 void ctx_set_launches(pbag_ctx* c, int64_t n) {
   if (c) c->launches = n;
+}
+
+bool ctx_syn_bank(pbag_ctx* c, int syn_method, DevGrid* g) {
+  if (!c || !g || !c->syn_tc_enabled()) return false;
+  return c->syn_bank(pbag_ctx::syn_class(syn_method), &g->synbank) == cudaSuccess;
 }
 
 bool ctx_view(const pbag_ctx* c, CtxView* v) {

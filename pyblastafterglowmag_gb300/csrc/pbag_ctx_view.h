@@ -21,6 +21,9 @@ struct CtxView {
 bool ctx_view(const pbag_ctx* c, CtxView* v);
 // The kernel count pbag_last_launch_count reports for c's last run.
 void ctx_set_launches(pbag_ctx* c, int64_t n);
+// The tensor-core synchrotron bank of syn_method into g->synbank (built on
+// first use); false when the context's grid or the environment rules it out.
+bool ctx_syn_bank(pbag_ctx* c, int syn_method, DevGrid* g);
 
 // A per-context workspace owned by an entry point of another translation
 // unit: created on first use, destroyed with the context.

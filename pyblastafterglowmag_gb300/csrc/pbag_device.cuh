@@ -328,6 +328,34 @@ __device__ __forceinline__ double unscale_from_exp(int E) {
   return (E <= 26 || E >= 2019) ? 1. : __hiloint2double((E + 1) << 20, 0);
 }
 
+// ---- the synchrotron kernel bank's interpolation (pbag_syn_tc.cu) ---------
+// Cubic Lagrange weights at the nodes -1, 0, 1, 2 for 0 <= r < 1.
+__device__ __forceinline__ void bank_weights(float r, float (&L)[4]) {
+  L[0] = -r * (r - 1.f) * (r - 2.f) * (1.f / 6.f);
+  L[1] = (r + 1.f) * (r - 1.f) * (r - 2.f) * 0.5f;
+  L[2] = -(r + 1.f) * r * (r - 2.f) * 0.5f;
+  L[3] = (r + 1.f) * r * (r - 1.f) * (1.f / 6.f);
+}
+// The interpolated sum from the four node values d: in log space when all
+// four have one sign (exact on the exponential tails of the synchrotron
+// function, where neighbouring nodes differ by orders of magnitude and a
+// linear-space cubic would swing negative), else in linear space.
+__device__ __forceinline__ float bank_interp(const float (&L)[4], const float (&d)[4]) {
+  const bool pos = d[0] > 0.f && d[1] > 0.f && d[2] > 0.f && d[3] > 0.f;
+  const bool neg = d[0] < 0.f && d[1] < 0.f && d[2] < 0.f && d[3] < 0.f;
+  if (pos || neg) {
+    float lg = 0.f;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) lg = fmaf(L[a], logf(fabsf(d[a])), lg);
+    const float v = expf(lg);
+    return pos ? v : -v;
+  }
+  float v = 0.f;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) v = fmaf(L[a], d[a], v);
+  return v;
+}
+
 // ---- synchrotron kernel functions in FP32 (kernels.h) ---------------------
 // All return the dimensionless shape R; the caller multiplies by the FP64
 // prefactor sqrt(3) q^3 B / (m_e c^2) of kernels.h:427,434,471.

@@ -41,7 +41,9 @@ void syn_tc_geometry(double dnu, double nu0, double xs_gsl, int F, SynBankGeom* 
 // the bank of one synchrotron method (bins j < jc left out: CSYN's cyclotron bins)
 void build_syn_bank(int method, int jc, const double* gam, int G, int Gp, double dnu, const SynBankGeom& sg,
                     std::vector<uint16_t>& out);
-cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st);
+// rpb: weight rows per blastwave (2: synchrotron and SSA weights, the step's
+// tiles of sb_tbw blastwaves; 1: synchrotron only, tiles of 2 sb_tbw states)
+cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st, int rpb = 2);
 
 // tensor-core SSC contraction (pbag_ssc_tc.cu), for F = 128 or 256
 bool ssc_tc_supported(int F);

@@ -613,8 +613,8 @@ inline int evolve_kint_stage(const DevGrid& g, int nbw) {
 // Every global load that does not depend on another is issued at the start
 // (grid tables by one bulk copy into shared memory, the blastwave's state into
 // registers), so that the step pays few dependent memory round trips.
-template <int C, int FQ>
-__global__ void __launch_bounds__(kStepThreads, 1)
+template <int C, int FQ, int MINB>
+__global__ void __launch_bounds__(kStepThreads, MINB)
 k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const StepScal* __restrict__ ss,
          const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm, int step, pbag_outputs out,
          int kstage) {
@@ -1344,9 +1344,8 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
     const double shd = scal[kScalSynShift];
     const double fl = floor(shd);
     const int n = (int)fl;
-    const float r = (float)(shd - fl);
-    const float L[4] = {-r * (r - 1.f) * (r - 2.f) * (1.f / 6.f), (r + 1.f) * (r - 1.f) * (r - 2.f) * 0.5f,
-                        -(r + 1.f) * r * (r - 2.f) * 0.5f, (r + 1.f) * r * (r - 1.f) * (1.f / 6.f)};
+    float L[4];
+    bank_weights((float)(shd - fl), L);
     const int tbw = g.sb_tbw, M = g.sb_M, Pb = g.sb_P;
     const float* Dt = S.Dsyn + ((size_t)(b / tbw) * Pb * 2 * tbw + 2 * (b % tbw)) * M;
     int base[4];
@@ -1365,12 +1364,15 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
       const int k = tid + q * kStepThreads;
       float sj = 0.f, sa = 0.f;
       if (k < F) {
+        float dj[4], da[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
           const float* d = Dt + base[a] + k;
-          sj = fmaf(L[a], d[0], sj);
-          if (P.ssa_on) sa = fmaf(L[a], d[M], sa);
+          dj[a] = d[0];
+          da[a] = P.ssa_on ? d[M] : 0.f;
         }
+        sj = fmaxf(bank_interp(L, dj), 0.f);  // every synchrotron term is non-negative
+        if (P.ssa_on) sa = bank_interp(L, da);
         if (cyc) {
           const float xl = g.nu32[k] * inlar;
           for (int j = 0; j < g.n_cyc; ++j) {
@@ -1617,11 +1619,21 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
   const int c = (g.G + kStepThreads - 1) / kStepThreads;
   const int fq = (g.F + kStepThreads - 1) / kStepThreads;
   auto go = [&](auto kern) { kern<<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out, kstage); };
+  // large batches (the kernel-integral table not staged, small shared
+  // memory): the register budget of four CTAs per SM, for more resident
+  // blastwaves (no spills at 128 registers for grids up to 256 x 256)
+  if (kstage == 0 && nbw > kStageMaxBw && c <= 2 && fq <= 2) {
+    if (c <= 1)
+      fq <= 1 ? go(k_evolve<1, 1, 4>) : go(k_evolve<1, 2, 4>);
+    else
+      fq <= 1 ? go(k_evolve<2, 1, 4>) : go(k_evolve<2, 2, 4>);
+    return cudaGetLastError();
+  }
 #define PBAG_EVOLVE_FQ(CC)                 \
-  if (fq <= 1) go(k_evolve<CC, 1>);        \
-  else if (fq <= 2) go(k_evolve<CC, 2>);   \
-  else if (fq <= 4) go(k_evolve<CC, 4>);   \
-  else go(k_evolve<CC, 8>);
+  if (fq <= 1) go(k_evolve<CC, 1, 1>);     \
+  else if (fq <= 2) go(k_evolve<CC, 2, 1>); \
+  else if (fq <= 4) go(k_evolve<CC, 4, 1>); \
+  else go(k_evolve<CC, 8, 1>);
   if (c <= 1) {
     PBAG_EVOLVE_FQ(1)
   } else if (c <= 2) {
@@ -1679,15 +1691,19 @@ cudaError_t configure_kernels() {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   };
 #define PBAG_EVOLVE_ATTR(CC)                                   \
-  attr((const void*)k_evolve<CC, 1>, esmem);                   \
-  attr((const void*)k_evolve<CC, 2>, esmem);                   \
-  attr((const void*)k_evolve<CC, 4>, esmem);                   \
-  attr((const void*)k_evolve<CC, 8>, esmem);
+  attr((const void*)k_evolve<CC, 1, 1>, esmem);                \
+  attr((const void*)k_evolve<CC, 2, 1>, esmem);                \
+  attr((const void*)k_evolve<CC, 4, 1>, esmem);                \
+  attr((const void*)k_evolve<CC, 8, 1>, esmem);
   PBAG_EVOLVE_ATTR(1)
   PBAG_EVOLVE_ATTR(2)
   PBAG_EVOLVE_ATTR(4)
   PBAG_EVOLVE_ATTR(8)
 #undef PBAG_EVOLVE_ATTR
+  attr((const void*)k_evolve<1, 1, 4>, esmem);
+  attr((const void*)k_evolve<1, 2, 4>, esmem);
+  attr((const void*)k_evolve<2, 1, 4>, esmem);
+  attr((const void*)k_evolve<2, 2, 4>, esmem);
   attr((const void*)k_rad_ssc<1>, smem);
   attr((const void*)k_rad_ssc<2>, smem);
   attr((const void*)k_rad_ssc<4>, smem);

@@ -12,13 +12,18 @@
 // covers every s: with s / h = n + r (n integer, 0 <= r < 1), node n_a =
 // n - 1 + a (a = 0..3) is q_a P + p_a, i.e. the shift q_a dnu + p_a h, whose
 // kernel row for output k is row k - q_a of K_{p_a}. The blastwave's kernel
-// is the cubic Lagrange interpolation over the four nodes, so
-//   sum_j K[k][j] w_j = pref sum_a L_a(r) D_{p_a}[k - q_a],   D_p = K_p w,
-// where D_p is a plain GEMM of the fixed bank against the weights of every
-// blastwave (N = 2 per blastwave: the synchrotron weights w and the SSA
-// weights v). Interpolation error ~1e-7 with P = 8; split-BF16 operands with
-// FP32 accumulation add ~3e-6 (synchrotron) and ~7e-6 (SSA, signed terms)
-// relative L2. CSYN's cyclotron bins (gamma <= 2) depend on nu / nu_Larmor
+// is the cubic Lagrange interpolation over the four nodes, taken on the node
+// sums D_p = K_p w (a plain GEMM of the fixed bank against the weights of
+// every blastwave; N = 2 per blastwave: the synchrotron weights w and the SSA
+// weights v):
+//   sum_j K[k][j] w_j = pref interp_a(L_a(r), D_{p_a}[k - q_a]).
+// The interpolation runs in log space where the four node values share a
+// sign: on the exponential tail of the synchrotron function neighbouring
+// nodes differ by orders of magnitude and a linear-space cubic swings
+// negative there, while the log-space one stays within ~1e-5 of every entry
+// (per-entry relative error, down to entries 1e-30 below the row's largest).
+// Interpolation error ~1e-7 relative L2 with P = 8; split-BF16 operands with
+// FP32 accumulation add ~3e-6 (synchrotron) and ~7e-6 (SSA, signed terms). CSYN's cyclotron bins (gamma <= 2) depend on nu / nu_Larmor
 // and gamma separately: they stay out of the bank (zero columns) and the step
 // completion adds them on CUDA cores.
 //
@@ -72,10 +77,17 @@ float bf16_value_host(uint16_t h) {
 
 __device__ __forceinline__ size_t slab_bytes(int Gp) { return (size_t)2 * 128 * Gp * 2; }
 
+__device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// rpb: weight rows per blastwave (2: synchrotron and SSA, 1: synchrotron
+// only); tbw blastwaves per stored tile of rpb tbw rows. scal: the per-
+// blastwave scalars (the bank shift at kScalSynShift), F: outputs per
+// blastwave, mlo: index of the bank's first row.
 template <bool kSplit>
 __global__ void __launch_bounds__(kSbThreads, 1)
 k_syn_tc(const unsigned char* __restrict__ bank, const unsigned char* __restrict__ Sbf, int Gp, int nbw, int tbw,
-         int Mt, int P, const int* __restrict__ flags, float* __restrict__ D, int* __restrict__ err) {
+         int rpb, int Mt, int P, int F, int mlo, const int* __restrict__ flags, const double* __restrict__ scal,
+         float* __restrict__ D, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint64_t bars[2];  // copies, MMAs
   __shared__ uint32_t tmem_slot;
@@ -83,12 +95,19 @@ k_syn_tc(const unsigned char* __restrict__ bank, const unsigned char* __restrict
   const int tid = threadIdx.x, warp = tid >> 5;
   const int p = blockIdx.x / Mt, mt = blockIdx.x % Mt, tile = blockIdx.y;
   const int b0 = tile * tbw, nb = min(tbw, nbw - b0);
-  const int rows_tile = 2 * tbw;            // weight rows of a stored tile
-  const int N = (2 * nb + 15) / 16 * 16;    // weight rows this CTA multiplies
+  const int rows_tile = rpb * tbw;          // weight rows of a stored tile
+  const int N = (rpb * nb + 15) / 16 * 16;  // weight rows this CTA multiplies
   const int M = Mt * 128;
-  // any active blastwave in the tile (warp-uniform answer by a block vote)
+  // does an active blastwave of the tile read a row of this 128-row part of
+  // the bank? Its shift s / h = n + r reads rows k - q - mlo, k < F, for the
+  // nodes' q in [floor((n - 1) / P), floor((n + 2) / P)]
   bool mine = false;
-  for (int b = tid; b < nb; b += kSbThreads) mine |= (flags[b0 + b] & kFlagActive) != 0;
+  for (int b = tid; b < nb; b += kSbThreads) {
+    if (!(flags[b0 + b] & kFlagActive)) continue;
+    const int n = (int)floor(scal[(size_t)(b0 + b) * kScal + kScalSynShift]);
+    const int lo = -floor_div(n + 2, P) - mlo, hi = F - 1 - floor_div(n - 1, P) - mlo;
+    mine |= lo <= mt * 128 + 127 && hi >= mt * 128;
+  }
   if (!__syncthreads_or(mine ? 1 : 0)) return;
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -169,7 +188,7 @@ k_syn_tc(const unsigned char* __restrict__ bank, const unsigned char* __restrict
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const int col = cb * 16 + c;
-        if (col < 2 * nb) Dt[(size_t)col * M] = __uint_as_float(v[c]);
+        if (col < rpb * nb) Dt[(size_t)col * M] = __uint_as_float(v[c]);
       }
     }
   }
@@ -237,11 +256,11 @@ void build_syn_bank(int method, int jc, const double* gam, int G, int Gp, double
     }
 }
 
-cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st) {
+cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStream_t st, int rpb) {
   if (nbw <= 0) return cudaSuccess;
-  const int tbw = g.sb_tbw, Mt = g.sb_M / 128;
+  const int tbw = g.sb_tbw * 2 / rpb, Mt = g.sb_M / 128;
   const int ntiles = (nbw + tbw - 1) / tbw;
-  const int nmax = (2 * std::min(tbw, nbw) + 15) / 16 * 16;
+  const int nmax = (rpb * std::min(tbw, nbw) + 15) / 16 * 16;
   const size_t smem = 1024 + (size_t)2 * 128 * g.Gp * 2 + (size_t)2 * nmax * g.Gp * 2 + 64;
   static bool attr = false;
   if (!attr) {
@@ -251,7 +270,7 @@ cudaError_t launch_syn_tc(const DevGrid& g, const DevState& S, int nbw, cudaStre
   }
   k_syn_tc<true><<<dim3(g.sb_P * Mt, ntiles), kSbThreads, smem, st>>>(
       reinterpret_cast<const unsigned char*>(g.synbank), reinterpret_cast<const unsigned char*>(S.Sbf), g.Gp, nbw,
-      tbw, Mt, g.sb_P, S.flags, S.Dsyn, S.err);
+      tbw, rpb, Mt, g.sb_P, g.F, g.sb_mlo, S.flags, S.scal, S.Dsyn, S.err);
   return cudaGetLastError();
 }
 

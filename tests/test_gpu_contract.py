@@ -175,3 +175,23 @@ def test_every_contraction_kernel_on_a_small_batch(lib, oracle, cuda_device, mon
                             d_jc.data_ptr())
         rel, z = rel_l2_rows(d_jc.cpu().numpy(), jssc_o)
         assert z == 0 and rel.max() <= tol, (kernel, abi.PRECISION_NAMES[prec], rel.max())
+
+
+def test_contract_synchrotron_bank_on_256_grid(lib, oracle, cuda_device):
+    """The contraction microbenchmark's grid (256 gamma x 256 nu): the
+    synchrotron sums of a large batch through the tensor-core kernel bank,
+    against the FP64 oracle."""
+    import torch
+    n = 640
+    g = CT.grid_desc(ngam=256, nfreq=256)
+    gam, freq = oracle.grids(g)
+    f, B = CT.states(gam, n, seed=16)
+    jsyn_o, _ = oracle.contract(g, f, B=B, ssc=False, threads=os.cpu_count() or 1)
+    ctx = lib.Context(g, cuda_device, ssc=False)
+    dev = torch.device("cuda", cuda_device)
+    d_f, d_B = torch.from_numpy(f).to(dev), torch.from_numpy(B).to(dev)
+    d_js = torch.zeros((n, 256), dtype=torch.float64, device=dev)
+    ctx.contract_device(n, d_f.data_ptr(), d_B.data_ptr(), 0, abi.PBAG_SYN_CSYN, abi.PBAG_PREC_FP32, d_js.data_ptr(), 0)
+    rel, z = rel_l2_rows(d_js.cpu().numpy(), jsyn_o)
+    assert z == 0 and rel.max() <= 1e-4, rel.max()
+    ctx.close()

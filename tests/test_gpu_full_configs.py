@@ -73,3 +73,12 @@ def test_jet_window_systolic_substeps(lib, oracle, cuda_device):
     to 184 substeps (systolic solve)."""
     got, ref = _run_both(lib, oracle, cases.jet_window(lib, (0, 2), 380, 90))
     _check(got, ref, cases.ALL_OUTPUTS)
+
+
+def test_gaussian_jet_full_size_tensor_core_sums(lib, oracle, cuda_device, monkeypatch):
+    """The full jet with the synchrotron / SSA sums on the tensor cores (the
+    kernel bank at 8 sub-shifts, log-space cubic interpolation), every history
+    against the oracle."""
+    monkeypatch.setenv("PBAG_SYN_TC", "1")
+    got, ref = _run_both(lib, oracle, cases.gaussian_jet(lib))
+    _check(got, ref, cases.ALL_OUTPUTS)

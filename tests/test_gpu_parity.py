@@ -165,6 +165,7 @@ def test_tensor_core_synchrotron_sums_match_cuda_core_sums(lib, cuda_device, mon
     the synchrotron and SSA histories agree to far below the plain-path bar."""
     recs, off, prm, grid = cases.tophat(lib, nsteps=120, ssa=True, syn_method=method)
     outs = ("syn_j_all", "syn_a_all", "j_all", "a_all")
+    monkeypatch.setenv("PBAG_SYN_TC", "1")
     ctx = Context(grid, device=0, ssc=False)
     tc = ctx.run(recs, off, prm, outputs=outs)
     ctx.close()
@@ -177,11 +178,19 @@ def test_tensor_core_synchrotron_sums_match_cuda_core_sums(lib, cuda_device, mon
         assert zm == 0 and rel.max() <= 2e-5, (k, rel.max())
 
 
-def test_field_outside_synchrotron_bank_falls_back(lib, oracle, cuda_device):
+def test_field_outside_synchrotron_bank_falls_back(lib, oracle, cuda_device, monkeypatch):
     """A magnetic field outside the range the tensor-core bank covers
     (1e-12..1e12 G) sends the whole batch to the CUDA-core sums; the result
     still matches the oracle."""
+    monkeypatch.setenv("PBAG_SYN_TC", "1")
     recs, off, prm, grid = cases.tophat(lib, nsteps=40, ssa=True)
     recs = recs.copy()
     recs["B"][20:] *= 1e-14
     _compare(lib, oracle, (recs, off, prm, grid), outputs=cases.TOTALS)
+
+
+def test_uneven_batch_tensor_core_sums(lib, oracle, cuda_device, monkeypatch):
+    """The uneven batch with the synchrotron / SSA sums on the tensor cores
+    (the path large batches take), every history against the oracle."""
+    monkeypatch.setenv("PBAG_SYN_TC", "1")
+    _compare(lib, oracle, cases.uneven(lib))
