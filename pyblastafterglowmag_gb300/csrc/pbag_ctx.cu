@@ -64,7 +64,9 @@ struct GraphKey {
   int64_t sur_gen;
   const void* synbank;
   const void* out[kOutputs];
+  std::vector<int64_t> lens;  // history length of every blastwave (the step launches' extents)
   bool operator==(const GraphKey& o) const {
+    if (lens != o.lens) return false;
     if (nbw != o.nbw || max_len != o.max_len || nrec != o.nrec || recs != o.recs || prm != o.prm ||
         state != o.state || ss != o.ss || ssc != o.ssc || ssc_path != o.ssc_path || sur_gen != o.sur_gen ||
         synbank != o.synbank)
@@ -103,6 +105,7 @@ struct pbag_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaError_t launch_radiation(const DevGrid& gg, const DevState& SS, const pbag_shock_params* d_prm, int nbw, int s) {
+    if (nbw <= 0) return cudaSuccess;
     const bool syn_tc = SS.Dsyn != nullptr;  // synchrotron / SSA sums on the tensor cores
     if (!ssc_on_tensor_cores())
       return syn_tc ? launch_syn_tc(gg, SS, nbw, stream) : launch_rad_ssc(gg, SS, d_prm, nbw, ssc, s, stream);
@@ -170,6 +173,8 @@ struct pbag_ctx {
   StepScal* d_ss = nullptr;         // per-record scalars
   int64_t* d_off = nullptr;
   int64_t* d_first = nullptr;
+  int* d_slot = nullptr;  // slot -> blastwave of the running batch (uneven histories)
+  std::vector<int> slot_of;  // blastwave -> slot of the last batch (empty: the same index)
   pbag_shock_params* d_prm = nullptr;
   DevState S{};
   std::vector<void*> state_mem;
@@ -218,6 +223,7 @@ struct pbag_ctx {
     cap_bw = 0;
     d_off = nullptr;
     d_first = nullptr;
+    d_slot = nullptr;
     d_prm = nullptr;
   }
 
@@ -244,6 +250,7 @@ struct pbag_ctx {
     cudaError_t e;
     if ((e = state_alloc(&d_off, cap + 1)) != cudaSuccess) return e;
     if ((e = state_alloc(&d_first, cap)) != cudaSuccess) return e;
+    if ((e = state_alloc(&d_slot, cap)) != cudaSuccess) return e;
     if ((e = state_alloc(&d_prm, cap)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.f, cap * G)) != cudaSuccess) return e;
     if ((e = state_alloc(&S.dfde, cap * G)) != cudaSuccess) return e;
@@ -371,6 +378,41 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
   }
   int64_t max_len = 0;
   for (int b = 0; b < nbw; ++b) max_len = std::max<int64_t>(max_len, off_h[b + 1] - off_h[b]);
+  // Slots: the blastwaves of a batch of uneven histories run in slots ordered
+  // by decreasing length, so that those still running at step s are the
+  // first n(s) slots and each step launches over them only (finished
+  // blastwaves get no CTA and no contraction row). A batch of equal lengths
+  // keeps slot = blastwave.
+  std::vector<int64_t> lens((size_t)nbw);
+  for (int b = 0; b < nbw; ++b) lens[b] = off_h[b + 1] - off_h[b];
+  bool uneven = false;
+  for (int b = 1; b < nbw && !uneven; ++b) uneven = lens[b] != lens[0];
+  std::vector<int64_t> slot_len = lens;  // history length by slot, decreasing when uneven
+  if (uneven) {
+    std::vector<int> slot((size_t)nbw);
+    for (int b = 0; b < nbw; ++b) slot[b] = b;
+    std::stable_sort(slot.begin(), slot.end(), [&](int a, int b) { return lens[a] > lens[b]; });
+    for (int k = 0; k < nbw; ++k) slot_len[k] = lens[slot[k]];
+    if (cudaMemcpyAsync(c->d_slot, slot.data(), sizeof(int) * nbw, cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)  // the host vector goes out of scope
+      return PBAG_ERR_CUDA;
+    SS.slot_bw = c->d_slot;
+    c->slot_of.assign((size_t)nbw, 0);
+    for (int k = 0; k < nbw; ++k) c->slot_of[slot[k]] = k;
+  } else {
+    c->slot_of.clear();
+  }
+  // slots whose history is longer than x steps
+  auto longer = [&](int64_t x) -> int {
+    if (!uneven) return nbw > 0 && slot_len[0] > x ? nbw : 0;
+    return (int)(std::partition_point(slot_len.begin(), slot_len.end(), [&](int64_t v) { return v > x; }) -
+                 slot_len.begin());
+  };
+  // step s: evolve completes step s-1 of every slot that ran it and runs step
+  // s; the radiation covers the slots that run step s
+  auto n_evolve = [&](int64_t s) { return longer(s > 0 ? s - 1 : 0); };
+  auto n_radiate = [&](int64_t s) { return longer(s); };
   c->launches = 0;
   if (c->ssc_path == PBAG_SSC_SURROGATE && nbw > 0 && (e = surrogate_reserve(c, nbw)) != cudaSuccess)
     return cuda_code(e);
@@ -398,14 +440,15 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
     GraphKey key{nbw, max_len, nrec, d_recs, d_prm, c->S.f, c->d_ss, c->ssc, c->ssc_path, surrogate_generation(c),
                  gg.synbank, {}};
     std::memcpy(key.out, &d_out, sizeof(d_out));
+    key.lens = lens;
     if (!c->graph_exec || !(key == c->graph_key)) {
       if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
       c->graph_exec = nullptr;
       cudaGraph_t graph = nullptr;
-      // the contraction autotuner measures outside the capture: one SSC
-      // launch on this batch's buffers with every row active (the flags are
-      // saved and restored; the step writes the contraction's outputs before
-      // it reads them)
+      // the contraction autotuner measures outside the capture: SSC launches
+      // on this batch's buffers with every row active, one per size class of
+      // the steps' row counts (the flags are saved and restored; the step
+      // writes the contraction's outputs before it reads them)
       if (nbw > 0 && c->ssc_on_tensor_cores() && c->ssc_path != PBAG_SSC_SURROGATE) {
         int* saved = nullptr;
         if (cudaMalloc(&saved, (size_t)nbw * sizeof(int)) == cudaSuccess) {
@@ -415,8 +458,15 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
             k_fill_flags<<<(nbw + 255) / 256, 256, 0, c->stream>>>(c->S.flags, nbw, kFlagActive);
             te = cudaGetLastError();
           }
-          if (te == cudaSuccess)
-            te = launch_ssc_tc(c->dg, c->S, c->dg.Bt, nbw, c->ssc_path != PBAG_SSC_TC_BF16, c->stream);
+          int last_octave = -1;
+          for (int64_t s = 0; s < max_len && te == cudaSuccess; ++s) {
+            const int n = n_radiate(s);  // decreasing in s
+            int o = 0;
+            while ((2 << o) <= n) ++o;
+            if (n <= 0 || o == last_octave) continue;
+            last_octave = o;
+            te = launch_ssc_tc(c->dg, c->S, c->dg.Bt, n, c->ssc_path != PBAG_SSC_TC_BF16, c->stream);
+          }
           cudaMemcpyAsync(c->S.flags, saved, (size_t)nbw * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
           const cudaError_t se = cudaStreamSynchronize(c->stream);
           cudaFree(saved);
@@ -426,11 +476,11 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
       if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PBAG_ERR_CUDA;
       cudaError_t ce = cudaSuccess;
       for (int64_t s = 0; s < max_len && ce == cudaSuccess; ++s) {
-        ce = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream);
-        if (ce == cudaSuccess) ce = c->launch_radiation(gg, SS, d_prm, nbw, (int)s);
+        ce = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, n_evolve(s), (int)s, d_out, c->stream);
+        if (ce == cudaSuccess) ce = c->launch_radiation(gg, SS, d_prm, n_radiate(s), (int)s);
       }
       if (ce == cudaSuccess)
-        ce = launch_finalize(gg, SS, c->d_off, d_prm, nbw, (int)(max_len - 1), d_out, c->stream);
+        ce = launch_finalize(gg, SS, c->d_off, d_prm, longer(max_len - 1), (int)(max_len - 1), d_out, c->stream);
       cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
       if (ce != cudaSuccess || ee != cudaSuccess || !graph) {
         if (graph) cudaGraphDestroy(graph);
@@ -450,17 +500,17 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
   }
   for (int64_t s = 0; s < max_len; ++s) {
     if (!mark(kClassEvolve, true)) return PBAG_ERR_CUDA;
-    if ((e = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) !=
+    if ((e = launch_evolve(gg, SS, d_recs, c->d_ss, c->d_off, d_prm, n_evolve(s), (int)s, d_out, c->stream)) !=
         cudaSuccess)
       return PBAG_ERR_CUDA;
     if (!mark(kClassEvolve, false)) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, true)) return PBAG_ERR_CUDA;
-    if ((e = c->launch_radiation(gg, SS, d_prm, nbw, (int)s)) != cudaSuccess) return PBAG_ERR_CUDA;
+    if ((e = c->launch_radiation(gg, SS, d_prm, n_radiate(s), (int)s)) != cudaSuccess) return PBAG_ERR_CUDA;
     if (!mark(kClassSsc, false)) return PBAG_ERR_CUDA;
     c->launches += c->ssc_on_tensor_cores() ? 3 : 2;
     if (s == max_len - 1) {
       if (!mark(kClassFinalize, true)) return PBAG_ERR_CUDA;
-      if ((e = launch_finalize(gg, SS, c->d_off, d_prm, nbw, (int)s, d_out, c->stream)) != cudaSuccess)
+      if ((e = launch_finalize(gg, SS, c->d_off, d_prm, longer(s), (int)s, d_out, c->stream)) != cudaSuccess)
         return PBAG_ERR_CUDA;
       if (!mark(kClassFinalize, false)) return PBAG_ERR_CUDA;
       c->launches += 1;
@@ -480,11 +530,12 @@ int run_device_once(pbag_ctx* c, const pbag_shock_params* d_prm, int nbw, const 
   // the reference stops at the first failure in time order (then blastwave order)
   int code = PBAG_OK, fb = -1, fs = -1, site = 0;
   for (int b = 0; b < nbw; ++b) {
-    if (err[4 * b] != 0 && (fs < 0 || err[4 * b + 1] < fs)) {
-      code = err[4 * b];
+    const size_t k = 4 * (size_t)(c->slot_of.empty() ? b : c->slot_of[b]);  // the blastwave's slot
+    if (err[k] != 0 && (fs < 0 || err[k + 1] < fs)) {
+      code = err[k];
       fb = b;
-      fs = err[4 * b + 1];
-      site = err[4 * b + 2];
+      fs = err[k + 1];
+      site = err[k + 2];
     }
   }
   if (st) {
@@ -605,6 +656,9 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
   {
     const char* sf = std::getenv("PBAG_SCAN_FP64");
     d.scan_fp64 = (sf && sf[0] == '1') ? 1 : 0;
+    const char* sm = std::getenv("PBAG_SYSTOLIC_MIN");
+    const int v = sm ? std::atoi(sm) : 0;
+    d.sys_min_sub = v >= 2 ? v : kScanMaxSub;
   }
   d.dlog_gam = (e[1] - e[0]) / e[0];
   cudaError_t err = cudaSuccess;

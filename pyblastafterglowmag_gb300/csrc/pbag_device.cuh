@@ -19,7 +19,7 @@ constexpr int kRadFreqs = kRadThreads / kRadLanes;  // frequencies per radiation
 constexpr int kStepWarps = kStepThreads / 32;
 constexpr int kFinalPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // frequencies per thread in finalize
 constexpr int kKintStageMax = 112 * 1024;  // largest SSC kernel-integral table staged in shared memory
-constexpr int kScanMaxSub = 96;       // below this many substeps the solve is a parallel scan
+constexpr int kScanMaxSub = 32;       // below this many substeps the solve is a parallel scan, else systolic
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
 constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 constexpr int kSiteSynBank = 900001;  // status site: a field outside the synchrotron bank's range
@@ -30,7 +30,8 @@ constexpr int kSiteSynBank = 900001;  // status site: a field outside the synchr
 struct DevGrid {
   int G, F, Gp;          // Gp: G rounded up to a multiple of 16 (padded SSC operand)
   int n_cyc;             // number of bins with e[j] <= 2 (cyclotron branch of cycSynch)
-  int scan_fp64;         // Chang-Cooper scan in FP64 only (PBAG_SCAN_FP64=1), else double-float first
+  int scan_fp64;         // Chang-Cooper substeps in FP64 only (PBAG_SCAN_FP64=1), else double-float first
+  int sys_min_sub;       // substep count from which the solve is the systolic pipeline (PBAG_SYSTOLIC_MIN)
   double dlog_gam;       // (e[1]-e[0])/e[0] (microphysics.h:413)
   const double* e;       // [G]   gamma grid e[i] = step^i
   const double* inv_e;   // [G]   1/e
@@ -156,7 +157,16 @@ struct DevState {
   // 2b+1: v), and the bank products D [tile][P][2 sb_tbw][sb_M]
   uint16_t* Sbf;
   float* Dsyn;
+  // slot -> the caller's blastwave (null: the same index). Every array above
+  // is indexed by slot, except powp, which follows the caller's blastwave
+  // like the offsets, the parameters and the step records. A batch of uneven
+  // histories runs in slots ordered by decreasing length, so that the
+  // blastwaves still running at a step are a prefix of the slots and each
+  // step's launches cover only that prefix.
+  const int* slot_bw;
 };
+
+__device__ __forceinline__ int slot_bw(const DevState& S, int slot) { return S.slot_bw ? S.slot_bw[slot] : slot; }
 
 enum : int {
   kScalDr = 0,     // dr_comov of this step

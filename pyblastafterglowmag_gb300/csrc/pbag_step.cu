@@ -289,7 +289,7 @@ __global__ void k_prep(DevGrid g, const pbag_step_rec* __restrict__ recs, const 
 }
 
 template <int FQ>
-__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
+__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, int64_t r0,
                            const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
                            float* sh_v, double* sh_usv, int* sh_state, float* sh_pp);
 
@@ -427,7 +427,7 @@ __device__ __forceinline__ dfl dfl_shfl_down(dfl a, int d) {
 // cc_scan in double-float: the same recurrence, scan tree and order of
 // operations, with the state and source scaled by 2^s (s from the block's
 // largest exponent of f and Q dt / b, so that the values stay far inside the
-// FP32 range for the <= kScanMaxSub substeps of this path). Returns false
+// FP32 range for the substeps of this path). Returns false
 // (and leaves fr untouched) when a coefficient or product leaves the FP32
 // range: the caller then runs the FP64 scan. *bad as cc_scan's result.
 template <int C>
@@ -556,6 +556,66 @@ __device__ bool cc_systolic(double (&fr)[C], const double (&ib)[C], const double
   return bad;
 }
 
+// cc_systolic in double-float, with cc_scan_df's power-of-two scaling and
+// range checks. Each tick is C dependent pair FMAs on the FP32 pipe instead of
+// FP64 ones (which hold a sub-partition's FP64 unit for 64 cycles each, and are
+// shared by every CTA on the SM), so the pipeline stays latency-bound when
+// several blastwaves run their long substep loops side by side. Returns false
+// (fr untouched) when a coefficient or the state leaves the FP32 range; the
+// caller then runs cc_systolic. *bad as cc_systolic's result.
+template <int C>
+__device__ bool cc_systolic_df(double (&fr)[C], const double (&ib)[C], const double (&qb)[C], const double (&bt)[C],
+                               int n_sub, int T, double (*xs)[kStepWarps], int* red, bool* bad_out) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  bool bad = false;
+  int E = 0;
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    bad |= bad_value(fr[q]);  // the check before the first substep, on the FP64 values
+    E = max(E, max(exp_field(fr[q]), exp_field(qb[q])));
+  }
+  E = block_max_int(E, red);
+  const int s = 1023 - E - 8;  // largest scaled input ~2^-8
+  dfl f[C], ibd[C], qbd[C], btd[C];
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    f[q] = dfl_from(fr[q], s);
+    ibd[q] = dfl_from(ib[q], 0);
+    qbd[q] = dfl_from(qb[q], s);
+    btd[q] = dfl_from(bt[q], 0);
+    ok &= isfinite(ibd[q].hi) && isfinite(qbd[q].hi) && isfinite(btd[q].hi) && isfinite(f[q].hi) && !bad_value(fr[q]);
+  }
+  if (!__syncthreads_and(ok ? 1 : 0)) return false;
+  dfl(*xd)[kStepWarps] = reinterpret_cast<dfl(*)[kStepWarps]>(xs);
+  if (tid < 2 * kStepWarps) (&xd[0][0])[tid] = dfl{0.f, 0.f};
+  __syncthreads();
+  dfl low = {0.f, 0.f};
+  const int ticks = n_sub + T - 1;
+  for (int tau = 0; tau < ticks; ++tau) {
+    dfl up = dfl_shfl_down(low, 1);
+    if (lane == 31) up = warp + 1 < kStepWarps ? xd[tau & 1][warp + 1] : dfl{0.f, 0.f};
+    const int m = tau - (T - 1 - tid);
+    if (tid < T && m >= 0 && m < n_sub) {
+      dfl fn = up;
+#pragma unroll
+      for (int q = C - 1; q >= 0; --q) {
+        if (m > 0) bad |= dfl_bad(f[q]);
+        const dfl a = dfl_fma(f[q], ibd[q], qbd[q]);
+        f[q] = dfl_fma(btd[q], fn, a);
+        fn = f[q];
+      }
+      low = f[0];
+    }
+    if (lane == 0) xd[(tau + 1) & 1][warp] = low;
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < C; ++q) fr[q] = dfl_to(f[q], s);
+  *bad_out = bad;
+  return true;
+}
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -648,12 +708,13 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     bulk_to_smem(sh_tab, g.etab, tb, smem_addr(&bars[0]));
   }
   // independent loads of this blastwave
+  const int bw = slot_bw(S, b);  // the caller's blastwave in this slot
   const int flags0 = S.flags[b];
   const int err0 = S.err[4 * b];
-  const int64_t r0 = off[b], len = off[b + 1] - r0;
-  const pbag_shock_params P = prm[b];
+  const int64_t r0 = off[bw], len = off[bw + 1] - r0;
+  const pbag_shock_params P = prm[bw];
   double* f = S.f + (size_t)b * G;
-  const double* pp = S.powp + (size_t)b * G;
+  const double* pp = S.powp + (size_t)bw * G;
   double* dfde = S.dfde + (size_t)b * G;
   double fr[C], ppq[C], dpre[C];
 #pragma unroll
@@ -717,7 +778,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   bool have_v = false;
   if (step > 0) {
     const int fin =
-        finalize_bw<FQ>(g, T, S, off, P, b, step - 1, out, flags0, err0, sh_v, &sh_usv, sh_state, sh_pp);
+        finalize_bw<FQ>(g, T, S, r0, P, b, step - 1, out, flags0, err0, sh_v, &sh_usv, sh_state, sh_pp);
     if (fin) {
       __syncthreads();
       flags = sh_state[0];
@@ -930,9 +991,10 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
     }
     const int Tn = (G + C - 1) / C;  // threads that own bins
     bool sbad = false;
-    if (n_sub >= kScanMaxSub)
-      sbad = cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
-    else if (g.scan_fp64 || !cc_scan_df<C>(fr, ib, qb, bt, n_sub, xs, pw0, red_i[0], &sbad))
+    if (n_sub >= g.sys_min_sub) {
+      if (g.scan_fp64 || !cc_systolic_df<C>(fr, ib, qb, bt, n_sub, Tn, xs, red_i[0], &sbad))
+        sbad = cc_systolic<C>(fr, ib, qb, bt, n_sub, Tn, xs);
+    } else if (g.scan_fp64 || !cc_scan_df<C>(fr, ib, qb, bt, n_sub, xs, pw0, red_i[0], &sbad))
       sbad = cc_scan<C>(fr, ib, qb, bt, n_sub, xs, pw0);
     __syncthreads();  // every heating value has been read: sh_f takes N(gamma)
 #pragma unroll
@@ -1120,8 +1182,9 @@ __device__ void radiate_block(const DevGrid& g, const DevState& S, const pbag_sh
   const int tid = threadIdx.x;
   const int G = g.G, F = g.F;
   if (!(S.flags[b] & kFlagActive)) return;
-  const bool ssa = prm[b].ssa_on != 0;
-  const int method = prm[b].syn_method;
+  const pbag_shock_params* pb = prm + slot_bw(S, b);
+  const bool ssa = pb->ssa_on != 0;
+  const int method = pb->syn_method;
   // GSL and Bessel: the tabulated functions, no cyclotron branch
   const bool tab = method == PBAG_SYN_GSL || method == PBAG_SYN_BESSEL;
   const float* stab = g.syntab + (method == PBAG_SYN_BESSEL ? kSynTabN : 0);
@@ -1187,7 +1250,7 @@ __device__ void radiate_block_regs(const DevGrid& g, const DevState& S, const pb
   const int G = g.G, F = g.F;
   const int kq = tid / kRadLanes, jl = tid % kRadLanes;
   const int flg = S.flags[b];
-  const pbag_shock_params* pb = prm + b;
+  const pbag_shock_params* pb = prm + slot_bw(S, b);
   const int ssa_on = pb->ssa_on, method = pb->syn_method;
   const float4 rp = *reinterpret_cast<const float4*>(S.rad32 + (size_t)b * 4);
   float nuv[RM], nu13v[RM], lnuv[RM];
@@ -1315,7 +1378,7 @@ __device__ __forceinline__ double intensity_approx(double em, double dtau) {
 // Returns 0 (nothing to do), 1 (rows written) or 2 (a synchrotron value failed
 // its check; nothing written). FQ frequencies per thread (F <= 128 FQ).
 template <int FQ>
-__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, const int64_t* __restrict__ off,
+__device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S, int64_t r0,
                             const pbag_shock_params& P, int b, int step, const pbag_outputs& out, int flags, int err,
                             float* sh_v, double* sh_usv, int* sh_state, float* sh_pp) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1326,7 +1389,7 @@ __device__ int finalize_bw(const DevGrid& g, const GridTab& T, const DevState& S
   const bool num = P.ele_method == PBAG_ELE_NUMERIC;
   const bool ssc = P.ssc_on && g.K32 != nullptr;
   const bool dense_syn = out.syn_j_all || out.syn_a_all || out.syn_i_all;
-  const size_t row = (size_t)(off[b] + step);
+  const size_t row = (size_t)(r0 + step);
   const float* syn32 = S.syn32 + (size_t)b * F;
   const float2* ssa32 = S.ssa32 + (size_t)b * F;
   const double* jssc = S.jssc + (size_t)b * F;
@@ -1579,23 +1642,24 @@ __device__ void history_rows_g(const DevGrid& g, const DevState& S, size_t row, 
 __global__ void __launch_bounds__(kStepThreads)
 k_finalize(DevGrid g, DevState S, const int64_t* __restrict__ off, const pbag_shock_params* __restrict__ prm,
            int step, pbag_outputs out) {
-  const int b = blockIdx.x;
+  const int b = blockIdx.x, bw = slot_bw(S, b);
   const int flags = S.flags[b], err = S.err[4 * b];
-  if (step >= off[b + 1] - off[b]) return;
-  const pbag_shock_params P = prm[b];
+  const int64_t r0 = off[bw];
+  if (step >= off[bw + 1] - r0) return;
+  const pbag_shock_params P = prm[bw];
   const GridTab T{g.etab, g.Ge, g.Fe};
   __shared__ float sh_pp[PBAG_MAX_BINS];
   const int fq = (g.F + kStepThreads - 1) / kStepThreads;
   int fin;
   if (fq <= 1)
-    fin = finalize_bw<1>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
+    fin = finalize_bw<1>(g, T, S, r0, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else if (fq <= 2)
-    fin = finalize_bw<2>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
+    fin = finalize_bw<2>(g, T, S, r0, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else if (fq <= 4)
-    fin = finalize_bw<4>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
+    fin = finalize_bw<4>(g, T, S, r0, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
   else
-    fin = finalize_bw<8>(g, T, S, off, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
-  if (fin == 1) history_rows_g(g, S, (size_t)(off[b] + step), b, out);
+    fin = finalize_bw<8>(g, T, S, r0, P, b, step, out, flags, err, nullptr, nullptr, nullptr, sh_pp);
+  if (fin == 1) history_rows_g(g, S, (size_t)(r0 + step), b, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1614,6 +1678,7 @@ cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_
 cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const StepScal* ss,
                           const int64_t* off, const pbag_shock_params* prm, int nbw, int step,
                           const pbag_outputs& out, cudaStream_t st) {
+  if (nbw <= 0) return cudaSuccess;
   const int kstage = evolve_kint_stage(g, nbw);
   const size_t smem = evolve_bytes(g, kstage);
   const int c = (g.G + kStepThreads - 1) / kStepThreads;
@@ -1677,6 +1742,7 @@ cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock
 
 cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* off, const pbag_shock_params* prm,
                             int nbw, int step, const pbag_outputs& out, cudaStream_t st) {
+  if (nbw <= 0) return cudaSuccess;
   k_finalize<<<nbw, kStepThreads, 0, st>>>(g, S, off, prm, step, out);
   return cudaGetLastError();
 }

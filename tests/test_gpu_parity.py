@@ -76,9 +76,10 @@ def test_gaussian_ssc_small_batch_kernel(lib, oracle, cuda_device, monkeypatch):
 
 
 def test_gaussian_ssc_fp64_scan(lib, oracle, cuda_device, monkeypatch):
-    """The Chang-Cooper substeps with the FP64 scan forced (the path a step
-    takes when its coefficients leave the FP32 range of the double-float scan),
-    on a window of the jet whose Chang-Cooper steps take 2-95 substeps."""
+    """The Chang-Cooper substeps with the FP64 scan and systolic pipeline
+    forced (the paths a step takes when its coefficients leave the FP32 range
+    of the double-float ones), on a window of the jet whose Chang-Cooper steps
+    take 2-125 substeps."""
     monkeypatch.setenv("PBAG_SCAN_FP64", "1")
     _compare(lib, oracle, cases.jet_window(lib, (0, 1, 2, 3), 280, 140))
 
@@ -88,7 +89,7 @@ def test_double_float_scan_matches_fp64_scan(lib, cuda_device, monkeypatch):
     electron histories agree to far below the plain-path bar (the pairs carry
     ~48 significant bits); the emissivities, formed from FP32 weights of those
     histories, to within an FP32 rounding. The window's Chang-Cooper steps
-    take 2-95 substeps (242 steps) or 96-125 (36 steps)."""
+    take 2-125 substeps (scan below 32, systolic pipeline from 32)."""
     recs, off, prm, grid = cases.jet_window(lib, (0, 1, 2, 3), 280, 140)
     outs = ("ele_f_all", "j_all")
     ctx = Context(grid, device=0, ssc=True)
@@ -104,13 +105,41 @@ def test_double_float_scan_matches_fp64_scan(lib, cuda_device, monkeypatch):
         assert rel.max() <= tol, (k, rel.max())
 
 
+def test_double_float_systolic_matches_fp64_systolic(lib, cuda_device, monkeypatch):
+    """The systolic pipeline in double-float against the FP64 one on the
+    uneven batch, whose long steps take up to 1000 substeps: electron
+    histories within 1e-9, emissivities within an FP32 rounding."""
+    recs, off, prm, grid = cases.uneven(lib)
+    outs = ("ele_f_all", "j_all")
+    ctx = Context(grid, device=0, ssc=True)
+    df = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    monkeypatch.setenv("PBAG_SCAN_FP64", "1")
+    ctx = Context(grid, device=0, ssc=True)
+    f64 = ctx.run(recs, off, prm, outputs=outs)
+    ctx.close()
+    for k, tol in (("ele_f_all", 1e-9), ("j_all", 1e-6)):
+        rel, zero_mismatch = rel_l2_rows(df[k], f64[k])
+        assert zero_mismatch == 0, k
+        assert rel.max() <= tol, (k, rel.max())
+
+
+def test_systolic_from_two_substeps(lib, oracle, cuda_device, monkeypatch):
+    """Every Chang-Cooper step with two or more substeps on the systolic
+    pipeline (PBAG_SYSTOLIC_MIN=2): the jet window of 2-125 substeps per step,
+    every history against the oracle."""
+    monkeypatch.setenv("PBAG_SYSTOLIC_MIN", "2")
+    _compare(lib, oracle, cases.jet_window(lib, (0, 1, 2, 3), 280, 140))
+
+
 def test_gaussian_late_window(lib, oracle, cuda_device):
     _compare(lib, oracle, cases.gaussian_window(lib, start=380, nsteps=60))
 
 
 def test_uneven_batch(lib, oracle, cuda_device):
     """Three seeded sweep jets with uneven histories (up to 1000 substeps per
-    step, 59 steps on the systolic path), every history."""
+    step; the blastwaves run in slots ordered by history length), every
+    history."""
     _compare(lib, oracle, cases.uneven(lib))
 
 
@@ -124,6 +153,24 @@ def test_error_status_matches_oracle(lib, oracle, cuda_device):
     with pytest.raises(PbagError) as ei:
         ctx.run(bad, off, prm)
     assert ei.value.code == abi.PBAG_ERR_DLNVDT and (ei.value.bw, ei.value.step) == (0, 37)
+
+
+def test_error_status_in_uneven_batch(lib, oracle, cuda_device):
+    """An uneven batch runs its blastwaves in slots ordered by history length;
+    the first failure is still reported as the caller's blastwave and step."""
+    recs, off, prm, grid = cases.uneven(lib)
+    lens = np.diff(off)
+    b = int(np.argsort(lens)[len(lens) // 2])  # a blastwave of middle length
+    valid = np.flatnonzero(recs["mode"][off[b]:off[b + 1]] != 0)
+    s = int(valid[len(valid) // 2])
+    bad = recs.copy()
+    bad["m_p1"][off[b] + s] = bad["m"][off[b] + s] * 0.5  # dlnV/dt < 0 (microphysics.h:406-409)
+    rc, where, _ = oracle.run(grid, bad, off, prm, outputs=cases.TOTALS)
+    assert rc == abi.PBAG_ERR_DLNVDT
+    ctx = Context(grid, device=0, ssc=True)
+    with pytest.raises(PbagError) as ei:
+        ctx.run(bad, off, prm)
+    assert ei.value.code == rc and (ei.value.bw, ei.value.step) == where
 
 
 def test_empty_and_zero_length(lib, oracle, cuda_device):
