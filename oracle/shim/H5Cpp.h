@@ -1,16 +1,18 @@
 // No-op stand-in for the HDF5 C++ API header.
 //
 // Test infrastructure only. The reference's microphysics headers include
-// <H5Cpp.h> through src/utilitites/pch.h:49, and src/utilitites/utils.h:624-1380
-// (struct Output) writes HDF5 files. None of that is on the comoving-radiation
-// path the oracle drives, so these declarations only need to let the headers
-// compile; every method is an empty inline body that is never called.
+// <H5Cpp.h> through src/utilitites/pch.h:49, src/utilitites/utils.h:624-1380
+// (struct Output) writes HDF5 files and src/utilitites/H5Easy.h reads them
+// (pulled in by the blastwave and EATS headers). None of that is on the paths
+// the oracle harnesses drive, so these declarations only need to let the
+// headers compile; every method is an empty inline body that is never called.
 #ifndef PBAG_ORACLE_SHIM_H5CPP_H
 #define PBAG_ORACLE_SHIM_H5CPP_H
 
 #include <string>
 
 typedef unsigned long long hsize_t;
+typedef long long hid_t;
 typedef std::string H5std_string;
 enum H5T_class_t { H5T_NO_CLASS = -1, H5T_INTEGER = 0, H5T_FLOAT = 1 };
 enum H5T_order_t { H5T_ORDER_ERROR = -1, H5T_ORDER_LE = 0, H5T_ORDER_BE = 1 };
@@ -22,10 +24,25 @@ enum H5S_class_t { H5S_SCALAR = 0, H5S_SIMPLE = 1 };
 
 namespace H5 {
 struct PredType {
-  static const PredType NATIVE_DOUBLE, NATIVE_INT, IEEE_F32LE, IEEE_F64LE, IEEE_F32BE, IEEE_F64BE;
+  static const PredType NATIVE_DOUBLE, NATIVE_INT, IEEE_F32LE, IEEE_F64LE, IEEE_F32BE, IEEE_F64BE, STD_I8LE,
+      STD_I8BE, STD_I16LE, STD_I16BE, STD_I32LE, STD_I32BE, STD_I64LE, STD_I64BE, STD_U32LE;
+  bool operator==(const PredType&) const { return false; }
 };
 inline const PredType PredType::NATIVE_DOUBLE{}, PredType::NATIVE_INT{}, PredType::IEEE_F32LE{},
-    PredType::IEEE_F64LE{}, PredType::IEEE_F32BE{}, PredType::IEEE_F64BE{};
+    PredType::IEEE_F64LE{}, PredType::IEEE_F32BE{}, PredType::IEEE_F64BE{}, PredType::STD_I8LE{},
+    PredType::STD_I8BE{}, PredType::STD_I16LE{}, PredType::STD_I16BE{}, PredType::STD_I32LE{},
+    PredType::STD_I32BE{}, PredType::STD_I64LE{}, PredType::STD_I64BE{}, PredType::STD_U32LE{};
+struct Exception {
+  static void dontPrint() {}
+  void printErrorStack() const {}
+  std::string getDetailMsg() const { return {}; }
+};
+struct FileIException : Exception {};
+struct GroupIException : Exception {};
+struct DataSetIException : Exception {};
+struct DataSpaceIException : Exception {};
+struct AttributeIException : Exception {};
+struct DataTypeIException : Exception {};
 
 struct DataType {
   DataType() {}
@@ -37,6 +54,8 @@ struct DataType {
 struct IntType : DataType {
   IntType() {}
   IntType(const PredType&) {}
+  H5T_order_t getOrder(H5std_string&) const { return H5T_ORDER_LE; }
+  H5T_order_t getOrder() const { return H5T_ORDER_LE; }
 };
 struct FloatType : DataType {
   H5T_order_t getOrder(H5std_string&) const { return H5T_ORDER_LE; }
@@ -55,6 +74,7 @@ struct Attribute {
   template <typename... A> void write(A&&...) {}
   template <typename... A> void read(A&&...) const {}
   DataType getDataType() const { return {}; }
+  unsigned long long getStorageSize() const { return 0; }
 };
 struct DataSet {
   void write(const void*, const PredType&) {}
@@ -63,6 +83,7 @@ struct DataSet {
   DataType getDataType() const { return {}; }
   DataSpace getSpace() const { return {}; }
   FloatType getFloatType() const { return {}; }
+  IntType getIntType() const { return {}; }
 };
 struct Group {
   Group() {}
@@ -81,8 +102,11 @@ struct H5File {
   Group openGroup(const std::string&) { return {}; }
   DataSet openDataSet(const std::string&) const { return {}; }
   Attribute openAttribute(const std::string&) const { return {}; }
+  bool attrExists(const std::string&) const { return false; }
+  hid_t getId() const { return 0; }
   void close() {}
 };
 }  // namespace H5
+inline int H5Lexists(hid_t, const char*, int) { return 0; }
 
 #endif
