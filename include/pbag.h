@@ -45,7 +45,8 @@ enum pbag_status_code {
   PBAG_ERR_UNSUPPORTED = -7,/* option the GPU path does not implement          */
   PBAG_ERR_TIMEOUT = -8,    /* a bounded device-side wait ran out              */
   PBAG_ERR_NOMEM = -9,      /* device allocation failed                        */
-  PBAG_ERR_RANGE = -10      /* frequency outside the grid (microphysics.h:1190-1201) */
+  PBAG_ERR_RANGE = -10,     /* frequency outside the grid (microphysics.h:1190-1201) */
+  PBAG_ERR_EVALS = -11      /* EATS quadrature past 1e7 integrand evaluations (eats.h:536-541) */
 };
 
 /* ---- options (same meaning as the reference's parfile options) ----------- */
@@ -391,6 +392,62 @@ typedef struct pbag_flux_query {
 int pbag_flux_dens(pbag_ctx* ctx, const pbag_flux_opts* opts, int nbw, const int64_t* offsets,
                    const double* d_j_all, const double* d_a_all, const double* d_r_all, int nq,
                    const pbag_flux_query* d_q, double* d_flux, pbag_status* st);
+
+/* ---- adaptive EATS light curve (method_eats = "adaptive") -----------------
+ * The observed flux density of a jet layer at (t_obs, nu_obs), integrated
+ * over the equal-arrival-time surface: EATS::evalFluxDensA (eats.h:820-850)
+ * with atol 0 as evalLightCurve passes it for a fresh layer (eats.h:808-818),
+ * integrate_theta_phi (eats.h:587-700): phi in [0, pi] outside, 1 - cos(theta)
+ * from the layer's lower cone edge to the jet edge of that phi (find_jet_edge,
+ * eats.h:103-173) inside, each by CADRE (quadratures.h:1613-2113, adaptive
+ * Romberg with trapezoid error control) or TRAP_FIXED (quadratures.h:939-951);
+ * the integrand (eats.h:175-232) interpolates the layer's dynamics at the
+ * emission time of that direction and calls fluxDens on the layer's forward
+ * and reverse shock histories (fluxDensAdaptiveWithComov,
+ * blastwave_radiation.h:75-150); the counter jet (obsAngleCJ) adds a second
+ * integral. Output in mJy. One query = one (layer, t_obs, nu_obs). FP64. */
+enum pbag_eats_quad { PBAG_QUAD_CADRE = 0, PBAG_QUAD_TRAP_FIXED = 1 };          /* "method_quad" */
+/* the dynamics a layer's EATS reads, per time index (BW::Q of blastwave_pars.h:211-229) */
+enum pbag_eats_q {
+  PBAG_EQ_TBURST = 0, PBAG_EQ_R, PBAG_EQ_THETA, PBAG_EQ_GAMMA, PBAG_EQ_BETA, PBAG_EQ_GAMMA_FSH,
+  PBAG_EQ_THICKNESS, PBAG_EQ_M2, PBAG_EQ_RHO2, PBAG_EQ_RSH, PBAG_EQ_ACC_FRAC, PBAG_EQ_CTHETA,
+  PBAG_EQ_GAMMA_RSH, PBAG_EQ_THICKNESS_RS, PBAG_EQ_M3, PBAG_EQ_RHO3, PBAG_EQ_RRSH, PBAG_EQ_ACC_FRAC_RS,
+  PBAG_EQ_N
+};
+typedef struct pbag_eats_opts {
+  double theta_obs, z, d_l;      /* observer angle [rad], redshift, luminosity distance [cm] */
+  double rtol_theta, rtol_phi;   /* "rtol_theta", "rtol_phi" */
+  int32_t nmax_theta, nmax_phi;  /* "nmax_theta", "nmax_phi": evaluation limits */
+  int32_t method_quad;           /* pbag_eats_quad */
+  int32_t counter_jet;           /* "counter_jet": 1 adds the counter jet */
+  pbag_flux_opts flux;           /* method_vel / method_ne / method_tau of the layer's shocks */
+} pbag_eats_opts;
+typedef struct pbag_eats_layer {
+  int32_t i_end_r;               /* time indices of the layer's dynamics in use (m_i_end_r) */
+  int32_t bw_fs, bw_rs;          /* blastwaves whose histories are the layer's forward / reverse
+                                    shock (bw_rs < 0: no reverse-shock radiation) */
+  int32_t pad;
+  double theta_c_l, theta_c_h;   /* the layer's cone (setEatsPars, eats.h:721-731) */
+  double ncells;                 /* cells of the layer (fluxDens' ncells) */
+} pbag_eats_layer;
+typedef struct pbag_eats_query {
+  int32_t layer, pad;
+  double t_obs, nu_obs;
+} pbag_eats_query;
+/* nl layers; d_dyn [nl][PBAG_EQ_N][nr] (device): the dynamics of layer l at
+ * d_dyn + (l * PBAG_EQ_N + q) * nr; h_layers (host) [nl]; offsets (host,
+ * nbw + 1) and d_j_all / d_a_all [nrec][nfreq] (device): the histories of the
+ * batch that evolved the layers' shocks (blastwave b's row i is its time
+ * index i); d_q [nq], d_flux [nq] (device). Synchronous. Failures where the
+ * reference exits: PBAG_ERR_RANGE (a comoving frequency outside the grid),
+ * PBAG_ERR_NONFINITE (a negative or non-finite intensity, luminosity or
+ * interpolated dynamics value), PBAG_ERR_EVALS (more than 1e7 integrand
+ * evaluations, eats.h:536-541), PBAG_ERR_NOMEM (an integration needed more
+ * intervals than the workspace holds: nmax + 8 per level), each with st->step
+ * = the first failing query and st->bw = its layer. */
+int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int nl, const pbag_eats_layer* h_layers, int nr,
+                     const double* d_dyn, int nbw, const int64_t* offsets, const double* d_j_all,
+                     const double* d_a_all, int nq, const pbag_eats_query* d_q, double* d_flux, pbag_status* st);
 
 /* Contraction autotuner: the first tensor-core SSC contraction of a shape
  * (precision, grid, outputs, batch size to a factor of two) launched outside

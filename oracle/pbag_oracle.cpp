@@ -11,6 +11,7 @@
 // value is the next point of the logspace grid, freq[F-1]*base.
 #include "pbag_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -24,6 +25,7 @@ namespace {
 // utilitites/utils.h:18-60 (CGS constants)
 constexpr double c_light = 2.99792458e10;
 constexpr double pi_ = 3.141592653589793;
+constexpr double cgs2mJy = 1.e26;  // utils.h:40
 constexpr double m_p = 1.6726e-24;
 constexpr double m_e = 9.1094e-28;
 constexpr double q_e = 4.803204e-10;
@@ -750,9 +752,91 @@ int orc_contract(const pbag_grid_desc* g, int n, const double* f, const double* 
   return PBAG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
 // ElectronAndRadiation::fluxDens (microphysics.h:1185-1217) with
-// computeFluxDensity (:799-867) and computeIntensity (:11-58), FP64, one query
-// at a time; the frequency grid and the histories of the query's blastwave.
+// computeFluxDensity (:799-867) and computeIntensity (:11-58), FP64, for one
+// query on the histories of its blastwave (rows r0 + ia, r0 + ib of J / A
+// and R). Returns PBAG_OK, PBAG_ERR_RANGE or PBAG_ERR_NONFINITE.
+int flux_dens_one(const double* nu, int F, const pbag_flux_opts* o, const double* J, const double* A,
+                  const double* R, int64_t r0, const pbag_flux_query& q, double* out) {
+  *out = 0.;
+  if (q.freq >= nu[F - 1] || q.freq <= nu[0]) return PBAG_ERR_RANGE;  // microphysics.h:1190-1201
+  // findIndex (interpolators.h:13-35)
+  size_t ia_nu;
+  if (q.freq <= nu[0])
+    ia_nu = 0;
+  else if (q.freq >= nu[F - 1])
+    ia_nu = F - 2;
+  else {
+    unsigned a = 0, b = (unsigned)F - 1;
+    while (b - a > 1u) {
+      unsigned i = (b + a) >> 1;
+      if (nu[i] > q.freq)
+        b = i;
+      else
+        a = i;
+    }
+    ia_nu = a;
+  }
+  const size_t ib_nu = ia_nu + 1;
+  // Interp2d::InterpolateBilinear / BilinearInterpolation (interpolators.h:708-801)
+  auto interp = [&](const double* Z) {
+    double q11 = Z[(r0 + q.ia) * F + ia_nu], q12 = Z[(r0 + q.ib) * F + ia_nu];
+    double q21 = Z[(r0 + q.ia) * F + ib_nu], q22 = Z[(r0 + q.ib) * F + ib_nu];
+    double x1 = nu[ia_nu], x2 = nu[ib_nu], y1 = R[r0 + q.ia], y2 = R[r0 + q.ib];
+    double x2x1 = x2 - x1, y2y1 = y2 - y1, x2x = x2 - q.freq, y2y = y2 - q.r, yy1 = q.r - y1, xx1 = q.freq - x1;
+    return 1.0 / (x2x1 * y2y1) * (q11 * x2x * y2y + q21 * xx1 * y2y + q12 * x2x * yy1 + q22 * xx1 * yy1);
+  };
+  const double em_prime = interp(J), abs_prime = interp(A);
+  auto beta_of = [](double gm) { return std::sqrt((gm - 1.) * (gm + 1.)) / gm; };  // blastwave_components.h:36
+  double beta = beta_of(q.Gamma);
+  double a = 1.0 - beta * q.mu;
+  double delta_D = q.Gamma * a;
+  double em_lab = em_prime / (delta_D * delta_D);
+  double abs_lab = abs_prime * delta_D;
+  double beta_shock = o->shock_vel == PBAG_VEL_SHOCK ? beta_of(q.GammaSh) : beta_of(q.Gamma);
+  double m2 = q.ne * m_p;
+  double dr = m2 / (2. * pi_ * m_p * q.r * q.r * (1. - std::cos(q.theta) / q.ncells) * q.Gamma * q.n_prime);
+  double dtau;
+  if (q.mu == beta_shock)
+    dtau = 1.0e100;
+  else
+    dtau = abs_lab * dr * (1. - q.mu * beta_shock) / (q.mu - beta_shock);
+  double intensity = em_lab;
+  if (dtau != 0) {
+    double thick = dtau > 0 ? em_lab / dtau : 0.;
+    double u = 1. / 2. + std::exp(-dtau) / dtau - (1 - std::exp(-dtau)) / (dtau * dtau);
+    double approx = dtau > 1.e-3 ? em_lab * (3. * u / dtau) : em_lab;
+    double abs_fac = dtau > 0.0 ? -std::expm1(-dtau) / dtau : std::expm1(dtau) / dtau;
+    double smooth = em_lab * abs_fac;
+    double sharp = em_lab;
+    if (dtau > 1.0)
+      sharp = em_lab / dtau;
+    else if (dtau < -1.0)
+      sharp = 0.0;
+    intensity = o->method_tau == PBAG_TAU_THICK    ? thick
+                : o->method_tau == PBAG_TAU_SMOOTH ? smooth
+                : o->method_tau == PBAG_TAU_SHARP  ? sharp
+                                                   : approx;
+  }
+  if (intensity < 0 || !std::isfinite(intensity)) return PBAG_ERR_NONFINITE;
+  double ashock = 1.0 - q.mu * beta_shock;
+  double lum = o->method_ne == PBAG_NE_USE_NPRIME
+                   ? intensity * q.r * q.r * (dr / ashock)
+                   : intensity * q.ne / (2. * pi_ * (1. - std::cos(q.theta) / q.ncells)) / q.Gamma / ashock;
+  if (lum < 0 || !std::isfinite(lum)) return PBAG_ERR_NONFINITE;
+  *out = lum;
+  return PBAG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ElectronAndRadiation::fluxDens for a batch of queries (flux_dens_one each).
 int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_t* offsets, const double* j_all,
                   const double* a_all, const double* r_all, int nq, const pbag_flux_query* qs, double* flux,
                   int* fail_index) {
@@ -761,84 +845,11 @@ int orc_flux_dens(const pbag_grid_desc* g, const pbag_flux_opts* o, const int64_
   orc_build_grids(g, gam.data(), nu.data());
   *fail_index = -1;
   for (int t = 0; t < nq; ++t) {
-    const pbag_flux_query& q = qs[t];
-    flux[t] = 0.;
-    if (q.freq >= nu[F - 1] || q.freq <= nu[0]) {  // microphysics.h:1190-1201
+    const int rc = flux_dens_one(nu.data(), F, o, j_all, a_all, r_all, offsets[qs[t].bw], qs[t], &flux[t]);
+    if (rc != PBAG_OK) {
       *fail_index = t;
-      return PBAG_ERR_RANGE;
+      return rc;
     }
-    // findIndex (interpolators.h:13-35)
-    size_t ia_nu;
-    if (q.freq <= nu[0])
-      ia_nu = 0;
-    else if (q.freq >= nu[F - 1])
-      ia_nu = F - 2;
-    else {
-      unsigned a = 0, b = (unsigned)F - 1;
-      while (b - a > 1u) {
-        unsigned i = (b + a) >> 1;
-        if (nu[i] > q.freq)
-          b = i;
-        else
-          a = i;
-      }
-      ia_nu = a;
-    }
-    const size_t ib_nu = ia_nu + 1;
-    const int64_t r0 = offsets[q.bw];
-    // Interp2d::InterpolateBilinear / BilinearInterpolation (interpolators.h:708-801)
-    auto interp = [&](const double* Z) {
-      double q11 = Z[(r0 + q.ia) * F + ia_nu], q12 = Z[(r0 + q.ib) * F + ia_nu];
-      double q21 = Z[(r0 + q.ia) * F + ib_nu], q22 = Z[(r0 + q.ib) * F + ib_nu];
-      double x1 = nu[ia_nu], x2 = nu[ib_nu], y1 = r_all[r0 + q.ia], y2 = r_all[r0 + q.ib];
-      double x2x1 = x2 - x1, y2y1 = y2 - y1, x2x = x2 - q.freq, y2y = y2 - q.r, yy1 = q.r - y1, xx1 = q.freq - x1;
-      return 1.0 / (x2x1 * y2y1) * (q11 * x2x * y2y + q21 * xx1 * y2y + q12 * x2x * yy1 + q22 * xx1 * yy1);
-    };
-    const double em_prime = interp(j_all), abs_prime = interp(a_all);
-    auto beta_of = [](double gm) { return std::sqrt((gm - 1.) * (gm + 1.)) / gm; };  // blastwave_components.h:36
-    double beta = beta_of(q.Gamma);
-    double a = 1.0 - beta * q.mu;
-    double delta_D = q.Gamma * a;
-    double em_lab = em_prime / (delta_D * delta_D);
-    double abs_lab = abs_prime * delta_D;
-    double beta_shock = o->shock_vel == PBAG_VEL_SHOCK ? beta_of(q.GammaSh) : beta_of(q.Gamma);
-    double m2 = q.ne * m_p;
-    double dr = m2 / (2. * pi_ * m_p * q.r * q.r * (1. - std::cos(q.theta) / q.ncells) * q.Gamma * q.n_prime);
-    double dtau;
-    if (q.mu == beta_shock)
-      dtau = 1.0e100;
-    else
-      dtau = abs_lab * dr * (1. - q.mu * beta_shock) / (q.mu - beta_shock);
-    double intensity = em_lab;
-    if (dtau != 0) {
-      double thick = dtau > 0 ? em_lab / dtau : 0.;
-      double u = 1. / 2. + std::exp(-dtau) / dtau - (1 - std::exp(-dtau)) / (dtau * dtau);
-      double approx = dtau > 1.e-3 ? em_lab * (3. * u / dtau) : em_lab;
-      double abs_fac = dtau > 0.0 ? -std::expm1(-dtau) / dtau : std::expm1(dtau) / dtau;
-      double smooth = em_lab * abs_fac;
-      double sharp = em_lab;
-      if (dtau > 1.0)
-        sharp = em_lab / dtau;
-      else if (dtau < -1.0)
-        sharp = 0.0;
-      intensity = o->method_tau == PBAG_TAU_THICK    ? thick
-                  : o->method_tau == PBAG_TAU_SMOOTH ? smooth
-                  : o->method_tau == PBAG_TAU_SHARP  ? sharp
-                                                     : approx;
-    }
-    if (intensity < 0 || !std::isfinite(intensity)) {
-      *fail_index = t;
-      return PBAG_ERR_NONFINITE;
-    }
-    double ashock = 1.0 - q.mu * beta_shock;
-    double lum = o->method_ne == PBAG_NE_USE_NPRIME
-                     ? intensity * q.r * q.r * (dr / ashock)
-                     : intensity * q.ne / (2. * pi_ * (1. - std::cos(q.theta) / q.ncells)) / q.Gamma / ashock;
-    if (lum < 0 || !std::isfinite(lum)) {
-      *fail_index = t;
-      return PBAG_ERR_NONFINITE;
-    }
-    flux[t] = lum;
   }
   return PBAG_OK;
 }
@@ -973,5 +984,539 @@ extern "C" int orc_shock_limits(const pbag_limits_opts* o, const double* gam, in
   }
   state[0] = m.gamma_min, state[1] = m.gamma_max, state[2] = m.gamma_c, state[3] = m.accel_frac;
   state[4] = m.B, state[5] = m.Theta, state[6] = m.z_cool;
+  return PBAG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adaptive EATS light curve: EATS::evalFluxDensA (eats.h:820-850) with atol 0,
+// parsPars' mu array (eats.h:917-948), integrate_theta_phi (:587-700),
+// phi_integrand (:449-586) with find_jet_edge (:103-173), costheta_integrand
+// (:435-448), integrand (:175-232) with check_emission_time (:24-38), the
+// flux of fluxDensAdaptiveWithComov (blastwave_radiation.h:75-150), and the
+// quadratures trap (quadratures.h:939-951) and cadre_adapt = m9_adapt with
+// cadreInitInterval / cadreProcessInterval / cadreSplitInterval and the mesh9
+// heap (quadratures.h:182-208, 657-770, 1613-2113), in their loop structure
+// and operation order.
+namespace {
+
+struct Iv9 {  // Interval9 (quadratures.h:182-198)
+  double a, b, I, err, fa, fll, fl, flr, fm, frl, fr, frr, fb;
+  int refinement;
+};
+
+struct Mesh9 {  // quadratures.h:201-208, 657-770
+  std::vector<Iv9> heap;
+  void insert(const Iv9& i) {
+    heap.push_back(i);
+    size_t c = heap.size() - 1, p = (c - 1) / 2;
+    while (c != 0 && heap[p].err < heap[c].err) {
+      std::swap(heap[p], heap[c]);
+      c = p;
+      p = (c - 1) / 2;
+    }
+  }
+  void extract(Iv9* worst) {
+    *worst = heap[0];
+    heap[0] = heap[heap.size() - 1];
+    heap.pop_back();
+    size_t p = 0, c1 = 1, c2 = 2;
+    while (c1 < heap.size()) {
+      size_t c = c1;
+      double e = heap[c1].err;
+      if (c2 < heap.size() && heap[c2].err > e) {
+        c = c2;
+        e = heap[c2].err;
+      }
+      if (e <= heap[p].err) break;
+      std::swap(heap[p], heap[c]);
+      p = c;
+      c1 = 2 * p + 1;
+      c2 = c1 + 1;
+    }
+  }
+  double total_I() const {
+    double I = 0.0;
+    for (const Iv9& i : heap) I += i.I;
+    return I;
+  }
+  double total_err() const {
+    double e = 0.0;
+    for (const Iv9& i : heap) e += i.err;
+    return e;
+  }
+};
+
+// cadre_adapt over f (a callable double(double)); err() stops the quadrature
+// as the reference's errf does (its result is then 0).
+template <class Fn, class Err>
+struct Cadre {
+  Fn& f;
+  Err& errf;
+  int init(Iv9* i) {  // cadreInitInterval with pfa = pfb = NULL
+    int count = 0;
+    i->fa = f(i->a);
+    count++;
+    if (errf()) return count;
+    i->fb = f(i->b);
+    count++;
+    if (errf()) return count;
+    i->fm = f(0.5 * (i->a + i->b));
+    count++;
+    return count;
+  }
+  int process(Iv9* i) {  // cadreProcessInterval
+    const double scaleTol = 0.2;
+    int count = 0;
+    if (i->refinement < 4) {
+      double fa = i->fa, fm = i->fm, fb = i->fb;
+      double fl, fr;
+      if (i->refinement == 0) {
+        fl = f(0.75 * i->a + 0.25 * i->b);
+        count++;
+        if (errf()) return count;
+        fr = f(0.25 * i->a + 0.75 * i->b);
+        count++;
+        if (errf()) return count;
+        i->fl = fl;
+        i->fr = fr;
+      } else {
+        fl = i->fl;
+        fr = i->fr;
+        i->refinement = 0;
+      }
+      double h = 0.25 * (i->b - i->a);
+      double T0 = 2 * h * (fa + fb);
+      double T1 = 0.5 * T0 + 2 * h * fm;
+      double T2 = 0.5 * T1 + h * (fl + fr);
+      double R0 = (T1 - T0) / (T2 - T1);
+      if (R0 > 4 - scaleTol && R0 < 4 + scaleTol) {
+        double fll = f(0.875 * i->a + 0.125 * i->b);
+        count++;
+        if (errf()) return count;
+        double flr = f(0.625 * i->a + 0.375 * i->b);
+        count++;
+        if (errf()) return count;
+        double frl = f(0.375 * i->a + 0.625 * i->b);
+        count++;
+        if (errf()) return count;
+        double frr = f(0.125 * i->a + 0.875 * i->b);
+        count++;
+        if (errf()) return count;
+        i->fll = fll;
+        i->flr = flr;
+        i->frl = frl;
+        i->frr = frr;
+        i->refinement = 1;
+        double T3 = 0.5 * T2 + 0.5 * h * (fll + flr + frl + frr);
+        double R1 = (T2 - T1) / (T3 - T2);
+        if (R1 > 4 - scaleTol && R1 < 4 + scaleTol) {
+          double R11 = (4 * T1 - T0) / 3.0;
+          double R21 = (4 * T2 - T1) / 3.0;
+          double R22 = (16 * R21 - R11) / 15.0;
+          i->fa = T3;
+          i->fll = (4 * T3 - T2) / 3.0;
+          i->fl = (16 * i->fll - R21) / 15.0;
+          i->flr = (64 * i->fl - R22) / 63.0;
+          i->I = i->flr;
+          i->err = std::fabs((i->fl - R22) / 63.0);
+          i->refinement = 4;
+          return count;
+        }
+        double errt = (T3 - T2) / 3.0;
+        i->err = std::fabs(errt);
+        i->I = T3 + errt;
+        return count;
+      } else if (R0 >= 4 + scaleTol || R0 < 2 || R0 != R0) {
+        double err10 = std::fabs(T1 - T0);
+        double err21 = std::fabs(T2 - T1);
+        i->err = err10 > err21 ? err10 : err21;
+        i->I = T2;
+        return count;
+      } else {
+        double err = -(T2 - T1) * (T2 - T1) / (T2 - 2 * T1 + T0);
+        i->err = std::fabs(err);
+        if (std::fabs(T2 + err) < 1.0e-14 * std::fabs(T2))
+          i->I = 1.0e-14 * T2;
+        else
+          i->I = T2 + err;
+        return count;
+      }
+    }
+    if (i->refinement < 0) return 0;
+    int nint = 1;
+    for (int n = 0; n < i->refinement; n++) nint *= 2;
+    double h = (i->b - i->a) / nint;
+    double sum = 0;
+    for (int n = 1; n < nint; n += 2) {
+      sum += f(i->a + h * n);
+      count++;
+      if (errf()) return count;
+    }
+    // the Romberg tableau in fa, fll, fl, flr, fm, frl, fr, frr, fb (m = 1..9)
+    double* tab[9] = {&i->fa, &i->fll, &i->fl, &i->flr, &i->fm, &i->frl, &i->fr, &i->frr, &i->fb};
+    double T = 0.5 * i->fa + h * sum;
+    double Rnm = i->fa;
+    double Rnmp = i->fll;
+    i->fa = T;
+    i->fll = (4.0 * i->fa - Rnm) / 3.0;
+    if (i->refinement == 1) {
+      i->I = i->fll;
+      i->err = std::fabs((i->fa - Rnm) / 3.0);
+      i->refinement += 1;
+      return count;
+    }
+    double pw = 4.0;
+    for (int m = 2; m <= 8; ++m) {
+      pw *= 4.0;
+      Rnm = Rnmp;
+      Rnmp = *tab[m];
+      *tab[m] = (pw * *tab[m - 1] - Rnm) / (pw - 1.0);
+      if (i->refinement == m) {
+        i->I = *tab[m];
+        i->err = std::fabs((*tab[m - 1] - Rnm) / (pw - 1.0));
+        i->refinement += 1;
+        return count;
+      }
+    }
+    Rnm = Rnmp;  // m = 9
+    i->I = (262144 * i->fb - Rnm) / 262143.0;
+    i->err = std::fabs((i->fb - Rnm) / 262143.0);
+    i->refinement += 1;
+    return count;
+  }
+  int split(Iv9* i0, Iv9* i1, Iv9* i2) {  // cadreSplitInterval
+    double xm = 0.5 * (i0->a + i0->b);
+    i1->a = i0->a;
+    i1->b = xm;
+    i2->a = xm;
+    i2->b = i0->b;
+    i1->fa = i0->fa;
+    i1->fl = i0->fll;
+    i1->fm = i0->fl;
+    i1->fr = i0->flr;
+    i1->fb = i0->fm;
+    i1->refinement = i0->refinement;
+    i2->fa = i0->fm;
+    i2->fl = i0->frl;
+    i2->fm = i0->fr;
+    i2->fr = i0->frr;
+    i2->fb = i0->fb;
+    i2->refinement = i0->refinement;
+    int n = 0;
+    n += process(i1);
+    n += process(i2);
+    return n;
+  }
+  double adapt(double xa, double xb, int Nmax, double atol, double rtol) {  // m9_adapt
+    Mesh9 m;
+    Iv9 i{};
+    i.a = xa;
+    i.b = xb;
+    int n = init(&i);
+    if (errf()) return 0.0;
+    n += process(&i);
+    if (errf()) return 0.0;
+    m.insert(i);
+    double I = i.I, err = i.err;
+    int num_intervals = 1, num_iterations = 0, last_check = 0;
+    while (n < Nmax && err > atol + rtol * std::fabs(I)) {
+      m.extract(&i);
+      if (i.refinement >= 4) {
+        double oldI = i.I, olderr = i.err;
+        n += process(&i);
+        if (errf()) return 0.0;
+        m.insert(i);
+        err += i.err - olderr;
+        I += i.I - oldI;
+      } else {
+        Iv9 i1{}, i2{};
+        n += split(&i, &i1, &i2);
+        if (errf()) return 0.0;
+        m.insert(i1);
+        m.insert(i2);
+        num_intervals++;
+        err += i1.err + i2.err - i.err;
+        I += i1.I + i2.I - i.I;
+      }
+      if (num_iterations == 2 * last_check) {
+        err = m.total_err();
+        I = m.total_I();
+        last_check = num_intervals;
+      }
+      num_iterations++;
+    }
+    return m.total_I();
+  }
+};
+
+template <class Fn, class Err>
+double trap_fixed(Fn& f, Err& errf, double xa, double xb, int N) {  // trap (quadratures.h:939-951)
+  double dx = (xb - xa) / N;
+  double fa = f(xa);
+  double I = 0.5 * (fa + f(xb));
+  for (int i = 1; i < N; i++) {
+    I += f(xa + i * dx);
+    if (errf()) return 0.0;
+  }
+  return I * dx;
+}
+
+// findIndex (interpolators.h:13-35)
+size_t find_index(double x, const double* arr, size_t N) {
+  if (x <= arr[0]) return 0;
+  if (x >= arr[N - 1]) return N - 2;
+  unsigned a = 0, b = (unsigned)N - 1;
+  while (b - a > 1u) {
+    unsigned i = (b + a) >> 1;
+    if (arr[i] > x)
+      b = i;
+    else
+      a = i;
+  }
+  return a;
+}
+double seg_lin(size_t a, size_t b, double x, const double* X, const double* Y) {  // interpSegLin (:98-106)
+  return Y[a] + (Y[b] - Y[a]) * (x - X[a]) / (X[b] - X[a]);
+}
+double seg_log(size_t a, size_t b, double x, const double* X, const double* Y) {  // interpSegLog (:114-122)
+  return Y[a] * std::pow(Y[b] / Y[a], std::log(x / X[a]) / std::log(X[b] / X[a]));
+}
+double obs_angle(double theta, double phi, double a) {  // image.h:361-375
+  return std::sin(a) * (std::sin(theta) * std::sin(phi)) + std::cos(a) * std::cos(theta);
+}
+double obs_angle_cj(double theta, double phi, double a) {  // image.h:376-378
+  return std::sin(a) * (std::sin(pi_ - theta) * std::sin(phi)) + std::cos(a) * std::cos(pi_ - theta);
+}
+
+// the state an EATS object holds while it integrates one (layer, t_obs, nu_obs)
+struct EatsRun {
+  const pbag_eats_opts* o;
+  const pbag_eats_layer* L;
+  int nr;
+  const double* dyn;  // [PBAG_EQ_N][nr]
+  const double* nu;
+  int F;
+  const double *J, *A, *Rh;  // histories and their radius rows (the layer's dynamics R)
+  int64_t r_fs, r_rs;        // first history rows of the layer's shocks (r_rs < 0: none)
+  std::vector<double> mu;
+  bool cj = false;
+  double t_obs = 0, nu_obs = 0, phi = 0;
+  long nevals = 0;
+  int code = PBAG_OK;
+  const double* q(int k) const { return dyn + (size_t)k * nr; }
+  double angle(double th, double ph) const { return cj ? obs_angle_cj(th, ph, o->theta_obs) : obs_angle(th, ph, o->theta_obs); }
+
+  // fluxDensAdaptiveWithComov (blastwave_radiation.h:75-150)
+  double flux_a(double theta_in, size_t ia, size_t ib, double mu_, double t_e) {
+    const double* tb = q(PBAG_EQ_TBURST);
+    const double* R = q(PBAG_EQ_R);
+    double r = seg_log(ia, ib, t_e, tb, R);
+    if (r <= 0.0 || !std::isfinite(r)) return 0.0;
+    double Gamma = seg_log(ia, ib, r, R, q(PBAG_EQ_GAMMA));
+    double beta = seg_log(ia, ib, r, R, q(PBAG_EQ_BETA));
+    double GammaShock = seg_log(ia, ib, r, R, q(PBAG_EQ_GAMMA_FSH));
+    double dr = seg_log(ia, ib, r, R, q(PBAG_EQ_THICKNESS));
+    double ne = seg_log(ia, ib, r, R, q(PBAG_EQ_M2)) / m_p;
+    double n_prime = seg_log(ia, ib, r, R, q(PBAG_EQ_RHO2)) / m_p;
+    double rsh = seg_log(ia, ib, r, R, q(PBAG_EQ_RSH));
+    double acc_fac = seg_log(ia, ib, r, R, q(PBAG_EQ_ACC_FRAC));
+    double a = 1.0 - beta * mu_;
+    double delta_D = Gamma * a;
+    double nuprime = (1.0 + o->z) * nu_obs * delta_D;
+    double theta = seg_log(ia, ib, r, R, q(PBAG_EQ_THETA));
+    (void)theta_in;
+    pbag_flux_query fq{};
+    fq.ia = (int)ia;
+    fq.ib = (int)ib;
+    fq.theta = theta;
+    fq.ncells = L->ncells;
+    fq.freq = nuprime;
+    fq.Gamma = Gamma;
+    fq.GammaSh = GammaShock;
+    fq.acc_fac = acc_fac;
+    fq.mu = mu_;
+    fq.r = r;
+    fq.rsh = rsh;
+    fq.dr = dr;
+    fq.n_prime = n_prime;
+    fq.ne = ne;
+    double flux = 0.;
+    int rc = flux_dens_one(nu, F, &o->flux, J, A, Rh, r_fs, fq, &flux);
+    if (rc != PBAG_OK) {
+      code = rc;
+      return 0.0;
+    }
+    if (r_rs >= 0) {
+      const double* th_rs = q(PBAG_EQ_THICKNESS_RS);
+      if (th_rs[ia] > 0 && th_rs[ib] > 0) {
+        fq.GammaSh = seg_log(ia, ib, r, R, q(PBAG_EQ_GAMMA_RSH));
+        fq.dr = seg_log(ia, ib, r, R, th_rs);
+        fq.ne = seg_log(ia, ib, r, R, q(PBAG_EQ_M3)) / m_p;
+        fq.n_prime = seg_log(ia, ib, r, R, q(PBAG_EQ_RHO3)) / m_p;
+        fq.rsh = seg_log(ia, ib, r, R, q(PBAG_EQ_RRSH));
+        fq.acc_fac = seg_log(ia, ib, r, R, q(PBAG_EQ_ACC_FRAC_RS));
+        double frs = 0.;
+        rc = flux_dens_one(nu, F, &o->flux, J, A, Rh, r_rs, fq, &frs);
+        if (rc != PBAG_OK) {
+          code = rc;
+          return 0.0;
+        }
+        flux += frs;
+      }
+    }
+    return flux;
+  }
+  // integrand (eats.h:175-232)
+  double integrand(double i_cos_theta, double i_phi) {
+    const double* R = q(PBAG_EQ_R);
+    const int ie = L->i_end_r;
+    if (R[0] == 0.0 && R[ie - 1] == 0.0) return 0.0;
+    double a_theta = 2.0 * std::asin(std::sqrt(0.5 * (1.0 - i_cos_theta)));  // arccos (image.h:357-360)
+    double mu_ = angle(a_theta, i_phi);
+    if (mu_ < mu[0]) return 0.;
+    if (mu_ > mu[ie - 1]) return 0.;
+    size_t ia = find_index(mu_, mu.data(), ie), ib = ia + 1;
+    double t_e = seg_lin(ia, ib, mu_, mu.data(), q(PBAG_EQ_TBURST));
+    // check_emission_time (eats.h:24-38)
+    if (mu_ > mu[ie - 1] || mu[0] >= mu_) t_e = -1;
+    if (t_e < 0.0 || !std::isfinite(t_e)) return 0.;
+    return flux_a(a_theta, ia, ib, mu_, t_e);
+  }
+  // find_jet_edge (eats.h:103-173)
+  double jet_edge(double ph, double th_con_hi) {
+    const double* thj = q(PBAG_EQ_THETA);
+    const int N = L->i_end_r;
+    double mu_ = angle(th_con_hi, ph);
+    size_t ia = find_index(mu_, mu.data(), N);
+    if (thj[ia] <= th_con_hi && th_con_hi <= thj[ia + 1]) return th_con_hi;
+    double theta_a, theta_b;
+    if (th_con_hi < thj[ia]) {
+      theta_a = th_con_hi;
+      theta_b = 0.5 * pi_;
+    } else {
+      theta_a = 0.0;
+      theta_b = th_con_hi;
+    }
+    int i = 0;
+    while (theta_b - theta_a > 1.0e-5 && i < 100) {
+      double theta_c_i = 0.5 * (theta_a + theta_b);
+      mu_ = angle(theta_c_i, ph);
+      ia = find_index(mu_, mu.data(), N);
+      if (theta_c_i < thj[ia])
+        theta_a = theta_c_i;
+      else
+        theta_b = theta_c_i;
+      i++;
+    }
+    return theta_a;
+  }
+  bool stop() const { return code != PBAG_OK; }
+  // costheta_integrand (eats.h:435-448)
+  double costheta(double aomct) {
+    nevals += 1;
+    if (nevals > (long)1e7) {
+      code = PBAG_ERR_EVALS;
+      return 0.0;
+    }
+    return integrand(1 - aomct, phi);
+  }
+  // phi_integrand (eats.h:449-586)
+  double phi_integrand(double a_phi) {
+    phi = a_phi;
+    double theta_1 = L->theta_c_h, theta_0 = L->theta_c_l;
+    double th_1 = jet_edge(a_phi, theta_1);
+    double frac = theta_0 / theta_1;
+    double th_0 = frac * th_1;
+    theta_0 = th_0;
+    theta_1 = th_1;
+    if (theta_0 > 0.5 * pi_) theta_0 = 0.5 * pi_;
+    if (theta_1 > 0.5 * pi_) theta_1 = 0.5 * pi_;
+    double s0 = std::sin(0.5 * theta_0), s1 = std::sin(0.5 * theta_1);
+    double omc0 = 2.0 * s0 * s0, omc1 = 2.0 * s1 * s1;
+    auto fth = [&](double x) { return costheta(x); };
+    auto st = [&]() { return stop(); };
+    double result;
+    if (o->method_quad == PBAG_QUAD_TRAP_FIXED) {
+      result = trap_fixed(fth, st, omc0, omc1, o->nmax_theta);
+    } else {
+      Cadre<decltype(fth), decltype(st)> c{fth, st};
+      result = c.adapt(omc0, omc1, o->nmax_theta, 0.0, o->rtol_theta);
+    }
+    if (result != result || result < 0.0) return 0.;
+    if (nevals > (long)1e7) {
+      code = PBAG_ERR_EVALS;
+      return 0.;
+    }
+    return result;
+  }
+  // integrate_theta_phi (eats.h:587-700)
+  double theta_phi() {
+    nevals = 0;
+    double Fcoeff = cgs2mJy / (4 * pi_ * o->d_l * o->d_l);
+    auto fph = [&](double x) { return phi_integrand(x); };
+    auto st = [&]() { return stop(); };
+    if (o->method_quad == PBAG_QUAD_TRAP_FIXED) return 2 * Fcoeff * trap_fixed(fph, st, 0.0, pi_, o->nmax_phi);
+    Cadre<decltype(fph), decltype(st)> c{fph, st};
+    return 2 * Fcoeff * c.adapt(0.0, pi_, o->nmax_phi, 0.0, o->rtol_phi);
+  }
+  // parsPars' mu array (eats.h:941-947)
+  void set_mu() {
+    const double* tb = q(PBAG_EQ_TBURST);
+    const double* R = q(PBAG_EQ_R);
+    mu.assign((size_t)nr, 0.0);
+    for (int i = 0; i < L->i_end_r; i++) mu[i] = (tb[i] - t_obs / (1.0 + o->z)) / R[i] * c_light;
+  }
+};
+
+}  // namespace
+
+extern "C" int orc_eats_flux(const pbag_grid_desc* g, const pbag_eats_opts* o, int nl, const pbag_eats_layer* layers,
+                             int nr, const double* dyn, const int64_t* offsets, const double* j_all,
+                             const double* a_all, int nq, const pbag_eats_query* qs, double* flux, int* fail_index) {
+  const int F = g->nfreq;
+  std::vector<double> gam(g->ngam), nu(F + 1);
+  orc_build_grids(g, gam.data(), nu.data());
+  *fail_index = -1;
+  // the fluxDens radius rows of every history row: the layer's dynamics R
+  int64_t nrec = 0;
+  for (int l = 0; l < nl; ++l) {
+    nrec = std::max<int64_t>(nrec, offsets[layers[l].bw_fs + 1]);
+    if (layers[l].bw_rs >= 0) nrec = std::max<int64_t>(nrec, offsets[layers[l].bw_rs + 1]);
+  }
+  std::vector<double> Rh((size_t)nrec, 0.0);
+  for (int l = 0; l < nl; ++l) {
+    const double* R = dyn + ((size_t)l * PBAG_EQ_N + PBAG_EQ_R) * nr;
+    for (int b : {layers[l].bw_fs, layers[l].bw_rs}) {
+      if (b < 0) continue;
+      for (int64_t k = 0; k < offsets[b + 1] - offsets[b] && k < nr; ++k) Rh[offsets[b] + k] = R[k];
+    }
+  }
+  for (int t = 0; t < nq; ++t) {
+    const pbag_eats_query& qq = qs[t];
+    const pbag_eats_layer& L = layers[qq.layer];
+    const double* tb = dyn + ((size_t)qq.layer * PBAG_EQ_N + PBAG_EQ_TBURST) * nr;
+    if (L.i_end_r > 0 && (qq.t_obs < tb[0] || qq.t_obs > tb[L.i_end_r - 1])) {  // eats.h:822-827
+      flux[t] = 0.;
+      *fail_index = t;
+      return PBAG_ERR_RANGE;
+    }
+    EatsRun e{o, &L, nr, dyn + (size_t)qq.layer * PBAG_EQ_N * nr, nu.data(), F, j_all, a_all, Rh.data(),
+              offsets[L.bw_fs], L.bw_rs >= 0 ? offsets[L.bw_rs] : -1};
+    e.t_obs = qq.t_obs;
+    e.nu_obs = qq.nu_obs;
+    e.set_mu();
+    double fd = e.theta_phi();  // evalFluxDensA: the principal jet
+    if (o->counter_jet && e.code == PBAG_OK) {
+      e.cj = true;
+      e.set_mu();
+      fd += e.theta_phi();
+    }
+    flux[t] = fd;
+    if (e.code != PBAG_OK) {
+      flux[t] = 0.;
+      *fail_index = t;
+      return e.code;
+    }
+  }
   return PBAG_OK;
 }

@@ -67,6 +67,14 @@ int orc_run(const pbag_grid_desc* g, const pbag_shock_params* prm, int nbw, cons
             const pbag_step_rec* recs, pbag_outputs* out, int flags, int outer_threads,
             int inner_threads, pbag_status* st);
 
+/* Adaptive EATS light curve of nl layers (pbag_eats_flux_a's inputs on the
+ * host): flux[q] in mJy for every query; histories j_all / a_all of the
+ * blastwaves the layers name (offsets as for orc_run). Returns PBAG_OK or the
+ * first failure (*fail_index = its query). */
+int orc_eats_flux(const pbag_grid_desc* g, const pbag_eats_opts* o, int nl, const pbag_eats_layer* layers, int nr,
+                  const double* dyn, const int64_t* offsets, const double* j_all, const double* a_all, int nq,
+                  const pbag_eats_query* qs, double* flux, int* fail_index);
+
 #ifdef __cplusplus
 }
 #endif

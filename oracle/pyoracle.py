@@ -6,6 +6,8 @@
 * ``Reference`` wraps oracle/_ref/libpbaref.so, the reference's own
   src/microphysics headers compiled in place (``make -C oracle ref``; only
   where the reference sources exist).
+* ``ReferenceEats`` wraps oracle/_ref/libpbaref_eats.so, the reference's EATS
+  integrator compiled in place with its blastwave headers (same target).
 
 Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
 """
@@ -20,6 +22,7 @@ from pyblastafterglowmag_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpbag_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpbaref.so")
+REF_EATS_SO = os.path.join(HERE, "_ref", "libpbaref_eats.so")
 # the reference project's src/ directory: PBAG_REF_SRC, else a checkout named
 # "reference" next to this repository
 REF_SRC = os.environ.get("PBAG_REF_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")
@@ -69,7 +72,24 @@ class Oracle:
                                       P(C.c_double), C.c_int, C.c_void_p, P(C.c_double), P(C.c_int)]
         lib.orc_shock_limits.argtypes = [P(abi.LimitsOpts), P(C.c_double), C.c_int, C.c_int, C.c_void_p,
                                          P(C.c_double), C.c_void_p]
+        lib.orc_eats_flux.argtypes = [P(abi.GridDesc), P(abi.EatsOpts), C.c_int, C.c_void_p, C.c_int,
+                                      P(C.c_double), P(C.c_int64), P(C.c_double), P(C.c_double), C.c_int,
+                                      C.c_void_p, P(C.c_double), P(C.c_int)]
         self.lib = lib
+
+    def eats_flux(self, grid, opts, layers, dyn, offsets, j_all, a_all, queries):
+        """orc_eats_flux: (status, failing query, flux[nq] in mJy)."""
+        layers = np.ascontiguousarray(layers, dtype=abi.EATS_LAYER_DTYPE)
+        dyn = np.ascontiguousarray(dyn, dtype=np.float64)
+        q = np.ascontiguousarray(queries, dtype=abi.EATS_QUERY_DTYPE)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        flux = np.zeros(len(q))
+        fail = C.c_int(-1)
+        rc = self.lib.orc_eats_flux(C.byref(grid), C.byref(opts), len(layers), layers.ctypes.data, dyn.shape[-1],
+                                    abi.dptr(dyn), off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                    abi.dptr(np.ascontiguousarray(j_all)), abi.dptr(np.ascontiguousarray(a_all)),
+                                    len(q), q.ctypes.data, abi.dptr(flux), C.byref(fail))
+        return rc, fail.value, flux
 
     def shock_limits(self, opts, gam, states, state=None):
         """orc_shock_limits over a sequence of shock states of one blastwave
@@ -250,3 +270,40 @@ class Reference:
                          offsets.ctypes.data_as(C.POINTER(C.c_int64)), recs.ctypes.data,
                          C.byref(out))
         return arrays
+
+
+class ReferenceEats:
+    """The reference's EATS::evalFluxDensA on one layer at a time."""
+
+    def __init__(self, path=REF_EATS_SO):
+        if not os.path.exists(path) and not build_reference():
+            raise FileNotFoundError("reference sources not available")
+        lib = C.CDLL(path)
+        P = C.POINTER
+        lib.ref_eats_flux.argtypes = [P(abi.GridDesc), P(abi.EatsOpts), C.c_void_p, C.c_int, P(C.c_double),
+                                      P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double), C.c_int,
+                                      P(C.c_double), P(C.c_double), P(C.c_double)]
+        self.lib = lib
+
+    def eats_flux(self, grid, opts, layers, dyn, offsets, j_all, a_all, queries):
+        """flux[nq] in mJy, layer by layer (the same inputs as Oracle.eats_flux)."""
+        q = np.ascontiguousarray(queries, dtype=abi.EATS_QUERY_DTYPE)
+        flux = np.zeros(len(q))
+        nr = dyn.shape[-1]
+        for l in np.unique(q["layer"]):
+            L = np.ascontiguousarray(layers[l:l + 1], dtype=abi.EATS_LAYER_DTYPE)
+            sel = np.flatnonzero(q["layer"] == l)
+            rows = lambda b: (offsets[b], offsets[b] + nr)
+            bf, br = int(L["bw_fs"][0]), int(L["bw_rs"][0])
+            jf = np.ascontiguousarray(j_all[slice(*rows(bf))])
+            af = np.ascontiguousarray(a_all[slice(*rows(bf))])
+            jr = np.ascontiguousarray(j_all[slice(*rows(br))]) if br >= 0 else None
+            ar = np.ascontiguousarray(a_all[slice(*rows(br))]) if br >= 0 else None
+            t = np.ascontiguousarray(q["t_obs"][sel])
+            nu = np.ascontiguousarray(q["nu_obs"][sel])
+            out = np.zeros(len(sel))
+            self.lib.ref_eats_flux(C.byref(grid), C.byref(opts), L.ctypes.data, nr,
+                                   abi.dptr(np.ascontiguousarray(dyn[l])), abi.dptr(jf), abi.dptr(af),
+                                   abi.dptr(jr), abi.dptr(ar), len(sel), abi.dptr(t), abi.dptr(nu), abi.dptr(out))
+            flux[sel] = out
+        return flux

@@ -101,6 +101,24 @@ def flux_dens(ctx, opts, offsets, d_j_all, d_a_all, d_r_all, nq, d_q, d_flux):
                               C.c_void_p(d_q), C.c_void_p(d_flux), C.byref(st)), "pbag_flux_dens", st)
 
 
+def eats_flux_a(ctx, opts, layers, d_dyn, nr, offsets, d_j_all, d_a_all, nq, d_q, d_flux):
+    """pbag_eats_flux_a: the adaptive EATS flux density [mJy] of nq (layer,
+    t_obs, nu_obs) queries. layers: host EATS_LAYER_DTYPE array; d_dyn
+    [nlayers][PBAG_EQ_N][nr], d_j_all / d_a_all, d_q, d_flux: device
+    addresses; offsets: host int64 array of nbw+1."""
+    lib = load()
+    lib.pbag_eats_flux_a.argtypes = [C.c_void_p, C.POINTER(abi.EatsOpts), C.c_int, C.c_void_p, C.c_int,
+                                     C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.c_void_p, C.c_void_p, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.POINTER(abi.Status)]
+    layers = np.ascontiguousarray(layers, dtype=abi.EATS_LAYER_DTYPE)
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    st = abi.Status()
+    _check(lib.pbag_eats_flux_a(ctx.handle, C.byref(opts), len(layers), layers.ctypes.data, int(nr),
+                                C.c_void_p(d_dyn), len(off) - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                C.c_void_p(d_j_all), C.c_void_p(d_a_all), int(nq), C.c_void_p(d_q),
+                                C.c_void_p(d_flux), C.byref(st)), "pbag_eats_flux_a", st)
+
+
 def autotune(enable=True):
     """Switch the contraction autotuner (pbag_autotune) on or off."""
     lib = load()

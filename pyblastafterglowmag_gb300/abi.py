@@ -18,6 +18,7 @@ PBAG_ERR_UNSUPPORTED = -7
 PBAG_ERR_TIMEOUT = -8
 PBAG_ERR_NOMEM = -9
 PBAG_ERR_RANGE = -10
+PBAG_ERR_EVALS = -11
 
 STATUS_NAMES = {
     PBAG_OK: "ok",
@@ -31,6 +32,7 @@ STATUS_NAMES = {
     PBAG_ERR_TIMEOUT: "device wait timed out",
     PBAG_ERR_RANGE: "frequency outside the grid",
     PBAG_ERR_NOMEM: "device allocation failed",
+    PBAG_ERR_EVALS: "EATS quadrature past 1e7 integrand evaluations",
 }
 
 PBAG_SKIP, PBAG_INIT, PBAG_EVOLVE = 0, 1, 2
@@ -142,3 +144,24 @@ class FluxOpts(C.Structure):
 FLUX_QUERY_DTYPE = np.dtype([("bw", np.int32), ("ia", np.int32), ("ib", np.int32), ("pad", np.int32)] +
                             [(f, np.float64) for f in ("theta", "ncells", "freq", "Gamma", "GammaSh", "acc_fac",
                                                         "mu", "r", "rsh", "dr", "n_prime", "ne")])
+
+
+# ---- adaptive EATS light curve (pbag_eats_flux_a) ------------------------------
+PBAG_QUAD_CADRE, PBAG_QUAD_TRAP_FIXED = 0, 1
+# the dynamics of a layer, in the order of enum pbag_eats_q
+EATS_Q = ("tburst", "R", "theta", "Gamma", "beta", "GammaFsh", "thickness", "M2", "rho2", "Rsh", "acc_frac",
+          "ctheta", "GammaRsh", "thickness_rs", "M3", "rho3", "Rrsh", "acc_frac_rs")
+PBAG_EQ_N = len(EATS_Q)
+
+
+class EatsOpts(C.Structure):
+    _fields_ = [("theta_obs", C.c_double), ("z", C.c_double), ("d_l", C.c_double),
+                ("rtol_theta", C.c_double), ("rtol_phi", C.c_double),
+                ("nmax_theta", C.c_int32), ("nmax_phi", C.c_int32),
+                ("method_quad", C.c_int32), ("counter_jet", C.c_int32),
+                ("flux", FluxOpts)]
+
+
+EATS_LAYER_DTYPE = np.dtype([("i_end_r", np.int32), ("bw_fs", np.int32), ("bw_rs", np.int32), ("pad", np.int32),
+                             ("theta_c_l", np.float64), ("theta_c_h", np.float64), ("ncells", np.float64)])
+EATS_QUERY_DTYPE = np.dtype([("layer", np.int32), ("pad", np.int32), ("t_obs", np.float64), ("nu_obs", np.float64)])

@@ -1,0 +1,692 @@
+// pbag_eats.cu - the adaptive EATS light curve (method_eats = "adaptive") on
+// the GPU, from the layer dynamics and the comoving histories the step left
+// on the device.
+//
+// One work item = one (query, jet side): the principal jet and, with
+// counter_jet, the counter jet are separate items (their sum is taken in the
+// reference's order at the end), each a nested quadrature run by one thread:
+// phi in [0, pi] outside, 1 - cos(theta) inside (integrate_theta_phi,
+// eats.h:587-700; phi_integrand :449-586 with find_jet_edge :103-173;
+// costheta_integrand :435-448), by CADRE - m9_adapt with the cautious Romberg
+// interval rules and a max-heap of intervals on the error (quadratures.h:
+// 1613-2113, 657-770) - or by the fixed trapezoid rule (:939-951). The
+// integrand (eats.h:175-232) finds the emission time of a direction on the
+// item's mu array, interpolates the dynamics log-linearly in radius
+// (fluxDensAdaptiveWithComov, blastwave_radiation.h:75-150) and evaluates
+// fluxDens (microphysics.h:1185-1217) on the forward- and reverse-shock
+// histories.
+//
+// GB300 layout: every FP64 quantity that does not depend on the direction is
+// computed once, in parallel, before the quadratures: each item's mu array
+// (nr divisions) and, per layer and segment, the logarithms of the ratios of
+// neighbouring dynamics values, so that each log-linear interpolation is one
+// exp (ya exp(t ln(yb/ya)), t = ln(x/xa) / ln(xb/xa)) instead of a pow and two
+// logs; t is formed once per radius and shared by every quantity. The
+// intervals of both quadrature levels live in a per-item workspace in global
+// memory (nmax + 8 intervals per level); an item whose integration would need
+// more stops with PBAG_ERR_NOMEM instead of growing it.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "pbag.h"
+#include "pbag_const.h"
+#include "pbag_ctx_view.h"
+#include "pbag_device.cuh"
+
+namespace pbag {
+namespace {
+
+constexpr int kEatsThreads = 64;
+constexpr long kMaxEvals = 10000000L;  // eats.h:536-541
+// dynamics interpolated log-linearly in radius, in their pbag_eats_q order
+__constant__ const int kLogQ[] = {PBAG_EQ_GAMMA,     PBAG_EQ_BETA,         PBAG_EQ_GAMMA_FSH, PBAG_EQ_THICKNESS,
+                         PBAG_EQ_M2,        PBAG_EQ_RHO2,         PBAG_EQ_RSH,       PBAG_EQ_ACC_FRAC,
+                         PBAG_EQ_THETA,     PBAG_EQ_GAMMA_RSH,    PBAG_EQ_THICKNESS_RS, PBAG_EQ_M3,
+                         PBAG_EQ_RHO3,      PBAG_EQ_RRSH,         PBAG_EQ_ACC_FRAC_RS};
+constexpr int kNLog = 15;
+static_assert(sizeof(kLogQ) == kNLog * sizeof(int), "kNLog counts kLogQ");
+enum : int { kLnR = kNLog, kLnT = kNLog + 1, kNLn = kNLog + 2 };  // ln(R ratio), ln(t_burst ratio)
+
+struct Iv9 {  // an interval of CADRE: f[] = fa, fll, fl, flr, fm, frl, fr, frr, fb
+  double a, b, I, err;
+  double f[9];
+  int refinement;
+};
+
+struct Heap {  // max-heap on err
+  Iv9* h;
+  int n, cap;
+  __device__ bool insert(const Iv9& v) {
+    if (n >= cap) return false;
+    int c = n++;
+    h[c] = v;
+    while (c != 0) {
+      const int p = (c - 1) / 2;
+      if (!(h[p].err < h[c].err)) break;
+      const Iv9 t = h[p];
+      h[p] = h[c];
+      h[c] = t;
+      c = p;
+    }
+    return true;
+  }
+  __device__ void extract(Iv9* w) {
+    *w = h[0];
+    h[0] = h[n - 1];
+    --n;
+    int p = 0;
+    for (;;) {
+      const int c1 = 2 * p + 1, c2 = c1 + 1;
+      if (c1 >= n) break;
+      int c = c1;
+      double e = h[c1].err;
+      if (c2 < n && h[c2].err > e) {
+        c = c2;
+        e = h[c2].err;
+      }
+      if (e <= h[p].err) break;
+      const Iv9 t = h[p];
+      h[p] = h[c];
+      h[c] = t;
+      p = c;
+    }
+  }
+  __device__ double total_I() const {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += h[i].I;
+    return s;
+  }
+  __device__ double total_err() const {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += h[i].err;
+    return s;
+  }
+};
+
+// findIndex (interpolators.h:13-35)
+__device__ int find_index(double x, const double* __restrict__ a, int n) {
+  if (x <= a[0]) return 0;
+  if (x >= a[n - 1]) return n - 2;
+  unsigned lo = 0, hi = (unsigned)n - 1;
+  while (hi - lo > 1u) {
+    const unsigned m = (hi + lo) >> 1;
+    if (a[m] > x)
+      hi = m;
+    else
+      lo = m;
+  }
+  return (int)lo;
+}
+
+__device__ __forceinline__ double beta_from_gamma(double g) { return sqrt((g - 1.) * (g + 1.)) / g; }
+
+// computeIntensity (microphysics.h:11-58)
+__device__ double intensity_of(double em, double dtau, int method) {
+  if (dtau == 0) return em;
+  switch (method) {
+    case PBAG_TAU_THICK:
+      return dtau > 0 ? em / dtau : 0.;
+    case PBAG_TAU_SMOOTH:
+      return em * (dtau > 0.0 ? -expm1(-dtau) / dtau : expm1(dtau) / dtau);
+    case PBAG_TAU_SHARP:
+      return dtau > 1.0 ? em / dtau : dtau < -1.0 ? 0.0 : em;
+    default: {
+      if (!(dtau > 1.e-3)) return em;
+      const double e = exp(-dtau);
+      const double u = 1. / 2. + e / dtau - (1 - e) / (dtau * dtau);
+      return em * (3. * u / dtau);
+    }
+  }
+}
+
+struct EatsArgs {
+  pbag_eats_opts o;
+  int nr, F;
+  const double* nu;         // [F] photon grid
+  const double* dyn;        // [nl][PBAG_EQ_N][nr]
+  const double* ln;         // [nl][kNLn][nr]: ln(y[i+1]/y[i]) of the interpolated quantities
+  const pbag_eats_layer* layers;
+  const int64_t* off;       // history rows of the batch's blastwaves
+  const double* j_all;
+  const double* a_all;
+  const pbag_eats_query* q;
+  int nq, sides;
+  double* mu;               // [items][nr]
+  Iv9* ws;                  // [items][cap_phi + cap_theta]
+  int cap_phi, cap_theta;
+  double* part;             // [items]
+  unsigned long long* first;
+};
+
+// The EATS object of one work item.
+struct Eats {
+  const EatsArgs& A;
+  const pbag_eats_layer L;
+  const double* dyn;
+  const double* ln;
+  const double* mu;
+  int64_t r_fs, r_rs;
+  double t_obs, nu_obs, phi = 0., sin_obs, cos_obs;
+  bool cj;
+  long nevals = 0;
+  int code = PBAG_OK;
+  Heap inner;
+
+  __device__ const double* qv(int k) const { return dyn + (size_t)k * A.nr; }
+  __device__ double angle(double th, double ph) const {  // obsAngle / obsAngleCJ (image.h:361-378)
+    const double t = cj ? cgs::pi_ - th : th;
+    return sin_obs * (sin(t) * sin(ph)) + cos_obs * cos(t);
+  }
+  // ya (yb/ya)^t with ln(yb/ya) from the table
+  __device__ double seg(int li, int a, double t) const { return qv(kLogQ[li])[a] * exp(t * ln[(size_t)li * A.nr + a]); }
+
+  // fluxDens (microphysics.h:1185-1217) + computeFluxDensity (:799-867) on the
+  // history rows r0 + ia, r0 + ib
+  __device__ double flux_dens(int64_t r0, int ia, int ib, double freq, double theta, double Gamma, double GammaSh,
+                              double mu_, double r, double n_prime, double ne, const double* R) {
+    const int F = A.F;
+    const double* nu = A.nu;
+    if (freq >= nu[F - 1] || freq <= nu[0]) {
+      code = PBAG_ERR_RANGE;
+      return 0.;
+    }
+    const int ia_nu = find_index(freq, nu, F), ib_nu = ia_nu + 1;
+    const double* ja = A.j_all + (size_t)(r0 + ia) * F;
+    const double* jb = A.j_all + (size_t)(r0 + ib) * F;
+    const double* aa = A.a_all + (size_t)(r0 + ia) * F;
+    const double* ab = A.a_all + (size_t)(r0 + ib) * F;
+    const double x1 = nu[ia_nu], x2 = nu[ib_nu], y1 = R[ia], y2 = R[ib];
+    const double x2x1 = x2 - x1, y2y1 = y2 - y1, x2x = x2 - freq, y2y = y2 - r, yy1 = r - y1, xx1 = freq - x1;
+    const double w = 1.0 / (x2x1 * y2y1);
+    const double em_prime = w * (ja[ia_nu] * x2x * y2y + ja[ib_nu] * xx1 * y2y + jb[ia_nu] * x2x * yy1 +
+                                 jb[ib_nu] * xx1 * yy1);
+    const double abs_prime = w * (aa[ia_nu] * x2x * y2y + aa[ib_nu] * xx1 * y2y + ab[ia_nu] * x2x * yy1 +
+                                  ab[ib_nu] * xx1 * yy1);
+    const double beta = beta_from_gamma(Gamma);
+    const double delta_D = Gamma * (1.0 - beta * mu_);
+    const double em_lab = em_prime / (delta_D * delta_D);
+    const double abs_lab = abs_prime * delta_D;
+    const double beta_shock = beta_from_gamma(A.o.flux.shock_vel == PBAG_VEL_SHOCK ? GammaSh : Gamma);
+    const double ring = 1. - cos(theta) / L.ncells;
+    const double dr = ne * cgs::m_p / (2. * cgs::pi_ * cgs::m_p * r * r * ring * Gamma * n_prime);
+    const double dtau = mu_ == beta_shock ? 1.0e100 : abs_lab * dr * (1. - mu_ * beta_shock) / (mu_ - beta_shock);
+    const double intensity = intensity_of(em_lab, dtau, A.o.flux.method_tau);
+    if (intensity < 0 || !isfinite(intensity)) {
+      code = PBAG_ERR_NONFINITE;
+      return 0.;
+    }
+    const double ashock = 1.0 - mu_ * beta_shock;
+    const double lum = A.o.flux.method_ne == PBAG_NE_USE_NPRIME
+                           ? intensity * r * r * (dr / ashock)
+                           : intensity * ne / (2. * cgs::pi_ * ring) / Gamma / ashock;
+    if (lum < 0 || !isfinite(lum)) {
+      code = PBAG_ERR_NONFINITE;
+      return 0.;
+    }
+    return lum;
+  }
+
+  // the integrand (eats.h:175-232) with fluxDensAdaptiveWithComov
+  __device__ double integrand(double i_cos_theta, double i_phi) {
+    const double* R = qv(PBAG_EQ_R);
+    const int ie = L.i_end_r;
+    if (R[0] == 0.0 && R[ie - 1] == 0.0) return 0.0;
+    const double a_theta = 2.0 * asin(sqrt(0.5 * (1.0 - i_cos_theta)));
+    const double m = angle(a_theta, i_phi);
+    if (m < mu[0] || m > mu[ie - 1]) return 0.;
+    const int ia = find_index(m, mu, ie), ib = ia + 1;
+    const double* tb = qv(PBAG_EQ_TBURST);
+    double t_e = tb[ia] + (tb[ib] - tb[ia]) * (m - mu[ia]) / (mu[ib] - mu[ia]);
+    if (mu[0] >= m) t_e = -1;  // check_emission_time (eats.h:24-38)
+    if (t_e < 0.0 || !isfinite(t_e)) return 0.;
+    // radius at t_e, then every quantity at that radius
+    const double r = R[ia] * exp(log(t_e / tb[ia]) / ln[(size_t)kLnT * A.nr + ia] * ln[(size_t)kLnR * A.nr + ia]);
+    if (r <= 0.0 || !isfinite(r)) return 0.0;
+    const double t = log(r / R[ia]) / ln[(size_t)kLnR * A.nr + ia];
+    const double Gamma = seg(0, ia, t), beta = seg(1, ia, t), GammaSh = seg(2, ia, t);
+    const double ne = seg(4, ia, t) / cgs::m_p, n_prime = seg(5, ia, t) / cgs::m_p;
+    const double theta = seg(8, ia, t);
+    const double nuprime = (1.0 + A.o.z) * nu_obs * (Gamma * (1.0 - beta * m));
+    double flux = flux_dens(r_fs, ia, ib, nuprime, theta, Gamma, GammaSh, m, r, n_prime, ne, R);
+    if (code != PBAG_OK) return 0.;
+    if (r_rs >= 0) {
+      const double* th_rs = qv(PBAG_EQ_THICKNESS_RS);
+      if (th_rs[ia] > 0 && th_rs[ib] > 0) {
+        const double fr = flux_dens(r_rs, ia, ib, nuprime, theta, Gamma, seg(9, ia, t), m, r,
+                                    seg(12, ia, t) / cgs::m_p, seg(11, ia, t) / cgs::m_p, R);
+        if (code != PBAG_OK) return 0.;
+        flux += fr;
+      }
+    }
+    return flux;
+  }
+
+  // find_jet_edge (eats.h:103-173)
+  __device__ double jet_edge(double ph, double th_con_hi) const {
+    const double* thj = qv(PBAG_EQ_THETA);
+    const int N = L.i_end_r;
+    int ia = find_index(angle(th_con_hi, ph), mu, N);
+    if (thj[ia] <= th_con_hi && th_con_hi <= thj[ia + 1]) return th_con_hi;
+    double theta_a, theta_b;
+    if (th_con_hi < thj[ia]) {
+      theta_a = th_con_hi;
+      theta_b = 0.5 * cgs::pi_;
+    } else {
+      theta_a = 0.0;
+      theta_b = th_con_hi;
+    }
+    for (int i = 0; theta_b - theta_a > 1.0e-5 && i < 100; ++i) {
+      const double c = 0.5 * (theta_a + theta_b);
+      ia = find_index(angle(c, ph), mu, N);
+      if (c < thj[ia])
+        theta_a = c;
+      else
+        theta_b = c;
+    }
+    return theta_a;
+  }
+
+  __device__ bool stop() const { return code != PBAG_OK; }
+
+  // CADRE (m9_adapt with the cautious Romberg interval rules) over f
+  template <class Fn>
+  __device__ int process(Fn& f, Iv9* i) {
+    const double scaleTol = 0.2;
+    int count = 0;
+    if (i->refinement < 4) {
+      const double fa = i->f[0], fm = i->f[4], fb = i->f[8];
+      double fl, fr;
+      if (i->refinement == 0) {
+        fl = f(0.75 * i->a + 0.25 * i->b);
+        count++;
+        if (stop()) return count;
+        fr = f(0.25 * i->a + 0.75 * i->b);
+        count++;
+        if (stop()) return count;
+        i->f[2] = fl;
+        i->f[6] = fr;
+      } else {
+        fl = i->f[2];
+        fr = i->f[6];
+        i->refinement = 0;
+      }
+      const double h = 0.25 * (i->b - i->a);
+      const double T0 = 2 * h * (fa + fb);
+      const double T1 = 0.5 * T0 + 2 * h * fm;
+      const double T2 = 0.5 * T1 + h * (fl + fr);
+      const double R0 = (T1 - T0) / (T2 - T1);
+      if (R0 > 4 - scaleTol && R0 < 4 + scaleTol) {
+        const double x[4] = {0.875 * i->a + 0.125 * i->b, 0.625 * i->a + 0.375 * i->b,
+                             0.375 * i->a + 0.625 * i->b, 0.125 * i->a + 0.875 * i->b};
+        double v[4];
+        for (int k = 0; k < 4; ++k) {
+          v[k] = f(x[k]);
+          count++;
+          if (stop()) return count;
+        }
+        i->f[1] = v[0];
+        i->f[3] = v[1];
+        i->f[5] = v[2];
+        i->f[7] = v[3];
+        i->refinement = 1;
+        const double T3 = 0.5 * T2 + 0.5 * h * (v[0] + v[1] + v[2] + v[3]);
+        const double R1 = (T2 - T1) / (T3 - T2);
+        if (R1 > 4 - scaleTol && R1 < 4 + scaleTol) {
+          const double R11 = (4 * T1 - T0) / 3.0;
+          const double R21 = (4 * T2 - T1) / 3.0;
+          const double R22 = (16 * R21 - R11) / 15.0;
+          i->f[0] = T3;
+          i->f[1] = (4 * T3 - T2) / 3.0;
+          i->f[2] = (16 * i->f[1] - R21) / 15.0;
+          i->f[3] = (64 * i->f[2] - R22) / 63.0;
+          i->I = i->f[3];
+          i->err = fabs((i->f[2] - R22) / 63.0);
+          i->refinement = 4;
+          return count;
+        }
+        const double errt = (T3 - T2) / 3.0;
+        i->err = fabs(errt);
+        i->I = T3 + errt;
+        return count;
+      }
+      if (R0 >= 4 + scaleTol || R0 < 2 || R0 != R0) {
+        const double e10 = fabs(T1 - T0), e21 = fabs(T2 - T1);
+        i->err = e10 > e21 ? e10 : e21;
+        i->I = T2;
+        return count;
+      }
+      const double err = -(T2 - T1) * (T2 - T1) / (T2 - 2 * T1 + T0);
+      i->err = fabs(err);
+      i->I = fabs(T2 + err) < 1.0e-14 * fabs(T2) ? 1.0e-14 * T2 : T2 + err;
+      return count;
+    }
+    // Romberg mode: one more level of the tableau held in f[]
+    int nint = 1;
+    for (int n = 0; n < i->refinement; n++) nint *= 2;
+    const double h = (i->b - i->a) / nint;
+    double sum = 0;
+    for (int n = 1; n < nint; n += 2) {
+      sum += f(i->a + h * n);
+      count++;
+      if (stop()) return count;
+    }
+    double Rnm = i->f[0], Rnmp = i->f[1];
+    i->f[0] = 0.5 * i->f[0] + h * sum;
+    i->f[1] = (4.0 * i->f[0] - Rnm) / 3.0;
+    if (i->refinement == 1) {
+      i->I = i->f[1];
+      i->err = fabs((i->f[0] - Rnm) / 3.0);
+      i->refinement += 1;
+      return count;
+    }
+    double pw = 4.0;
+    for (int m = 2; m <= 8; ++m) {
+      pw *= 4.0;
+      Rnm = Rnmp;
+      Rnmp = i->f[m];
+      i->f[m] = (pw * i->f[m - 1] - Rnm) / (pw - 1.0);
+      if (i->refinement == m) {
+        i->I = i->f[m];
+        i->err = fabs((i->f[m - 1] - Rnm) / (pw - 1.0));
+        i->refinement += 1;
+        return count;
+      }
+    }
+    i->I = (262144 * i->f[8] - Rnmp) / 262143.0;
+    i->err = fabs((i->f[8] - Rnmp) / 262143.0);
+    i->refinement += 1;
+    return count;
+  }
+
+  template <class Fn>
+  __device__ double cadre(Fn& f, double xa, double xb, int nmax, double rtol, Heap& m) {
+    m.n = 0;
+    Iv9 i{};
+    i.a = xa;
+    i.b = xb;
+    i.f[0] = f(xa);
+    if (stop()) return 0.0;
+    i.f[8] = f(xb);
+    if (stop()) return 0.0;
+    i.f[4] = f(0.5 * (xa + xb));
+    if (stop()) return 0.0;
+    int n = 3 + process(f, &i);
+    if (stop()) return 0.0;
+    m.insert(i);
+    double I = i.I, err = i.err;
+    int num_intervals = 1, num_iterations = 0, last_check = 0;
+    while (n < nmax && err > rtol * fabs(I)) {  // atol 0
+      m.extract(&i);
+      if (i.refinement >= 4) {
+        const double oldI = i.I, olderr = i.err;
+        n += process(f, &i);
+        if (stop()) return 0.0;
+        m.insert(i);
+        err += i.err - olderr;
+        I += i.I - oldI;
+      } else {
+        Iv9 i1{}, i2{};
+        const double xm = 0.5 * (i.a + i.b);
+        i1.a = i.a;
+        i1.b = xm;
+        i2.a = xm;
+        i2.b = i.b;
+        i1.f[0] = i.f[0];
+        i1.f[2] = i.f[1];
+        i1.f[4] = i.f[2];
+        i1.f[6] = i.f[3];
+        i1.f[8] = i.f[4];
+        i1.refinement = i.refinement;
+        i2.f[0] = i.f[4];
+        i2.f[2] = i.f[5];
+        i2.f[4] = i.f[6];
+        i2.f[6] = i.f[7];
+        i2.f[8] = i.f[8];
+        i2.refinement = i.refinement;
+        n += process(f, &i1);
+        n += process(f, &i2);
+        if (stop()) return 0.0;
+        if (!m.insert(i1) || !m.insert(i2)) {
+          code = PBAG_ERR_NOMEM;
+          return 0.0;
+        }
+        num_intervals++;
+        err += i1.err + i2.err - i.err;
+        I += i1.I + i2.I - i.I;
+      }
+      if (num_iterations == 2 * last_check) {
+        err = m.total_err();
+        I = m.total_I();
+        last_check = num_intervals;
+      }
+      num_iterations++;
+    }
+    return m.total_I();
+  }
+
+  template <class Fn>
+  __device__ double trap(Fn& f, double xa, double xb, int N) {
+    const double dx = (xb - xa) / N;
+    const double fa = f(xa);
+    double I = 0.5 * (fa + f(xb));
+    for (int i = 1; i < N; i++) {
+      I += f(xa + i * dx);
+      if (stop()) return 0.0;
+    }
+    return I * dx;
+  }
+
+  // phi_integrand (eats.h:449-586): the inner integral over 1 - cos(theta)
+  __device__ double phi_integrand(double a_phi) {
+    phi = a_phi;
+    double theta_1 = L.theta_c_h, theta_0 = L.theta_c_l;
+    const double th_1 = jet_edge(a_phi, theta_1);
+    const double frac = theta_0 / theta_1;
+    theta_0 = frac * th_1;
+    theta_1 = th_1;
+    if (theta_0 > 0.5 * cgs::pi_) theta_0 = 0.5 * cgs::pi_;
+    if (theta_1 > 0.5 * cgs::pi_) theta_1 = 0.5 * cgs::pi_;
+    const double s0 = sin(0.5 * theta_0), s1 = sin(0.5 * theta_1);
+    auto f = [&](double aomct) -> double {  // costheta_integrand (eats.h:435-448)
+      if (++nevals > kMaxEvals) {
+        code = PBAG_ERR_EVALS;
+        return 0.0;
+      }
+      return integrand(1 - aomct, phi);
+    };
+    const double result = A.o.method_quad == PBAG_QUAD_TRAP_FIXED
+                              ? trap(f, 2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta)
+                              : cadre(f, 2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta, A.o.rtol_theta, inner);
+    if (result != result || result < 0.0) return 0.;
+    return result;
+  }
+};
+
+// each item's mu array (parsPars, eats.h:941-947): one thread per (item, i)
+__global__ void k_eats_mu(EatsArgs A, int items) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)items * A.nr) return;
+  const int item = (int)(t / A.nr), i = (int)(t % A.nr);
+  const pbag_eats_query q = A.q[item / A.sides];
+  const double* d = A.dyn + (size_t)q.layer * PBAG_EQ_N * A.nr;
+  A.mu[t] = i < A.layers[q.layer].i_end_r
+                ? (d[(size_t)PBAG_EQ_TBURST * A.nr + i] - q.t_obs / (1.0 + A.o.z)) / d[(size_t)PBAG_EQ_R * A.nr + i] *
+                      cgs::c_light
+                : 0.0;
+}
+
+// ln(y[i+1] / y[i]) of every interpolated quantity of every layer
+__global__ void k_eats_ln(EatsArgs A, double* ln, int nl) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nl * kNLn * A.nr) return;
+  const int i = (int)(t % A.nr), k = (int)((t / A.nr) % kNLn), l = (int)(t / ((int64_t)A.nr * kNLn));
+  if (i + 1 >= A.nr) {
+    ln[t] = 0.0;
+    return;
+  }
+  const int q = k < kNLog ? kLogQ[k] : k == kLnR ? PBAG_EQ_R : PBAG_EQ_TBURST;
+  const double* y = A.dyn + ((size_t)l * PBAG_EQ_N + q) * A.nr;
+  ln[t] = log(y[i + 1] / y[i]);
+}
+
+__global__ void __launch_bounds__(kEatsThreads) k_eats(EatsArgs A, int items) {
+  const int item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= items) return;
+  const int qi = item / A.sides;
+  const pbag_eats_query q = A.q[qi];
+  const pbag_eats_layer L = A.layers[q.layer];
+  Iv9* ws = A.ws + (size_t)item * (A.cap_phi + A.cap_theta);
+  Eats e{A, L, A.dyn + (size_t)q.layer * PBAG_EQ_N * A.nr, A.ln + (size_t)q.layer * kNLn * A.nr,
+         A.mu + (size_t)item * A.nr, A.off[L.bw_fs], L.bw_rs >= 0 ? A.off[L.bw_rs] : -1,
+         q.t_obs, q.nu_obs};
+  e.sin_obs = sin(A.o.theta_obs);
+  e.cos_obs = cos(A.o.theta_obs);
+  e.cj = (item % A.sides) == 1;
+  e.inner = Heap{ws + A.cap_phi, 0, A.cap_theta};
+  double I = 0.0;
+  const double* tb = e.qv(PBAG_EQ_TBURST);
+  if (L.i_end_r > 0 && (q.t_obs < tb[0] || q.t_obs > tb[L.i_end_r - 1])) {  // eats.h:822-827
+    e.code = PBAG_ERR_RANGE;
+  } else {
+    auto f = [&](double a_phi) -> double { return e.phi_integrand(a_phi); };
+    if (A.o.method_quad == PBAG_QUAD_TRAP_FIXED) {
+      I = e.trap(f, 0.0, cgs::pi_, A.o.nmax_phi);
+    } else {
+      Heap outer{ws, 0, A.cap_phi};
+      I = e.cadre(f, 0.0, cgs::pi_, A.o.nmax_phi, A.o.rtol_phi, outer);
+    }
+  }
+  const double Fcoeff = 1.e26 / (4 * cgs::pi_ * A.o.d_l * A.o.d_l);  // cgs2mJy (utils.h:40)
+  A.part[item] = 2 * Fcoeff * I;
+  if (e.code != PBAG_OK)
+    atomicMin(A.first, ((unsigned long long)qi << 8) | (unsigned long long)(-e.code & 0xff));
+}
+
+// flux = principal jet + counter jet, in evalFluxDensA's order
+__global__ void k_eats_sum(const double* __restrict__ part, int nq, int sides, double* __restrict__ flux) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq) return;
+  double f = part[(size_t)t * sides];
+  if (sides == 2) f += part[(size_t)t * sides + 1];
+  flux[t] = f;
+}
+
+}  // namespace
+}  // namespace pbag
+
+using namespace pbag;
+
+extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int nl, const pbag_eats_layer* h_layers,
+                                int nr, const double* d_dyn, int nbw, const int64_t* offsets, const double* d_j_all,
+                                const double* d_a_all, int nq, const pbag_eats_query* d_q, double* d_flux,
+                                pbag_status* st) {
+  if (st) {
+    st->code = PBAG_ERR_ARG;
+    st->bw = st->step = -1;
+    st->site = 0;
+  }
+  CtxView v;
+  if (!ctx_view(ctx, &v) || !opts || nl <= 0 || nr < 2 || nbw <= 0 || nq < 0 || !h_layers || !offsets)
+    return PBAG_ERR_ARG;
+  const pbag_eats_opts& o = *opts;
+  if (o.method_quad != PBAG_QUAD_CADRE && o.method_quad != PBAG_QUAD_TRAP_FIXED) return PBAG_ERR_ARG;
+  if (o.nmax_theta < 1 || o.nmax_phi < 1 || o.nmax_theta > (1 << 20) || o.nmax_phi > (1 << 20) ||
+      !(o.rtol_theta >= 0) || !(o.rtol_phi >= 0) || !(o.d_l > 0))
+    return PBAG_ERR_ARG;
+  if (o.flux.shock_vel < PBAG_VEL_SAME_AS_BW || o.flux.shock_vel > PBAG_VEL_SHOCK ||
+      o.flux.method_ne < PBAG_NE_USE_NPRIME || o.flux.method_ne > PBAG_NE_USE_NE ||
+      o.flux.method_tau < PBAG_TAU_APPROX || o.flux.method_tau > PBAG_TAU_SHARP)
+    return PBAG_ERR_ARG;
+  for (int l = 0; l < nl; ++l) {
+    const pbag_eats_layer& L = h_layers[l];
+    if (L.i_end_r < 2 || L.i_end_r > nr || L.bw_fs < 0 || L.bw_fs >= nbw || L.bw_rs >= nbw) return PBAG_ERR_ARG;
+    for (int b : {L.bw_fs, L.bw_rs})
+      if (b >= 0 && offsets[b + 1] - offsets[b] < L.i_end_r) return PBAG_ERR_ARG;
+    if (!(L.ncells > 0) || !(L.theta_c_h > 0) || !(L.theta_c_l >= 0)) return PBAG_ERR_ARG;
+  }
+  if (nq == 0) {
+    if (st) st->code = PBAG_OK;
+    return PBAG_OK;
+  }
+  if (!d_dyn || !d_j_all || !d_a_all || !d_q || !d_flux) return PBAG_ERR_ARG;
+  if (cudaSetDevice(v.device) != cudaSuccess) return PBAG_ERR_CUDA;
+  // the queries' layers are checked on the host
+  std::vector<pbag_eats_query> hq((size_t)nq);
+  if (cudaMemcpy(hq.data(), d_q, (size_t)nq * sizeof(pbag_eats_query), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PBAG_ERR_CUDA;
+  for (const pbag_eats_query& q : hq)
+    if (q.layer < 0 || q.layer >= nl || !(q.nu_obs > 0) || !(q.t_obs > 0)) return PBAG_ERR_ARG;
+
+  const int sides = o.counter_jet ? 2 : 1;
+  const int items = nq * sides;
+  EatsArgs A{};
+  A.o = o;
+  A.nr = nr;
+  A.F = v.F;
+  A.nu = v.dg.nu;
+  A.dyn = d_dyn;
+  A.j_all = d_j_all;
+  A.a_all = d_a_all;
+  A.q = d_q;
+  A.nq = nq;
+  A.sides = sides;
+  A.cap_phi = o.method_quad == PBAG_QUAD_CADRE ? o.nmax_phi + 8 : 0;
+  A.cap_theta = o.method_quad == PBAG_QUAD_CADRE ? o.nmax_theta + 8 : 0;
+  const size_t n_ln = (size_t)nl * kNLn * nr, n_mu = (size_t)items * nr;
+  const size_t n_ws = (size_t)items * (A.cap_phi + A.cap_theta);
+  double *d_ln = nullptr, *d_mu = nullptr, *d_part = nullptr;
+  Iv9* d_ws = nullptr;
+  pbag_eats_layer* d_layers = nullptr;
+  int64_t* d_off = nullptr;
+  unsigned long long* d_first = nullptr;
+  cudaError_t e = cudaMalloc(&d_ln, n_ln * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&d_mu, n_mu * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&d_part, (size_t)items * sizeof(double));
+  if (e == cudaSuccess && n_ws) e = cudaMalloc(&d_ws, n_ws * sizeof(Iv9));
+  if (e == cudaSuccess) e = cudaMalloc(&d_layers, (size_t)nl * sizeof(pbag_eats_layer));
+  if (e == cudaSuccess) e = cudaMalloc(&d_off, (size_t)(nbw + 1) * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&d_first, sizeof(unsigned long long));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_layers, h_layers, (size_t)nl * sizeof(pbag_eats_layer), cudaMemcpyHostToDevice, v.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_off, offsets, (size_t)(nbw + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, v.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_first, 0xff, sizeof(unsigned long long), v.stream);
+  A.ln = d_ln;
+  A.mu = d_mu;
+  A.part = d_part;
+  A.ws = d_ws;
+  A.layers = d_layers;
+  A.off = d_off;
+  A.first = d_first;
+  if (e == cudaSuccess) {
+    k_eats_ln<<<(unsigned)((n_ln + 255) / 256), 256, 0, v.stream>>>(A, d_ln, nl);
+    k_eats_mu<<<(unsigned)((n_mu + 255) / 256), 256, 0, v.stream>>>(A, items);
+    k_eats<<<(items + kEatsThreads - 1) / kEatsThreads, kEatsThreads, 0, v.stream>>>(A, items);
+    k_eats_sum<<<(nq + 127) / 128, 128, 0, v.stream>>>(d_part, nq, sides, d_flux);
+    e = cudaGetLastError();
+  }
+  unsigned long long first = ~0ull;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&first, d_first, sizeof(first), cudaMemcpyDeviceToHost, v.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
+  cudaFree(d_ln);
+  cudaFree(d_mu);
+  cudaFree(d_part);
+  cudaFree(d_ws);
+  cudaFree(d_layers);
+  cudaFree(d_off);
+  cudaFree(d_first);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PBAG_ERR_NOMEM : PBAG_ERR_CUDA;
+  if (first != ~0ull) {
+    const int qi = (int)(first >> 8), code = -(int)(first & 0xffull);
+    if (st) {
+      st->code = code;
+      st->bw = hq[(size_t)qi].layer;
+      st->step = qi;
+    }
+    return code;
+  }
+  if (st) st->code = PBAG_OK;
+  return PBAG_OK;
+}

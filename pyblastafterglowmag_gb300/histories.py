@@ -337,6 +337,47 @@ def make_batch(lib, cfg, nsteps=None):
     return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid
 
 
+def eats_inputs(cfg, recs, offsets, nsteps=None):
+    """The dynamics each layer's EATS reads (pbag_eats_q order), from the same
+    thin-shell model make_batch records, and the layer table: (layers
+    [nlayers] EATS_LAYER_DTYPE, dyn [nlayers][PBAG_EQ_N][nr]). recs / offsets:
+    make_batch's records of the jet (their accel_frac; blastwave 2 l is layer
+    l's forward shock and 2 l + 1 its reverse shock when cfg.rs is set). The
+    jet does not spread: the edge theta is the layer's upper cone angle."""
+    tb = np.logspace(np.log10(cfg.tb1), np.log10(cfg.tb2), cfg.ntb)
+    if nsteps is not None:
+        tb = tb[:nsteps]
+    nr = len(tb)
+    lo, hi, E, G0 = layer_table(cfg)
+    omega = 2 * np.pi * (np.cos(lo) - np.cos(hi)) * 2
+    dynl = layer_dynamics_many(E, G0, cfg.n_ism, tb, omega)
+    per = 2 if cfg.rs is not None else 1
+    layers = np.zeros(cfg.nlayers, dtype=abi.EATS_LAYER_DTYPE)
+    dyn = np.zeros((cfg.nlayers, abi.PBAG_EQ_N, nr))
+    q = {k: i for i, k in enumerate(abi.EATS_Q)}
+    for il in range(cfg.nlayers):
+        d = dynl[il]
+        fs = fs_state(d)
+        b = per * il
+        acc = recs["accel_frac"][offsets[b]:offsets[b + 1]]
+        row = dyn[il]
+        row[q["tburst"]], row[q["R"]], row[q["Rsh"]] = tb, d["R"], d["R"]
+        row[q["theta"]], row[q["ctheta"]] = hi[il], 0.5 * (lo[il] + hi[il])
+        row[q["Gamma"]], row[q["beta"]], row[q["GammaFsh"]] = d["Gamma"], d["beta"], fs["GammaSh"]
+        row[q["thickness"]], row[q["M2"]], row[q["rho2"]] = fs["thick"], fs["m2"], fs["rho2"]
+        row[q["acc_frac"]] = np.where(acc > 0, acc, 1.0)
+        layers[il] = (nr, b, b + 1 if per == 2 else -1, 0, lo[il], hi[il], 1.0)
+        if per == 2:
+            rs = rs_state(d)
+            acr = recs["accel_frac"][offsets[b + 1]:offsets[b + 2]]
+            # reverse-shock radiation only where its shell exists (thickness > 0 at both ends of a segment)
+            row[q["GammaRsh"]], row[q["Rrsh"]] = rs["GammaSh"], d["R"]
+            row[q["thickness_rs"]] = np.where(rs["valid"], rs["thick"], 0.0)
+            row[q["M3"]], row[q["rho3"]] = rs["m2"], rs["rho2"]
+            row[q["acc_frac_rs"]] = np.where(acr > 0, acr, 1.0)
+    return layers, dyn
+
+
 def driver_arrays(lib, cfg, nsteps=None):
     """Per blastwave (ordered as make_batch orders them) the quantities the
     reference's blastwave driver passes to ElectronAndRadiation at every
