@@ -39,12 +39,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="gaussian-jet", choices=["gaussian-jet", "contraction", "uneven-sweep", "surrogate"],
+    ap.add_argument("--workload", default="gaussian-jet",
+                    choices=["gaussian-jet", "contraction", "uneven-sweep", "surrogate", "eats-lc"],
                     help="gaussian-jet: the step benchmark (default); contraction: the emissivity-"
                          "contraction microbenchmark (65536 states, 256 gamma x 256 nu); uneven-sweep: a "
                          "seeded sample of the 4096-set parameter sweep with uneven step counts; surrogate: train "
                          "the SSC surrogate on states of the sweep, time it against the exact contraction and "
-                         "deploy it on the Gaussian jet")
+                         "deploy it on the Gaussian jet; eats-lc: the adaptive EATS light curve of the Gaussian jet "
+                         "from the step's device-resident histories")
     ap.add_argument("--sets", type=int, default=64, help="parameter sets of the uneven-sweep workload")
     ap.add_argument("--train-states", type=int, default=1000000, help="training states of the surrogate workload")
     ap.add_argument("--epochs", type=int, default=8, help="training epochs of the surrogate workload")
@@ -54,6 +56,8 @@ def parse():
                     help="states of the FP32 CUDA-core variant of the contraction benchmark")
     ap.add_argument("--check-states", type=int, default=64,
                     help="states checked against the FP64 oracle in the contraction benchmark")
+    ap.add_argument("--lc-times", type=int, default=32, help="observer times of the eats-lc workload")
+    ap.add_argument("--quad", default="cadre", choices=["cadre", "trap"], help="quadrature of the eats-lc workload")
     ap.add_argument("--profile", type=int, default=0,
                     help="run this many device passes of the workload and exit (for ncu captures)")
     return ap.parse_args()
@@ -805,6 +809,89 @@ def surrogate_arm(args):
                                         "blastwave_steps_per_s_plain": nvalid / t_plain}}
     print(json.dumps(line), flush=True)
 
+# ------------------------------------------------------------ eats-lc arm ---
+def eats_arm(args):
+    """The adaptive EATS light curve of the 21-layer Gaussian jet (forward and
+    reverse shocks, theta_obs = 20.8 deg, nu = 1e15 Hz, args.lc_times observer
+    times in [3e3, 1e9] s, CADRE with rtol 1e-6 or TRAP_FIXED 100 x 100): the
+    GPU step leaves the histories on the device, pbag_eats_flux_a integrates
+    them there. The CPU figure is the oracle's restatement of the reference's
+    EATS integrator on one host core over a sample of the queries; the
+    line's parity compares the GPU light curve with the oracle's on that
+    sample (same histories)."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from pyblastafterglowmag_gb300 import _lib, abi, build, histories as H
+    build.build()
+    pyoracle.build_oracle()
+    orc = pyoracle.Oracle()
+    cfg, recs, off, prm, grid = workload()
+    dev = torch.device("cuda", 0)
+    ctx = _lib.Context(grid, device=0, ssc=True)
+    nrec = len(recs)
+    d_recs = torch.from_numpy(recs.view(np.uint8).copy()).to(dev)
+    d_prm = torch.from_numpy(prm.view(np.uint8).copy()).to(dev)
+    d_out = {k: torch.zeros((nrec, grid.nfreq), dtype=torch.float64, device=dev) for k in ("j_all", "a_all")}
+    ctx.run_device(d_prm.data_ptr(), len(prm), off, d_recs.data_ptr(), {k: v.data_ptr() for k, v in d_out.items()})
+    layers, dyn = H.eats_inputs(cfg, recs, off)
+    o = abi.EatsOpts()
+    o.theta_obs, o.z, o.d_l = np.deg2rad(20.8), 0.0, 3.09e26
+    o.rtol_theta = o.rtol_phi = 1e-6
+    o.method_quad = abi.PBAG_QUAD_CADRE if args.quad == "cadre" else abi.PBAG_QUAD_TRAP_FIXED
+    o.nmax_theta = o.nmax_phi = 1000 if args.quad == "cadre" else 100
+    o.counter_jet = 1
+    o.flux.shock_vel, o.flux.method_ne, o.flux.method_tau = abi.PBAG_VEL_SHOCK, abi.PBAG_NE_USE_NE, abi.PBAG_TAU_APPROX
+    t_obs = np.logspace(np.log10(3e3), np.log10(1e9), args.lc_times)
+    q = np.zeros(len(layers) * len(t_obs), dtype=abi.EATS_QUERY_DTYPE)
+    q["layer"] = np.repeat(np.arange(len(layers)), len(t_obs))
+    q["t_obs"] = np.tile(t_obs, len(layers))
+    q["nu_obs"] = 1e15
+    d_dyn = torch.from_numpy(np.ascontiguousarray(dyn)).to(dev)
+    d_q = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
+    d_f = torch.zeros(len(q), dtype=torch.float64, device=dev)
+
+    def one_pass():
+        _lib.eats_flux_a(ctx, o, layers, d_dyn.data_ptr(), dyn.shape[-1], off, d_out["j_all"].data_ptr(),
+                         d_out["a_all"].data_ptr(), len(q), d_q.data_ptr(), d_f.data_ptr())
+
+    for _ in range(args.warmup):
+        one_pass()
+    ms = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            one_pass()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t = statistics.median(ms)
+    got = d_f.cpu().numpy()
+    # the oracle on a sample: every 4th observer time of every layer
+    sel = np.flatnonzero(np.tile(np.arange(len(t_obs)) % 4 == 0, len(layers)))
+    j, a = d_out["j_all"].cpu().numpy(), d_out["a_all"].cpu().numpy()
+    t0 = time.perf_counter()
+    rc, fail, ref = orc.eats_flux(grid, o, layers, dyn, off, j, a, q[sel])
+    cpu_s = time.perf_counter() - t0
+    rel = np.abs(got[sel] - ref) / ref
+    line = {"metric": "EATS light-curve points/s (adaptive quadrature) on 1 GB300", "value": len(q) / (t * 1e-3),
+            "unit": "points/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"eats-lc-gaussian-jet-21-layers-fs-rs-{args.quad}",
+                       "layers": len(layers), "lc_times": len(t_obs), "queries": len(q), "theta_obs_deg": 20.8,
+                       "nu_obs": 1e15, "quadrature": args.quad, "nmax": o.nmax_phi, "rtol": o.rtol_phi,
+                       "counter_jet": True, "histories": "the GPU step's, device-resident"},
+            "clocks": clk.summary(),
+            "cpu_baseline": {"value": len(sel) / cpu_s, "unit": "points/s", "cores": 1, "kind": "port",
+                             "sample": f"{len(sel)} of the {len(q)} queries (every 4th observer time), the oracle's "
+                                       "restatement of the reference's EATS integrator (equal to it bit for bit)"},
+            "parity": {"max_rel": float(rel.max()), "oracle_status": int(rc), "tol": 1e-5,
+                       "ok": bool(rc == 0 and rel.max() <= 1e-5)}}
+    print(json.dumps(line), flush=True)
+
 
 def timeit_run(ctx, recs, off, prm):
     t0 = time.perf_counter()
@@ -816,6 +903,9 @@ def main():
     args = parse()
     if args.workload == "surrogate":
         surrogate_arm(args)
+        return
+    if args.workload == "eats-lc":
+        eats_arm(args)
         return
     if args.workload == "contraction":
         contraction_arm(args)

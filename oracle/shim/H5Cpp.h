@@ -5,11 +5,16 @@
 // (struct Output) writes HDF5 files and src/utilitites/H5Easy.h reads them
 // (pulled in by the blastwave and EATS headers). None of that is on the paths
 // the oracle harnesses drive, so these declarations only need to let the
-// headers compile; every method is an empty inline body that is never called.
+// headers compile; writing is a no-op. Reading serves datasets and scalar
+// attributes that a harness registered in memory (pbag_h5::put / put_attr,
+// keyed by file path and name), so that the reference's own loaders (e.g. the
+// ejecta initial data, ejecta_id.h) run on inputs given without a file.
 #ifndef PBAG_ORACLE_SHIM_H5CPP_H
 #define PBAG_ORACLE_SHIM_H5CPP_H
 
+#include <map>
 #include <string>
+#include <vector>
 
 typedef unsigned long long hsize_t;
 typedef long long hid_t;
@@ -21,6 +26,32 @@ enum H5S_class_t { H5S_SCALAR = 0, H5S_SIMPLE = 1 };
 #define H5F_ACC_RDONLY 0u
 #define H5F_ACC_RDWR 1u
 #define H5P_DEFAULT 0
+
+namespace pbag_h5 {
+struct Entry {
+  std::vector<double> data;
+  std::vector<unsigned long long> dims;
+};
+inline std::map<std::string, Entry>& datasets() {
+  static std::map<std::string, Entry> m;
+  return m;
+}
+inline std::map<std::string, double>& attributes() {
+  static std::map<std::string, double> m;
+  return m;
+}
+inline void put(const std::string& file, const std::string& name, const std::vector<double>& data,
+                const std::vector<unsigned long long>& dims) {
+  datasets()[file + "//" + name] = Entry{data, dims};
+}
+inline void put_attr(const std::string& file, const std::string& name, double v) {
+  attributes()[file + "//" + name] = v;
+}
+inline const Entry* find(const std::string& key) {
+  auto it = datasets().find(key);
+  return it == datasets().end() ? nullptr : &it->second;
+}
+}  // namespace pbag_h5
 
 namespace H5 {
 struct PredType {
@@ -61,27 +92,49 @@ struct FloatType : DataType {
   H5T_order_t getOrder(H5std_string&) const { return H5T_ORDER_LE; }
 };
 struct DataSpace {
+  std::vector<unsigned long long> dims;
   DataSpace() {}
   DataSpace(int) {}
   DataSpace(int, const hsize_t*) {}
   DataSpace(H5S_class_t) {}
-  int getSimpleExtentNdims() const { return 0; }
-  int getSimpleExtentDims(hsize_t*, hsize_t* = nullptr) const { return 0; }
-  long getSimpleExtentNpoints() const { return 0; }
+  int getSimpleExtentNdims() const { return (int)dims.size(); }
+  int getSimpleExtentDims(hsize_t* d, hsize_t* = nullptr) const {
+    for (size_t i = 0; i < dims.size(); ++i) d[i] = dims[i];
+    return (int)dims.size();
+  }
+  long getSimpleExtentNpoints() const {
+    long n = dims.empty() ? 0 : 1;
+    for (unsigned long long d : dims) n *= (long)d;
+    return n;
+  }
   void close() {}
 };
 struct Attribute {
+  std::string key;
   template <typename... A> void write(A&&...) {}
-  template <typename... A> void read(A&&...) const {}
+  void read(const DataType&, void* v) const {
+    auto it = pbag_h5::attributes().find(key);
+    *static_cast<double*>(v) = it == pbag_h5::attributes().end() ? -1. : it->second;
+  }
   DataType getDataType() const { return {}; }
   unsigned long long getStorageSize() const { return 0; }
 };
 struct DataSet {
+  std::string key;
   void write(const void*, const PredType&) {}
-  void read(void*, const PredType&) const {}
+  void read(void* buf, const PredType&) const {
+    if (const pbag_h5::Entry* e = pbag_h5::find(key)) {
+      double* out = static_cast<double*>(buf);
+      for (size_t i = 0; i < e->data.size(); ++i) out[i] = e->data[i];
+    }
+  }
   void close() {}
   DataType getDataType() const { return {}; }
-  DataSpace getSpace() const { return {}; }
+  DataSpace getSpace() const {
+    DataSpace s;
+    if (const pbag_h5::Entry* e = pbag_h5::find(key)) s.dims = e->dims;
+    return s;
+  }
   FloatType getFloatType() const { return {}; }
   IntType getIntType() const { return {}; }
 };
@@ -94,15 +147,16 @@ struct Group {
   void close() {}
 };
 struct H5File {
+  std::string name;
   H5File() {}
-  H5File(const std::string&, unsigned) {}
+  H5File(const std::string& n, unsigned) : name(n) {}
   template <typename... A> DataSet createDataSet(A&&...) { return {}; }
   template <typename... A> Attribute createAttribute(A&&...) { return {}; }
   Group createGroup(const std::string&) { return {}; }
   Group openGroup(const std::string&) { return {}; }
-  DataSet openDataSet(const std::string&) const { return {}; }
-  Attribute openAttribute(const std::string&) const { return {}; }
-  bool attrExists(const std::string&) const { return false; }
+  DataSet openDataSet(const std::string& v) const { return DataSet{name + "//" + v}; }
+  Attribute openAttribute(const std::string& k) const { return Attribute{name + "//" + k}; }
+  bool attrExists(const std::string& k) const { return pbag_h5::attributes().count(name + "//" + k) > 0; }
   hid_t getId() const { return 0; }
   void close() {}
 };

@@ -659,6 +659,8 @@ int pbag_create(const pbag_grid_desc* g, int device, int ssc_tables, pbag_ctx** 
     const char* sm = std::getenv("PBAG_SYSTOLIC_MIN");
     const int v = sm ? std::atoi(sm) : 0;
     d.sys_min_sub = v >= 2 ? v : kScanMaxSub;
+    const char* ec = std::getenv("PBAG_EVOLVE_CTAS");
+    d.evolve_ctas = ec ? std::atoi(ec) : 4;
   }
   d.dlog_gam = (e[1] - e[0]) / e[0];
   cudaError_t err = cudaSuccess;

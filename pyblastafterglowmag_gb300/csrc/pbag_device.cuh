@@ -32,6 +32,7 @@ struct DevGrid {
   int n_cyc;             // number of bins with e[j] <= 2 (cyclotron branch of cycSynch)
   int scan_fp64;         // Chang-Cooper substeps in FP64 only (PBAG_SCAN_FP64=1), else double-float first
   int sys_min_sub;       // substep count from which the solve is the systolic pipeline (PBAG_SYSTOLIC_MIN)
+  int evolve_ctas;       // evolve CTAs per SM for large batches: 4, 6 or 8 (PBAG_EVOLVE_CTAS)
   double dlog_gam;       // (e[1]-e[0])/e[0] (microphysics.h:413)
   const double* e;       // [G]   gamma grid e[i] = step^i
   const double* inv_e;   // [G]   1/e

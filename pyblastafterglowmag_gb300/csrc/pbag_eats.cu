@@ -4,7 +4,7 @@
 //
 // One work item = one (query, jet side): the principal jet and, with
 // counter_jet, the counter jet are separate items (their sum is taken in the
-// reference's order at the end), each a nested quadrature run by one thread:
+// reference's order at the end), each a nested quadrature run by one warp:
 // phi in [0, pi] outside, 1 - cos(theta) inside (integrate_theta_phi,
 // eats.h:587-700; phi_integrand :449-586 with find_jet_edge :103-173;
 // costheta_integrand :435-448), by CADRE - m9_adapt with the cautious Romberg
@@ -16,7 +16,18 @@
 // fluxDens (microphysics.h:1185-1217) on the forward- and reverse-shock
 // histories.
 //
-// GB300 layout: every FP64 quantity that does not depend on the direction is
+// GB300 layout. An FP64 warp instruction holds its sub-partition's FP64 unit
+// for 64 cycles however many lanes are active, so lanes of one warp must not
+// each follow their own adaptive quadrature (divergent paths issue one after
+// another). A warp owns one item: every lane runs the quadratures' control
+// with the same values (converged; their identical stores to the interval
+// workspace coincide), and the points an inner step needs are evaluated by
+// the lanes together - the 2 or 4 new points of a CADRE interval, the 2^k
+// odd points of its Romberg refinement, every point of a trapezoid sum -
+// while the outer (phi) points, each an inner integral, follow in order.
+// Sums over a batch are warp reductions (the reference adds point after
+// point: the same terms, another rounding order). Every FP64 quantity that
+// does not depend on the direction is
 // computed once, in parallel, before the quadratures: each item's mu array
 // (nr divisions) and, per layer and segment, the logarithms of the ratios of
 // neighbouring dynamics values, so that each log-linear interpolation is one
@@ -38,7 +49,7 @@
 namespace pbag {
 namespace {
 
-constexpr int kEatsThreads = 64;
+constexpr int kEatsThreads = 128;  // four items (warps) per CTA
 constexpr long kMaxEvals = 10000000L;  // eats.h:536-541
 // dynamics interpolated log-linearly in radius, in their pbag_eats_q order
 __constant__ const int kLogQ[] = {PBAG_EQ_GAMMA,     PBAG_EQ_BETA,         PBAG_EQ_GAMMA_FSH, PBAG_EQ_THICKNESS,
@@ -168,28 +179,25 @@ struct Eats {
   const double* ln;
   const double* mu;
   int64_t r_fs, r_rs;
-  double t_obs, nu_obs, phi = 0., sin_obs, cos_obs;
+  double t_obs, nu_obs, sin_obs, cos_obs;
   bool cj;
+  int lane;
   long nevals = 0;
   int code = PBAG_OK;
   Heap inner;
 
   __device__ const double* qv(int k) const { return dyn + (size_t)k * A.nr; }
-  __device__ double angle(double th, double ph) const {  // obsAngle / obsAngleCJ (image.h:361-378)
-    const double t = cj ? cgs::pi_ - th : th;
-    return sin_obs * (sin(t) * sin(ph)) + cos_obs * cos(t);
-  }
   // ya (yb/ya)^t with ln(yb/ya) from the table
   __device__ double seg(int li, int a, double t) const { return qv(kLogQ[li])[a] * exp(t * ln[(size_t)li * A.nr + a]); }
 
   // fluxDens (microphysics.h:1185-1217) + computeFluxDensity (:799-867) on the
   // history rows r0 + ia, r0 + ib
   __device__ double flux_dens(int64_t r0, int ia, int ib, double freq, double theta, double Gamma, double GammaSh,
-                              double mu_, double r, double n_prime, double ne, const double* R) {
+                              double mu_, double r, double n_prime, double ne, const double* R, int* rc) const {
     const int F = A.F;
     const double* nu = A.nu;
     if (freq >= nu[F - 1] || freq <= nu[0]) {
-      code = PBAG_ERR_RANGE;
+      *rc = PBAG_ERR_RANGE;
       return 0.;
     }
     const int ia_nu = find_index(freq, nu, F), ib_nu = ia_nu + 1;
@@ -214,7 +222,7 @@ struct Eats {
     const double dtau = mu_ == beta_shock ? 1.0e100 : abs_lab * dr * (1. - mu_ * beta_shock) / (mu_ - beta_shock);
     const double intensity = intensity_of(em_lab, dtau, A.o.flux.method_tau);
     if (intensity < 0 || !isfinite(intensity)) {
-      code = PBAG_ERR_NONFINITE;
+      *rc = PBAG_ERR_NONFINITE;
       return 0.;
     }
     const double ashock = 1.0 - mu_ * beta_shock;
@@ -222,19 +230,24 @@ struct Eats {
                            ? intensity * r * r * (dr / ashock)
                            : intensity * ne / (2. * cgs::pi_ * ring) / Gamma / ashock;
     if (lum < 0 || !isfinite(lum)) {
-      code = PBAG_ERR_NONFINITE;
+      *rc = PBAG_ERR_NONFINITE;
       return 0.;
     }
+    *rc = PBAG_OK;
     return lum;
   }
 
-  // the integrand (eats.h:175-232) with fluxDensAdaptiveWithComov
-  __device__ double integrand(double i_cos_theta, double i_phi) {
+  // the integrand (eats.h:175-232) with fluxDensAdaptiveWithComov at this
+  // lane's own point (sin_phi = sin(i_phi)); *rc: PBAG_OK or where the
+  // reference exits
+  __device__ double integrand(double i_cos_theta, double sin_phi, int* rc) const {
+    *rc = PBAG_OK;
     const double* R = qv(PBAG_EQ_R);
     const int ie = L.i_end_r;
     if (R[0] == 0.0 && R[ie - 1] == 0.0) return 0.0;
     const double a_theta = 2.0 * asin(sqrt(0.5 * (1.0 - i_cos_theta)));
-    const double m = angle(a_theta, i_phi);
+    const double th = cj ? cgs::pi_ - a_theta : a_theta;  // obsAngle / obsAngleCJ
+    const double m = sin_obs * (sin(th) * sin_phi) + cos_obs * cos(th);
     if (m < mu[0] || m > mu[ie - 1]) return 0.;
     const int ia = find_index(m, mu, ie), ib = ia + 1;
     const double* tb = qv(PBAG_EQ_TBURST);
@@ -245,20 +258,17 @@ struct Eats {
     const double r = R[ia] * exp(log(t_e / tb[ia]) / ln[(size_t)kLnT * A.nr + ia] * ln[(size_t)kLnR * A.nr + ia]);
     if (r <= 0.0 || !isfinite(r)) return 0.0;
     const double t = log(r / R[ia]) / ln[(size_t)kLnR * A.nr + ia];
-    const double Gamma = seg(0, ia, t), beta = seg(1, ia, t), GammaSh = seg(2, ia, t);
-    const double ne = seg(4, ia, t) / cgs::m_p, n_prime = seg(5, ia, t) / cgs::m_p;
-    const double theta = seg(8, ia, t);
+    const double Gamma = seg(0, ia, t), beta = seg(1, ia, t), theta = seg(8, ia, t);
     const double nuprime = (1.0 + A.o.z) * nu_obs * (Gamma * (1.0 - beta * m));
-    double flux = flux_dens(r_fs, ia, ib, nuprime, theta, Gamma, GammaSh, m, r, n_prime, ne, R);
-    if (code != PBAG_OK) return 0.;
-    if (r_rs >= 0) {
-      const double* th_rs = qv(PBAG_EQ_THICKNESS_RS);
-      if (th_rs[ia] > 0 && th_rs[ib] > 0) {
-        const double fr = flux_dens(r_rs, ia, ib, nuprime, theta, Gamma, seg(9, ia, t), m, r,
-                                    seg(12, ia, t) / cgs::m_p, seg(11, ia, t) / cgs::m_p, R);
-        if (code != PBAG_OK) return 0.;
-        flux += fr;
-      }
+    double flux = flux_dens(r_fs, ia, ib, nuprime, theta, Gamma, seg(2, ia, t), m, r, seg(5, ia, t) / cgs::m_p,
+                            seg(4, ia, t) / cgs::m_p, R, rc);
+    if (*rc != PBAG_OK) return 0.;
+    const double* th_rs = qv(PBAG_EQ_THICKNESS_RS);
+    if (r_rs >= 0 && th_rs[ia] > 0 && th_rs[ib] > 0) {
+      const double fr = flux_dens(r_rs, ia, ib, nuprime, theta, Gamma, seg(9, ia, t), m, r, seg(12, ia, t) / cgs::m_p,
+                                  seg(11, ia, t) / cgs::m_p, R, rc);
+      if (*rc != PBAG_OK) return 0.;
+      flux += fr;
     }
     return flux;
   }
@@ -267,7 +277,11 @@ struct Eats {
   __device__ double jet_edge(double ph, double th_con_hi) const {
     const double* thj = qv(PBAG_EQ_THETA);
     const int N = L.i_end_r;
-    int ia = find_index(angle(th_con_hi, ph), mu, N);
+    auto angle = [&](double th) {
+      const double x = cj ? cgs::pi_ - th : th;
+      return sin_obs * (sin(x) * sin(ph)) + cos_obs * cos(x);
+    };
+    int ia = find_index(angle(th_con_hi), mu, N);
     if (thj[ia] <= th_con_hi && th_con_hi <= thj[ia + 1]) return th_con_hi;
     double theta_a, theta_b;
     if (th_con_hi < thj[ia]) {
@@ -279,7 +293,7 @@ struct Eats {
     }
     for (int i = 0; theta_b - theta_a > 1.0e-5 && i < 100; ++i) {
       const double c = 0.5 * (theta_a + theta_b);
-      ia = find_index(angle(c, ph), mu, N);
+      ia = find_index(angle(c), mu, N);
       if (c < thj[ia])
         theta_a = c;
       else
@@ -290,21 +304,109 @@ struct Eats {
 
   __device__ bool stop() const { return code != PBAG_OK; }
 
-  // CADRE (m9_adapt with the cautious Romberg interval rules) over f
-  template <class Fn>
-  __device__ int process(Fn& f, Iv9* i) {
+  // ---- the inner integral's points, evaluated by the lanes together
+  // (costheta_integrand, eats.h:435-448). A batch stops at its first failing
+  // point as the sequential loop would; the evaluation count (the reference's
+  // 1e7 limit) grows by the batch.
+  __device__ void count_evals(int n) {
+    nevals += n;
+    if (nevals > kMaxEvals && code == PBAG_OK) code = PBAG_ERR_EVALS;
+  }
+  __device__ void first_failure(int rc) {
+    const unsigned bad = __ballot_sync(0xffffffffu, rc != PBAG_OK);
+    if (bad) code = __shfl_sync(0xffffffffu, rc, __ffs(bad) - 1);
+  }
+  struct Inner {  // the points of one inner integral: the lanes evaluate them together
+    Eats& e;
+    double sphi;
+    __device__ void eval(const double* xs, int n, double* ys) {  // n <= 32
+      int rc = PBAG_OK;
+      const double y = e.lane < n ? e.integrand(1 - xs[e.lane], sphi, &rc) : 0.;
+      e.first_failure(rc);
+      e.count_evals(n);
+      for (int k = 0; k < n; ++k) ys[k] = __shfl_sync(0xffffffffu, y, k);
+    }
+    // sum of f(a + h j) over odd j < nint
+    __device__ double sum_odd(double a, double h, int nint) {
+      double s = 0.;
+      for (int base = 1; base < nint; base += 64) {
+        const int j = base + 2 * e.lane;
+        int rc = PBAG_OK;
+        double y = j < nint ? e.integrand(1 - (a + h * j), sphi, &rc) : 0.;
+        e.first_failure(rc);
+        e.count_evals(min(32, (nint - base + 1) / 2));
+        if (e.stop()) return 0.;
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        s += y;
+      }
+      return s;
+    }
+    // trap (quadratures.h:939-951)
+    __device__ double trap(double xa, double xb, int N) {
+      const double dx = (xb - xa) / N;
+      double ends[2];
+      const double x2[2] = {xa, xb};
+      eval(x2, 2, ends);
+      if (e.stop()) return 0.;
+      double I = 0.5 * (ends[0] + ends[1]);
+      for (int base = 1; base < N; base += 32) {
+        const int i = base + e.lane;
+        int rc = PBAG_OK;
+        double y = i < N ? e.integrand(1 - (xa + i * dx), sphi, &rc) : 0.;
+        e.first_failure(rc);
+        e.count_evals(min(32, N - base));
+        if (e.stop()) return 0.;
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        I += y;
+      }
+      return I * dx;
+    }
+  };
+  struct Outer {  // the points of the phi integral: one inner integral each, in order
+    Eats& e;
+    __device__ void eval(const double* xs, int n, double* ys) {
+      for (int k = 0; k < n; ++k) {
+        ys[k] = e.phi_integrand(xs[k]);
+        if (e.stop()) return;
+      }
+    }
+    __device__ double sum_odd(double a, double h, int nint) {
+      double s = 0.;
+      for (int j = 1; j < nint; j += 2) {
+        s += e.phi_integrand(a + h * j);
+        if (e.stop()) return 0.;
+      }
+      return s;
+    }
+    __device__ double trap(double xa, double xb, int N) {
+      const double dx = (xb - xa) / N;
+      const double fa = e.phi_integrand(xa);
+      if (e.stop()) return 0.;
+      double I = 0.5 * (fa + e.phi_integrand(xb));
+      for (int i = 1; i < N; i++) {
+        I += e.phi_integrand(xa + i * dx);
+        if (e.stop()) return 0.0;
+      }
+      return I * dx;
+    }
+  };
+
+  // CADRE's interval rules (cadreProcessInterval, quadratures.h:1653-1937)
+  template <class B>
+  __device__ int process(B& fb, Iv9* i) {
     const double scaleTol = 0.2;
     int count = 0;
     if (i->refinement < 4) {
-      const double fa = i->f[0], fm = i->f[4], fb = i->f[8];
+      const double fa = i->f[0], fm = i->f[4], fb_ = i->f[8];
       double fl, fr;
       if (i->refinement == 0) {
-        fl = f(0.75 * i->a + 0.25 * i->b);
-        count++;
+        const double xs[2] = {0.75 * i->a + 0.25 * i->b, 0.25 * i->a + 0.75 * i->b};
+        double ys[2];
+        fb.eval(xs, 2, ys);
+        count += 2;
         if (stop()) return count;
-        fr = f(0.25 * i->a + 0.75 * i->b);
-        count++;
-        if (stop()) return count;
+        fl = ys[0];
+        fr = ys[1];
         i->f[2] = fl;
         i->f[6] = fr;
       } else {
@@ -313,19 +415,17 @@ struct Eats {
         i->refinement = 0;
       }
       const double h = 0.25 * (i->b - i->a);
-      const double T0 = 2 * h * (fa + fb);
+      const double T0 = 2 * h * (fa + fb_);
       const double T1 = 0.5 * T0 + 2 * h * fm;
       const double T2 = 0.5 * T1 + h * (fl + fr);
       const double R0 = (T1 - T0) / (T2 - T1);
       if (R0 > 4 - scaleTol && R0 < 4 + scaleTol) {
-        const double x[4] = {0.875 * i->a + 0.125 * i->b, 0.625 * i->a + 0.375 * i->b,
-                             0.375 * i->a + 0.625 * i->b, 0.125 * i->a + 0.875 * i->b};
+        const double xs[4] = {0.875 * i->a + 0.125 * i->b, 0.625 * i->a + 0.375 * i->b,
+                              0.375 * i->a + 0.625 * i->b, 0.125 * i->a + 0.875 * i->b};
         double v[4];
-        for (int k = 0; k < 4; ++k) {
-          v[k] = f(x[k]);
-          count++;
-          if (stop()) return count;
-        }
+        fb.eval(xs, 4, v);
+        count += 4;
+        if (stop()) return count;
         i->f[1] = v[0];
         i->f[3] = v[1];
         i->f[5] = v[2];
@@ -366,12 +466,9 @@ struct Eats {
     int nint = 1;
     for (int n = 0; n < i->refinement; n++) nint *= 2;
     const double h = (i->b - i->a) / nint;
-    double sum = 0;
-    for (int n = 1; n < nint; n += 2) {
-      sum += f(i->a + h * n);
-      count++;
-      if (stop()) return count;
-    }
+    const double sum = fb.sum_odd(i->a, h, nint);
+    count += nint / 2;
+    if (stop()) return count;
     double Rnm = i->f[0], Rnmp = i->f[1];
     i->f[0] = 0.5 * i->f[0] + h * sum;
     i->f[1] = (4.0 * i->f[0] - Rnm) / 3.0;
@@ -400,34 +497,38 @@ struct Eats {
     return count;
   }
 
-  template <class Fn>
-  __device__ double cadre(Fn& f, double xa, double xb, int nmax, double rtol, Heap& m) {
+  // m9_adapt (quadratures.h:1969-2101) with atol 0
+  template <class B>
+  __device__ double cadre(B& fb, double xa, double xb, int nmax, double rtol, Heap& m) {
     m.n = 0;
     Iv9 i{};
     i.a = xa;
     i.b = xb;
-    i.f[0] = f(xa);
-    if (stop()) return 0.0;
-    i.f[8] = f(xb);
-    if (stop()) return 0.0;
-    i.f[4] = f(0.5 * (xa + xb));
-    if (stop()) return 0.0;
-    int n = 3 + process(f, &i);
+    {
+      const double xs[3] = {xa, xb, 0.5 * (xa + xb)};  // cadreInitInterval: f(a), f(b), f(m)
+      double ys[3];
+      fb.eval(xs, 3, ys);
+      if (stop()) return 0.0;
+      i.f[0] = ys[0];
+      i.f[8] = ys[1];
+      i.f[4] = ys[2];
+    }
+    int n = 3 + process(fb, &i);
     if (stop()) return 0.0;
     m.insert(i);
     double I = i.I, err = i.err;
     int num_intervals = 1, num_iterations = 0, last_check = 0;
-    while (n < nmax && err > rtol * fabs(I)) {  // atol 0
+    while (n < nmax && err > rtol * fabs(I)) {
       m.extract(&i);
       if (i.refinement >= 4) {
         const double oldI = i.I, olderr = i.err;
-        n += process(f, &i);
+        n += process(fb, &i);
         if (stop()) return 0.0;
         m.insert(i);
         err += i.err - olderr;
         I += i.I - oldI;
       } else {
-        Iv9 i1{}, i2{};
+        Iv9 i1{}, i2{};  // cadreSplitInterval
         const double xm = 0.5 * (i.a + i.b);
         i1.a = i.a;
         i1.b = xm;
@@ -445,8 +546,8 @@ struct Eats {
         i2.f[6] = i.f[7];
         i2.f[8] = i.f[8];
         i2.refinement = i.refinement;
-        n += process(f, &i1);
-        n += process(f, &i2);
+        n += process(fb, &i1);
+        n += process(fb, &i2);
         if (stop()) return 0.0;
         if (!m.insert(i1) || !m.insert(i2)) {
           code = PBAG_ERR_NOMEM;
@@ -466,21 +567,8 @@ struct Eats {
     return m.total_I();
   }
 
-  template <class Fn>
-  __device__ double trap(Fn& f, double xa, double xb, int N) {
-    const double dx = (xb - xa) / N;
-    const double fa = f(xa);
-    double I = 0.5 * (fa + f(xb));
-    for (int i = 1; i < N; i++) {
-      I += f(xa + i * dx);
-      if (stop()) return 0.0;
-    }
-    return I * dx;
-  }
-
   // phi_integrand (eats.h:449-586): the inner integral over 1 - cos(theta)
   __device__ double phi_integrand(double a_phi) {
-    phi = a_phi;
     double theta_1 = L.theta_c_h, theta_0 = L.theta_c_l;
     const double th_1 = jet_edge(a_phi, theta_1);
     const double frac = theta_0 / theta_1;
@@ -489,16 +577,10 @@ struct Eats {
     if (theta_0 > 0.5 * cgs::pi_) theta_0 = 0.5 * cgs::pi_;
     if (theta_1 > 0.5 * cgs::pi_) theta_1 = 0.5 * cgs::pi_;
     const double s0 = sin(0.5 * theta_0), s1 = sin(0.5 * theta_1);
-    auto f = [&](double aomct) -> double {  // costheta_integrand (eats.h:435-448)
-      if (++nevals > kMaxEvals) {
-        code = PBAG_ERR_EVALS;
-        return 0.0;
-      }
-      return integrand(1 - aomct, phi);
-    };
+    Inner fin{*this, sin(a_phi)};
     const double result = A.o.method_quad == PBAG_QUAD_TRAP_FIXED
-                              ? trap(f, 2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta)
-                              : cadre(f, 2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta, A.o.rtol_theta, inner);
+                              ? fin.trap(2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta)
+                              : cadre(fin, 2.0 * s0 * s0, 2.0 * s1 * s1, A.o.nmax_theta, A.o.rtol_theta, inner);
     if (result != result || result < 0.0) return 0.;
     return result;
   }
@@ -532,7 +614,7 @@ __global__ void k_eats_ln(EatsArgs A, double* ln, int nl) {
 }
 
 __global__ void __launch_bounds__(kEatsThreads) k_eats(EatsArgs A, int items) {
-  const int item = blockIdx.x * blockDim.x + threadIdx.x;
+  const int item = blockIdx.x * (kEatsThreads / 32) + (threadIdx.x >> 5);  // one item per warp
   if (item >= items) return;
   const int qi = item / A.sides;
   const pbag_eats_query q = A.q[qi];
@@ -544,24 +626,27 @@ __global__ void __launch_bounds__(kEatsThreads) k_eats(EatsArgs A, int items) {
   e.sin_obs = sin(A.o.theta_obs);
   e.cos_obs = cos(A.o.theta_obs);
   e.cj = (item % A.sides) == 1;
+  e.lane = threadIdx.x & 31;
   e.inner = Heap{ws + A.cap_phi, 0, A.cap_theta};
   double I = 0.0;
   const double* tb = e.qv(PBAG_EQ_TBURST);
   if (L.i_end_r > 0 && (q.t_obs < tb[0] || q.t_obs > tb[L.i_end_r - 1])) {  // eats.h:822-827
     e.code = PBAG_ERR_RANGE;
   } else {
-    auto f = [&](double a_phi) -> double { return e.phi_integrand(a_phi); };
+    Eats::Outer fo{e};
     if (A.o.method_quad == PBAG_QUAD_TRAP_FIXED) {
-      I = e.trap(f, 0.0, cgs::pi_, A.o.nmax_phi);
+      I = fo.trap(0.0, cgs::pi_, A.o.nmax_phi);
     } else {
       Heap outer{ws, 0, A.cap_phi};
-      I = e.cadre(f, 0.0, cgs::pi_, A.o.nmax_phi, A.o.rtol_phi, outer);
+      I = e.cadre(fo, 0.0, cgs::pi_, A.o.nmax_phi, A.o.rtol_phi, outer);
     }
   }
   const double Fcoeff = 1.e26 / (4 * cgs::pi_ * A.o.d_l * A.o.d_l);  // cgs2mJy (utils.h:40)
-  A.part[item] = 2 * Fcoeff * I;
-  if (e.code != PBAG_OK)
-    atomicMin(A.first, ((unsigned long long)qi << 8) | (unsigned long long)(-e.code & 0xff));
+  if (e.lane == 0) {
+    A.part[item] = 2 * Fcoeff * I;
+    if (e.code != PBAG_OK)
+      atomicMin(A.first, ((unsigned long long)qi << 8) | (unsigned long long)(-e.code & 0xff));
+  }
 }
 
 // flux = principal jet + counter jet, in evalFluxDensA's order
@@ -663,7 +748,7 @@ extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int n
   if (e == cudaSuccess) {
     k_eats_ln<<<(unsigned)((n_ln + 255) / 256), 256, 0, v.stream>>>(A, d_ln, nl);
     k_eats_mu<<<(unsigned)((n_mu + 255) / 256), 256, 0, v.stream>>>(A, items);
-    k_eats<<<(items + kEatsThreads - 1) / kEatsThreads, kEatsThreads, 0, v.stream>>>(A, items);
+    k_eats<<<(items + kEatsThreads / 32 - 1) / (kEatsThreads / 32), kEatsThreads, 0, v.stream>>>(A, items);
     k_eats_sum<<<(nq + 127) / 128, 128, 0, v.stream>>>(d_part, nq, sides, d_flux);
     e = cudaGetLastError();
   }

@@ -1686,9 +1686,15 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
   auto go = [&](auto kern) { kern<<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out, kstage); };
   // large batches (the kernel-integral table not staged, small shared
   // memory): the register budget of four CTAs per SM, for more resident
-  // blastwaves (no spills at 128 registers for grids up to 256 x 256)
+  // blastwaves (no spills at 128 registers for grids up to 256 x 256); for
+  // grids of at most 256 gamma and 128 nu also six or eight (80 / 64
+  // registers, PBAG_EVOLVE_CTAS)
   if (kstage == 0 && nbw > kStageMaxBw && c <= 2 && fq <= 2) {
-    if (c <= 1)
+    if (c == 2 && fq == 1 && g.evolve_ctas >= 8)
+      go(k_evolve<2, 1, 8>);
+    else if (c == 2 && fq == 1 && g.evolve_ctas >= 6)
+      go(k_evolve<2, 1, 6>);
+    else if (c <= 1)
       fq <= 1 ? go(k_evolve<1, 1, 4>) : go(k_evolve<1, 2, 4>);
     else
       fq <= 1 ? go(k_evolve<2, 1, 4>) : go(k_evolve<2, 2, 4>);
@@ -1770,6 +1776,8 @@ cudaError_t configure_kernels() {
   attr((const void*)k_evolve<1, 2, 4>, esmem);
   attr((const void*)k_evolve<2, 1, 4>, esmem);
   attr((const void*)k_evolve<2, 2, 4>, esmem);
+  attr((const void*)k_evolve<2, 1, 6>, esmem);
+  attr((const void*)k_evolve<2, 1, 8>, esmem);
   attr((const void*)k_rad_ssc<1>, smem);
   attr((const void*)k_rad_ssc<2>, smem);
   attr((const void*)k_rad_ssc<4>, smem);
