@@ -5,6 +5,12 @@ SSC + SSA) on the 21-layer Gaussian jet with forward and reverse shocks
 
 One bench "step" is one pass of the whole batch through the step: every
 blastwave evolved over its 1000-time history (all valid blastwave-steps).
+The inputs are, by default, the reference program's own run of that jet: the
+dynamics its blastwave driver saved (tests/golden/refdrv_gaussian.npz,
+recorded by tests/golden/make_reference_run.py), turned into step records
+exactly as the driver passes them to its radiation step, so that the step
+mix (valid steps, cooling regimes, substep counts) is the reference's own;
+--inputs thin-shell uses the seeded thin-shell histories instead.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -47,6 +53,9 @@ def parse():
                          "the SSC surrogate on states of the sweep, time it against the exact contraction and "
                          "deploy it on the Gaussian jet; eats-lc: the adaptive EATS light curve of the Gaussian jet "
                          "from the step's device-resident histories")
+    ap.add_argument("--inputs", default="driver", choices=["driver", "thin-shell"],
+                    help="driver: step records from the reference program's own Gaussian-jet run (default); "
+                         "thin-shell: seeded thin-shell histories")
     ap.add_argument("--sets", type=int, default=64, help="parameter sets of the uneven-sweep workload")
     ap.add_argument("--train-states", type=int, default=1000000, help="training states of the surrogate workload")
     ap.add_argument("--epochs", type=int, default=8, help="training epochs of the surrogate workload")
@@ -67,26 +76,44 @@ from pyblastafterglowmag_gb300.replicas import dist_info  # noqa: E402
 from pyblastafterglowmag_gb300 import replicas  # noqa: E402
 
 
-def workload(tables=None):
-    """The Gaussian jet's step records. tables: what builds the grids and the
-    shock scalars - the library (default) or, for the CPU arm, the oracle,
-    which produces the same bytes without loading the library."""
+DRIVER_RUN = os.path.join(ROOT, "tests", "golden", "refdrv_gaussian.npz")
+INPUTS = {"driver": "the reference program's own run of the jet: the dynamics its blastwave driver saved "
+                    "(refdrv_gaussian.npz), step records rebuilt as the driver passes them to its step",
+          "thin-shell": "seeded synthetic blastwave histories (thin-shell dynamics)"}
+
+
+def driver_run():
+    from pyblastafterglowmag_gb300 import histories as H
+    return H.DriverRun(DRIVER_RUN)
+
+
+def workload(inputs, tables=None):
+    """The Gaussian jet's step records from `inputs` (INPUTS). tables:
+    what builds the grids and the shock scalars - the library (default) or,
+    for the CPU arm, the oracle, which produces the same bytes without
+    loading the library."""
     from pyblastafterglowmag_gb300 import histories as H
     if tables is None:
         from pyblastafterglowmag_gb300 import _lib as tables
     cfg = H.config_gaussian_ssc()
-    recs, off, prm, grid = H.make_batch(tables, cfg)
+    if inputs == "driver":
+        run = driver_run()
+        assert (run.grid.ngam, run.grid.nfreq, run.nlayers) == (cfg.ngam, cfg.nfreq, cfg.nlayers)
+        recs, off, prm = run.records(tables)
+        grid = run.grid
+    else:
+        recs, off, prm, grid = H.make_batch(tables, cfg)
     return cfg, recs, off, prm, grid
 
 
-def config_dict(cfg, recs, prm, extra=None):
+def config_dict(cfg, recs, prm, inputs, extra=None):
     d = {"workload": WORKLOAD, "blastwaves": int(len(prm)), "layers": cfg.nlayers,
          "shocks": "forward+reverse", "ngam": cfg.ngam, "nfreq": cfg.nfreq, "ntb": cfg.ntb,
          "valid_blastwave_steps_per_pass": int((recs["mode"] != 0).sum()),
          "radiation": "synchrotron(CSYN)+SSA+SSC", "solve": "Chang-Cooper, FP64 state, double-float substeps",
          "ssc_contraction": "FP32 accumulate, per-blastwave power-of-two scaling",
          "l2": "flushed with a 256 MiB device write before every timed pass",
-         "inputs": "seeded synthetic blastwave histories (thin-shell dynamics)"}
+         "inputs": INPUTS[inputs]}
     if extra:
         d.update(extra)
     return d
@@ -212,7 +239,7 @@ def reference_arm(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build_oracle()
-    cfg, recs, off, prm, grid = workload(pyoracle.Oracle())
+    cfg, recs, off, prm, grid = workload(args.inputs, pyoracle.Oracle())
     threads = os.cpu_count() or 1
     per_step = max(10.0, min(60.0, 150.0 / max(args.steps + args.warmup, 1)))
     vals, dts, desc = [], [], ""
@@ -226,7 +253,7 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(dts),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": config_dict(cfg, recs, prm, {"sample": desc}),
+            "config": config_dict(cfg, recs, prm, args.inputs, {"sample": desc}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -240,7 +267,7 @@ def gb300_arm(args):
     replicas.init(world)
     from pyblastafterglowmag_gb300 import _lib, abi, build
     build.build()
-    cfg, recs, off, prm, grid = workload()
+    cfg, recs, off, prm, grid = workload(args.inputs)
     nvalid = int((recs["mode"] != 0).sum())
     nrec, nbw, F = len(recs), len(prm), grid.nfreq
     ctx = _lib.Context(grid, device=local, ssc=True)
@@ -388,7 +415,7 @@ def gb300_arm(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
-            "config": config_dict(cfg, recs, prm, {"parallelism": f"replicas{world}"}),
+            "config": config_dict(cfg, recs, prm, args.inputs, {"parallelism": f"replicas{world}"}),
             "clocks": clk.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
@@ -401,7 +428,7 @@ def gb300_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def output_check(recs, off, prm, grid, got, bws=(0, 1, 10, 11, 40, 41), tol=1e-4):
+def output_check(recs, off, prm, grid, got, bws=(0, 1, 10, 11, 16, 17, 40), tol=1e-4):
     """The histories of the last end-to-end pass against the FP64 oracle on a
     sample of whole blastwaves (each blastwave's history is independent, so a
     subset runs exactly as in the batch): per-row relative L2 of every timed
@@ -695,7 +722,7 @@ def surrogate_arm(args):
     dev = torch.device("cuda", local)
     if args.profile:
         return surrogate_profile(args, dev)
-    cfg, recs, off, prm, g = workload()
+    cfg, recs, off, prm, g = workload(args.inputs)
     _, freq = _lib.grids(g)
     ctx = _lib.Context(g, device=local, ssc=True)
     SG.configure(ctx)
@@ -818,7 +845,10 @@ def eats_arm(args):
     them there. The CPU figure is the oracle's restatement of the reference's
     EATS integrator on one host core over a sample of the queries; the
     line's parity compares the GPU light curve with the oracle's on that
-    sample (same histories)."""
+    sample (same histories). With the default inputs (the reference
+    program's run) the layers, dynamics and EATS options are the run's, and
+    the parity also holds the GPU light curve at the run's own observer
+    times against the light curve the reference program wrote."""
     import torch
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
@@ -826,7 +856,7 @@ def eats_arm(args):
     build.build()
     pyoracle.build_oracle()
     orc = pyoracle.Oracle()
-    cfg, recs, off, prm, grid = workload()
+    cfg, recs, off, prm, grid = workload(args.inputs)
     dev = torch.device("cuda", 0)
     ctx = _lib.Context(grid, device=0, ssc=True)
     nrec = len(recs)
@@ -834,14 +864,22 @@ def eats_arm(args):
     d_prm = torch.from_numpy(prm.view(np.uint8).copy()).to(dev)
     d_out = {k: torch.zeros((nrec, grid.nfreq), dtype=torch.float64, device=dev) for k in ("j_all", "a_all")}
     ctx.run_device(d_prm.data_ptr(), len(prm), off, d_recs.data_ptr(), {k: v.data_ptr() for k, v in d_out.items()})
-    layers, dyn = H.eats_inputs(cfg, recs, off)
-    o = abi.EatsOpts()
-    o.theta_obs, o.z, o.d_l = np.deg2rad(20.8), 0.0, 3.09e26
-    o.rtol_theta = o.rtol_phi = 1e-6
+    run = None
+    if args.inputs == "driver":
+        # the reference run's layers, dynamics and parfile EATS options
+        run = driver_run()
+        layers, dyn, q_run = run.eats()
+        o = run.eats_opts()
+    else:
+        layers, dyn = H.eats_inputs(cfg, recs, off)
+        o = abi.EatsOpts()
+        o.theta_obs, o.z, o.d_l = np.deg2rad(20.8), 0.0, 3.09e26
+        o.rtol_theta = o.rtol_phi = 1e-6
+        o.counter_jet = 1
+        o.flux.shock_vel, o.flux.method_ne = abi.PBAG_VEL_SHOCK, abi.PBAG_NE_USE_NE
+        o.flux.method_tau = abi.PBAG_TAU_APPROX
     o.method_quad = abi.PBAG_QUAD_CADRE if args.quad == "cadre" else abi.PBAG_QUAD_TRAP_FIXED
     o.nmax_theta = o.nmax_phi = 1000 if args.quad == "cadre" else 100
-    o.counter_jet = 1
-    o.flux.shock_vel, o.flux.method_ne, o.flux.method_tau = abi.PBAG_VEL_SHOCK, abi.PBAG_NE_USE_NE, abi.PBAG_TAU_APPROX
     t_obs = np.logspace(np.log10(3e3), np.log10(1e9), args.lc_times)
     q = np.zeros(len(layers) * len(t_obs), dtype=abi.EATS_QUERY_DTYPE)
     q["layer"] = np.repeat(np.arange(len(layers)), len(t_obs))
@@ -877,19 +915,32 @@ def eats_arm(args):
     rc, fail, ref = orc.eats_flux(grid, o, layers, dyn, off, j, a, q[sel])
     cpu_s = time.perf_counter() - t0
     rel = np.abs(got[sel] - ref) / ref
+    parity = {"max_rel": float(rel.max()), "oracle_status": int(rc), "tol": 1e-5,
+              "ok": bool(rc == 0 and rel.max() <= 1e-5)}
+    if run is not None and args.quad == "cadre":
+        # the reference program's own light curve of the run (every layer at
+        # its recorded observer times), from the GPU step's histories
+        d_qr = torch.from_numpy(q_run.view(np.uint8).copy()).to(dev)
+        d_fr = torch.zeros(len(q_run), dtype=torch.float64, device=dev)
+        _lib.eats_flux_a(ctx, o, layers, d_dyn.data_ptr(), dyn.shape[-1], off, d_out["j_all"].data_ptr(),
+                         d_out["a_all"].data_ptr(), len(q_run), d_qr.data_ptr(), d_fr.data_ptr())
+        lc = run.lc.ravel()
+        parity["vs_reference_program"] = {"points": int(len(lc)),
+                                          "max_rel": float(np.max(np.abs(d_fr.cpu().numpy() - lc) / lc)),
+                                          "tol": 1e-4}
     line = {"metric": "EATS light-curve points/s (adaptive quadrature) on 1 GB300", "value": len(q) / (t * 1e-3),
             "unit": "points/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"eats-lc-gaussian-jet-21-layers-fs-rs-{args.quad}",
                        "layers": len(layers), "lc_times": len(t_obs), "queries": len(q), "theta_obs_deg": 20.8,
                        "nu_obs": 1e15, "quadrature": args.quad, "nmax": o.nmax_phi, "rtol": o.rtol_phi,
-                       "counter_jet": True, "histories": "the GPU step's, device-resident"},
+                       "counter_jet": True, "histories": "the GPU step's, device-resident",
+                       "inputs": INPUTS[args.inputs]},
             "clocks": clk.summary(),
             "cpu_baseline": {"value": len(sel) / cpu_s, "unit": "points/s", "cores": 1, "kind": "port",
                              "sample": f"{len(sel)} of the {len(q)} queries (every 4th observer time), the oracle's "
                                        "restatement of the reference's EATS integrator (equal to it bit for bit)"},
-            "parity": {"max_rel": float(rel.max()), "oracle_status": int(rc), "tol": 1e-5,
-                       "ok": bool(rc == 0 and rel.max() <= 1e-5)}}
+            "parity": parity}
     print(json.dumps(line), flush=True)
 
 

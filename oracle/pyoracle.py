@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpbag_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpbaref.so")
 REF_EATS_SO = os.path.join(HERE, "_ref", "libpbaref_eats.so")
+REF_RUN_SO = os.path.join(HERE, "_ref", "libpbaref_run.so")
 # the reference project's src/ directory: PBAG_REF_SRC, else a checkout named
 # "reference" next to this repository
 REF_SRC = os.environ.get("PBAG_REF_SRC") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")

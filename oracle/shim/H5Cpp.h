@@ -5,10 +5,11 @@
 // (struct Output) writes HDF5 files and src/utilitites/H5Easy.h reads them
 // (pulled in by the blastwave and EATS headers). None of that is on the paths
 // the oracle harnesses drive, so these declarations only need to let the
-// headers compile; writing is a no-op. Reading serves datasets and scalar
-// attributes that a harness registered in memory (pbag_h5::put / put_attr,
-// keyed by file path and name), so that the reference's own loaders (e.g. the
-// ejecta initial data, ejecta_id.h) run on inputs given without a file.
+// headers compile. Datasets and scalar attributes live in an in-memory store
+// keyed by "file//group/name" (pbag_h5): what the reference writes is kept
+// there instead of in a file (its dynamics and spectrum writers, read back by
+// a harness), and what a harness puts there is what the reference's loaders
+// read (e.g. the ejecta initial data of ejecta_id.h), without HDF5.
 #ifndef PBAG_ORACLE_SHIM_H5CPP_H
 #define PBAG_ORACLE_SHIM_H5CPP_H
 
@@ -95,7 +96,7 @@ struct DataSpace {
   std::vector<unsigned long long> dims;
   DataSpace() {}
   DataSpace(int) {}
-  DataSpace(int, const hsize_t*) {}
+  DataSpace(int rank, const hsize_t* d) : dims(d, d + rank) {}
   DataSpace(H5S_class_t) {}
   int getSimpleExtentNdims() const { return (int)dims.size(); }
   int getSimpleExtentDims(hsize_t* d, hsize_t* = nullptr) const {
@@ -111,7 +112,9 @@ struct DataSpace {
 };
 struct Attribute {
   std::string key;
-  template <typename... A> void write(A&&...) {}
+  void write(const DataType&, const void* v) {
+    if (!key.empty()) pbag_h5::attributes()[key] = *static_cast<const double*>(v);
+  }
   void read(const DataType&, void* v) const {
     auto it = pbag_h5::attributes().find(key);
     *static_cast<double*>(v) = it == pbag_h5::attributes().end() ? -1. : it->second;
@@ -121,7 +124,14 @@ struct Attribute {
 };
 struct DataSet {
   std::string key;
-  void write(const void*, const PredType&) {}
+  std::vector<unsigned long long> dims;
+  void write(const void* buf, const PredType&) {
+    if (key.empty()) return;
+    size_t n = dims.empty() ? 0 : 1;
+    for (unsigned long long d : dims) n *= (size_t)d;
+    const double* in = static_cast<const double*>(buf);
+    pbag_h5::datasets()[key] = pbag_h5::Entry{std::vector<double>(in, in + n), dims};
+  }
   void read(void* buf, const PredType&) const {
     if (const pbag_h5::Entry* e = pbag_h5::find(key)) {
       double* out = static_cast<double*>(buf);
@@ -139,10 +149,19 @@ struct DataSet {
   IntType getIntType() const { return {}; }
 };
 struct Group {
+  std::string path;
   Group() {}
-  template <typename... A> DataSet createDataSet(A&&...) { return {}; }
-  template <typename... A> Attribute createAttribute(A&&...) { return {}; }
-  DataSet openDataSet(const std::string&) const { return {}; }
+  explicit Group(const std::string& p) : path(p) {}
+  DataSet createDataSet(const std::string& n, const DataType&, const DataSpace& sp) {
+    return DataSet{path + "/" + n, sp.dims};
+  }
+  DataSet createDataSet(const std::string& n, const PredType&, const DataSpace& sp) {
+    return DataSet{path + "/" + n, sp.dims};
+  }
+  Attribute createAttribute(const std::string& n, const DataType&, const DataSpace&) {
+    return Attribute{path + "/" + n};
+  }
+  DataSet openDataSet(const std::string& n) const { return DataSet{path + "/" + n}; }
   long getId() const { return 0; }
   void close() {}
 };
@@ -150,10 +169,17 @@ struct H5File {
   std::string name;
   H5File() {}
   H5File(const std::string& n, unsigned) : name(n) {}
-  template <typename... A> DataSet createDataSet(A&&...) { return {}; }
-  template <typename... A> Attribute createAttribute(A&&...) { return {}; }
-  Group createGroup(const std::string&) { return {}; }
-  Group openGroup(const std::string&) { return {}; }
+  DataSet createDataSet(const std::string& n, const DataType&, const DataSpace& sp) {
+    return DataSet{name + "//" + n, sp.dims};
+  }
+  DataSet createDataSet(const std::string& n, const PredType&, const DataSpace& sp) {
+    return DataSet{name + "//" + n, sp.dims};
+  }
+  Attribute createAttribute(const std::string& n, const DataType&, const DataSpace&) {
+    return Attribute{name + "//" + n};
+  }
+  Group createGroup(const std::string& g) { return Group(name + "//" + g); }
+  Group openGroup(const std::string& g) { return Group(name + "//" + g); }
   DataSet openDataSet(const std::string& v) const { return DataSet{name + "//" + v}; }
   Attribute openAttribute(const std::string& k) const { return Attribute{name + "//" + k}; }
   bool attrExists(const std::string& k) const { return pbag_h5::attributes().count(name + "//" + k) > 0; }

@@ -15,6 +15,10 @@ The value ranges (Lorentz factors, densities, cooling regimes, substep
 counts from 1 to max_substeps, the gamma_min <= 2 analytic fallback late on)
 follow the reference's configurations; the exact dynamics do not matter for the
 comoving step, whose parity is checked on identical records.
+
+driver_records / DriverRun build the same records from the dynamics the
+reference's own program saved (a recorded run), exactly as its driver passes
+them to the step, so that the step mix is the reference's own.
 """
 from dataclasses import dataclass, field
 
@@ -38,6 +42,14 @@ class Shock:
     ele_method: int = abi.PBAG_ELE_NUMERIC
     syn_method: int = abi.PBAG_SYN_CSYN
     adi: bool = True
+    # computeEleSpectrumLimits' methods (pbag_limits_opts codes; the
+    # reference's parfile defaults are useNumeric / useTcomov / useB /
+    # useU_b / use_Sironi = 1, 1, 0, 0, 3)
+    method_gamma_min: int = 0
+    method_gamma_c: int = 0
+    method_gamma_max: int = 0
+    method_B: int = 0
+    method_nonrel: int = 0
 
 
 @dataclass
@@ -200,11 +212,11 @@ def limits_opts(sh):
     o = abi.LimitsOpts()
     o.p, o.eps_e, o.eps_b, o.eps_t = sh.p, sh.eps_e, sh.eps_b, 0.0
     o.beta_min, o.mu, o.mu_e = 1e-5, 0.62, 1.18
-    o.method_B = 0          # useU_b
-    o.method_gamma_min = 0  # useU_e
-    o.method_gamma_c = 0    # useTe
-    o.method_gamma_max = 0  # useB
-    o.method_nonrel = 0     # none
+    o.method_B = sh.method_B
+    o.method_gamma_min = sh.method_gamma_min
+    o.method_gamma_c = sh.method_gamma_c
+    o.method_gamma_max = sh.method_gamma_max
+    o.method_nonrel = sh.method_nonrel
     o.ele_analytic = 0
     return o
 
@@ -335,6 +347,203 @@ def make_batch(lib, cfg, nsteps=None):
     offsets = np.zeros(len(recs) + 1, dtype=np.int64)
     offsets[1:] = np.cumsum([len(r) for r in recs])
     return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE), grid
+
+
+def driver_records(lib, dyn, shocks, gam, beta_min=1e-5):
+    """Step records of every blastwave of a jet from the dynamics its ODE
+    driver saved, following the driver's in-situ calls
+    (blastwave_radiation.h:881-1198): at every time index `it` the blastwave
+    is valid (isBlastWaveValidForElectronCalc, :881-959: R >= 1, beta >=
+    beta_min, U_p > 0, rho2 > 0); the forward shock's limits come from
+    updateSockProperties(U_p, Gamma, GammaFsh, tt, tburst, tcomov, rho2/m_p,
+    M2/m_p) (:1047-1066), its step is initializeElectronDistribution(tcomov,
+    M2, rho2, U_p, thickness) on the first valid index and
+    evaluateElectronDistributionNumericMixed with the comoving thickness
+    thickness * GammaFsh at it-1 and it afterwards (:1147-1182); the reverse
+    shock, where considerReverseShock holds (:961-974: it > 0, the RS
+    thickness at it-1, GammaRsh and U_p3 positive), the same with U_p3,
+    GammaRsh, rho3, M3, thichness_rs - its comoving thickness at `it` is
+    multiplied by GammaRsh at it-1, as the driver does (:1125-1129).
+
+    dyn: one dict per layer of the saved histories by their names
+    (BW::VARNAMES); shocks: (forward, reverse-or-None) Shock options.
+    Returns (recs, offsets, params); blastwaves layer by layer, forward shock
+    then reverse shock."""
+    recs, params = [], []
+    mp = M_P
+    for d in dyn:
+        n = len(d["tburst"])
+        valid = (d["R"] >= 1) & (d["beta"] >= beta_min) & (d["U_p"] > 0) & (d["rho2"] > 0)
+        for is_rs, sh in ((False, shocks[0]), (True, shocks[1])):
+            if sh is None:
+                continue
+            if is_rs and "U_p3" not in d:
+                # a layer whose Gamma0 is below min_Gamma0_for_rs runs no
+                # reverse shock (blastwave_base.h:449-453) and saves no
+                # reverse-shock quantities: its blastwave is all skips
+                r = np.zeros(n, dtype=abi.STEP_DTYPE)
+                r["mode"] = abi.PBAG_SKIP
+                recs.append(r)
+                params.append(shock_params(sh))
+                continue
+            if is_rs:
+                up, gsh, rho, m, th = d["U_p3"], d["GammaRsh"], d["rho3"], d["M3"], d["thichness_rs"]
+                prev_th = np.concatenate([[0.0], th[:-1]])
+                ok = valid & (np.arange(n) > 0) & (prev_th > 0) & (gsh > 0) & (up > 0)
+            else:
+                up, gsh, rho, m, th = d["U_p"], d["GammaFsh"], d["rho2"], d["M2"], d["thickness"]
+                ok = valid.copy()
+            ss = np.zeros(n, dtype=abi.SHOCK_STATE_DTYPE)
+            ss["e_prime"], ss["Gamma"], ss["GammaSh"] = up, d["Gamma"], gsh
+            ss["t_e"], ss["t_b"], ss["tcomov"] = d["tt"], d["tburst"], d["tcomov"]
+            ss["n_prime"], ss["n_protons"] = rho / mp, m / mp
+            # the driver updates the shock only at the steps it runs, in order
+            lim = np.zeros(n, dtype=abi.LIMITS_DTYPE)
+            if ok.any():
+                lim[ok] = lib.shock_limits(limits_opts(sh), gam, ss[ok])
+            r = np.zeros(n, dtype=abi.STEP_DTYPE)
+            r["mode"] = np.where(ok, abi.PBAG_EVOLVE, abi.PBAG_SKIP)
+            first = int(np.argmax(ok)) if ok.any() else n
+            if first < n:
+                r["mode"][first] = abi.PBAG_INIT
+            prev = lambda a: np.concatenate([a[:1], a[:-1]])
+            r["tc"], r["tc_p1"] = prev(d["tcomov"]), d["tcomov"]
+            r["m"], r["m_p1"] = prev(m), m
+            r["rho"], r["rho_p1"] = prev(rho), rho
+            r["u_p"], r["u_p_p1"] = prev(up), up
+            gprev = prev(gsh)
+            r["dr"] = prev(th) * gprev
+            r["dr_p1"] = th * (gprev if is_rs else gsh)
+            if first < n:
+                r["dr"][first] = th[first]
+            for k in ("B", "gamma_min", "gamma_max", "gamma_c", "accel_frac"):
+                r[k] = lim[k]
+            r["n_prime"] = ss["n_prime"]
+            recs.append(r)
+            params.append(shock_params(sh))
+    offsets = np.zeros(len(recs) + 1, dtype=np.int64)
+    offsets[1:] = np.cumsum([len(r) for r in recs])
+    return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE)
+
+
+# the saved dynamics (BW::VARNAMES) each pbag_eats_q quantity is read from
+DRIVER_EATS_Q = {"tburst": "tburst", "R": "R", "theta": "theta", "Gamma": "Gamma", "beta": "beta",
+                 "GammaFsh": "GammaFsh", "thickness": "thickness", "M2": "M2", "rho2": "rho2", "Rsh": "Rsh",
+                 "acc_frac": "accel_frac", "ctheta": "ctheta", "GammaRsh": "GammaRsh",
+                 "thickness_rs": "thichness_rs", "M3": "M3", "rho3": "rho3", "Rrsh": "Rsh_rs",
+                 "acc_frac_rs": "accel_frac_rs"}
+
+
+def driver_eats_inputs(dyn, theta_wing, rs):
+    """The layer table and the EATS dynamics of a jet from the dynamics its
+    ODE driver saved, as the reference's adaptive light curve reads them
+    (Ejecta::computeEjectaLightCurve, ejecta_base.h:1160-1190 over
+    EATS::evalFluxDensA, eats.h:823-850): layer l spans theta_pw[l] ..
+    theta_pw[l+1], theta_pw[i] = 2 asin(i / nlayers sin(theta_wing / 2)) -
+    the 1D initial data's loader sets up the adaptive grid and then the
+    piece-wise one over it (EjectaID2::_init_pw_grid, ejecta_id.h:161-181,
+    called after _init_a_grid at :293-296), so the piece-wise edges are the
+    ones the light curve reads; its histories end at the first R == 0
+    (checkEvolutionEnd, blastwave.h:243-253). Blastwave numbering as
+    driver_records: 2 l and 2 l + 1 with the reverse shock, l without.
+    Returns (layers, dyn [nlayers][PBAG_EQ_N][nr])."""
+    nl = len(dyn)
+    nr = len(dyn[0]["tburst"])
+    layers = np.zeros(nl, dtype=abi.EATS_LAYER_DTYPE)
+    out = np.zeros((nl, abi.PBAG_EQ_N, nr))
+    edge = [2.0 * np.arcsin(i / nl * np.sin(theta_wing / 2.0)) for i in range(nl + 1)]
+    per = 2 if rs else 1
+    for il, d in enumerate(dyn):
+        for iq, q in enumerate(abi.EATS_Q):
+            src = DRIVER_EATS_Q[q]
+            if src in d:
+                out[il, iq] = d[src]
+        zero = np.flatnonzero(d["R"] == 0.0)
+        i_end = int(zero[0]) if len(zero) else nr
+        has_rs = rs and "U_p3" in d  # no reverse shock below min_Gamma0_for_rs
+        layers[il] = (i_end, per * il, per * il + 1 if has_rs else -1, 0, edge[il], edge[il + 1], 1.0)
+    return layers, out
+
+
+# the parfile's microphysics methods of a recorded run (method_gamma_min
+# useNumeric, method_gamma_c useTcomov, method_gamma_max useB, method_B
+# useU_b, method_nonrel_dist use_Sironi) and max_substeps
+DRIVER_METHODS = dict(method_gamma_min=1, method_gamma_c=1, method_gamma_max=0, method_B=0, method_nonrel=3,
+                      max_substeps=2000)
+
+
+class DriverRun:
+    """A run of the reference's own program recorded to an .npz (the dynamics
+    its blastwave driver saved, saveEjectaBWsDynamics; the comoving spectra
+    its step wrote, computeSaveEjectaSpectrum; its adaptive-EATS light curve,
+    computeSaveEjectaLightCurve; the run's options): grid, per-layer
+    dynamics, shock options, the reference's spectra
+    (spec[(layer, "fs"|"rs", "j"|"a")], every `every`-th time index) and
+    light curve (lc [nlayers][ntimes])."""
+
+    def __init__(self, path):
+        z = np.load(path)
+        g = z["grid"]
+        self.grid = abi.GridDesc(int(g[0]), int(g[1]), g[2], g[3], g[4], g[5])
+        self.nlayers = int(z["layers"])
+        # per layer the quantities its blastwave saved (no reverse-shock ones
+        # where the driver ran none)
+        self.dyn = [{k.split("_", 1)[1]: z[k] for k in z.files if k.startswith(f"dyn{il}_")}
+                    for il in range(self.nlayers)]
+        self.rs = bool(z["opt_rs"])
+        ssc, ssa = bool(z["opt_ssc"]), bool(z["opt_ssa"])
+        fs = Shock(eps_e=float(z["par_eps_e_fs"]), eps_b=float(z["par_eps_b_fs"]), p=float(z["par_p_fs"]),
+                   ssc=ssc, ssa=ssa, **DRIVER_METHODS)
+        rs = Shock(eps_e=float(z["par_eps_e_rs"]), eps_b=float(z["par_eps_b_rs"]), p=float(z["par_p_rs"]),
+                   ssc=ssc, ssa=ssa, **DRIVER_METHODS) if self.rs else None
+        self.shocks = (fs, rs)
+        self.every = int(z["spec_every"])
+        self.spec = {}
+        for k in z.files:
+            if k.startswith("spec") and k[4].isdigit():
+                il, rest = k[4:].split("_", 1)           # "<il>_total_<q>_<shock>"
+                _, q, shock = rest.split("_")
+                self.spec[(int(il), shock, q)] = z[k]
+        self.theta_wing = float(z["id_theta_wing"])
+        self.theta_obs, self.z, self.d_l = float(z["par_theta_obs"]), float(z["par_z"]), float(z["par_d_l"])
+        self.lc_times, self.lc_freqs = z["lc_times"], z["lc_freqs"]
+        self.lc = np.array([z[f"lc{il}"] for il in range(self.nlayers)])
+
+    def blastwave(self, il, shock):
+        """Index of (layer, "fs"|"rs") among driver_records' blastwaves."""
+        return (2 * il + (shock == "rs")) if self.rs else il
+
+    def records(self, tables, layers=None):
+        """driver_records over the first `layers` layers (all by default);
+        tables: what provides grids and shock_limits (the library, or the
+        oracle where the library must not be loaded)."""
+        gam, _ = tables.grids(self.grid)
+        dyn = self.dyn if layers is None else self.dyn[:layers]
+        return driver_records(tables, dyn, self.shocks, gam)
+
+    def eats_opts(self):
+        """The parfile's EATS options: CADRE, counter jet, rtol 1e-6 and
+        nmax 1000 in theta and phi, method_vel sameAsBW, method_ne useNe,
+        method_tau smooth."""
+        o = abi.EatsOpts()
+        o.theta_obs, o.z, o.d_l = self.theta_obs, self.z, self.d_l
+        o.rtol_theta = o.rtol_phi = 1e-6
+        o.nmax_theta = o.nmax_phi = 1000
+        o.method_quad = abi.PBAG_QUAD_CADRE
+        o.counter_jet = 1
+        o.flux.shock_vel = abi.PBAG_VEL_SAME_AS_BW
+        o.flux.method_ne, o.flux.method_tau = abi.PBAG_NE_USE_NE, abi.PBAG_TAU_SMOOTH
+        return o
+
+    def eats(self):
+        """(layers, dyn, queries): every layer at every light-curve time."""
+        layers, dyn = driver_eats_inputs(self.dyn, self.theta_wing, self.rs)
+        nt = len(self.lc_times)
+        q = np.zeros(self.nlayers * nt, dtype=abi.EATS_QUERY_DTYPE)
+        for il in range(self.nlayers):
+            for k in range(nt):
+                q[il * nt + k] = (il, 0, self.lc_times[k], self.lc_freqs[k])
+        return layers, dyn, q
 
 
 def eats_inputs(cfg, recs, offsets, nsteps=None):
