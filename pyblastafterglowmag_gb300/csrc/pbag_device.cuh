@@ -20,6 +20,7 @@ constexpr int kStepWarps = kStepThreads / 32;
 constexpr int kFinalPerThread = (PBAG_MAX_BINS + kStepThreads - 1) / kStepThreads;  // frequencies per thread in finalize
 constexpr int kKintStageMax = 112 * 1024;  // largest SSC kernel-integral table staged in shared memory
 constexpr int kScanMaxSub = 32;       // below this many substeps the solve is a parallel scan, else systolic
+constexpr int kFirstValidThreads = 256;  // records one k_first_valid CTA tests at a time
 constexpr int kKernelClasses = 3;     // evolve, ssc (+radiation), finalize (pbag_kernel_class)
 constexpr int kClassEvolve = PBAG_K_EVOLVE, kClassSsc = PBAG_K_SSC, kClassFinalize = PBAG_K_FINALIZE;
 constexpr int kSiteSynBank = 900001;  // status site: a field outside the synchrotron bank's range

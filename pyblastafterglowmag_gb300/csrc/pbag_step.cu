@@ -112,14 +112,30 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-__global__ void k_first_valid(const pbag_step_rec* __restrict__ recs, const int64_t* __restrict__ off, int nbw,
-                              int64_t* __restrict__ first) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+// One CTA per blastwave: its threads test kFirstValidThreads consecutive
+// records at a time (independent loads, not one dependent chain per
+// blastwave - a history that is never valid would otherwise cost one load
+// latency per record).
+__global__ void __launch_bounds__(kFirstValidThreads) k_first_valid(const pbag_step_rec* __restrict__ recs,
+                                                                    const int64_t* __restrict__ off, int nbw,
+                                                                    int64_t* __restrict__ first) {
+  const int b = blockIdx.x;
   if (b >= nbw) return;
-  int64_t r = off[b];
-  const int64_t end = off[b + 1];
-  while (r < end && recs[r].mode == PBAG_SKIP) ++r;
-  first[b] = r;  // == end when the blastwave is never valid
+  const int64_t beg = off[b], end = off[b + 1];
+  for (int64_t r0 = beg; r0 < end; r0 += kFirstValidThreads) {
+    const int64_t r = r0 + threadIdx.x;
+    const bool hit = r < end && recs[r].mode != PBAG_SKIP;
+    if (__syncthreads_or(hit)) {
+      __shared__ int lo;
+      if (threadIdx.x == 0) lo = kFirstValidThreads;
+      __syncthreads();
+      if (hit) atomicMin(&lo, (int)threadIdx.x);
+      __syncthreads();
+      if (threadIdx.x == 0) first[b] = r0 + lo;
+      return;
+    }
+  }
+  if (threadIdx.x == 0) first[b] = end;  // the blastwave is never valid
 }
 
 __global__ void k_powp(DevGrid g, const pbag_shock_params* __restrict__ prm, int nbw, double* __restrict__ powp) {
@@ -1667,7 +1683,7 @@ cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_
                            const pbag_shock_params* prm, int nbw, int64_t nrec, int64_t* first, StepScal* ss,
                            cudaStream_t st) {
   if (nbw <= 0) return cudaSuccess;
-  k_first_valid<<<(nbw + 127) / 128, 128, 0, st>>>(recs, off, nbw, first);
+  k_first_valid<<<nbw, kFirstValidThreads, 0, st>>>(recs, off, nbw, first);
   const int64_t npw = (int64_t)nbw * g.G;
   k_powp<<<(unsigned)((npw + 255) / 256), 256, 0, st>>>(g, prm, nbw, S.powp);
   if (nrec > 0)
