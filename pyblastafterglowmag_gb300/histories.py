@@ -426,6 +426,69 @@ def driver_records(lib, dyn, shocks, gam, beta_min=1e-5):
     return np.concatenate(recs), offsets, np.array(params, dtype=abi.SHOCK_PARAMS_DTYPE)
 
 
+SIGMA_T = 6.6524e-25
+M_E = 9.1094e-28
+
+
+def substeps(recs, offsets, params, gam):
+    """Chang-Cooper substeps of every record as the step counts them
+    (microphysics.h:412-435): -1 for a blastwave's first valid record (the
+    initialisation), 0 for skipped records and for the analytic gamma_min <= 2
+    law (:446-448), else the substep count of the record's time step."""
+    n = np.zeros(len(recs), dtype=np.int64)
+    dlog = (gam[1] - gam[0]) / gam[0]
+    for b in range(len(params)):
+        r = recs[offsets[b]:offsets[b + 1]]
+        v = np.flatnonzero(r["mode"] != 0)
+        if not len(v):
+            continue
+        out = n[offsets[b]:offsets[b + 1]]
+        out[v[0]] = -1
+        x = r[v[1:]]
+        dt = x["tc_p1"] - x["tc"]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dlnv = 1.0 / dt * (1.0 - (x["m"] / x["rho"]) / (x["m_p1"] / x["rho_p1"]))
+            if not params[b]["adi_on"]:
+                dlnv = np.zeros_like(dt)
+            dts = SIGMA_T * x["gamma_max"] * x["B"] ** 2 / (6.0 * np.pi * M_E * C_LIGHT)
+            dta = (x["gamma_max"] ** 2 - 1.0) / (3.0 * x["gamma_max"] ** 2) * dlnv
+            d = dlog / (dts + dta)
+            ms = int(params[b]["max_substeps"])
+            k = np.where(d >= dt, 1, np.where(d < dt / ms, ms, np.floor(dt / np.where(d > 0, d, 1.0))))
+        k = np.where(x["gamma_min"] <= 2.0, 0, k)
+        if params[b]["ele_method"] == abi.PBAG_ELE_MIX:
+            k[:] = 0
+        out[v[1:]] = k.astype(np.int64)
+    return n
+
+
+def split_chain(recs, offsets, params, gam):
+    """The blastwaves' Chang-Cooper chains and the rest: (chain, rest) where
+    chain = (recs, offsets, params) of every blastwave with Chang-Cooper
+    records, cut after its last one, and rest = (recs, offsets, params) of
+    every other valid record as a one-step blastwave. A timing aid: the
+    chain is the part of a batch whose steps depend on one another through
+    N(gamma); the rest still depends on its previous step through the photon
+    field when SSC is on, so the one-step form computes other numbers."""
+    ns = substeps(recs, offsets, params, gam)
+    cr, cl, cp, rest = [], [], [], []
+    for b in range(len(params)):
+        cc = np.flatnonzero(ns[offsets[b]:offsets[b + 1]] > 0)
+        end = int(cc[-1]) + 1 if len(cc) else 0
+        if end:
+            cr.append(recs[offsets[b]:offsets[b] + end])
+            cl.append(end)
+            cp.append(params[b])
+        rest.extend(range(offsets[b] + end, offsets[b + 1]))
+    co = np.zeros(len(cl) + 1, dtype=np.int64)
+    co[1:] = np.cumsum(cl)
+    chain = (np.concatenate(cr) if cr else recs[:0], co, np.array(cp, dtype=abi.SHOCK_PARAMS_DTYPE))
+    rest = np.array(rest, dtype=np.int64)
+    rest = rest[recs["mode"][rest] != 0]
+    bw = np.searchsorted(offsets, rest, side="right") - 1
+    return chain, (recs[rest].copy(), np.arange(len(rest) + 1, dtype=np.int64), params[bw])
+
+
 # the saved dynamics (BW::VARNAMES) each pbag_eats_q quantity is read from
 DRIVER_EATS_Q = {"tburst": "tburst", "R": "R", "theta": "theta", "Gamma": "Gamma", "beta": "beta",
                  "GammaFsh": "GammaFsh", "thickness": "thickness", "M2": "M2", "rho2": "rho2", "Rsh": "Rsh",
