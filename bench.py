@@ -46,13 +46,14 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="gaussian-jet",
-                    choices=["gaussian-jet", "contraction", "uneven-sweep", "surrogate", "eats-lc"],
+                    choices=["gaussian-jet", "contraction", "uneven-sweep", "surrogate", "eats-lc", "bw-rhs"],
                     help="gaussian-jet: the step benchmark (default); contraction: the emissivity-"
                          "contraction microbenchmark (65536 states, 256 gamma x 256 nu); uneven-sweep: a "
                          "seeded sample of the 4096-set parameter sweep with uneven step counts; surrogate: train "
                          "the SSC surrogate on states of the sweep, time it against the exact contraction and "
                          "deploy it on the Gaussian jet; eats-lc: the adaptive EATS light curve of the Gaussian jet "
-                         "from the step's device-resident histories")
+                         "from the step's device-resident histories; bw-rhs: the blastwave ODE right-hand side "
+                         "over a large batch of blastwave states")
     ap.add_argument("--inputs", default="driver", choices=["driver", "thin-shell"],
                     help="driver: step records from the reference program's own Gaussian-jet run (default); "
                          "thin-shell: seeded thin-shell histories")
@@ -71,6 +72,7 @@ def parse():
                     help="states checked against the FP64 oracle in the contraction benchmark")
     ap.add_argument("--lc-times", type=int, default=32, help="observer times of the eats-lc workload")
     ap.add_argument("--quad", default="cadre", choices=["cadre", "trap"], help="quadrature of the eats-lc workload")
+    ap.add_argument("--rhs-states", type=int, default=1 << 20, help="blastwave states of the bw-rhs workload")
     ap.add_argument("--profile", type=int, default=0,
                     help="run this many device passes of the workload and exit (for ncu captures)")
     return ap.parse_args()
@@ -958,6 +960,139 @@ def eats_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- bw-rhs arm ---
+def bw_rhs_arm(args):
+    """The blastwave ODE right-hand side (rhs_fs / rhs_fsrs with the
+    radiative-loss term) over args.rhs_states blastwave states on the GPU, one
+    thread per state: the Gaussian jet's right-hand-side evaluations as the
+    reference program sampled them (refdrv_gaussian.npz: forward-shock and
+    forward+reverse-shock layers), drawn with replacement and perturbed
+    (R, Gamma, Eint2, M2 by 1e-3 relative), resident in HBM. The CPU figure is
+    the same restatement on the host (pbag_bw_rhs) on a sample, one core; the
+    parity compares a sample of the GPU's derivatives with the host's and the
+    reference's own sampled evaluations with the GPU's."""
+    import torch
+    from pyblastafterglowmag_gb300 import _lib, abi, build
+    build.build()
+    z = np.load(DRIVER_RUN)
+    P, B, A, D = z["rhs_pars"], z["rhs_before"], z["rhs_after"], z["rhs_dydt"]
+    rng = np.random.default_rng(11)
+    n = args.rhs_states
+    idx = rng.integers(0, len(P), n)
+    P2, B2 = P[idx].copy(), B[idx].copy()
+    for q in ("R", "Gamma", "Eint2", "M2"):
+        k = abi.BW_Q.index(q)
+        B2["Y"][:, k] *= 1.0 + 1e-3 * rng.standard_normal(n)
+    gk = abi.BW_Q.index("Gamma")
+    B2["Y"][:, gk] = np.maximum(B2["Y"][:, gk], 1.0 + 1e-6)
+    dev = torch.device("cuda", 0)
+    ctx = _lib.Context(driver_run().grid, device=0, ssc=False)
+    d_p = torch.from_numpy(P2.view(np.uint8).copy()).to(dev)
+    h_s = torch.from_numpy(B2.view(np.uint8).copy())
+    d_s0 = h_s.to(dev)
+    d_s = d_s0.clone()
+    d_y = torch.zeros((n, abi.PBAG_Y_N), dtype=torch.float64, device=dev)
+
+    def one_pass():
+        d_s.copy_(d_s0)  # the carried members start from the same values every pass
+        _lib.bw_rhs_device(ctx, n, d_p.data_ptr(), d_s.data_ptr(), d_y.data_ptr())
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        one_pass()
+    ms = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            one_pass()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t = statistics.median(ms)
+    # end to end: host states in (pinned), derivatives and states out
+    h_p = torch.from_numpy(P2.view(np.uint8).copy()).pin_memory()
+    h_s = h_s.pin_memory()
+    h_y = torch.empty((n, abi.PBAG_Y_N), dtype=torch.float64).pin_memory()
+    h_s_out = torch.empty_like(h_s).pin_memory()
+
+    def e2e_pass():
+        d_p.copy_(h_p, non_blocking=True)
+        d_s.copy_(h_s, non_blocking=True)
+        _lib.bw_rhs_device(ctx, n, d_p.data_ptr(), d_s.data_ptr(), d_y.data_ptr())
+        h_y.copy_(d_y, non_blocking=True)
+        h_s_out.copy_(d_s, non_blocking=True)
+        torch.cuda.synchronize(dev)
+
+    e2e_pass()
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_pass()
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e)
+    # parity: the host restatement on a sample of the batch, the reference's own evaluations
+    sel = rng.integers(0, n, 20000)
+    t0 = time.perf_counter()
+    ref_y, ref_after = _lib.bw_rhs(P2[sel], B2[sel])
+    cpu_s = time.perf_counter() - t0
+    got = d_y.cpu().numpy()[sel]
+    writes = np.zeros((len(sel), abi.PBAG_Y_N), dtype=bool)
+    for t_, names in ((abi.PBAG_BW_FS, abi.BW_Q_FS), (abi.PBAG_BW_FSRS, abi.BW_Q_FSRS)):
+        for q in names:
+            writes[P2["type"][sel] == t_, abi.BW_Q.index(q)] = True
+    den = np.abs(ref_y)
+    rel = np.where(den > 0, np.abs(got - ref_y) / np.where(den > 0, den, 1.0), np.abs(got))[writes]
+    d_p1 = torch.from_numpy(P.view(np.uint8).copy()).to(dev)
+    d_s1 = torch.from_numpy(B.view(np.uint8).copy()).to(dev)
+    d_y1 = torch.zeros((len(P), abi.PBAG_Y_N), dtype=torch.float64, device=dev)
+    _lib.bw_rhs_device(ctx, len(P), d_p1.data_ptr(), d_s1.data_ptr(), d_y1.data_ptr())
+    g1 = d_y1.cpu().numpy()
+    w1 = np.zeros_like(g1, dtype=bool)
+    for t_, names in ((abi.PBAG_BW_FS, abi.BW_Q_FS), (abi.PBAG_BW_FSRS, abi.BW_Q_FSRS)):
+        for q in names:
+            w1[P["type"] == t_, abi.BW_Q.index(q)] = True
+    den1 = np.abs(D)
+    rel1 = np.where(den1 > 0, np.abs(g1 - D) / np.where(den1 > 0, den1, 1.0), np.abs(g1))[w1]
+    ctx.close()
+    bytes_per = abi.BW_RHS_PARS_DTYPE.itemsize + 2 * abi.BW_RHS_STATE_DTYPE.itemsize + 2 * 8 * abi.PBAG_Y_N
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = n * bytes_per / (t * 1e-3) / 1e9
+    line = {"metric": "blastwave ODE right-hand-side evaluations/s on 1 GB300", "value": n / (t * 1e-3),
+            "unit": "evaluations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "bw-rhs-gaussian-jet-fs-fsrs", "states": n,
+                       "fsrs_fraction": float(np.mean(P2["type"] == abi.PBAG_BW_FSRS)),
+                       "inputs": "the reference program's sampled right-hand-side evaluations of the 21-layer "
+                                 "Gaussian jet, drawn with replacement, R/Gamma/Eint2/M2 perturbed by 1e-3",
+                       "l2": "flushed with a 256 MiB device write before every timed pass"},
+            "clocks": clk.summary(),
+            "e2e": {"value": n / e2e_s, "unit": "evaluations/s",
+                    "h2d_bytes_per_step": int(h_p.numel() + h_s.numel()),
+                    "d2h_bytes_per_step": int(h_y.numel() * 8 + h_s_out.numel())},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "kernel": "k_bw_rhs", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                         "bytes_per_state": bytes_per,
+                         "note": "FP64-bound in practice (transcendentals per state); the HBM figure is the "
+                                 "algorithmic bytes of one evaluation"},
+            "cpu_baseline": {"value": len(sel) / cpu_s, "unit": "evaluations/s", "cores": 1, "kind": "port",
+                             "sample": f"{len(sel)} of the {n} states through pbag_bw_rhs on one host core (the "
+                                       "restatement equal bit for bit to the reference's rhs_fs evaluations)"},
+            "parity": {"max_rel_vs_host": float(rel.max()), "max_rel_vs_reference": float(rel1.max()),
+                       "reference_evaluations": int(len(P)), "tol": 1e-9,
+                       "ok": bool(rel.max() <= 1e-9 and rel1.max() <= 1e-9)}}
+    print(json.dumps(line), flush=True)
+
+
 def timeit_run(ctx, recs, off, prm):
     t0 = time.perf_counter()
     ctx.run(recs, off, prm, outputs=("j_all", "a_all", "f_all", "i_all"))
@@ -971,6 +1106,9 @@ def main():
         return
     if args.workload == "eats-lc":
         eats_arm(args)
+        return
+    if args.workload == "bw-rhs":
+        bw_rhs_arm(args)
         return
     if args.workload == "contraction":
         contraction_arm(args)

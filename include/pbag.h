@@ -449,6 +449,86 @@ int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int nl, const pb
                      const double* d_dyn, int nbw, const int64_t* offsets, const double* d_j_all,
                      const double* d_a_all, int nq, const pbag_eats_query* d_q, double* d_flux, pbag_status* st);
 
+/* ---- the blastwave ODE right-hand side ----------------------------------- */
+
+/* Evolution equations of a blastwave: forward shock (BlastWave::rhs_fs,
+ * blastwave/blastwave.h:1515-1768) or forward and reverse shock
+ * (BlastWave::rhs_fsrs, :1771-2118), selected by BW_TYPES iFS / iFSRS. */
+enum pbag_bw_type { PBAG_BW_FS = 0, PBAG_BW_FSRS = 1 };
+/* The ODE state of one blastwave, SOL::QS order (blastwave_pars.h:308-310). */
+enum pbag_bw_q {
+  PBAG_Y_R, PBAG_Y_RSH, PBAG_Y_TT, PBAG_Y_TCOMOV, PBAG_Y_GAMMA, PBAG_Y_EINT2, PBAG_Y_EINT3, PBAG_Y_THETA,
+  PBAG_Y_RRSH, PBAG_Y_ERAD2, PBAG_Y_ERAD3, PBAG_Y_ESH2, PBAG_Y_ESH3, PBAG_Y_EAD2, PBAG_Y_EAD3, PBAG_Y_M2,
+  PBAG_Y_M3, PBAG_Y_DELTAR4, PBAG_Y_N
+};
+enum pbag_eos { PBAG_EOS_PEER12 = 0, PBAG_EOS_NAVA13 = 1 };                 /* "method_eos"    */
+enum pbag_spread { PBAG_SPREAD_NULL = 0, PBAG_SPREAD_ADI = 1, PBAG_SPREAD_AA = 2,
+                   PBAG_SPREAD_AFGPY = 3, PBAG_SPREAD_OUR = 4 };           /* "method_spread" */
+enum pbag_limit_spread { PBAG_LIMIT_SPREAD_NONE = 0, PBAG_LIMIT_SPREAD_GAMMA0_FRAC = 1,
+                         PBAG_LIMIT_SPREAD_GAMMA_VAL = 2, PBAG_LIMIT_SPREAD_RD = 3 }; /* "method_limit_spread" */
+enum pbag_dmdr { PBAG_DMDR_USING_A = 0, PBAG_DMDR_USING_DTHDR = 1, PBAG_DMDR_NONE = 2 }; /* "method_dmdr" */
+enum pbag_dgdr { PBAG_DGDR_OUR = 0, PBAG_DGDR_PEER = 1 };                    /* "method_dgdr"   */
+
+/* One shock's ElectronAndRadiation as its radiative-loss term reads it
+ * (computeRadiationLoss, microphysics.h:749-791; computePtot :204-219). */
+typedef struct pbag_bw_mphys {
+  int32_t method_B;          /* as pbag_limits_opts: 0 useU_b, 1 useMAG21, 2 useGammaSh         */
+  int32_t method_gamma_max;  /* as pbag_limits_opts: 0 useB, 1 useConst                         */
+  int32_t method_nonrel;     /* 0 none, 1 useGm, 2 useAyache, 3 use_Sironi (method_nonrel_dist)  */
+  int32_t method_up;         /* 0 useEint2, 1 useGamma (method_Up_{fs,rs})                      */
+  int32_t ele_analytic;      /* method_ele = analytic: no clamps to the electron grid            */
+  int32_t pad;
+  double eps_e, eps_b, eps_t, p, mu, mu_e, beta_min;
+  double gam_lo, gam_hi;     /* first and last point of the electron grid                        */
+} pbag_bw_mphys;
+
+/* The constant parameters of one blastwave (BW::Pars, blastwave_pars.h:13-203,
+ * and the RhoISM / LatSpread / EOSadi objects it owns). */
+typedef struct pbag_bw_rhs_pars {
+  int32_t type;                /* pbag_bw_type                                          */
+  int32_t method_dmdr, method_dgdr, method_limit_spread, method_spread, method_eos;
+  int32_t adiab_loss, adiab_loss_rs, exponential_rho4;
+  int32_t ilayer, nlayers;     /* the layer and the number of layers (EjectaID2::ctheta) */
+  int32_t pad;
+  double Gamma0, beta0, M0, mom0, ncells, theta_a, theta_max, Rd;
+  double frac_mom0_spread;     /* fraction_of_mom0_when_spread_start                    */
+  double mom_spread;           /* value_of_mom_when_spread_start                        */
+  double spread_aa, spread_theta_max, spread_theta_c, spread_theta_w, spread_theta_b0; /* LatSpread */
+  double eps_rad_fs, eps_rad_rs; /* epsilon_e_rad_{fs,rs}; < 0: from the loss term       */
+  double tprompt, rs_Gamma0_frac_no_exceed;
+  double n_ism, A0, s, R_ej, R_ism;  /* RhoISM: uniform for n_ism > 0, else the step profile */
+  pbag_bw_mphys fs, rs;
+} pbag_bw_rhs_pars;
+
+/* What one evaluation reads besides the constants: the state Y, the flags the
+ * reference keeps in BW::Pars, and the members of the shocks'
+ * ElectronAndRadiation objects that the loss term reads (tcomov) and carries
+ * from call to call (gamma_max with method_gamma_max = const, accel_frac when
+ * gamma_min >= 2); the evaluation updates the carried members. */
+typedef struct pbag_bw_rhs_state {
+  double x;                          /* burster time of the evaluation                 */
+  double Y[PBAG_Y_N];
+  int32_t end_spreading, shut_off;   /* BW::Pars end_spreading, shutOff                */
+  int32_t first_step;                /* BW::Pars prev_idx_x == 0                       */
+  int32_t pad;
+  double fs_tcomov, fs_gamma_max, fs_accel_frac;
+  double rs_tcomov, rs_gamma_max, rs_accel_frac;
+} pbag_bw_rhs_state;
+
+/* dY/dt of n blastwave states (one ODE right-hand side each, as the
+ * reference's RHS_comb calls rhs_dispatcher per blastwave,
+ * model_evolve.h:1587-1624): pars[b], state[b] (carried members updated in
+ * place) -> dydt[b][PBAG_Y_N]. rhs_fs writes R, Rsh, tt, tcomov, Gamma, Eint2,
+ * theta, Erad2, Esh2, Ead2, M2; rhs_fsrs also Rsh_rs, Eint3, Erad3, Esh3,
+ * Ead3, M3, deltaR4; entries a function does not write are left as they are.
+ * pbag_bw_rhs runs on the host, pbag_bw_rhs_device on the GPU (one thread per
+ * blastwave; device pointers; synchronous). Where the reference exits: the
+ * first failing blastwave in st->bw, PBAG_ERR_NONFINITE or PBAG_ERR_PARAM,
+ * st->site the condition (pbag_rhs.cuh Site). */
+int pbag_bw_rhs(int n, const pbag_bw_rhs_pars* pars, pbag_bw_rhs_state* state, double* dydt, pbag_status* st);
+int pbag_bw_rhs_device(pbag_ctx* ctx, int n, const pbag_bw_rhs_pars* d_pars, pbag_bw_rhs_state* d_state,
+                       double* d_dydt, pbag_status* st);
+
 /* Contraction autotuner: the first tensor-core SSC contraction of a shape
  * (precision, grid, outputs, batch size to a factor of two) launched outside
  * a graph capture times the candidate kernels and shapes (slab per CTA, or

@@ -13,6 +13,9 @@
 #ifndef PBAG_ORACLE_SHIM_H5CPP_H
 #define PBAG_ORACLE_SHIM_H5CPP_H
 
+#include <unistd.h>
+
+#include <cstdint>
 #include <map>
 #include <string>
 #include <vector>
@@ -51,6 +54,44 @@ inline void put_attr(const std::string& file, const std::string& name, double v)
 inline const Entry* find(const std::string& key) {
   auto it = datasets().find(key);
   return it == datasets().end() ? nullptr : &it->second;
+}
+// Optional write-through log of what the program writes (a file descriptor,
+// -1: off): per dataset 'D', key, rank, dims, count, values; per attribute 'A',
+// key, value. Written with write(2) as each write happens, so that it holds
+// everything written before the program's exit path misbehaves.
+inline int& log_fd() {
+  static int fd = -1;
+  return fd;
+}
+inline void log_bytes(const void* p, size_t n) {
+  const char* c = static_cast<const char*>(p);
+  while (n > 0 && log_fd() >= 0) {
+    const long w = (long)::write(log_fd(), c, n);
+    if (w <= 0) return;
+    c += w;
+    n -= (size_t)w;
+  }
+}
+inline void log_key(char tag, const std::string& key) {
+  const uint32_t n = (uint32_t)key.size();
+  log_bytes(&tag, 1);
+  log_bytes(&n, sizeof n);
+  log_bytes(key.data(), n);
+}
+inline void log_dataset(const std::string& key, const std::vector<unsigned long long>& dims, const double* v,
+                        uint64_t n) {
+  if (log_fd() < 0) return;
+  log_key('D', key);
+  const uint32_t r = (uint32_t)dims.size();
+  log_bytes(&r, sizeof r);
+  log_bytes(dims.data(), sizeof(unsigned long long) * r);
+  log_bytes(&n, sizeof n);
+  log_bytes(v, sizeof(double) * n);
+}
+inline void log_attr(const std::string& key, double v) {
+  if (log_fd() < 0) return;
+  log_key('A', key);
+  log_bytes(&v, sizeof v);
 }
 }  // namespace pbag_h5
 
@@ -113,7 +154,9 @@ struct DataSpace {
 struct Attribute {
   std::string key;
   void write(const DataType&, const void* v) {
-    if (!key.empty()) pbag_h5::attributes()[key] = *static_cast<const double*>(v);
+    if (key.empty()) return;
+    pbag_h5::attributes()[key] = *static_cast<const double*>(v);
+    pbag_h5::log_attr(key, *static_cast<const double*>(v));
   }
   void read(const DataType&, void* v) const {
     auto it = pbag_h5::attributes().find(key);
@@ -131,6 +174,7 @@ struct DataSet {
     for (unsigned long long d : dims) n *= (size_t)d;
     const double* in = static_cast<const double*>(buf);
     pbag_h5::datasets()[key] = pbag_h5::Entry{std::vector<double>(in, in + n), dims};
+    pbag_h5::log_dataset(key, dims, in, n);
   }
   void read(void* buf, const PredType&) const {
     if (const pbag_h5::Entry* e = pbag_h5::find(key)) {

@@ -170,6 +170,37 @@ def shock_limits_device(ctx, off, d_opts, d_in, d_state, d_out):
     return st
 
 
+def bw_rhs(pars, state, dydt=None):
+    """pbag_bw_rhs on the host: dY/dt of the blastwave states (pars
+    BW_RHS_PARS_DTYPE, state BW_RHS_STATE_DTYPE, one each per blastwave).
+    Returns (dydt [n][PBAG_Y_N], state after the evaluation: the carried
+    microphysics members updated). dydt: the values of the entries the
+    blastwave's function does not write (zeros by default)."""
+    lib = load()
+    lib.pbag_bw_rhs.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(abi.Status)]
+    pars = np.ascontiguousarray(pars, dtype=abi.BW_RHS_PARS_DTYPE)
+    state = np.array(state, dtype=abi.BW_RHS_STATE_DTYPE, copy=True)
+    out = np.zeros((len(pars), abi.PBAG_Y_N)) if dydt is None else np.array(dydt, dtype=np.float64, copy=True)
+    st = abi.Status()
+    rc = lib.pbag_bw_rhs(len(pars), pars.ctypes.data, state.ctypes.data, out.ctypes.data, C.byref(st))
+    if rc != 0:
+        raise PbagError(rc, "pbag_bw_rhs", st.bw, st.step, st.site)
+    return out, state
+
+
+def bw_rhs_device(ctx, n, d_pars, d_state, d_dydt):
+    """pbag_bw_rhs_device (device addresses); returns the pbag_status."""
+    lib = load()
+    lib.pbag_bw_rhs_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(abi.Status)]
+    st = abi.Status()
+    rc = lib.pbag_bw_rhs_device(ctx.handle, int(n), C.c_void_p(d_pars), C.c_void_p(d_state), C.c_void_p(d_dydt),
+                                C.byref(st))
+    if rc != 0:
+        raise PbagError(rc, "pbag_bw_rhs_device", st.bw, st.step, st.site)
+    return st
+
+
 class Context:
     """One device context: one grid (a CommonTables entry) on one GPU."""
 

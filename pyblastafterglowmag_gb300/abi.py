@@ -165,3 +165,33 @@ class EatsOpts(C.Structure):
 EATS_LAYER_DTYPE = np.dtype([("i_end_r", np.int32), ("bw_fs", np.int32), ("bw_rs", np.int32), ("pad", np.int32),
                              ("theta_c_l", np.float64), ("theta_c_h", np.float64), ("ncells", np.float64)])
 EATS_QUERY_DTYPE = np.dtype([("layer", np.int32), ("pad", np.int32), ("t_obs", np.float64), ("nu_obs", np.float64)])
+
+
+# ---- the blastwave ODE right-hand side (pbag_bw_rhs) ----------------------
+PBAG_BW_FS, PBAG_BW_FSRS = 0, 1
+BW_Q = ("R", "Rsh", "tt", "tcomov", "Gamma", "Eint2", "Eint3", "theta", "Rsh_rs", "Erad2", "Erad3", "Esh2",
+        "Esh3", "Ead2", "Ead3", "M2", "M3", "deltaR4")
+PBAG_Y_N = len(BW_Q)
+# the entries rhs_fs / rhs_fsrs write (blastwave.h:1757-1767, 2092-2111)
+BW_Q_FS = ("R", "Rsh", "tt", "tcomov", "Gamma", "Eint2", "theta", "Erad2", "Esh2", "Ead2", "M2")
+BW_Q_FSRS = BW_Q
+PBAG_EOS_PEER12, PBAG_EOS_NAVA13 = 0, 1
+PBAG_SPREAD_NULL, PBAG_SPREAD_ADI, PBAG_SPREAD_AA, PBAG_SPREAD_AFGPY, PBAG_SPREAD_OUR = 0, 1, 2, 3, 4
+BW_MPHYS_DTYPE = np.dtype([(f, np.int32) for f in ("method_B", "method_gamma_max", "method_nonrel", "method_up",
+                                                  "ele_analytic", "pad")] +
+                          [(f, np.float64) for f in ("eps_e", "eps_b", "eps_t", "p", "mu", "mu_e", "beta_min",
+                                                     "gam_lo", "gam_hi")])
+BW_RHS_PARS_DTYPE = np.dtype(
+    [(f, np.int32) for f in ("type", "method_dmdr", "method_dgdr", "method_limit_spread", "method_spread",
+                             "method_eos", "adiab_loss", "adiab_loss_rs", "exponential_rho4", "ilayer", "nlayers",
+                             "pad")] +
+    [(f, np.float64) for f in ("Gamma0", "beta0", "M0", "mom0", "ncells", "theta_a", "theta_max", "Rd",
+                               "frac_mom0_spread", "mom_spread", "spread_aa", "spread_theta_max", "spread_theta_c",
+                               "spread_theta_w", "spread_theta_b0", "eps_rad_fs", "eps_rad_rs", "tprompt",
+                               "rs_Gamma0_frac_no_exceed", "n_ism", "A0", "s", "R_ej", "R_ism")] +
+    [("fs", BW_MPHYS_DTYPE), ("rs", BW_MPHYS_DTYPE)])
+BW_RHS_STATE_DTYPE = np.dtype(
+    [("x", np.float64), ("Y", np.float64, (PBAG_Y_N,))] +
+    [(f, np.int32) for f in ("end_spreading", "shut_off", "first_step", "pad")] +
+    [(f, np.float64) for f in ("fs_tcomov", "fs_gamma_max", "fs_accel_frac", "rs_tcomov", "rs_gamma_max",
+                               "rs_accel_frac")])

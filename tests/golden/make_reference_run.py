@@ -18,7 +18,11 @@ modules), runs the program in a child process and stores, per case:
     total_j / total_a of the forward and reverse shocks), all rows for the
     top-hat, every 10th time index of the first layers' shocks for the jet;
   * its light curve (computeSaveEjectaLightCurve, adaptive EATS: CADRE,
-    counter jet, rtol 1e-6, nmax 1000 - the parfile defaults) per layer.
+    counter jet, rtol 1e-6, nmax 1000 - the parfile defaults) per layer;
+  * sampled evaluations of its ODE right-hand side (rhs_fs / rhs_fsrs through
+    the integrator's RHS_comb): every layer's inputs - state, parameters,
+    flags, the microphysics members its radiative-loss term reads - and
+    outputs, in the layout of pbag_bw_rhs, at calls spread over the run.
 
     python tests/golden/make_reference_run.py [tophat|gaussian ...]
 """
@@ -39,6 +43,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pyoracle  # noqa: E402
+from pyblastafterglowmag_gb300 import abi  # noqa: E402
 
 # dynamics quantities kept (BW::VARNAMES of blastwave_pars.h)
 DYN = ("tburst", "tt", "tcomov", "R", "Rsh", "Gamma", "beta", "GammaFsh", "U_p", "rho2", "M2", "thickness",
@@ -62,6 +67,8 @@ def reference_tools():
             importlib.import_module("PyBlastAfterglowMag.id_analytic"))
 
 
+RHS_EVERY = 97  # the harness samples every 97th right-hand-side call
+
 CASES = {
     # one top-hat layer, forward shock, synchrotron only (151 gamma, 96 nu)
     "tophat": dict(
@@ -70,7 +77,7 @@ CASES = {
         struct=dict(struct="tophat", Eiso_c=1e52, Gamma0c=300., M0c=-1., theta_c=0.1, theta_w=0.1),
         grb=dict(eps_e_fs=0.1, eps_b_fs=1e-3, p_fs=2.2, gam1_fs=1., gam2_fs=1e8, ngam_fs=151, freq1_fs=1e8,
                  freq2_fs=1e29, nfreq_fs=96, method_ele_fs="numeric", method_synchrotron_fs="CSYN"),
-        keep_layers=1, every=1),
+        keep_layers=1, every=1, rhs_calls=600),
     # the 21-layer Gaussian jet, forward and reverse shocks, synchrotron + SSC + SSA (201 gamma, 128 nu)
     "gaussian": dict(
         main=dict(d_l=3.09e26, z=0.0, n_ism=10 ** -1.6, theta_obs=np.deg2rad(20.8), rtol=5e-7,
@@ -83,23 +90,52 @@ CASES = {
                  do_rs="yes", bw_type="fsrs", do_rs_radiation="yes",
                  method_ele_fs="numeric", method_synchrotron_fs="CSYN", method_ssc_fs="numeric", use_ssa_fs="yes",
                  method_ele_rs="numeric", method_synchrotron_rs="CSYN", method_ssc_rs="numeric", use_ssa_rs="yes"),
-        keep_layers=6, every=10),
+        keep_layers=6, every=10, rhs_calls=100),
 }
 
 
+# one sampled evaluation of a blastwave's ODE right-hand side (oracle/ref_run.cpp)
+RHS_SAMPLE_DTYPE = np.dtype([("call", np.int32), ("layer", np.int32), ("pars", abi.BW_RHS_PARS_DTYPE),
+                             ("before", abi.BW_RHS_STATE_DTYPE), ("after", abi.BW_RHS_STATE_DTYPE),
+                             ("dydt", np.float64, (abi.PBAG_Y_N,))], align=True)
+
+
 def read_store(path):
-    d, a = {}, {}
+    """What the program wrote, from the harness's write-through log
+    (oracle/shim/H5Cpp.h): datasets {key: array}, attributes {key: value} and
+    the sampled right-hand-side evaluations (RHS_SAMPLE_DTYPE)."""
+    d, a, rhs = {}, {}, []
     with open(path, "rb") as f:
-        for _ in range(struct.unpack("<Q", f.read(8))[0]):
-            k = f.read(struct.unpack("<I", f.read(4))[0]).decode()
-            r = struct.unpack("<I", f.read(4))[0]
-            dims = struct.unpack("<%dQ" % r, f.read(8 * r))
-            v = np.frombuffer(f.read(8 * struct.unpack("<Q", f.read(8))[0]), dtype=np.float64)
+        buf = f.read()
+    i = 0
+
+    def take(n):
+        nonlocal i
+        b = buf[i:i + n]
+        i += n
+        return b
+
+    while i < len(buf):
+        tag = take(1)
+        if tag == b"R":
+            (sz,) = struct.unpack("<Q", take(8))
+            assert sz == RHS_SAMPLE_DTYPE.itemsize, (sz, RHS_SAMPLE_DTYPE.itemsize)
+            rhs.append(take(sz))
+            continue
+        (kl,) = struct.unpack("<I", take(4))
+        k = take(kl).decode()
+        if tag == b"A":
+            a[k] = struct.unpack("<d", take(8))[0]
+        elif tag == b"D":
+            (r,) = struct.unpack("<I", take(4))
+            dims = struct.unpack("<%dQ" % r, take(8 * r))
+            (n,) = struct.unpack("<Q", take(8))
+            v = np.frombuffer(take(8 * n), dtype=np.float64).copy()
             d[k] = v.reshape(dims) if r > 1 else v
-        for _ in range(struct.unpack("<Q", f.read(8))[0]):
-            k = f.read(struct.unpack("<I", f.read(4))[0]).decode()
-            a[k] = struct.unpack("<d", f.read(8))[0]
-    return d, a
+        else:
+            raise ValueError(f"bad record tag {tag!r} at {i - 1}")
+    rhs = np.frombuffer(b"".join(rhs), dtype=RHS_SAMPLE_DTYPE).copy()
+    return d, a, rhs
 
 
 def run_case(name):
@@ -109,6 +145,9 @@ def run_case(name):
     lib.ref_h5_put.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_int]
     lib.ref_h5_put_attr.argtypes = [C.c_char_p, C.c_char_p, C.c_double]
     lib.ref_run.argtypes = [C.c_char_p] * 4
+    lib.ref_rhs_record.argtypes = [C.c_long, C.c_long]
+    lib.ref_rhs_record.restype = C.c_int
+    assert lib.ref_rhs_record(RHS_EVERY, 200000) == 0
     wd = tempfile.mkdtemp() + "/"
     # the jet's initial data as the front end writes id_a.h5 (the adaptive EATS discretisation)
     st = copy.deepcopy(case["struct"])
@@ -132,7 +171,7 @@ def run_case(name):
     t = time.time()
     rc = lib.ref_run(wd.encode(), b"parfile.par", b"err", (wd + "store.bin").encode())
     print(f"{name}: reference program exit {rc} after {time.time() - t:.1f} s")
-    d, attrs = read_store(wd + "store.bin")
+    d, attrs, rhs = read_store(wd + "store.bin")
     out = {"grid": np.array([case["grb"]["ngam_fs"], case["grb"]["nfreq_fs"], case["grb"]["gam1_fs"],
                              case["grb"]["gam2_fs"], case["grb"]["freq1_fs"], case["grb"]["freq2_fs"]]),
            "layers": np.array(nl)}
@@ -161,6 +200,13 @@ def run_case(name):
     out["lc_freqs"] = d[wd + "lc.h5//freqs"]
     for il in range(nl):
         out[f"lc{il}"] = d[f"{wd}lc.h5//shell=0 layer={il}/fluxdens"]
+    # the sampled ODE right-hand-side evaluations: every layer at case["rhs_calls"]
+    # sampled calls spread over the run
+    calls = np.unique(rhs["call"])
+    keep = calls[np.linspace(0, len(calls) - 1, min(case["rhs_calls"], len(calls))).astype(int)]
+    rhs = rhs[np.isin(rhs["call"], keep)]
+    for k in ("call", "layer", "pars", "before", "after", "dydt"):
+        out["rhs_" + k] = rhs[k]
     path = os.path.join(HERE, f"refdrv_{name}.npz")
     np.savez_compressed(path, **out)
     print(f"refdrv_{name}.npz: {os.path.getsize(path) / 1024:.0f} KiB")
