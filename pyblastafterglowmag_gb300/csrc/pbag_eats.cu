@@ -16,6 +16,9 @@
 // fluxDens (microphysics.h:1185-1217) on the forward- and reverse-shock
 // histories.
 //
+// The integrand and the inner integral are out-of-line functions: one copy of
+// their code serves every call site of the quadratures.
+//
 // GB300 layout. An FP64 warp instruction holds its sub-partition's FP64 unit
 // for 64 cycles however many lanes are active, so lanes of one warp must not
 // each follow their own adaptive quadrature (divergent paths issue one after
@@ -39,6 +42,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 #include "pbag.h"
@@ -50,6 +54,7 @@ namespace pbag {
 namespace {
 
 constexpr int kEatsThreads = 128;  // four items (warps) per CTA
+constexpr int kCrewChunk = 32;     // phi points per batch of the crew kernel
 constexpr long kMaxEvals = 10000000L;  // eats.h:536-541
 // dynamics interpolated log-linearly in radius, in their pbag_eats_q order
 __constant__ const int kLogQ[] = {PBAG_EQ_GAMMA,     PBAG_EQ_BETA,         PBAG_EQ_GAMMA_FSH, PBAG_EQ_THICKNESS,
@@ -185,6 +190,7 @@ struct Eats {
   long nevals = 0;
   int code = PBAG_OK;
   Heap inner;
+  unsigned long long* evals_sh = nullptr;  // the item's count shared by its warps (crew kernel)
 
   __device__ const double* qv(int k) const { return dyn + (size_t)k * A.nr; }
   // ya (yb/ya)^t with ln(yb/ya) from the table
@@ -240,7 +246,7 @@ struct Eats {
   // the integrand (eats.h:175-232) with fluxDensAdaptiveWithComov at this
   // lane's own point (sin_phi = sin(i_phi)); *rc: PBAG_OK or where the
   // reference exits
-  __device__ double integrand(double i_cos_theta, double sin_phi, int* rc) const {
+  __device__ __noinline__ double integrand(double i_cos_theta, double sin_phi, int* rc) const {
     *rc = PBAG_OK;
     const double* R = qv(PBAG_EQ_R);
     const int ie = L.i_end_r;
@@ -309,6 +315,13 @@ struct Eats {
   // point as the sequential loop would; the evaluation count (the reference's
   // 1e7 limit) grows by the batch.
   __device__ void count_evals(int n) {
+    if (evals_sh) {
+      unsigned long long tot = 0;
+      if (lane == 0) tot = atomicAdd(evals_sh, (unsigned long long)n) + (unsigned long long)n;
+      tot = __shfl_sync(0xffffffffu, tot, 0);
+      if (tot > (unsigned long long)kMaxEvals && code == PBAG_OK) code = PBAG_ERR_EVALS;
+      return;
+    }
     nevals += n;
     if (nevals > kMaxEvals && code == PBAG_OK) code = PBAG_ERR_EVALS;
   }
@@ -385,6 +398,72 @@ struct Eats {
       double I = 0.5 * (fa + e.phi_integrand(xb));
       for (int i = 1; i < N; i++) {
         I += e.phi_integrand(xa + i * dx);
+        if (e.stop()) return 0.0;
+      }
+      return I * dx;
+    }
+  };
+
+  // The points of the phi integral spread over the item's W warps (crew
+  // kernel): warp w evaluates points w, w + W, ... of a batch (each one inner
+  // integral with its own lanes and its own interval workspace) and leaves
+  // value and status in shared memory; after the barrier every warp reads the
+  // batch in point order, so all warps hold the same values and sums (the
+  // sums in the sequential loop's order) and take the same control path,
+  // their own copy of the phi intervals included. A batch's status is its
+  // first failing point's.
+  struct Crew {
+    Eats& e;
+    double* ysh;
+    int* csh;
+    int w, W;
+    template <class X>
+    __device__ void batch(X xk, int n) {  // n <= kCrewChunk; the caller reads ysh, then calls done()
+      for (int k = w; k < n; k += W) {
+        e.code = PBAG_OK;
+        const double y = e.phi_integrand(xk(k));
+        if (e.lane == 0) {
+          ysh[k] = y;
+          csh[k] = e.code;
+        }
+      }
+      __syncthreads();
+      int c = PBAG_OK;
+      for (int k = 0; k < n && c == PBAG_OK; ++k) c = csh[k];
+      e.code = c;
+    }
+    __device__ void done() { __syncthreads(); }  // every warp has read the batch
+    __device__ void eval(const double* xs, int n, double* ys) {
+      batch([&](int k) { return xs[k]; }, n);
+      for (int k = 0; k < n; ++k) ys[k] = ysh[k];
+      done();
+    }
+    __device__ double sum_odd(double a, double h, int nint) {
+      double s = 0.;
+      const int m = nint / 2;  // odd j < nint: j = 2 i + 1
+      for (int base = 0; base < m; base += kCrewChunk) {
+        const int n = min(kCrewChunk, m - base);
+        batch([&](int k) { return a + h * (2 * (base + k) + 1); }, n);
+        if (!e.stop())
+          for (int k = 0; k < n; ++k) s += ysh[k];
+        done();
+        if (e.stop()) return 0.;
+      }
+      return s;
+    }
+    __device__ double trap(double xa, double xb, int N) {
+      const double dx = (xb - xa) / N;
+      batch([&](int k) { return k == 0 ? xa : xb; }, 2);
+      const double fa = ysh[0], fb = ysh[1];
+      done();
+      if (e.stop()) return 0.;
+      double I = 0.5 * (fa + fb);
+      for (int base = 1; base < N; base += kCrewChunk) {
+        const int n = min(kCrewChunk, N - base);
+        batch([&](int k) { return xa + (base + k) * dx; }, n);
+        if (!e.stop())
+          for (int k = 0; k < n; ++k) I += ysh[k];
+        done();
         if (e.stop()) return 0.0;
       }
       return I * dx;
@@ -568,7 +647,7 @@ struct Eats {
   }
 
   // phi_integrand (eats.h:449-586): the inner integral over 1 - cos(theta)
-  __device__ double phi_integrand(double a_phi) {
+  __device__ __noinline__ double phi_integrand(double a_phi) {
     double theta_1 = L.theta_c_h, theta_0 = L.theta_c_l;
     const double th_1 = jet_edge(a_phi, theta_1);
     const double frac = theta_0 / theta_1;
@@ -649,6 +728,52 @@ __global__ void __launch_bounds__(kEatsThreads) k_eats(EatsArgs A, int items) {
   }
 }
 
+// One item per CTA of W warps: the phi points of each outer step spread over
+// the warps (Eats::Crew), each warp with its own interval workspaces.
+template <int W>
+__global__ void __launch_bounds__(32 * W) k_eats_crew(EatsArgs A, int items) {
+  const int item = blockIdx.x;
+  if (item >= items) return;
+  const int w = threadIdx.x >> 5;
+  __shared__ double ysh[kCrewChunk];
+  __shared__ int csh[kCrewChunk];
+  __shared__ unsigned long long evals;
+  if (threadIdx.x == 0) evals = 0ull;
+  __syncthreads();
+  const int qi = item / A.sides;
+  const pbag_eats_query q = A.q[qi];
+  const pbag_eats_layer L = A.layers[q.layer];
+  Iv9* ws = A.ws + ((size_t)item * W + w) * (A.cap_phi + A.cap_theta);
+  Eats e{A, L, A.dyn + (size_t)q.layer * PBAG_EQ_N * A.nr, A.ln + (size_t)q.layer * kNLn * A.nr,
+         A.mu + (size_t)item * A.nr, A.off[L.bw_fs], L.bw_rs >= 0 ? A.off[L.bw_rs] : -1,
+         q.t_obs, q.nu_obs};
+  e.sin_obs = sin(A.o.theta_obs);
+  e.cos_obs = cos(A.o.theta_obs);
+  e.cj = (item % A.sides) == 1;
+  e.lane = threadIdx.x & 31;
+  e.inner = Heap{ws + A.cap_phi, 0, A.cap_theta};
+  e.evals_sh = &evals;
+  double I = 0.0;
+  const double* tb = e.qv(PBAG_EQ_TBURST);
+  if (L.i_end_r > 0 && (q.t_obs < tb[0] || q.t_obs > tb[L.i_end_r - 1])) {  // eats.h:822-827
+    e.code = PBAG_ERR_RANGE;
+  } else {
+    Eats::Crew fo{e, ysh, csh, w, W};
+    if (A.o.method_quad == PBAG_QUAD_TRAP_FIXED) {
+      I = fo.trap(0.0, cgs::pi_, A.o.nmax_phi);
+    } else {
+      Heap outer{ws, 0, A.cap_phi};
+      I = e.cadre(fo, 0.0, cgs::pi_, A.o.nmax_phi, A.o.rtol_phi, outer);
+    }
+  }
+  const double Fcoeff = 1.e26 / (4 * cgs::pi_ * A.o.d_l * A.o.d_l);  // cgs2mJy (utils.h:40)
+  if (threadIdx.x == 0) {
+    A.part[item] = 2 * Fcoeff * I;
+    if (e.code != PBAG_OK)
+      atomicMin(A.first, ((unsigned long long)qi << 8) | (unsigned long long)(-e.code & 0xff));
+  }
+}
+
 // flux = principal jet + counter jet, in evalFluxDensA's order
 __global__ void k_eats_sum(const double* __restrict__ part, int nq, int sides, double* __restrict__ flux) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -720,7 +845,11 @@ extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int n
   A.cap_phi = o.method_quad == PBAG_QUAD_CADRE ? o.nmax_phi + 8 : 0;
   A.cap_theta = o.method_quad == PBAG_QUAD_CADRE ? o.nmax_theta + 8 : 0;
   const size_t n_ln = (size_t)nl * kNLn * nr, n_mu = (size_t)items * nr;
-  const size_t n_ws = (size_t)items * (A.cap_phi + A.cap_theta);
+  // warps per item (PBAG_EATS_WARPS = 1 or 4, default 4): the crew kernel
+  // spreads each outer step's phi points over four warps
+  int crew = 4;
+  if (const char* cw = std::getenv("PBAG_EATS_WARPS")) crew = std::atoi(cw) == 1 ? 1 : 4;
+  const size_t n_ws = (size_t)items * crew * (A.cap_phi + A.cap_theta);
   double *d_ln = nullptr, *d_mu = nullptr, *d_part = nullptr;
   Iv9* d_ws = nullptr;
   pbag_eats_layer* d_layers = nullptr;
@@ -748,7 +877,10 @@ extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int n
   if (e == cudaSuccess) {
     k_eats_ln<<<(unsigned)((n_ln + 255) / 256), 256, 0, v.stream>>>(A, d_ln, nl);
     k_eats_mu<<<(unsigned)((n_mu + 255) / 256), 256, 0, v.stream>>>(A, items);
-    k_eats<<<(items + kEatsThreads / 32 - 1) / (kEatsThreads / 32), kEatsThreads, 0, v.stream>>>(A, items);
+    if (crew == 1)
+      k_eats<<<(items + kEatsThreads / 32 - 1) / (kEatsThreads / 32), kEatsThreads, 0, v.stream>>>(A, items);
+    else
+      k_eats_crew<4><<<items, 128, 0, v.stream>>>(A, items);
     k_eats_sum<<<(nq + 127) / 128, 128, 0, v.stream>>>(d_part, nq, sides, d_flux);
     e = cudaGetLastError();
   }

@@ -68,6 +68,25 @@ def test_eats_device_resident(lib, oracle, cuda_device, eats_inputs):
     assert rel.max() <= 1e-4, (rel.max(), np.argmax(rel))
 
 
+@pytest.mark.parametrize("name", ["gaussian_fsrs", "gaussian_trap_no_cj"])
+def test_eats_crew_matches_single_warp(oracle, cuda_device, eats_inputs, monkeypatch, name):
+    """Four warps per item (the phi points of each outer step spread over
+    them, the default) and one warp per item give the same light curve bit
+    for bit: the same inner integrals, the outer sums in the same order."""
+    import torch
+    grid, o, layers, dyn, off, recs, prm, j, a, q = eats_inputs[name]
+    dev = torch.device("cuda", 0)
+    ctx = Context(grid, device=0, ssc=True)
+    d_j = torch.from_numpy(np.ascontiguousarray(j)).to(dev)
+    d_a = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    monkeypatch.setenv("PBAG_EATS_WARPS", "1")
+    one = _gpu_eats(ctx, o, layers, dyn, off, d_j.data_ptr(), d_a.data_ptr(), q)
+    monkeypatch.setenv("PBAG_EATS_WARPS", "4")
+    four = _gpu_eats(ctx, o, layers, dyn, off, d_j.data_ptr(), d_a.data_ptr(), q)
+    ctx.close()
+    np.testing.assert_array_equal(four, one)
+
+
 def test_eats_gpu_errors(oracle, cuda_device, eats_inputs):
     """Where the reference exits: an observer time outside the burster-time
     grid (PBAG_ERR_RANGE with the failing query), a query naming no layer
