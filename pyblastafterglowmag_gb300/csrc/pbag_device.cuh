@@ -170,6 +170,16 @@ struct DevState {
 
 __device__ __forceinline__ int slot_bw(const DevState& S, int slot) { return S.slot_bw ? S.slot_bw[slot] : slot; }
 
+// Programmatic dependent launch (griddepcontrol). A kernel launched with
+// programmatic stream serialization may be scheduled before the kernels it
+// depends on have finished: grid_dep_wait() returns once they have completed
+// and their memory operations are visible to this grid (at once for a kernel
+// launched without the attribute), so a kernel touches nothing those kernels
+// read or write before it. grid_dep_launch() lets the kernels that depend on
+// this one be scheduled (they still wait for its completion).
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 enum : int {
   kScalDr = 0,     // dr_comov of this step
   kScalVol = 1,    // source.vol of this step

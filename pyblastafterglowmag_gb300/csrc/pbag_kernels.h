@@ -10,6 +10,32 @@
 
 namespace pbag {
 
+// Launches of the step loop's kernels (k_evolve, k_rad_ssc and the three SSC
+// contractions). While pdl_scope() is set - around each evolve launch of the
+// capture of a batch's step loop into a CUDA graph - they carry programmatic
+// stream serialization, so that the kernel is resident and has loaded its
+// constant tables when the kernels before it end; otherwise they are plain
+// launches. Every kernel launched here calls grid_dep_wait() before it
+// touches memory that the kernels before it in the stream read or write, and
+// the radiation kernels release their dependents (grid_dep_launch) right
+// after it. The flag is per host thread, like the capture.
+bool& pdl_scope();
+template <typename... P, typename... A>
+inline cudaError_t launch_step_kernel(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                      A&&... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_scope() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(args)...);
+}
+
 // once per batch: init steps, e^-p tables, per-record scalars
 cudaError_t launch_prepare(const DevGrid& g, const DevState& S, const pbag_step_rec* recs, const int64_t* off,
                            const pbag_shock_params* prm, int nbw, int64_t nrec, int64_t* first, StepScal* ss,

@@ -86,6 +86,8 @@ k_ssc_rows(const unsigned char* __restrict__ Wt, const unsigned char* __restrict
   __shared__ volatile int fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.x * kRwRows;
+  grid_dep_wait();  // the weights, flags and row counts of the step's evolve launch
+  grid_dep_launch();
   if (nlive && row0 >= *nlive) return;  // a tile beyond the rows counted on the device
   const int o0 = blockIdx.y * gsz, no = min(gsz, nout - o0);
   if (no <= 0) return;
@@ -351,10 +353,9 @@ cudaError_t launch_rows(const unsigned char* Wt, const unsigned char* Kt, int Gp
   const int gsz = (nout + groups - 1) / groups;
   groups = (nout + gsz - 1) / gsz;
   dim3 grid(tiles, groups);
-  k_ssc_rows<MODE><<<grid, kRwThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, gsz, nout, plan.S, plan.cps, cfg.lsu, flags,
-                                                        U32, scal,
-                                                        oscale, ostride, out, err, rows.nlive, rows.rowmap);
-  return cudaGetLastError();
+  return launch_step_kernel(k_ssc_rows<MODE>, grid, dim3(kRwThreads), plan.smem, st, Wt, Kt, Gp, nrows, gsz, nout,
+                            plan.S, plan.cps, cfg.lsu, flags, U32, scal, oscale, ostride, out, err, rows.nlive,
+                            rows.rowmap);
 }
 
 }  // namespace

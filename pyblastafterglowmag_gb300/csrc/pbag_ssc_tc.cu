@@ -119,6 +119,8 @@ k_ssc_tc(const unsigned char* __restrict__ Wt, const unsigned char* __restrict__
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
   const int row0 = blockIdx.y * kTcCols;
+  grid_dep_wait();  // the weights, flags and row counts of the step's evolve launch
+  grid_dep_launch();
   if (nlive && row0 >= *nlive) return;  // a tile beyond the rows counted on the device
   const uint32_t stage_bytes = tc_stage_bytes(F, N);
   unsigned char* base =
@@ -396,13 +398,14 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
   const int tid = threadIdx.x, warp = tid >> 5;
   const int i = blockIdx.x;
   const int row0 = blockIdx.y * kTcCols;
-  if (nlive && row0 >= *nlive) return;
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   unsigned char* As = base;
   unsigned char* Bs = base + small_slab_bytes(Gp);
   float* Us = reinterpret_cast<float*>(Bs + small_w_bytes(N, Gp));
   const int nk8 = Gp / 8, nchunks = (nk8 + kK8 - 1) / kK8;
+  // the kernel slab (written once per context) streams in while the step's
+  // evolve launch finishes; everything else is read after it completed
   if (tid == 0) {
     fail = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&abar)));
@@ -416,6 +419,12 @@ k_ssc_tc_small(const unsigned char* __restrict__ Wt, const unsigned char* __rest
             smem_u32(As)),
         "l"(Kt + (size_t)i * tc_tile_bytes(F, Gp, 2)), "r"(bytes), "r"(smem_u32(&abar))
         : "memory");
+  }
+  grid_dep_wait();
+  grid_dep_launch();  // the next evolve launch may be scheduled
+  if (nlive && row0 >= *nlive) {  // a tile beyond the rows counted on the device: the copy lands first
+    if (tid == 0) mbar_wait(smem_u32(&abar), 0);
+    return;
   }
   // W rows [row0, row0 + N) of both parts of every chunk, and the U rows
   const unsigned char* Wtile = Wt + (size_t)blockIdx.y * tc_tile_bytes(kTcCols, Gp, 2);
@@ -561,9 +570,8 @@ cudaError_t launch_tc_small(const unsigned char* Wt, const unsigned char* Kt, in
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_ssc_tc_small<MODE><<<dim3(nout, 1), kTcThreads, small_smem(N, Gp), st>>>(
-      Wt, Kt, Gp, nrows, N, flags, U32, scal, oscale, ostride, out, err, rows.nlive, rows.rowmap);
-  return cudaGetLastError();
+  return launch_step_kernel(k_ssc_tc_small<MODE>, dim3(nout, 1), dim3(kTcThreads), small_smem(N, Gp), st, Wt, Kt,
+                            Gp, nrows, N, flags, U32, scal, oscale, ostride, out, err, rows.nlive, rows.rowmap);
 }
 
 template <int H, int MODE>
@@ -582,10 +590,9 @@ cudaError_t launch_tc(const unsigned char* Wt, const unsigned char* Kt, int Gp, 
     attr = true;
   }
   dim3 grid(nout, (nrows + kTcCols - 1) / kTcCols);
-  k_ssc_tc<H, MODE><<<grid, kTcThreads, plan.smem, st>>>(Wt, Kt, Gp, nrows, N, plan.S, plan.body, plan.ubytes,
-                                                           plan.uring, flags, U32, scal, oscale, ostride, out, err,
-                                                           rows.nlive, rows.rowmap);
-  return cudaGetLastError();
+  return launch_step_kernel(k_ssc_tc<H, MODE>, grid, dim3(kTcThreads), plan.smem, st, Wt, Kt, Gp, nrows, N, plan.S,
+                            plan.body, plan.ubytes, plan.uring, flags, U32, scal, oscale, ostride, out, err,
+                            rows.nlive, rows.rowmap);
 }
 
 uint16_t bf16_bits(float x) {  // round to nearest even (finite inputs)

@@ -723,10 +723,9 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
                  : "memory");
     bulk_to_smem(sh_tab, g.etab, tb, smem_addr(&bars[0]));
   }
-  // independent loads of this blastwave
+  // independent loads of this blastwave: first what no kernel of the pass
+  // writes (the slot map, records, step scalars, parameters, e^-p tables)
   const int bw = slot_bw(S, b);  // the caller's blastwave in this slot
-  const int flags0 = S.flags[b];
-  const int err0 = S.err[4 * b];
   const int64_t r0 = off[bw], len = off[bw + 1] - r0;
   const pbag_shock_params P = prm[bw];
   double* f = S.f + (size_t)b * G;
@@ -736,23 +735,7 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
 #pragma unroll
   for (int q = 0; q < C; ++q) {
     const int j = tid * C + q;  // solve: contiguous bins per thread
-    fr[q] = j < G ? f[j] : 0.;
     ppq[q] = j < G ? pp[j] : 0.;
-    const int i = tid + q * kStepThreads;  // everything else: strided bins
-    dpre[q] = (P.ssa_on && i < G) ? dfde[i] : 0.;
-  }
-  // gamma-grid history rows of the previous step, written once it completes
-  const bool hist_g = step > 0 && (out.ele_f_all || out.gdot_syn_all || out.gdot_adi_all || out.gdot_ssc_all);
-  double hf[C], hgs[C], hga[C], hgc[C];
-#pragma unroll
-  for (int q = 0; q < C; ++q) {
-    const int i = tid + q * kStepThreads;
-    const bool in = hist_g && i < G;
-    const double* gd = S.gdot + (size_t)b * 3 * G;
-    hf[q] = in ? f[i] : 0.;
-    hgs[q] = in ? gd[i] : 0.;
-    hga[q] = in ? gd[G + i] : 0.;
-    hgc[q] = in ? gd[2 * G + i] : 0.;
   }
   const bool in_range = step < len;
   StepScal sc{};
@@ -768,12 +751,39 @@ k_evolve(DevGrid g, DevState S, const pbag_step_rec* __restrict__ recs, const St
   const bool ssc = P.ssc_on && g.KintT != nullptr;
   // the kernel-integral table streams into shared memory while the previous
   // step completes, when this step runs the Chang-Cooper substeps with SSC
-  const bool staged = kstage > 0 && ssc && in_range && err0 == 0 && (sc.flags & kRecValid) && !sc.err &&
+  // (a blastwave stopped by an error returns before it reads the table)
+  const bool staged = kstage > 0 && ssc && in_range && (sc.flags & kRecValid) && !sc.err &&
                       !(sc.flags & kRecInit) && sc.n_sub > 0;
   if (staged && tid == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bars[1])), "r"(kstage)
                  : "memory");
     bulk_to_smem(sh_k, g.KintT, kstage, smem_addr(&bars[1]));
+  }
+  // then the state the previous step's kernels wrote, once they completed
+  // (no early release of this step's radiation kernels: resident next to
+  // these CTAs they slowed the pass)
+  grid_dep_wait();
+  const int flags0 = S.flags[b];
+  const int err0 = S.err[4 * b];
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    const int j = tid * C + q;
+    fr[q] = j < G ? f[j] : 0.;
+    const int i = tid + q * kStepThreads;  // everything else: strided bins
+    dpre[q] = (P.ssa_on && i < G) ? dfde[i] : 0.;
+  }
+  // gamma-grid history rows of the previous step, written once it completes
+  const bool hist_g = step > 0 && (out.ele_f_all || out.gdot_syn_all || out.gdot_adi_all || out.gdot_ssc_all);
+  double hf[C], hgs[C], hga[C], hgc[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    const int i = tid + q * kStepThreads;
+    const bool in = hist_g && i < G;
+    const double* gd = S.gdot + (size_t)b * 3 * G;
+    hf[q] = in ? f[i] : 0.;
+    hgs[q] = in ? gd[i] : 0.;
+    hga[q] = in ? gd[G + i] : 0.;
+    hgc[q] = in ? gd[2 * G + i] : 0.;
   }
   __syncthreads();  // the barriers are initialised
   auto drain = [&]() {  // copies must land before the CTA exits
@@ -1360,6 +1370,8 @@ template <int KPT>
 __global__ void __launch_bounds__(kRadThreads)
 k_rad_ssc(DevGrid g, DevState S, const pbag_shock_params* __restrict__ prm, int nbw, int rad_blocks, int R) {
   static_assert(kRadThreads == kSscThreads, "radiation and SSC tiles share the launch shape");
+  grid_dep_wait();    // the step's evolve launch has completed
+  grid_dep_launch();  // the next evolve launch may be scheduled
   const int blk = blockIdx.x;
   const int rc = (g.F + kRadFreqs * R - 1) / (kRadFreqs * R);
   if (blk < rad_blocks) {
@@ -1727,7 +1739,10 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
   const size_t smem = evolve_bytes(g, kstage);
   const int c = (g.G + kStepThreads - 1) / kStepThreads;
   const int fq = (g.F + kStepThreads - 1) / kStepThreads;
-  auto go = [&](auto kern) { kern<<<nbw, kStepThreads, smem, st>>>(g, S, recs, ss, off, prm, step, out, kstage); };
+  cudaError_t e = cudaSuccess;
+  auto go = [&](auto kern) {
+    e = launch_step_kernel(kern, dim3(nbw), dim3(kStepThreads), smem, st, g, S, recs, ss, off, prm, step, out, kstage);
+  };
   // large batches (the kernel-integral table not staged, small shared
   // memory): the register budget of four CTAs per SM, for more resident
   // blastwaves (no spills at 128 registers for grids up to 256 x 256); for
@@ -1742,7 +1757,7 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
       fq <= 1 ? go(k_evolve<1, 1, 4>) : go(k_evolve<1, 2, 4>);
     else
       fq <= 1 ? go(k_evolve<2, 1, 4>) : go(k_evolve<2, 2, 4>);
-    return cudaGetLastError();
+    return e;
   }
 #define PBAG_EVOLVE_FQ(CC)                 \
   if (fq <= 1) go(k_evolve<CC, 1, 1>);     \
@@ -1759,7 +1774,7 @@ cudaError_t launch_evolve(const DevGrid& g, const DevState& S, const pbag_step_r
     PBAG_EVOLVE_FQ(8)
   }
 #undef PBAG_EVOLVE_FQ
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock_params* prm, int nbw, bool ssc,
@@ -1779,15 +1794,13 @@ cudaError_t launch_rad_ssc(const DevGrid& g, const DevState& S, const pbag_shock
   if (total <= 0) return cudaSuccess;
   const int kpt = (g.F + kSscThreads - 1) / kSscThreads;
   const size_t smem = ssc ? (size_t)ssc_smem_bytes(g) : 0;
-  if (kpt <= 1)
-    k_rad_ssc<1><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
-  else if (kpt <= 2)
-    k_rad_ssc<2><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
-  else if (kpt <= 4)
-    k_rad_ssc<4><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
-  else
-    k_rad_ssc<8><<<total, kRadThreads, smem, st>>>(g, S, prm, nbw, rad_blocks, R);
-  return cudaGetLastError();
+  auto go = [&](auto kern) {
+    return launch_step_kernel(kern, dim3(total), dim3(kRadThreads), smem, st, g, S, prm, nbw, rad_blocks, R);
+  };
+  if (kpt <= 1) return go(k_rad_ssc<1>);
+  if (kpt <= 2) return go(k_rad_ssc<2>);
+  if (kpt <= 4) return go(k_rad_ssc<4>);
+  return go(k_rad_ssc<8>);
 }
 
 cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* off, const pbag_shock_params* prm,
@@ -1795,6 +1808,11 @@ cudaError_t launch_finalize(const DevGrid& g, const DevState& S, const int64_t* 
   if (nbw <= 0) return cudaSuccess;
   k_finalize<<<nbw, kStepThreads, 0, st>>>(g, S, off, prm, step, out);
   return cudaGetLastError();
+}
+
+bool& pdl_scope() {
+  thread_local bool on = false;
+  return on;
 }
 
 size_t evolve_smem_max_bytes() { return kEvolveSmemMax; }
