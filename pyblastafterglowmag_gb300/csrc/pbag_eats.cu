@@ -69,7 +69,33 @@ struct Iv9 {  // an interval of CADRE: f[] = fa, fll, fl, flr, fm, frl, fr, frr,
   double a, b, I, err;
   double f[9];
   int refinement;
+  // inner integral only: points evaluated ahead of their request (kAhead*
+  // bits): own quarters in f[2], f[6], own eighths in f[1], f[3], f[5], f[7],
+  // the quarter and eighth points of the two halves a split would make, the
+  // sum over the next Romberg level's odd points
+  int ahead;
+  double hq[4], he[8], rs;
 };
+enum : int { kAheadQ = 1, kAheadE = 2, kAheadHQ = 4, kAheadHE = 8, kAheadR = 16 };
+
+// The abscissae of CADRE's interval rules, every operation rounded on its own
+// (no contraction into FMAs), so that a point evaluated ahead of its request
+// has the request's abscissa bit for bit.
+__device__ __forceinline__ double lin2(double ca, double a, double cb, double b) {
+  return __dadd_rn(__dmul_rn(ca, a), __dmul_rn(cb, b));
+}
+__device__ __forceinline__ double mid2(double a, double b) { return __dmul_rn(0.5, __dadd_rn(a, b)); }
+__device__ __forceinline__ double romberg_h(double a, double b, int nint) {
+  return __ddiv_rn(__dsub_rn(b, a), (double)nint);
+}
+__device__ __forceinline__ double romberg_x(double a, double h, int j) { return __dadd_rn(a, __dmul_rn(h, (double)j)); }
+// the four eighth points of [a, b] in the order fll, flr, frl, frr
+__device__ __forceinline__ void eighths(double a, double b, double* x) {
+  x[0] = lin2(0.875, a, 0.125, b);
+  x[1] = lin2(0.625, a, 0.375, b);
+  x[2] = lin2(0.375, a, 0.625, b);
+  x[3] = lin2(0.125, a, 0.875, b);
+}
 
 struct Heap {  // max-heap on err
   Iv9* h;
@@ -329,7 +355,17 @@ struct Eats {
     const unsigned bad = __ballot_sync(0xffffffffu, rc != PBAG_OK);
     if (bad) code = __shfl_sync(0xffffffffu, rc, __ffs(bad) - 1);
   }
-  struct Inner {  // the points of one inner integral: the lanes evaluate them together
+  // The points of one inner integral: the lanes evaluate them together. A
+  // batch needs 2-4 points in most steps of the quadrature, and a warp's FP64
+  // instruction costs the same however many lanes are active, so the idle
+  // lanes evaluate the points the next steps may request (kAhead): a point's
+  // value depends on its abscissa alone, the abscissae are formed the same
+  // way, so the results are those of evaluating on request, bit for bit,
+  // while the chain of dependent batches shrinks (to about a third on the
+  // tested light curves). Only the requested points count as evaluations and
+  // can stop the quadrature; a point evaluated ahead that fails is dropped.
+  struct Inner {
+    static constexpr bool kAhead = true;
     Eats& e;
     double sphi;
     __device__ void eval(const double* xs, int n, double* ys) {  // n <= 32
@@ -339,13 +375,52 @@ struct Eats {
       e.count_evals(n);
       for (int k = 0; k < n; ++k) ys[k] = __shfl_sync(0xffffffffu, y, k);
     }
+    // n requested points xs (lanes [0, n)) and na points ahead xa (lanes
+    // [n, n + na), n + na <= 32); returns the lanes of xa that failed
+    __device__ unsigned eval_ahead(const double* xs, int n, const double* xa, int na, double* ys, double* ya) {
+      int rc = PBAG_OK;
+      const int l = e.lane;
+      const double x = l < n ? xs[l] : l < n + na ? xa[l - n] : 0.;
+      const double y = l < n + na ? e.integrand(1 - x, sphi, &rc) : 0.;
+      const unsigned bad = __ballot_sync(0xffffffffu, rc != PBAG_OK);
+      const unsigned need = (1u << n) - 1u;
+      if (bad & need) e.code = __shfl_sync(0xffffffffu, rc, __ffs(bad & need) - 1);
+      e.count_evals(n);
+      for (int k = 0; k < n; ++k) ys[k] = __shfl_sync(0xffffffffu, y, k);
+      for (int k = 0; k < na; ++k) ya[k] = __shfl_sync(0xffffffffu, y, n + k);
+      return (bad >> n) & ((1u << na) - 1u);
+    }
+    // sum_odd(a, h, nint) for nint / 2 + nint <= 32, with the next level's sum
+    // over its odd points (a + h2 j, h2 = (b - a) / 2 nint) in *next (each sum
+    // over the lanes in sum_odd's order); returns whether *next is valid
+    __device__ double sum_odd_ahead(double a, double b, double h, int nint, double* next, bool* next_ok) {
+      const int l = e.lane, m = nint / 2;
+      const double h2 = romberg_h(a, b, 2 * nint);
+      int rc = PBAG_OK;
+      const double x = l < m ? romberg_x(a, h, 2 * l + 1) : l < m + nint ? romberg_x(a, h2, 2 * (l - m) + 1) : 0.;
+      const double y = l < m + nint ? e.integrand(1 - x, sphi, &rc) : 0.;
+      const unsigned bad = __ballot_sync(0xffffffffu, rc != PBAG_OK);
+      const unsigned need = (1u << m) - 1u;
+      if (bad & need) e.code = __shfl_sync(0xffffffffu, rc, __ffs(bad & need) - 1);
+      e.count_evals(m);
+      *next_ok = ((bad >> m) & ((1u << nint) - 1u)) == 0u;
+      double s = l < m ? y : 0.;
+      double t = __shfl_sync(0xffffffffu, y, min(l + m, 31));
+      t = l < nint ? t : 0.;
+      for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+      }
+      *next = 0. + t;  // as sum_odd accumulates its single chunk
+      return e.stop() ? 0. : 0. + s;
+    }
     // sum of f(a + h j) over odd j < nint
     __device__ double sum_odd(double a, double h, int nint) {
       double s = 0.;
       for (int base = 1; base < nint; base += 64) {
         const int j = base + 2 * e.lane;
         int rc = PBAG_OK;
-        double y = j < nint ? e.integrand(1 - (a + h * j), sphi, &rc) : 0.;
+        double y = j < nint ? e.integrand(1 - romberg_x(a, h, j), sphi, &rc) : 0.;
         e.first_failure(rc);
         e.count_evals(min(32, (nint - base + 1) / 2));
         if (e.stop()) return 0.;
@@ -376,6 +451,7 @@ struct Eats {
     }
   };
   struct Outer {  // the points of the phi integral: one inner integral each, in order
+    static constexpr bool kAhead = false;
     Eats& e;
     __device__ void eval(const double* xs, int n, double* ys) {
       for (int k = 0; k < n; ++k) {
@@ -386,7 +462,7 @@ struct Eats {
     __device__ double sum_odd(double a, double h, int nint) {
       double s = 0.;
       for (int j = 1; j < nint; j += 2) {
-        s += e.phi_integrand(a + h * j);
+        s += e.phi_integrand(romberg_x(a, h, j));
         if (e.stop()) return 0.;
       }
       return s;
@@ -413,6 +489,7 @@ struct Eats {
   // their own copy of the phi intervals included. A batch's status is its
   // first failing point's.
   struct Crew {
+    static constexpr bool kAhead = false;
     Eats& e;
     double* ysh;
     int* csh;
@@ -443,7 +520,7 @@ struct Eats {
       const int m = nint / 2;  // odd j < nint: j = 2 i + 1
       for (int base = 0; base < m; base += kCrewChunk) {
         const int n = min(kCrewChunk, m - base);
-        batch([&](int k) { return a + h * (2 * (base + k) + 1); }, n);
+        batch([&](int k) { return romberg_x(a, h, 2 * (base + k) + 1); }, n);
         if (!e.stop())
           for (int k = 0; k < n; ++k) s += ysh[k];
         done();
@@ -470,6 +547,45 @@ struct Eats {
     }
   };
 
+  // Points of [a, b] that later steps may request: its own eighths (with
+  // own), then the quarter points of its halves [a, m], [m, b] (m as a split
+  // forms it) and their eighth points.
+  __device__ static void ahead_points(double a, double b, bool own, double* x) {
+    if (own) {
+      eighths(a, b, x);
+      x += 4;
+    }
+    const double m = mid2(a, b);
+    x[0] = lin2(0.75, a, 0.25, m);
+    x[1] = lin2(0.25, a, 0.75, m);
+    x[2] = lin2(0.75, m, 0.25, b);
+    x[3] = lin2(0.25, m, 0.75, b);
+    eighths(a, m, x + 4);
+    eighths(m, b, x + 8);
+  }
+  // keeps the groups of ahead_points' values whose points all succeeded
+  __device__ static void keep_ahead(Iv9* i, bool own, const double* y, unsigned bad) {
+    if (own) {
+      if (!(bad & 0xFu)) {
+        i->f[1] = y[0];
+        i->f[3] = y[1];
+        i->f[5] = y[2];
+        i->f[7] = y[3];
+        i->ahead |= kAheadE;
+      }
+      y += 4;
+      bad >>= 4;
+    }
+    if (!(bad & 0xFu)) {
+      for (int k = 0; k < 4; ++k) i->hq[k] = y[k];
+      i->ahead |= kAheadHQ;
+    }
+    if (!(bad & 0xFF0u)) {
+      for (int k = 0; k < 8; ++k) i->he[k] = y[4 + k];
+      i->ahead |= kAheadHE;
+    }
+  }
+
   // CADRE's interval rules (cadreProcessInterval, quadratures.h:1653-1937)
   template <class B>
   __device__ int process(B& fb, Iv9* i) {
@@ -479,9 +595,22 @@ struct Eats {
       const double fa = i->f[0], fm = i->f[4], fb_ = i->f[8];
       double fl, fr;
       if (i->refinement == 0) {
-        const double xs[2] = {0.75 * i->a + 0.25 * i->b, 0.25 * i->a + 0.75 * i->b};
+        const double xs[2] = {lin2(0.75, i->a, 0.25, i->b), lin2(0.25, i->a, 0.75, i->b)};
         double ys[2];
-        fb.eval(xs, 2, ys);
+        if constexpr (B::kAhead) {
+          if (i->ahead & kAheadQ) {  // evaluated ahead
+            ys[0] = i->f[2];
+            ys[1] = i->f[6];
+            count_evals(2);
+          } else {  // ahead: own eighths, the quarters and eighths of the halves
+            double xa[16], ya[16];
+            ahead_points(i->a, i->b, true, xa);
+            const unsigned bad = fb.eval_ahead(xs, 2, xa, 16, ys, ya);
+            keep_ahead(i, true, ya, bad);
+          }
+        } else {
+          fb.eval(xs, 2, ys);
+        }
         count += 2;
         if (stop()) return count;
         fl = ys[0];
@@ -499,10 +628,25 @@ struct Eats {
       const double T2 = 0.5 * T1 + h * (fl + fr);
       const double R0 = (T1 - T0) / (T2 - T1);
       if (R0 > 4 - scaleTol && R0 < 4 + scaleTol) {
-        const double xs[4] = {0.875 * i->a + 0.125 * i->b, 0.625 * i->a + 0.375 * i->b,
-                              0.375 * i->a + 0.625 * i->b, 0.125 * i->a + 0.875 * i->b};
+        double xs[4];
+        eighths(i->a, i->b, xs);
         double v[4];
-        fb.eval(xs, 4, v);
+        if constexpr (B::kAhead) {
+          if (i->ahead & kAheadE) {  // evaluated ahead
+            v[0] = i->f[1];
+            v[1] = i->f[3];
+            v[2] = i->f[5];
+            v[3] = i->f[7];
+            count_evals(4);
+          } else {  // ahead: the quarters and eighths of the halves
+            double xa[12], ya[12];
+            ahead_points(i->a, i->b, false, xa);
+            const unsigned bad = fb.eval_ahead(xs, 4, xa, 12, v, ya);
+            keep_ahead(i, false, ya, bad);
+          }
+        } else {
+          fb.eval(xs, 4, v);
+        }
         count += 4;
         if (stop()) return count;
         i->f[1] = v[0];
@@ -544,8 +688,23 @@ struct Eats {
     // Romberg mode: one more level of the tableau held in f[]
     int nint = 1;
     for (int n = 0; n < i->refinement; n++) nint *= 2;
-    const double h = (i->b - i->a) / nint;
-    const double sum = fb.sum_odd(i->a, h, nint);
+    const double h = romberg_h(i->a, i->b, nint);
+    double sum;
+    if constexpr (B::kAhead) {
+      if (i->ahead & kAheadR) {  // evaluated ahead at the previous level
+        sum = i->rs;
+        count_evals(nint / 2);
+        i->ahead &= ~kAheadR;
+      } else if (nint / 2 + nint <= 32) {
+        bool ok = false;
+        sum = fb.sum_odd_ahead(i->a, i->b, h, nint, &i->rs, &ok);
+        if (ok) i->ahead |= kAheadR;
+      } else {
+        sum = fb.sum_odd(i->a, h, nint);
+      }
+    } else {
+      sum = fb.sum_odd(i->a, h, nint);
+    }
     count += nint / 2;
     if (stop()) return count;
     double Rnm = i->f[0], Rnmp = i->f[1];
@@ -584,9 +743,23 @@ struct Eats {
     i.a = xa;
     i.b = xb;
     {
-      const double xs[3] = {xa, xb, 0.5 * (xa + xb)};  // cadreInitInterval: f(a), f(b), f(m)
+      const double xs[3] = {xa, xb, mid2(xa, xb)};  // cadreInitInterval: f(a), f(b), f(m)
       double ys[3];
-      fb.eval(xs, 3, ys);
+      if constexpr (B::kAhead) {  // ahead: the quarters, then as for a quarter step
+        double xa2[18], ya[18];
+        xa2[0] = lin2(0.75, xa, 0.25, xb);
+        xa2[1] = lin2(0.25, xa, 0.75, xb);
+        ahead_points(xa, xb, true, xa2 + 2);
+        const unsigned bad = fb.eval_ahead(xs, 3, xa2, 18, ys, ya);
+        if (!(bad & 3u)) {
+          i.f[2] = ya[0];
+          i.f[6] = ya[1];
+          i.ahead |= kAheadQ;
+        }
+        keep_ahead(&i, true, ya + 2, bad >> 2);
+      } else {
+        fb.eval(xs, 3, ys);
+      }
       if (stop()) return 0.0;
       i.f[0] = ys[0];
       i.f[8] = ys[1];
@@ -608,7 +781,7 @@ struct Eats {
         I += i.I - oldI;
       } else {
         Iv9 i1{}, i2{};  // cadreSplitInterval
-        const double xm = 0.5 * (i.a + i.b);
+        const double xm = mid2(i.a, i.b);
         i1.a = i.a;
         i1.b = xm;
         i2.a = xm;
@@ -625,6 +798,28 @@ struct Eats {
         i2.f[6] = i.f[7];
         i2.f[8] = i.f[8];
         i2.refinement = i.refinement;
+        if constexpr (B::kAhead) {  // the halves' points evaluated ahead
+          if (i.refinement == 0 && (i.ahead & kAheadHQ)) {  // (otherwise the parent's eighths are their quarters)
+            i1.f[2] = i.hq[0];
+            i1.f[6] = i.hq[1];
+            i2.f[2] = i.hq[2];
+            i2.f[6] = i.hq[3];
+            i1.ahead |= kAheadQ;
+            i2.ahead |= kAheadQ;
+          }
+          if (i.ahead & kAheadHE) {
+            i1.f[1] = i.he[0];
+            i1.f[3] = i.he[1];
+            i1.f[5] = i.he[2];
+            i1.f[7] = i.he[3];
+            i2.f[1] = i.he[4];
+            i2.f[3] = i.he[5];
+            i2.f[5] = i.he[6];
+            i2.f[7] = i.he[7];
+            i1.ahead |= kAheadE;
+            i2.ahead |= kAheadE;
+          }
+        }
         n += process(fb, &i1);
         n += process(fb, &i2);
         if (stop()) return 0.0;
@@ -729,9 +924,14 @@ __global__ void __launch_bounds__(kEatsThreads) k_eats(EatsArgs A, int items) {
 }
 
 // One item per CTA of W warps: the phi points of each outer step spread over
-// the warps (Eats::Crew), each warp with its own interval workspaces.
-template <int W>
-__global__ void __launch_bounds__(32 * W) k_eats_crew(EatsArgs A, int items) {
+// the warps (Eats::Crew), each warp with its own interval workspaces. MINB:
+// CTAs per SM the registers are budgeted for - 1 for CADRE (255 registers:
+// its points evaluated ahead need them, and a light curve's time is its
+// slowest items'), 3 for the fixed trapezoid (168: the items are short and
+// many, occupancy counts; measured 20 600 against 18 800 points/s with 255,
+// CADRE 2 050 against 2 120 with 168).
+template <int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) k_eats_crew(EatsArgs A, int items) {
   const int item = blockIdx.x;
   if (item >= items) return;
   const int w = threadIdx.x >> 5;
@@ -879,8 +1079,10 @@ extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int n
     k_eats_mu<<<(unsigned)((n_mu + 255) / 256), 256, 0, v.stream>>>(A, items);
     if (crew == 1)
       k_eats<<<(items + kEatsThreads / 32 - 1) / (kEatsThreads / 32), kEatsThreads, 0, v.stream>>>(A, items);
+    else if (o.method_quad == PBAG_QUAD_CADRE)
+      k_eats_crew<4, 1><<<items, 128, 0, v.stream>>>(A, items);
     else
-      k_eats_crew<4><<<items, 128, 0, v.stream>>>(A, items);
+      k_eats_crew<4, 3><<<items, 128, 0, v.stream>>>(A, items);
     k_eats_sum<<<(nq + 127) / 128, 128, 0, v.stream>>>(d_part, nq, sides, d_flux);
     e = cudaGetLastError();
   }
