@@ -385,7 +385,7 @@ struct Eats {
       const unsigned bad = __ballot_sync(0xffffffffu, rc != PBAG_OK);
       const unsigned need = (1u << n) - 1u;
       if (bad & need) e.code = __shfl_sync(0xffffffffu, rc, __ffs(bad & need) - 1);
-      e.count_evals(n);
+      if (n > 0) e.count_evals(n);
       for (int k = 0; k < n; ++k) ys[k] = __shfl_sync(0xffffffffu, y, k);
       for (int k = 0; k < na; ++k) ya[k] = __shfl_sync(0xffffffffu, y, n + k);
       return (bad >> n) & ((1u << na) - 1u);
@@ -806,6 +806,36 @@ struct Eats {
             i2.f[6] = i.hq[3];
             i1.ahead |= kAheadQ;
             i2.ahead |= kAheadQ;
+          }
+          if (i.refinement == 0 && !(i.ahead & kAheadHQ)) {
+            // the halves' quarters were not evaluated ahead: one batch for
+            // both halves instead of one each - their quarters and eighths,
+            // the quarters of each one's halves, the eighths of the first
+            // one's halves (all ahead: process() requests them as usual)
+            double xa[28], ya[28];
+            xa[0] = lin2(0.75, i1.a, 0.25, i1.b);
+            xa[1] = lin2(0.25, i1.a, 0.75, i1.b);
+            ahead_points(i1.a, i1.b, true, xa + 2);
+            xa[18] = lin2(0.75, i2.a, 0.25, i2.b);
+            xa[19] = lin2(0.25, i2.a, 0.75, i2.b);
+            {
+              double t[16];
+              ahead_points(i2.a, i2.b, true, t);
+              for (int k = 0; k < 8; ++k) xa[20 + k] = t[k];  // its eighths and its halves' quarters
+            }
+            const unsigned bad = fb.eval_ahead(nullptr, 0, xa, 28, nullptr, ya);
+            if (!(bad & 3u)) {
+              i1.f[2] = ya[0];
+              i1.f[6] = ya[1];
+              i1.ahead |= kAheadQ;
+            }
+            keep_ahead(&i1, true, ya + 2, bad >> 2);
+            if (!((bad >> 18) & 3u)) {
+              i2.f[2] = ya[18];
+              i2.f[6] = ya[19];
+              i2.ahead |= kAheadQ;
+            }
+            keep_ahead(&i2, true, ya + 20, ((bad >> 20) & 0xFFu) | 0xFF00u);  // its halves' eighths: not evaluated
           }
           if (i.ahead & kAheadHE) {
             i1.f[1] = i.he[0];
