@@ -200,6 +200,7 @@ struct EatsArgs {
   int cap_phi, cap_theta;
   double* part;             // [items]
   unsigned long long* first;
+  int ahead;                // inner-integral points evaluated ahead (PBAG_EATS_AHEAD=0: on request only)
 };
 
 // The EATS object of one work item.
@@ -602,11 +603,13 @@ struct Eats {
             ys[0] = i->f[2];
             ys[1] = i->f[6];
             count_evals(2);
-          } else {  // ahead: own eighths, the quarters and eighths of the halves
+          } else if (A.ahead) {  // ahead: own eighths, the quarters and eighths of the halves
             double xa[16], ya[16];
             ahead_points(i->a, i->b, true, xa);
             const unsigned bad = fb.eval_ahead(xs, 2, xa, 16, ys, ya);
             keep_ahead(i, true, ya, bad);
+          } else {
+            fb.eval(xs, 2, ys);
           }
         } else {
           fb.eval(xs, 2, ys);
@@ -638,11 +641,13 @@ struct Eats {
             v[2] = i->f[5];
             v[3] = i->f[7];
             count_evals(4);
-          } else {  // ahead: the quarters and eighths of the halves
+          } else if (A.ahead) {  // ahead: the quarters and eighths of the halves
             double xa[12], ya[12];
             ahead_points(i->a, i->b, false, xa);
             const unsigned bad = fb.eval_ahead(xs, 4, xa, 12, v, ya);
             keep_ahead(i, false, ya, bad);
+          } else {
+            fb.eval(xs, 4, v);
           }
         } else {
           fb.eval(xs, 4, v);
@@ -695,7 +700,7 @@ struct Eats {
         sum = i->rs;
         count_evals(nint / 2);
         i->ahead &= ~kAheadR;
-      } else if (nint / 2 + nint <= 32) {
+      } else if (A.ahead && nint / 2 + nint <= 32) {
         bool ok = false;
         sum = fb.sum_odd_ahead(i->a, i->b, h, nint, &i->rs, &ok);
         if (ok) i->ahead |= kAheadR;
@@ -745,21 +750,24 @@ struct Eats {
     {
       const double xs[3] = {xa, xb, mid2(xa, xb)};  // cadreInitInterval: f(a), f(b), f(m)
       double ys[3];
-      if constexpr (B::kAhead) {  // ahead: the quarters, then as for a quarter step
-        double xa2[18], ya[18];
-        xa2[0] = lin2(0.75, xa, 0.25, xb);
-        xa2[1] = lin2(0.25, xa, 0.75, xb);
-        ahead_points(xa, xb, true, xa2 + 2);
-        const unsigned bad = fb.eval_ahead(xs, 3, xa2, 18, ys, ya);
-        if (!(bad & 3u)) {
-          i.f[2] = ya[0];
-          i.f[6] = ya[1];
-          i.ahead |= kAheadQ;
+      bool done = false;
+      if constexpr (B::kAhead) {
+        if (A.ahead) {  // ahead: the quarters, then as for a quarter step
+          double xa2[18], ya[18];
+          xa2[0] = lin2(0.75, xa, 0.25, xb);
+          xa2[1] = lin2(0.25, xa, 0.75, xb);
+          ahead_points(xa, xb, true, xa2 + 2);
+          const unsigned bad = fb.eval_ahead(xs, 3, xa2, 18, ys, ya);
+          if (!(bad & 3u)) {
+            i.f[2] = ya[0];
+            i.f[6] = ya[1];
+            i.ahead |= kAheadQ;
+          }
+          keep_ahead(&i, true, ya + 2, bad >> 2);
+          done = true;
         }
-        keep_ahead(&i, true, ya + 2, bad >> 2);
-      } else {
-        fb.eval(xs, 3, ys);
       }
+      if (!done) fb.eval(xs, 3, ys);
       if (stop()) return 0.0;
       i.f[0] = ys[0];
       i.f[8] = ys[1];
@@ -807,7 +815,7 @@ struct Eats {
             i1.ahead |= kAheadQ;
             i2.ahead |= kAheadQ;
           }
-          if (i.refinement == 0 && !(i.ahead & kAheadHQ)) {
+          if (A.ahead && i.refinement == 0 && !(i.ahead & kAheadHQ)) {
             // the halves' quarters were not evaluated ahead: one batch for
             // both halves instead of one each - their quarters and eighths,
             // the quarters of each one's halves, the eighths of the first
@@ -1079,6 +1087,8 @@ extern "C" int pbag_eats_flux_a(pbag_ctx* ctx, const pbag_eats_opts* opts, int n
   // spreads each outer step's phi points over four warps
   int crew = 4;
   if (const char* cw = std::getenv("PBAG_EATS_WARPS")) crew = std::atoi(cw) == 1 ? 1 : 4;
+  const char* ah = std::getenv("PBAG_EATS_AHEAD");
+  A.ahead = (ah && ah[0] == '0') ? 0 : 1;
   const size_t n_ws = (size_t)items * crew * (A.cap_phi + A.cap_theta);
   double *d_ln = nullptr, *d_mu = nullptr, *d_part = nullptr;
   Iv9* d_ws = nullptr;

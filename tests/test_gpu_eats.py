@@ -87,6 +87,28 @@ def test_eats_crew_matches_single_warp(oracle, cuda_device, eats_inputs, monkeyp
     np.testing.assert_array_equal(four, one)
 
 
+@pytest.mark.parametrize("name", ["gaussian_fsrs", "tophat_off_axis"])
+def test_eats_points_ahead_bit_identical(oracle, cuda_device, eats_inputs, monkeypatch, name):
+    """The inner integral's points evaluated ahead on idle lanes (the
+    default) and every point evaluated on request (PBAG_EATS_AHEAD=0) give
+    the same light curve bit for bit: a point's value depends on its
+    abscissa alone, and both form the abscissae the same way."""
+    import torch
+    grid, o, layers, dyn, off, recs, prm, j, a, q = eats_inputs[name]
+    assert o.method_quad == abi.PBAG_QUAD_CADRE
+    dev = torch.device("cuda", 0)
+    ctx = Context(grid, device=0, ssc=True)
+    d_j = torch.from_numpy(np.ascontiguousarray(j)).to(dev)
+    d_a = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    monkeypatch.setenv("PBAG_EATS_AHEAD", "0")
+    on_request = _gpu_eats(ctx, o, layers, dyn, off, d_j.data_ptr(), d_a.data_ptr(), q)
+    monkeypatch.delenv("PBAG_EATS_AHEAD")
+    ahead = _gpu_eats(ctx, o, layers, dyn, off, d_j.data_ptr(), d_a.data_ptr(), q)
+    ctx.close()
+    assert np.all(ahead > 0)
+    np.testing.assert_array_equal(ahead, on_request)
+
+
 def test_eats_gpu_errors(oracle, cuda_device, eats_inputs):
     """Where the reference exits: an observer time outside the burster-time
     grid (PBAG_ERR_RANGE with the failing query), a query naming no layer
