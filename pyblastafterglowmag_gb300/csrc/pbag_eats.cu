@@ -367,6 +367,7 @@ struct Eats {
   // can stop the quadrature; a point evaluated ahead that fails is dropped.
   struct Inner {
     static constexpr bool kAhead = true;
+    static constexpr bool kMergeSplit = false;  // (the ahead batches cover it)
     Eats& e;
     double sphi;
     __device__ void eval(const double* xs, int n, double* ys) {  // n <= 32
@@ -453,6 +454,7 @@ struct Eats {
   };
   struct Outer {  // the points of the phi integral: one inner integral each, in order
     static constexpr bool kAhead = false;
+    static constexpr bool kMergeSplit = false;
     Eats& e;
     __device__ void eval(const double* xs, int n, double* ys) {
       for (int k = 0; k < n; ++k) {
@@ -491,10 +493,32 @@ struct Eats {
   // first failing point's.
   struct Crew {
     static constexpr bool kAhead = false;
+    // a split's halves request their quarter points one after the other: the
+    // crew evaluates all four in one batch (eval_each) and the halves take
+    // them as evaluated ahead
+    static constexpr bool kMergeSplit = true;
     Eats& e;
     double* ysh;
     int* csh;
     int w, W;
+    // every point with its own status; the quadrature's status stays as it was
+    __device__ void eval_each(const double* xs, int n, double* ys, int* cs) {
+      for (int k = w; k < n; k += W) {
+        e.code = PBAG_OK;
+        const double y = e.phi_integrand(xs[k]);
+        if (e.lane == 0) {
+          ysh[k] = y;
+          csh[k] = e.code;
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < n; ++k) {
+        ys[k] = ysh[k];
+        cs[k] = csh[k];
+      }
+      e.code = PBAG_OK;
+      done();
+    }
     template <class X>
     __device__ void batch(X xk, int n) {  // n <= kCrewChunk; the caller reads ysh, then calls done()
       for (int k = w; k < n; k += W) {
@@ -598,12 +622,12 @@ struct Eats {
       if (i->refinement == 0) {
         const double xs[2] = {lin2(0.75, i->a, 0.25, i->b), lin2(0.25, i->a, 0.75, i->b)};
         double ys[2];
-        if constexpr (B::kAhead) {
-          if (i->ahead & kAheadQ) {  // evaluated ahead
-            ys[0] = i->f[2];
-            ys[1] = i->f[6];
-            count_evals(2);
-          } else if (A.ahead) {  // ahead: own eighths, the quarters and eighths of the halves
+        if (i->ahead & kAheadQ) {  // evaluated ahead
+          ys[0] = i->f[2];
+          ys[1] = i->f[6];
+          if constexpr (B::kAhead) count_evals(2);  // (the inner integral's points count)
+        } else if constexpr (B::kAhead) {
+          if (A.ahead) {  // ahead: own eighths, the quarters and eighths of the halves
             double xa[16], ya[16];
             ahead_points(i->a, i->b, true, xa);
             const unsigned bad = fb.eval_ahead(xs, 2, xa, 16, ys, ya);
@@ -806,6 +830,25 @@ struct Eats {
         i2.f[6] = i.f[7];
         i2.f[8] = i.f[8];
         i2.refinement = i.refinement;
+        if constexpr (B::kMergeSplit) {  // both halves' quarter points in one batch
+          if (i.refinement == 0) {
+            const double xs[4] = {lin2(0.75, i1.a, 0.25, i1.b), lin2(0.25, i1.a, 0.75, i1.b),
+                                  lin2(0.75, i2.a, 0.25, i2.b), lin2(0.25, i2.a, 0.75, i2.b)};
+            double ys[4];
+            int cs[4];
+            fb.eval_each(xs, 4, ys, cs);  // a failing point fails again when its half requests it
+            if (cs[0] == PBAG_OK && cs[1] == PBAG_OK) {
+              i1.f[2] = ys[0];
+              i1.f[6] = ys[1];
+              i1.ahead |= kAheadQ;
+            }
+            if (cs[2] == PBAG_OK && cs[3] == PBAG_OK) {
+              i2.f[2] = ys[2];
+              i2.f[6] = ys[3];
+              i2.ahead |= kAheadQ;
+            }
+          }
+        }
         if constexpr (B::kAhead) {  // the halves' points evaluated ahead
           if (i.refinement == 0 && (i.ahead & kAheadHQ)) {  // (otherwise the parent's eighths are their quarters)
             i1.f[2] = i.hq[0];
