@@ -78,6 +78,25 @@ struct Iv9 {  // an interval of CADRE: f[] = fa, fll, fl, flr, fm, frl, fr, frr,
 };
 enum : int { kAheadQ = 1, kAheadE = 2, kAheadHQ = 4, kAheadHE = 8, kAheadR = 16 };
 
+// e^x for the log-linear interpolation within one step of the dynamics grid,
+// where |x| = |t ln(y_{i+1}/y_i)| is small: for |x| <= 1/16 the Taylor series
+// through x^9 by Horner's rule (the next term is below 2e-19 relative), nine
+// FP64 FMAs instead of a full exp; larger |x| (tested on the exponent bits,
+// without an FP64 compare) and non-finite x take exp().
+__device__ __forceinline__ double exp_step(double x) {
+  if ((__double2hiint(x) & 0x7fffffff) > 0x3FB00000) return exp(x);  // |x| > 1/16
+  double p = 1.0 / 362880.0;
+  p = fma(p, x, 1.0 / 40320.0);
+  p = fma(p, x, 1.0 / 5040.0);
+  p = fma(p, x, 1.0 / 720.0);
+  p = fma(p, x, 1.0 / 120.0);
+  p = fma(p, x, 1.0 / 24.0);
+  p = fma(p, x, 1.0 / 6.0);
+  p = fma(p, x, 0.5);
+  p = fma(p, x, 1.0);
+  return fma(p, x, 1.0);
+}
+
 // The abscissae of CADRE's interval rules, every operation rounded on its own
 // (no contraction into FMAs), so that a point evaluated ahead of its request
 // has the request's abscissa bit for bit.
@@ -221,7 +240,9 @@ struct Eats {
 
   __device__ const double* qv(int k) const { return dyn + (size_t)k * A.nr; }
   // ya (yb/ya)^t with ln(yb/ya) from the table
-  __device__ double seg(int li, int a, double t) const { return qv(kLogQ[li])[a] * exp(t * ln[(size_t)li * A.nr + a]); }
+  __device__ double seg(int li, int a, double t) const {
+    return qv(kLogQ[li])[a] * exp_step(t * ln[(size_t)li * A.nr + a]);
+  }
 
   // fluxDens (microphysics.h:1185-1217) + computeFluxDensity (:799-867) on the
   // history rows r0 + ia, r0 + ib
@@ -288,7 +309,8 @@ struct Eats {
     if (mu[0] >= m) t_e = -1;  // check_emission_time (eats.h:24-38)
     if (t_e < 0.0 || !isfinite(t_e)) return 0.;
     // radius at t_e, then every quantity at that radius
-    const double r = R[ia] * exp(log(t_e / tb[ia]) / ln[(size_t)kLnT * A.nr + ia] * ln[(size_t)kLnR * A.nr + ia]);
+    const double r =
+        R[ia] * exp_step(log(t_e / tb[ia]) / ln[(size_t)kLnT * A.nr + ia] * ln[(size_t)kLnR * A.nr + ia]);
     if (r <= 0.0 || !isfinite(r)) return 0.0;
     const double t = log(r / R[ia]) / ln[(size_t)kLnR * A.nr + ia];
     const double Gamma = seg(0, ia, t), beta = seg(1, ia, t), theta = seg(8, ia, t);
